@@ -1,0 +1,333 @@
+"""ctypes front end for the CPU oracle and for the compiled reference integrator.
+
+TEST INFRASTRUCTURE ONLY. Only tests/, ``__graft_entry__.smoke()`` and
+bench.py's CPU-baseline / reference legs import this module; the product
+(lantern_gb300) never does.
+
+* ``liboracle.so`` -- oracle/lt_oracle.c, the project's C restatement of the
+  reference's per-pixel loop (built by :func:`build_oracle`).
+* ``liblantern_ref.so`` -- the reference's own integrator built by
+  oracle/build_ref.sh (present where the reference tree was staged).
+
+:func:`load_scene` reads a Lantern scene JSON and its LMF files the way
+``Scene::ParseJSON`` / ``AddLMF`` do (source/core/scene/scene.cpp:215-446,
+502-582; io/lantern_model_file.cpp:33-65) and hands it to the oracle.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import struct
+import subprocess
+import threading
+from contextlib import contextmanager
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+ORACLE_SO = os.path.join(BUILD, "liboracle.so")
+REF_SO = os.path.join(REF_DIR, "liblantern_ref.so")
+
+BSDF = {"lambert": 0, "mirror": 1, "ideal_specular_dielectric": 2}
+MED_NON_SCATTERING, MED_ISOTROPIC, MED_HG = 1, 2, 3
+KEY_TILE, KEY_PIXEL = 0, 1
+
+_lock = threading.Lock()
+_lib = None
+_ref = None
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile oracle/lt_oracle.c into oracle/_build/liboracle.so."""
+    src = os.path.join(HERE, "lt_oracle.c")
+    hdr = os.path.join(HERE, "lt_oracle.h")
+    os.makedirs(BUILD, exist_ok=True)
+    if (not force and os.path.exists(ORACLE_SO)
+            and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return ORACLE_SO
+    tmp = ORACLE_SO + f".{os.getpid()}.tmp"
+    subprocess.check_call(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
+                           "-o", tmp, src, "-lm", "-lpthread"])
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_reference() -> Optional[str]:
+    """Run oracle/build_ref.sh (stages from the reference tree when present,
+    else compiles already-staged sources). Returns the library path or None."""
+    if not (os.path.isdir("/root/reference/source") or os.path.isdir(os.path.join(REF_DIR, "src"))
+            or os.environ.get("LANTERN_REFERENCE")):
+        return None
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + r.stdout[-2000:] + r.stderr[-4000:])
+    return REF_SO
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = C.CDLL(build_oracle())
+            p, u32, u64, f32, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
+            fp = C.POINTER(C.c_float)
+            up = C.POINTER(C.c_uint32)
+            L.orc_scene_new.restype = p
+            L.orc_scene_free.argtypes = [p]
+            L.orc_set_camera.argtypes = [p, f32, f32, f32, u32, u32, fp, f32]
+            L.orc_set_background.argtypes = [p, fp]
+            L.orc_add_medium.argtypes = [p, i32, fp, fp, f32]
+            L.orc_add_medium.restype = i32
+            L.orc_add_medium_ref.argtypes = [p, i32, fp, f32, f32]
+            L.orc_add_medium_ref.restype = i32
+            L.orc_add_material.argtypes = [p, i32, fp, f32, i32]
+            L.orc_add_material.restype = i32
+            L.orc_add_mesh.argtypes = [p, fp, u32, fp, up, u32, i32, fp, f32]
+            L.orc_add_mesh.restype = i32
+            L.orc_scene_commit.argtypes = [p]
+            L.orc_light_info.argtypes = [p, i32, fp, fp, fp]
+            L.orc_num_triangles.argtypes = [p]
+            L.orc_num_triangles.restype = u32
+            L.orc_intersect.argtypes = [p, fp, up, u64, i32, up, i32]
+            L.orc_render.argtypes = [p, p, u32, u32, fp, up, up, fp, up, up, C.POINTER(C.c_uint64)]
+            L.orc_render_path.argtypes = [p, p, u32, u32, u32, fp, up]
+            L.orc_pcg_stream.argtypes = [u64, u64, u32, up, fp]
+            L.orc_tile_seed.argtypes = [u32, u32]
+            L.orc_tile_seed.restype = u32
+            L.orc_filter_sample.argtypes = [f32]
+            L.orc_filter_sample.restype = f32
+            L.orc_camera_ray.argtypes = [p, u32, u32, f32, f32, fp, fp]
+            _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The compiled reference integrator, or None when it is not built."""
+    global _ref
+    with _lock:
+        if _ref is None and os.path.exists(REF_SO):
+            L = C.CDLL(REF_SO)
+            p, u32 = C.c_void_p, C.c_uint32
+            fp = C.POINTER(C.c_float)
+            up = C.POINTER(C.c_uint32)
+            L.lref_scene_load.argtypes = [C.c_char_p]
+            L.lref_scene_load.restype = p
+            L.lref_scene_free.argtypes = [p]
+            L.lref_scene_size.argtypes = [p, up, up]
+            L.lref_render.argtypes = [p, u32, u32, u32, u32, fp, up, up, fp, up, up,
+                                      C.POINTER(C.c_ulonglong)]
+            L.lref_render.restype = C.c_double
+            L.lref_pcg_stream.argtypes = [C.c_ulonglong, C.c_ulonglong, u32, up, fp]
+            L.lref_filter_sample.argtypes = [fp, u32, fp]
+            L.lref_camera_ray.argtypes = [p, u32, u32, C.c_ulonglong, C.c_ulonglong, fp]
+            _ref = L
+    return _ref
+
+
+def fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+def uptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32)) if a is not None else None
+
+
+# ------------------------------------------------------------------ scene files
+def read_lmf(path: str) -> dict:
+    """ReadLMF (io/lantern_model_file.cpp:33-65)."""
+    with open(path, "rb") as fh:
+        data = fh.read()
+    if data[:4] != b"LMF\x00":
+        raise ValueError(f"{path}: bad LMF magic")
+    vpp = data[4]
+    flags = struct.unpack_from("<I", data, 5)[0]
+    off = 9
+    nv = struct.unpack_from("<Q", data, off)[0]
+    off += 8
+    pos = np.frombuffer(data, "<f4", nv * 3, off).reshape(-1, 3)
+    off += nv * 12
+    ni = struct.unpack_from("<Q", data, off)[0]
+    off += 8
+    idx = np.frombuffer(data, "<u4", ni, off)
+    off += ni * 4
+    nrm = tex = None
+    if flags & 1:
+        nn = struct.unpack_from("<Q", data, off)[0]
+        off += 8
+        nrm = np.frombuffer(data, "<f4", nn, off).reshape(-1, 3)
+        off += nn * 4
+    if flags & 2:
+        nt = struct.unpack_from("<Q", data, off)[0]
+        off += 8
+        tex = np.frombuffer(data, "<f4", nt, off).reshape(-1, 2)
+    return {"vpp": vpp, "positions": pos, "indices": idx, "normals": nrm, "texcoords": tex}
+
+
+def apply_transform(pos: np.ndarray, t: list) -> np.ndarray:
+    """``transform * float3a(p, 1)`` (scene.cpp:517-522, linearspace4.h:43-47,165):
+    row r = ((x*m[r][0] + y*m[r][1]) + z*m[r][2]) + 1*m[r][3] in float32."""
+    m = np.asarray(t, dtype=np.float32).reshape(4, 4)
+    x, y, z = pos[:, 0], pos[:, 1], pos[:, 2]
+    one = np.float32(1.0)
+    out = np.empty_like(pos, dtype=np.float32)
+    for r in range(3):
+        out[:, r] = ((x * m[r, 0] + y * m[r, 1]) + z * m[r, 2]) + one * m[r, 3]
+    return out
+
+
+class OracleScene:
+    """A scene loaded into the oracle."""
+
+    def __init__(self, json_path: str):
+        L = lib()
+        self.path = os.path.abspath(json_path)
+        with open(self.path) as fh:
+            j = json.load(fh)
+        self.json = j
+        self.h = L.orc_scene_new()
+        f32 = np.float32
+        cam = j["camera"]
+        self.width = int(cam["client_width"])
+        self.height = int(cam["client_height"])
+        tgt = np.array(cam.get("target", [0, 0, 0]), dtype=f32)
+        L.orc_set_camera(self.h, f32(cam.get("phi", np.pi / 4)), f32(cam.get("theta", 0.0)),
+                         f32(cam.get("radius", 10.0)), self.width, self.height, fptr(tgt),
+                         f32(cam.get("fov", np.pi / 4)))
+        bg = np.array(j.get("background_color", [0, 0, 0]), dtype=f32)
+        L.orc_set_background(self.h, fptr(bg))
+        media = {}
+        for m in j.get("media", []):
+            t = m["type"]
+            if t == "henyey_greenstein":
+                sa = np.array(m["sigma_a"], dtype=f32)
+                ss = np.array(m["sigma_s"], dtype=f32)
+                media[m["name"]] = L.orc_add_medium(self.h, MED_HG, fptr(sa), fptr(ss), f32(m.get("g", 0.0)))
+            else:
+                col = np.array(m["absorption_color"], dtype=f32)
+                typ = MED_ISOTROPIC if t == "isotropic_scattering" else MED_NON_SCATTERING
+                media[m["name"]] = L.orc_add_medium_ref(
+                    self.h, typ, fptr(col), f32(m["absorption_at_distance"]),
+                    f32(m.get("scattering_distance", 1.0)))
+        bsdfs = {b["name"]: b for b in j.get("bsdfs", [])}
+        mats = {}
+        for m in j.get("materials", []):
+            b = bsdfs[m["bsdf"]]
+            alb = np.array(b["albedo"].get("value", [0, 0, 0]), dtype=f32)
+            mats[m["name"]] = L.orc_add_material(self.h, BSDF[b["type"]], fptr(alb),
+                                                 f32(b.get("ior", 1.0)), media.get(m.get("medium"), -1))
+        self._keep = []
+        base = os.path.dirname(self.path)
+        for p in j.get("primitives", []):
+            if p["type"] != "lmf":
+                raise NotImplementedError("oracle scenes use LMF primitives")
+            lmf = read_lmf(os.path.join(base, p["file_path"]))
+            if lmf["vpp"] != 3:
+                raise NotImplementedError("triangle LMF only")
+            pos = np.ascontiguousarray(lmf["positions"], dtype=f32)
+            if "transform" in p:
+                pos = apply_transform(pos, p["transform"])
+            nrm = None if lmf["normals"] is None else np.ascontiguousarray(lmf["normals"], dtype=f32)
+            idx = np.ascontiguousarray(lmf["indices"], dtype=np.uint32)
+            em = None
+            power = f32(0)
+            if "emission" in p:
+                em = np.array(p["emission"]["color"], dtype=f32)
+                power = f32(p["emission"]["radiant_power"])
+            self._keep += [pos, nrm, idx, em]
+            L.orc_add_mesh(self.h, fptr(pos), pos.shape[0], fptr(nrm), uptr(idx), idx.size // 3,
+                           mats[p["material"]], fptr(em), power)
+        L.orc_scene_commit(self.h)
+        self._keep = []
+
+    def __del__(self):
+        try:
+            lib().orc_scene_free(self.h)
+        except Exception:
+            pass
+
+    @property
+    def num_triangles(self) -> int:
+        return int(lib().orc_num_triangles(self.h))
+
+    def intersect(self, rays: np.ndarray, use_bvh: bool = True, counters: bool = False,
+                  threads: int = 0):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[0]
+        hits = np.zeros((n, 4), dtype=np.uint32)
+        cnt = np.zeros((n, 2), dtype=np.uint32) if counters else None
+        lib().orc_intersect(self.h, fptr(rays), uptr(hits), n, int(use_bvh), uptr(cnt),
+                            threads or os.cpu_count())
+        return (hits, cnt) if counters else hits
+
+    def render(self, frames: int, first_frame: int = 0, max_depth: int = 1500, rr_depth: int = 3,
+               keying: int = KEY_PIXEL, threads: int = 0, two_films: bool = False):
+        class Opts(C.Structure):
+            _fields_ = [("max_depth", C.c_uint32), ("rr_depth", C.c_uint32),
+                        ("keying", C.c_uint32), ("threads", C.c_uint32)]
+        o = Opts(max_depth, rr_depth, keying, threads or os.cpu_count())
+        n = self.width * self.height
+        rgb_a = np.zeros((self.height, self.width, 3), np.float32)
+        b_a = np.zeros((self.height, self.width), np.uint32)
+        c_a = np.zeros_like(b_a)
+        rgb_b = b_b = c_b = None
+        if two_films:
+            rgb_b, b_b, c_b = np.zeros_like(rgb_a), np.zeros_like(b_a), np.zeros_like(c_a)
+        rc = (C.c_uint64 * 3)()
+        lib().orc_render(self.h, C.byref(o), first_frame, frames, fptr(rgb_a), uptr(b_a), uptr(c_a),
+                         fptr(rgb_b), uptr(b_b), uptr(c_b), rc)
+        del n
+        out = {"rgb": rgb_a, "bounces": b_a, "counts": c_a, "rays": [int(x) for x in rc]}
+        if two_films:
+            out.update({"rgb_b": rgb_b, "bounces_b": b_b, "counts_b": c_b})
+        return out
+
+
+@contextmanager
+def _cwd(path):
+    old = os.getcwd()
+    os.chdir(path)
+    try:
+        yield
+    finally:
+        os.chdir(old)
+
+
+class ReferenceScene:
+    """A scene loaded by the reference's own Scene::LoadSceneFromJSON."""
+
+    def __init__(self, json_path: str):
+        L = ref_lib()
+        if L is None:
+            raise RuntimeError("reference library not built (oracle/build_ref.sh)")
+        path = os.path.abspath(json_path)
+        # the reference looks for scene.schema.json in the working directory
+        with _cwd(REF_DIR):
+            self.h = L.lref_scene_load(path.encode())
+        if not self.h:
+            raise RuntimeError(f"reference failed to load {json_path}")
+        w, h = C.c_uint32(), C.c_uint32()
+        L.lref_scene_size(self.h, C.byref(w), C.byref(h))
+        self.width, self.height = w.value, h.value
+
+    def __del__(self):
+        try:
+            ref_lib().lref_scene_free(self.h)
+        except Exception:
+            pass
+
+    def render(self, frames: int, first_frame: int = 0, max_depth: int = 1500, rr_depth: int = 3):
+        """Returns films A and B and wall seconds; frame 0 lands in B."""
+        shp = (self.height, self.width)
+        rgb_a, rgb_b = np.zeros(shp + (3,), np.float32), np.zeros(shp + (3,), np.float32)
+        b_a, b_b = np.zeros(shp, np.uint32), np.zeros(shp, np.uint32)
+        c_a, c_b = np.zeros(shp, np.uint32), np.zeros(shp, np.uint32)
+        rays = C.c_ulonglong()
+        secs = ref_lib().lref_render(self.h, first_frame, frames, max_depth, rr_depth, fptr(rgb_a),
+                                     uptr(b_a), uptr(c_a), fptr(rgb_b), uptr(b_b), uptr(c_b),
+                                     C.byref(rays))
+        return {"rgb": rgb_a, "bounces": b_a, "counts": c_a, "rgb_b": rgb_b, "bounces_b": b_b,
+                "counts_b": c_b, "seconds": secs, "rays": rays.value}
