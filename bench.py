@@ -1,0 +1,345 @@
+"""Benchmark: Lantern's path-tracing loop on one GB300 (configs: BASELINE workload names).
+
+Default workload ("icosphere-1.3M"): the displaced icosphere scene --
+1,310,720 + 4 triangles, Lambert / mirror / dielectric meshes, 1024x1024,
+64 samples per pixel, max depth 10, roulette after bounce 3. One step = one
+complete render of that frame (67,108,864 path samples) through
+Integrator.RenderFrame (lt_render on device film buffers).
+
+Reported (one JSON line on rank 0):
+  value        Msamples/s over the K timed steps (device time, CUDA events on
+               the stream lt_render runs on; L2 flushed between steps by
+               writing a 256 MiB buffer outside the timed region)
+  e2e          the same metric through the C ABI with HOST film buffers: the
+               film is copied in, rendered and copied out every step
+  mrays        Mrays/s (path segments + light-sample + BSDF-MIS rays)
+  roofline     trace kernel: algorithmic bytes (32 B ray + 16 B hit + 32 B per
+               child-box test + 40 B per triangle test, node/triangle counts
+               from the oracle's BVH2 on a pixel-subsampled render of the same
+               frame) / trace-kernel device time, against measured HBM GB/s
+  cpu_baseline the reference integrator (oracle/_ref) on the host cores, one
+               frame of the same scene
+--impl reference runs only the reference CPU path (its own arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msamples/s & Mrays/s on 1 GB300 vs host CPU at matched RMSE; adjoint grads/s"
+SCENES = os.path.join(ROOT, "_scenes")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def make_scene(name: str):
+    import lantern_gb300.scenes as S
+    if name == "icosphere-1.3M":
+        sc = S.displaced_icosphere_scene(width=1024, height=1024, spp=64, max_depth=10, rr_depth=3,
+                                         name="bench_icosphere")
+        return sc, {"spp": 64, "max_depth": 10, "rr_depth": 3}
+    if name == "nine-spheres":
+        sc = S.nine_spheres(width=256, height=256, spp=16, max_depth=8, rr_depth=3, name="bench_nine")
+        return sc, {"spp": 16, "max_depth": 8, "rr_depth": 3}
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def bytes_per_ray(scene_path: str, width: int, height: int, max_depth: int, rr_depth: int):
+    """Oracle BVH2 node/triangle counts per ray on a pixel-subsampled 1-spp render."""
+    from oracle import oracle as O
+    import numpy as np
+    orc = O.OracleScene(scene_path)
+    # camera rays + bounce rays: trace the oracle's own path segments on a subsample
+    # of pixels by rendering at the full resolution's camera through a strided grid
+    rng = np.random.default_rng(0)
+    xs = rng.integers(0, width, 4096)
+    ys = rng.integers(0, height, 4096)
+    rays = []
+    import ctypes as C
+    L = O.lib()
+    for x, y in zip(xs, ys):
+        d, o = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        L.orc_camera_ray(orc.h, int(x), int(y), C.c_float(0.0), C.c_float(0.0), O.fptr(d), O.fptr(o))
+        rays.append(np.concatenate([o, [0.0], d, [np.inf]]).astype(np.float32))
+    rays = np.stack(rays)
+    hits, cnt = orc.intersect(rays, counters=True)
+    # secondary rays: cosine-ish directions from the primary hit points
+    hit = hits[:, 3] != 0xFFFFFFFF
+    t = hits[hit, 0].view(np.float32)
+    d = rays[hit, 4:7] / np.linalg.norm(rays[hit, 4:7], axis=1, keepdims=True)
+    p = rays[hit, 0:3] + d * t[:, None]
+    dd = rng.normal(size=p.shape)
+    dd /= np.linalg.norm(dd, axis=1, keepdims=True)
+    dd = np.where((dd * -d).sum(1, keepdims=True) > 0, dd, -dd)
+    sec = np.concatenate([p, np.full((p.shape[0], 1), 0.001), dd, np.full((p.shape[0], 1), np.inf)], 1)
+    _, cnt2 = orc.intersect(sec.astype(np.float32), counters=True)
+    allc = np.concatenate([cnt, cnt2]).astype(np.float64)
+    n_node, n_tri = allc[:, 0].mean(), allc[:, 1].mean()
+    return 48.0 + 32.0 * n_node + 40.0 * n_tri, float(n_node), float(n_tri)
+
+
+def run_reference(args, workload):
+    """The reference CPU integrator (oracle/_ref) on this host's cores."""
+    from oracle import oracle as O
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    try:
+        if not os.path.exists(O.REF_SO):
+            O.build_reference()
+    except RuntimeError as e:
+        print(json.dumps({"impl": "reference", "unavailable": f"reference build failed: {str(e)[:200]}"}))
+        return
+    if not os.path.exists(O.REF_SO):
+        print(json.dumps({"impl": "reference", "unavailable": "reference sources not staged (oracle/_ref/src)"}))
+        return
+    sc, rp = make_scene(workload)
+    path = __import__("lantern_gb300.scenes", fromlist=["x"]).ensure_written(sc, SCENES)
+    ref = O.ReferenceScene(path)
+    frames_per_step = 1
+    for _ in range(args.warmup):
+        ref.render(frames_per_step, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
+    secs, rays = 0.0, 0
+    for k in range(args.steps):
+        r = ref.render(frames_per_step, first_frame=1000 + k, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
+        secs += r["seconds"]
+        rays += r["rays"]
+    samples = sc.width * sc.height * frames_per_step * args.steps
+    v = samples / secs / 1e6
+    cores = int(os.environ.get("LT_REF_THREADS", os.cpu_count()))
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Msamples/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": workload, "width": sc.width, "height": sc.height, "spp_per_step": frames_per_step,
+                       "max_depth": rp["max_depth"], "rr_depth": rp["rr_depth"], "triangles": sc.num_triangles},
+            "mrays": round(rays / secs / 1e6, 4),
+            "cpu_baseline": {"value": round(v, 4), "unit": "Msamples/s", "cores": cores, "kind": "reference",
+                             "sample": f"{args.steps} x {frames_per_step} frame(s) of {sc.width}x{sc.height}"},
+            "e2e": {"value": round(v, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="icosphere-1.3M")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    if args.impl == "reference":
+        run_reference(args, args.workload)
+        return
+
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import lantern_gb300.scenes as S
+    from lantern_gb300.integrator import FrameBuffer, Integrator, Scene, render_host
+
+    sc, rp = make_scene(args.workload)
+    path = S.ensure_written(sc, SCENES) if rank == 0 or world == 1 else None
+    if dist:
+        dist.barrier()
+        path = os.path.join(SCENES, f"{sc.name}.json")
+    scene = Scene(local)
+    scene.LoadSceneFromJSON(path)
+    info = scene.info()
+    fb = FrameBuffer(scene.width, scene.height, f"cuda:{local}")
+    integ = Integrator(scene, fb, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
+    spp = rp["spp"]
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        integ.RenderFrame(spp)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total_ms, trace_ms, shade_ms, connect_ms, rays, launches = 0.0, 0.0, 0.0, 0.0, 0, 0
+    main_rays = 0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        integ.RenderFrame(spp)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        st = integ.stats()
+        trace_ms += st.trace_ms
+        shade_ms += st.shade_ms
+        connect_ms += st.connect_ms
+        rays += st.main_rays + st.light_rays + st.bsdf_rays
+        main_rays += st.main_rays
+        launches += st.kernel_launches
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    samples = scene.width * scene.height * spp * args.steps
+    t_ms = total_ms
+    if dist:
+        tt = torch.tensor([t_ms], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    value = samples * world / (t_ms / 1e3) / 1e6
+    mrays = rays * world / (t_ms / 1e3) / 1e6
+
+    e2e = None
+    if not args.no_e2e:
+        import numpy as np
+        npix = scene.width * scene.height
+        host = {"rgb": np.zeros((scene.height, scene.width, 3), np.float32),
+                "bounces": np.zeros((scene.height, scene.width), np.uint32),
+                "counts": np.zeros((scene.height, scene.width), np.uint32)}
+        host = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in host.items()}
+        render_host(scene.ctx, scene.width, scene.height, spp, 0, rp["max_depth"], rp["rr_depth"], host)
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            render_host(scene.ctx, scene.width, scene.height, spp, 7 + k, rp["max_depth"], rp["rr_depth"], host)
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": round(samples * world / e2e_s / 1e6, 3), "unit": "Msamples/s",
+               "h2d_bytes_per_step": npix * 20, "d2h_bytes_per_step": npix * 20}
+
+    line = None
+    if rank == 0:
+        peak, peak_kind = _peaks()
+        roof = None
+        try:
+            bpr, n_node, n_tri = bytes_per_ray(path, scene.width, scene.height, rp["max_depth"], rp["rr_depth"])
+            achieved = main_rays * bpr / (trace_ms / 1e3) / 1e9
+            roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_trace",
+                    "bytes_per_ray": round(bpr, 1), "node_tests_per_ray": round(n_node, 2),
+                    "tri_tests_per_ray": round(n_tri, 2), "peak_kind": peak_kind,
+                    "trace_share": round(trace_ms / max(total_ms, 1e-9), 3),
+                    "connect_share": round(connect_ms / max(total_ms, 1e-9), 3),
+                    "shade_share": round(shade_ms / max(total_ms, 1e-9), 3)}
+        except Exception as e:  # the oracle is a checker; report its absence
+            roof = {"error": str(e)[:200]}
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(path, rp)
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_ms / args.steps, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded procedural scene, written as Lantern JSON + LMF)",
+                "config": {"workload": args.workload, "width": scene.width, "height": scene.height, "spp": spp,
+                           "max_depth": rp["max_depth"], "rr_depth": rp["rr_depth"],
+                           "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
+                           "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1
+                           else "single GPU"},
+                "mrays": round(mrays, 2), "gpu_launches": launches,
+                "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline(path, rp):
+    """Reference CPU integrator on this host, one frame of the same scene."""
+    from oracle import oracle as O
+    try:
+        if not os.path.exists(O.REF_SO):
+            O.build_reference()
+        if not os.path.exists(O.REF_SO):
+            return None
+        ref = O.ReferenceScene(path)
+        r = ref.render(1, first_frame=99, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
+        n = ref.width * ref.height
+        return {"value": round(n / r["seconds"] / 1e6, 4), "unit": "Msamples/s",
+                "cores": int(os.environ.get("LT_REF_THREADS", os.cpu_count())), "kind": "reference",
+                "sample": f"1 frame (1 spp) of {ref.width}x{ref.height}", "mrays": round(r["rays"] / r["seconds"] / 1e6, 3)}
+    except Exception as e:
+        return {"error": str(e)[:200]}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,187 @@
+/*
+ * lantern_gpu.h -- C ABI of the GB300 path-tracing library (liblantern_gpu.so).
+ *
+ * The library renders Lantern scenes on one GPU with hand-written sm_103a CUDA:
+ * a wavefront integrator (camera rays, closest-hit traversal, shading with
+ * next-event estimation and MIS, light connection, Russian roulette, film
+ * accumulation) over the library's own BVH. It replaces, at the same contract:
+ *
+ *   - Integrator::RenderFrame            source/core/integrator/integrator.{h:24-51,cpp:28-43}
+ *   - Scene::LoadSceneFromJSON           source/core/scene/scene.{h:71,cpp:82-91,154-582}
+ *   - rtcCommitScene / rtcIntersect1     (Embree, called at scene.cpp:86,116-121)
+ *
+ * Plain pointers and sizes only; no exceptions cross this boundary. Every call
+ * returns an lt_status; lt_last_error() gives the message of the last failure
+ * on that context. One host thread drives one context; all GPU work is issued
+ * on the context's stream and lt_render/lt_intersect return once it is queued
+ * (device buffers) or finished (host buffers).
+ */
+#ifndef LANTERN_GPU_H
+#define LANTERN_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LT_ABI_VERSION 1
+
+typedef enum lt_status {
+    LT_OK = 0,
+    LT_ERR_INVALID = 1,     /* bad argument */
+    LT_ERR_CUDA = 2,        /* CUDA runtime error */
+    LT_ERR_OOM = 3,         /* device or host allocation failed */
+    LT_ERR_TIMEOUT = 4,     /* a bounded device-side wait ran out */
+    LT_ERR_IO = 5,          /* file missing or unreadable */
+    LT_ERR_PARSE = 6,       /* malformed scene JSON or LMF */
+    LT_ERR_UNSUPPORTED = 7, /* feature outside this build */
+    LT_ERR_STATE = 8        /* call out of order (e.g. render without a scene) */
+} lt_status;
+
+typedef struct lt_ctx lt_ctx;
+
+/* ---------------------------------------------------------------- context */
+/* Creates a context on CUDA device `device` with its own stream. */
+lt_status lt_ctx_create(int device, lt_ctx **out);
+void lt_ctx_destroy(lt_ctx *ctx);
+/* Message of the last failing call on ctx (or of the last failing
+ * lt_ctx_create on this thread when ctx is NULL). Never NULL. */
+const char *lt_last_error(const lt_ctx *ctx);
+/* Issue all further work on `stream` (a cudaStream_t; NULL is CUDA's legacy
+ * default stream). A new context uses a non-blocking stream of its own, which
+ * lt_get_stream returns before any lt_set_stream call. */
+lt_status lt_set_stream(lt_ctx *ctx, void *stream);
+void *lt_get_stream(const lt_ctx *ctx);
+/* Waits for all work queued on the context's stream. */
+lt_status lt_sync(lt_ctx *ctx);
+int lt_abi_version(void);
+
+/* ---------------------------------------------------------------- scene */
+/* BSDFs of source/core/materials/bsdfs: LambertBSDF, MirrorBSDF,
+ * IdealSpecularDielectric. Albedo is a constant texture. */
+enum { LT_BSDF_LAMBERT = 0, LT_BSDF_MIRROR = 1, LT_BSDF_DIELECTRIC = 2 };
+/* Media of source/core/materials/media (NonScattering, IsotropicScattering),
+ * plus LT_MEDIUM_HG: RGB sigma_s and a Henyey-Greenstein phase (extension). */
+enum { LT_MEDIUM_NON_SCATTERING = 1, LT_MEDIUM_ISOTROPIC = 2, LT_MEDIUM_HG = 3 };
+
+typedef struct lt_material_desc {
+    int32_t bsdf;      /* LT_BSDF_* */
+    float albedo[3];
+    float ior;         /* dielectric only */
+    int32_t medium;    /* index into lt_scene_desc.media, or -1 */
+} lt_material_desc;
+
+typedef struct lt_medium_desc {
+    int32_t type;      /* LT_MEDIUM_* */
+    float sigma_a[3];  /* per unit length */
+    float sigma_s[3];  /* isotropic: all three equal */
+    float g;           /* HG anisotropy; 0 for the reference media */
+} lt_medium_desc;
+
+typedef struct lt_mesh_desc {
+    const float *positions;   /* num_vertices * 3, world space */
+    const float *normals;     /* num_vertices * 3, or NULL */
+    const uint32_t *indices;  /* num_triangles * 3 */
+    uint32_t num_vertices;
+    uint32_t num_triangles;
+    int32_t material;         /* index into lt_scene_desc.materials */
+    int32_t emissive;         /* nonzero: the mesh is an area light */
+    float emission_color[3];  /* AreaLight: radiance = color * power / (pi * area) */
+    float radiant_power;
+} lt_mesh_desc;
+
+typedef struct lt_camera_desc {
+    float phi, theta, radius; /* spherical orbit about target (pinhole_camera.cpp:27-40) */
+    float fov;                /* horizontal field of view, radians */
+    float target[3];
+    uint32_t width, height;
+} lt_camera_desc;
+
+typedef struct lt_scene_desc {
+    lt_camera_desc camera;
+    float background[3];
+    const lt_material_desc *materials;
+    uint32_t num_materials;
+    const lt_medium_desc *media;
+    uint32_t num_media;
+    const lt_mesh_desc *meshes; /* geomID = position in this array */
+    uint32_t num_meshes;
+} lt_scene_desc;
+
+/* Uploads the scene and builds its BVH; replaces any previous scene.
+ * Replaces Scene::ParseJSON's AddMesh/AddLMF + rtcCommitScene
+ * (scene.cpp:451-582, :86): the library computes each light's area, bounding
+ * sphere and radiance the way AddLMF and AreaLight's constructor do. */
+lt_status lt_scene_create(lt_ctx *ctx, const lt_scene_desc *desc);
+
+/* Scene::LoadSceneFromJSON (scene.h:71): reads a Lantern scene JSON and the
+ * LMF files it names (triangle LMF, transform, constant albedo, media,
+ * emission), then lt_scene_create. */
+lt_status lt_scene_load_json(lt_ctx *ctx, const char *path);
+
+typedef struct lt_scene_info {
+    uint32_t width, height;
+    uint32_t num_triangles, num_meshes, num_lights;
+    uint32_t num_bvh_nodes;
+    uint64_t device_bytes;    /* scene + BVH bytes on the device */
+    float build_ms;           /* BVH build time */
+} lt_scene_info;
+lt_status lt_scene_info_get(lt_ctx *ctx, lt_scene_info *out);
+
+/* Per-mesh geometry offsets: first global triangle index of each mesh
+ * (global triangle index = first[geomID] + primID). `first` holds num_meshes. */
+lt_status lt_scene_mesh_offsets(lt_ctx *ctx, uint32_t *first, uint32_t capacity);
+
+/* ---------------------------------------------------------------- film + render */
+typedef struct lt_film {
+    float *rgb;          /* width*height*3: colour sums (FrameBuffer::ColorData) */
+    uint32_t *bounces;   /* width*height: summed path lengths (FrameBuffer::Bounces) */
+    uint32_t *counts;    /* width*height: sample counts (FrameBuffer::ColorSampleCount) */
+    uint32_t width, height;
+    int32_t on_device;   /* 1: device pointers; 0: host memory (copied in and out) */
+} lt_film;
+
+typedef struct lt_render_params {
+    uint32_t spp;          /* samples per pixel in this call (= RenderFrame calls) */
+    uint32_t first_frame;  /* frame number of the first sample (Integrator::m_frameNumber) */
+    uint32_t max_depth;    /* loop bound; the reference's constant is 1500 (integrator.cpp:114) */
+    uint32_t rr_depth;     /* roulette when bounces > rr_depth; the reference's is 3 (:235) */
+} lt_render_params;
+
+/* Integrator::RenderFrame, spp times: adds one sample per pixel per frame to
+ * the film (colour, path length, count), as integrator.cpp:245-249 does. The
+ * sampler of sample (pixel, frame) is PCG32 seeded with MurmurHash3(pixel,
+ * frame) and sequence frame -- the reference's per-tile seeding
+ * (integrator.cpp:84-89) keyed by pixel instead of tile. */
+lt_status lt_render(lt_ctx *ctx, const lt_render_params *params, lt_film *film);
+
+typedef struct lt_render_stats {
+    uint64_t main_rays;      /* closest-hit queries of path segments */
+    uint64_t light_rays;     /* light-sample connection rays (AreaLight::SampleLi) */
+    uint64_t bsdf_rays;      /* BSDF-sample MIS rays (AreaLight::PdfLi) */
+    uint64_t samples;
+    uint32_t iterations;     /* wavefront iterations */
+    uint32_t kernel_launches;
+    float gpu_ms;            /* device time of the last lt_render */
+    float trace_ms;          /* device time in the path-segment trace kernel */
+    float shade_ms;          /* ... in the shade kernel (incl. camera-ray generation) */
+    float connect_ms;        /* ... in the connection trace + resolve kernel */
+} lt_render_stats;
+lt_status lt_render_stats_get(lt_ctx *ctx, lt_render_stats *out);
+
+/* ---------------------------------------------------------------- rays */
+typedef struct lt_ray { float org[3]; float tnear; float dir[3]; float tfar; } lt_ray; /* 32 B */
+typedef struct lt_hit { float t, u, v; uint32_t prim; } lt_hit; /* 16 B; prim = global
+                                                               * triangle index, 0xFFFFFFFF = miss */
+
+/* rtcIntersect1 (Embree, scene.cpp:116-121) for n rays: closest hit with
+ * Embree's Moeller-Trumbore acceptance rule (tnear exclusive, tfar inclusive).
+ * rays/hits are device pointers when on_device, else host memory. */
+lt_status lt_intersect(lt_ctx *ctx, const lt_ray *rays, lt_hit *hits, uint64_t n, int32_t on_device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

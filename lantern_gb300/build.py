@@ -1,0 +1,88 @@
+"""Build liblantern_gpu.so in-tree (lantern_gb300/_build) for sm_103a.
+
+nvcc compiles the kernels with -gencode arch=compute_103a,code=sm_103a and
+-fmad=false (the integrator's arithmetic is spelled out operation by
+operation; the traversal writes its fused multiply-adds explicitly); g++
+compiles the host C++ with -ffp-contract=off for the same reason. Translation
+units are compiled in parallel; the CUDA runtime is linked statically.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liblantern_gpu.so")
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                     "-I" + INCLUDE, "-I" + CSRC]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+             "-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
+
+CU_SOURCES = ["lt_kernels.cu"]
+CPP_SOURCES = ["lt_api.cpp", "lt_scene.cpp", "lt_json.cpp"]
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in CU_SOURCES + CPP_SOURCES]
+
+
+def _headers():
+    return ([os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+            + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")])
+
+
+def up_to_date() -> bool:
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(f) <= t for f in _sources() + _headers() + [__file__])
+
+
+def build(force: bool = False, verbose: bool = False, extra_nvcc=()) -> str:
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    cxx = os.environ.get("CXX", shutil.which("g++") or "g++")
+    jobs = []
+    objs = []
+    for f in CU_SOURCES:
+        o = os.path.join(BUILD, f + ".o")
+        objs.append(o)
+        jobs.append([NVCC] + NVCC_FLAGS + list(extra_nvcc) + ["-c", os.path.join(CSRC, f), "-o", o])
+    for f in CPP_SOURCES:
+        o = os.path.join(BUILD, f + ".o")
+        objs.append(o)
+        jobs.append([cxx] + CXX_FLAGS + ["-c", os.path.join(CSRC, f), "-o", o])
+    procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)) for j in jobs]
+    failed = []
+    for j, p in procs:
+        out, _ = p.communicate()
+        if verbose and out:
+            sys.stdout.write(out)
+        if p.returncode != 0:
+            failed.append((j, out))
+    if failed:
+        msg = "\n".join(" ".join(j) + "\n" + out for j, out in failed)
+        raise RuntimeError("liblantern_gpu build failed:\n" + msg)
+    tmp = LIB + f".{os.getpid()}.tmp"
+    link = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+    r = subprocess.run(link, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                extra_nvcc=["-Xptxas", "-v"] if "--ptxas" in sys.argv else []))

@@ -1,0 +1,421 @@
+// lt_api.cpp -- the C ABI declared in include/lantern_gpu.h.
+//
+// A context owns a CUDA stream, the device copy of one scene (triangles, BVH,
+// shading tables) and the wavefront buffers, which are sized once and reused.
+// lt_render queues the wavefront: an initial camera-ray launch, then batches of
+// (trace, shade, connect) iterations, reading the queue length back once per
+// batch until no path is left.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lantern_gpu.h"
+#include "lt_device.h"
+#include "lt_scene.h"
+
+using namespace lt;
+
+struct lt_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string error;
+    LaunchShape shape;
+
+    // scene
+    bool has_scene = false;
+    HostScene host;
+    DevScene dev{};
+    std::vector<void *> scene_allocs;
+    uint64_t scene_bytes = 0;
+
+    // wavefront
+    Wavefront wave;
+    WaveCounters *counters_host = nullptr;  // pinned
+
+    // scratch for host-memory calls
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+
+    lt_render_stats stats{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // stage timing: one event before each stage launch and one after the last
+    std::vector<cudaEvent_t> stage_events;
+    std::vector<int> stage_of_event;
+};
+
+static thread_local std::string g_create_error;
+
+static lt_status fail(lt_ctx *c, lt_status st, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->error = buf;
+    else g_create_error = buf;
+    return st;
+}
+
+#define CUDA_TRY(c, expr)                                                                           \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(c, e_ == cudaErrorMemoryAllocation ? LT_ERR_OOM : LT_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #expr, cudaGetErrorString(e_), __FILE__, __LINE__);                         \
+    } while (0)
+
+static void free_scene(lt_ctx *c) {
+    for (void *p : c->scene_allocs) cudaFree(p);
+    c->scene_allocs.clear();
+    c->scene_bytes = 0;
+    c->has_scene = false;
+    c->dev = DevScene{};
+}
+
+static void free_wave(lt_ctx *c) {
+    if (c->wave.arena) cudaFree(c->wave.arena);
+    c->wave = Wavefront{};
+}
+
+extern "C" {
+
+int lt_abi_version(void) { return LT_ABI_VERSION; }
+
+lt_status lt_ctx_create(int device, lt_ctx **out) {
+    if (!out) return fail(nullptr, LT_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(nullptr, LT_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= n) return fail(nullptr, LT_ERR_INVALID, "device %d out of range", device);
+    lt_ctx *c = new (std::nothrow) lt_ctx();
+    if (!c) return fail(nullptr, LT_ERR_OOM, "context allocation failed");
+    c->device = device;
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->counters_host, sizeof(WaveCounters));
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e != cudaSuccess) {
+        lt_ctx_destroy(c);
+        return fail(nullptr, LT_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
+    }
+    c->stream = c->own_stream;
+    query_launch_shape(device, &c->shape);
+    *out = c;
+    return LT_OK;
+}
+
+void lt_ctx_destroy(lt_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_scene(c);
+    free_wave(c);
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->counters_host) cudaFreeHost(c->counters_host);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (cudaEvent_t e : c->stage_events) cudaEventDestroy(e);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+const char *lt_last_error(const lt_ctx *c) { return c ? c->error.c_str() : g_create_error.c_str(); }
+
+lt_status lt_set_stream(lt_ctx *c, void *stream) {
+    if (!c) return LT_ERR_INVALID;
+    c->stream = (cudaStream_t)stream;
+    return LT_OK;
+}
+
+void *lt_get_stream(const lt_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+lt_status lt_sync(lt_ctx *c) {
+    if (!c) return LT_ERR_INVALID;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return LT_OK;
+}
+
+}  // extern "C"
+
+template <typename T>
+static lt_status upload(lt_ctx *c, const std::vector<T> &v, const T **dst) {
+    size_t bytes = v.size() * sizeof(T);
+    void *p = nullptr;
+    CUDA_TRY(c, cudaMalloc(&p, bytes ? bytes : 16));
+    c->scene_allocs.push_back(p);
+    c->scene_bytes += bytes;
+    if (bytes) CUDA_TRY(c, cudaMemcpyAsync(p, v.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+    *dst = (const T *)p;
+    return LT_OK;
+}
+
+extern "C" {
+
+lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
+    if (!c || !desc) return fail(c, LT_ERR_INVALID, "NULL argument");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    free_scene(c);
+    std::string err;
+    lt_status st = build_host_scene(desc, &c->host, &err);
+    if (st != LT_OK) return fail(c, st, "%s", err.c_str());
+    build_bvh(&c->host);
+    if (c->host.max_depth >= 64)
+        return fail(c, LT_ERR_UNSUPPORTED, "BVH depth %u exceeds the traversal stack", c->host.max_depth);
+    HostScene &h = c->host;
+    DevScene &d = c->dev;
+    const float *nodes = nullptr, *tris = nullptr;
+    std::vector<float> nodes_f(h.nodes.size() * 16);
+    memcpy(nodes_f.data(), h.nodes.data(), nodes_f.size() * sizeof(float));
+    if ((st = upload(c, nodes_f, &nodes)) != LT_OK) return st;
+    if ((st = upload(c, h.leaf_tris, &tris)) != LT_OK) return st;
+    d.nodes = (const float4 *)nodes;
+    d.tris = (const float4 *)tris;
+    if ((st = upload(c, h.tri_geom, &d.tri_geom)) != LT_OK) return st;
+    if ((st = upload(c, h.tri_vidx, &d.tri_vidx)) != LT_OK) return st;
+    if ((st = upload(c, h.vnormal, &d.vnormal)) != LT_OK) return st;
+    if ((st = upload(c, h.geoms, &d.geoms)) != LT_OK) return st;
+    if ((st = upload(c, h.materials, &d.mats)) != LT_OK) return st;
+    if ((st = upload(c, h.media, &d.meds)) != LT_OK) return st;
+    if ((st = upload(c, h.lights, &d.lights)) != LT_OK) return st;
+    d.num_lights = (uint32_t)h.lights.size();
+    d.num_tris = (uint32_t)h.tri_geom.size();
+    d.background = h.background;
+    d.cam = h.camera;
+    d.filter = h.filter;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->has_scene = true;
+    return LT_OK;
+}
+
+lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) {
+    if (!c || !out) return LT_ERR_INVALID;
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
+    out->width = c->host.camera.width;
+    out->height = c->host.camera.height;
+    out->num_triangles = (uint32_t)c->host.tri_geom.size();
+    out->num_meshes = (uint32_t)c->host.geoms.size();
+    out->num_lights = (uint32_t)c->host.lights.size();
+    out->num_bvh_nodes = (uint32_t)c->host.nodes.size();
+    out->device_bytes = c->scene_bytes;
+    out->build_ms = c->host.build_ms;
+    return LT_OK;
+}
+
+lt_status lt_scene_mesh_offsets(lt_ctx *c, uint32_t *first, uint32_t capacity) {
+    if (!c || !first) return LT_ERR_INVALID;
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
+    if (capacity < c->host.geoms.size()) return fail(c, LT_ERR_INVALID, "capacity below mesh count");
+    for (size_t g = 0; g < c->host.geoms.size(); ++g) first[g] = c->host.geoms[g].first_tri;
+    return LT_OK;
+}
+
+}  // extern "C"
+
+static lt_status ensure_scratch(lt_ctx *c, size_t bytes) {
+    if (c->scratch_bytes >= bytes) return LT_OK;
+    if (c->scratch) cudaFree(c->scratch);
+    c->scratch = nullptr;
+    c->scratch_bytes = 0;
+    CUDA_TRY(c, cudaMalloc(&c->scratch, bytes));
+    c->scratch_bytes = bytes;
+    return LT_OK;
+}
+
+// Carves the wavefront buffers for `cap` path slots out of one allocation.
+static lt_status ensure_wave(lt_ctx *c, uint32_t cap) {
+    if (c->wave.capacity >= cap && c->wave.arena) return LT_OK;
+    free_wave(c);
+    size_t P = cap;
+    size_t bytes = 0;
+    auto take = [&](size_t n) { size_t o = bytes; bytes += (n + 255) & ~(size_t)255; return o; };
+    size_t o_rng = take(8 * P), o_pix = take(4 * P), o_frame = take(4 * P), o_T = take(12 * P),
+           o_col = take(12 * P), o_b = take(4 * P), o_fl = take(4 * P), o_ior = take(4 * P),
+           o_r0 = take(32 * P), o_r1 = take(32 * P), o_q0 = take(4 * P), o_q1 = take(4 * P),
+           o_hit = take(16 * P), o_cray = take(64 * P), o_crec = take(64 * P), o_cnt = take(sizeof(WaveCounters));
+    char *a = nullptr;
+    CUDA_TRY(c, cudaMalloc((void **)&a, bytes));
+    Wavefront &w = c->wave;
+    w.arena = a;
+    w.arena_bytes = bytes;
+    w.capacity = cap;
+    w.p.rng = (uint64_t *)(a + o_rng);
+    w.p.pixel = (uint32_t *)(a + o_pix);
+    w.p.frame = (uint32_t *)(a + o_frame);
+    w.p.T = (float *)(a + o_T);
+    w.p.color = (float *)(a + o_col);
+    w.p.bounces = (uint32_t *)(a + o_b);
+    w.p.flags = (uint32_t *)(a + o_fl);
+    w.p.iori = (float *)(a + o_ior);
+    w.ray[0] = (float4 *)(a + o_r0);
+    w.ray[1] = (float4 *)(a + o_r1);
+    w.queue[0] = (uint32_t *)(a + o_q0);
+    w.queue[1] = (uint32_t *)(a + o_q1);
+    w.hits = (float4 *)(a + o_hit);
+    w.cray = (float4 *)(a + o_cray);
+    w.crec = (float4 *)(a + o_crec);
+    w.counters = (WaveCounters *)(a + o_cnt);
+    return LT_OK;
+}
+
+static uint32_t default_capacity(unsigned long long total) {
+    const unsigned long long kMax = 1ull << 21;  // 2M path slots, ~560 MB
+    return (uint32_t)(total < kMax ? total : kMax);
+}
+
+extern "C" {
+
+lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
+    if (!c || !p || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "lt_render without a scene");
+    const uint32_t W = c->host.camera.width, H = c->host.camera.height;
+    if (film->width != W || film->height != H)
+        return fail(c, LT_ERR_INVALID, "film is %ux%u, scene camera is %ux%u", film->width, film->height, W, H);
+    if (!film->rgb || !film->bounces || !film->counts) return fail(c, LT_ERR_INVALID, "film buffers missing");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const size_t npix = (size_t)W * H;
+    FilmPtrs f;
+    if (film->on_device) {
+        f.rgb = film->rgb;
+        f.bounces = film->bounces;
+        f.counts = film->counts;
+    } else {
+        lt_status st = ensure_scratch(c, npix * 20 + 512);
+        if (st != LT_OK) return st;
+        char *s = (char *)c->scratch;
+        f.rgb = (float *)s;
+        f.bounces = (uint32_t *)(s + ((npix * 12 + 255) & ~(size_t)255));
+        f.counts = f.bounces + npix;
+        CUDA_TRY(c, cudaMemcpyAsync(f.rgb, film->rgb, npix * 12, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(f.bounces, film->bounces, npix * 4, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(f.counts, film->counts, npix * 4, cudaMemcpyHostToDevice, c->stream));
+    }
+    RenderArgs a;
+    a.width = W;
+    a.height = H;
+    a.first_frame = p->first_frame;
+    a.max_depth = p->max_depth;
+    a.rr_depth = p->rr_depth;
+    a.total = (unsigned long long)npix * p->spp;
+    c->stats = lt_render_stats{};
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    if (a.total > 0 && p->max_depth == 0) {
+        CUDA_TRY(c, launch_add_counts(f, (uint32_t)npix, p->spp, c->stream));
+        c->stats.kernel_launches = 1;
+    } else if (a.total > 0) {
+        lt_status st = ensure_wave(c, default_capacity(a.total));
+        if (st != LT_OK) return st;
+        CUDA_TRY(c, cudaMemsetAsync(c->wave.counters, 0, sizeof(WaveCounters), c->stream));
+        CUDA_TRY(c, launch_wave_init(c->dev, c->wave, a, f, c->shape, c->stream));
+        uint32_t launches = 1, iters = 0;
+        size_t nev = 0;
+        c->stage_of_event.clear();
+        int cur = 0;
+        const int kBatch = 4;
+        for (;;) {
+            for (int k = 0; k < kBatch; ++k) {
+                for (int stage = 0; stage < 3; ++stage) {
+                    if (nev == c->stage_events.size()) {
+                        cudaEvent_t e;
+                        CUDA_TRY(c, cudaEventCreate(&e));
+                        c->stage_events.push_back(e);
+                    }
+                    CUDA_TRY(c, cudaEventRecord(c->stage_events[nev++], c->stream));
+                    c->stage_of_event.push_back(stage);
+                    CUDA_TRY(c, launch_wave_stage(stage, c->dev, c->wave, a, f, cur, c->shape, c->stream));
+                }
+                launches += 3;
+                cur ^= 1;
+                ++iters;
+            }
+            CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, c->wave.counters, sizeof(WaveCounters),
+                                        cudaMemcpyDeviceToHost, c->stream));
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            if (c->counters_host->count[cur] == 0) break;
+            if (iters > 4u * (p->max_depth + 8u) * (uint32_t)((a.total + c->wave.capacity - 1) / c->wave.capacity) + 64u)
+                return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
+        }
+        c->stats.main_rays = c->counters_host->main_rays;
+        c->stats.light_rays = c->counters_host->light_rays;
+        c->stats.bsdf_rays = c->counters_host->bsdf_rays;
+        c->stats.iterations = iters;
+        c->stats.kernel_launches = launches;
+        if (nev == c->stage_events.size()) {
+            cudaEvent_t e;
+            CUDA_TRY(c, cudaEventCreate(&e));
+            c->stage_events.push_back(e);
+        }
+        CUDA_TRY(c, cudaEventRecord(c->stage_events[nev], c->stream));
+        CUDA_TRY(c, cudaEventSynchronize(c->stage_events[nev]));
+        float acc[3] = {0, 0, 0};
+        for (size_t i = 0; i < nev; ++i) {
+            float ms = 0.0f;
+            CUDA_TRY(c, cudaEventElapsedTime(&ms, c->stage_events[i], c->stage_events[i + 1]));
+            acc[c->stage_of_event[i]] += ms;
+        }
+        c->stats.trace_ms = acc[0];
+        c->stats.shade_ms = acc[1];
+        c->stats.connect_ms = acc[2];
+    }
+    c->stats.samples = a.total;
+    CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    if (!film->on_device) {
+        CUDA_TRY(c, cudaMemcpyAsync(film->rgb, f.rgb, npix * 12, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(film->bounces, f.bounces, npix * 4, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(film->counts, f.counts, npix * 4, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    return LT_OK;
+}
+
+lt_status lt_render_stats_get(lt_ctx *c, lt_render_stats *out) {
+    if (!c || !out) return LT_ERR_INVALID;
+    *out = c->stats;
+    float ms = 0.0f;
+    if (cudaEventSynchronize(c->ev1) == cudaSuccess && cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess)
+        out->gpu_ms = ms;
+    return LT_OK;
+}
+
+lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, int32_t on_device) {
+    if (!c || (n && (!rays || !hits))) return fail(c, LT_ERR_INVALID, "NULL argument");
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "lt_intersect without a scene");
+    if (n == 0) return LT_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (on_device) {
+        if (((uintptr_t)rays & 15u) || ((uintptr_t)hits & 15u))
+            return fail(c, LT_ERR_INVALID, "rays and hits must be 16-byte aligned");
+        CUDA_TRY(c, launch_intersect(c->dev, (const float4 *)rays, (float4 *)hits, n, c->shape, c->stream));
+        return LT_OK;
+    }
+    lt_status st = ensure_scratch(c, n * 48);
+    if (st != LT_OK) return st;
+    float4 *dr = (float4 *)c->scratch;
+    float4 *dh = dr + 2 * n;
+    CUDA_TRY(c, cudaMemcpyAsync(dr, rays, n * 32, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, launch_intersect(c->dev, dr, dh, n, c->shape, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(hits, dh, n * 16, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return LT_OK;
+}
+
+lt_status lt_scene_load_json(lt_ctx *c, const char *path) {
+    if (!c || !path) return fail(c, LT_ERR_INVALID, "NULL argument");
+    lt_scene_desc desc;
+    JsonSceneStorage storage;
+    std::string err;
+    lt_status st = load_scene_json(path, &desc, &storage, &err);
+    if (st != LT_OK) return fail(c, st, "%s", err.c_str());
+    return lt_scene_create(c, &desc);
+}
+
+}  // extern "C"

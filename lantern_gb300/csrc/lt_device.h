@@ -1,0 +1,93 @@
+// lt_device.h -- device-side scene and wavefront state shared by the kernels
+// (lt_kernels.cu) and the host driver (lt_api.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lt_math.h"
+#include "lt_scene.h"
+
+namespace lt {
+
+// Scene as the kernels see it; passed by value (lives in the constant bank).
+struct DevScene {
+    const float4 *nodes;        // BvhNode, 4 float4 each
+    const float4 *tris;         // leaf order, 3 float4 each: (v0, prim bits) (e1, 0) (e2, 0)
+    const uint32_t *tri_geom;   // per global triangle
+    const uint32_t *tri_vidx;   // 3 per global triangle
+    const float *vnormal;       // 3 per vertex
+    const GeomInfo *geoms;
+    const MaterialInfo *mats;
+    const MediumInfo *meds;
+    const LightInfo *lights;
+    uint32_t num_lights;
+    uint32_t num_tris;
+    v3 background;
+    Camera cam;
+    TentFilter filter;
+};
+
+// Path state, structure of arrays over `capacity` path slots.
+struct PathState {
+    uint64_t *rng;     // PCG32 state (increment = frame | 1)
+    uint32_t *pixel;
+    uint32_t *frame;
+    float *T;          // throughput, 3 planes of capacity
+    float *color;      // accumulated radiance, 3 planes
+    uint32_t *bounces;
+    uint32_t *flags;   // bits 0-7 sampled lobe, bits 8-23 medium index + 1
+    float *iori;
+};
+
+struct WaveCounters {
+    uint32_t count[2];           // queue lengths (ping-pong)
+    uint32_t ccount;             // connection records this iteration
+    uint32_t error;              // nonzero: a device-side bound was exceeded
+    unsigned long long work_next; // next (pixel, frame) work item
+    unsigned long long main_rays, light_rays, bsdf_rays;
+};
+
+struct Wavefront {
+    uint32_t capacity = 0;
+    PathState p{};
+    float4 *ray[2] = {nullptr, nullptr};    // 2 float4 per entry: (org, tnear) (dir, tfar)
+    uint32_t *queue[2] = {nullptr, nullptr};
+    float4 *hits = nullptr;                 // (t, u, v, prim bits)
+    float4 *cray = nullptr;                 // 2 float4 per record: (org, kind|light) (dir, pixel)
+    float4 *crec = nullptr;                 // 2 float4 per record: (f, bsdf pdf) (throughput, -)
+    WaveCounters *counters = nullptr;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+};
+
+struct FilmPtrs {
+    float *rgb;
+    uint32_t *bounces;
+    uint32_t *counts;
+};
+
+struct RenderArgs {
+    uint32_t width, height;
+    uint32_t first_frame;
+    uint32_t max_depth, rr_depth;
+    unsigned long long total;  // width * height * spp
+};
+
+struct LaunchShape {
+    int sms = 0;
+    int trace_blocks = 0, shade_blocks = 0, connect_blocks = 0, isect_blocks = 0;
+};
+
+// launchers (lt_kernels.cu)
+void query_launch_shape(int device, LaunchShape *out);
+cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
+                             const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st);
+cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
+                             const LaunchShape &ls, cudaStream_t st);
+enum WaveStage { kStageTrace = 0, kStageShade = 1, kStageConnect = 2 };
+cudaError_t launch_wave_stage(int stage, const DevScene &s, const Wavefront &w, const RenderArgs &a,
+                              const FilmPtrs &f, int cur, const LaunchShape &ls, cudaStream_t st);
+
+}  // namespace lt

@@ -1,0 +1,407 @@
+// lt_json.cpp -- Lantern scene JSON + LMF loading for lt_scene_load_json.
+//
+// Follows Scene::ParseJSON (source/core/scene/scene.cpp:215-446) and AddLMF
+// (:502-582) for the parts this library renders: background colour, the
+// orbiting pinhole camera with the reference's defaults, lambert / mirror /
+// ideal_specular_dielectric BSDFs with constant albedo, non_scattering and
+// isotropic_scattering media (plus the henyey_greenstein extension), materials,
+// and "lmf" primitives with an optional row-major 4x4 transform and emission.
+// Numbers are read as double and narrowed to float, as nlohmann's get<float>()
+// does. Unlike the reference, which prints and skips a primitive it cannot
+// load, every problem here is returned as an error.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "lt_scene.h"
+
+namespace lt {
+namespace {
+
+struct Json {
+    enum Type { Null, Bool, Number, String, Array, Object } type = Null;
+    bool b = false;
+    double num = 0.0;
+    std::string str;
+    std::vector<Json> arr;
+    std::vector<std::pair<std::string, Json>> obj;
+
+    const Json *get(const char *key) const {
+        if (type != Object) return nullptr;
+        for (auto &kv : obj)
+            if (kv.first == key) return &kv.second;
+        return nullptr;
+    }
+};
+
+struct Parser {
+    const char *p, *end;
+    std::string err;
+
+    void ws() {
+        while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) ++p;
+    }
+    bool fail(const char *m) {
+        if (err.empty()) err = m;
+        return false;
+    }
+    bool parse_string(std::string &out) {
+        if (p >= end || *p != '"') return fail("expected string");
+        ++p;
+        while (p < end && *p != '"') {
+            char ch = *p++;
+            if (ch == '\\') {
+                if (p >= end) return fail("bad escape");
+                char e = *p++;
+                switch (e) {
+                    case 'n': out += '\n'; break;
+                    case 't': out += '\t'; break;
+                    case 'r': out += '\r'; break;
+                    case 'b': out += '\b'; break;
+                    case 'f': out += '\f'; break;
+                    case 'u': {
+                        if (end - p < 4) return fail("bad unicode escape");
+                        unsigned cp = (unsigned)strtoul(std::string(p, p + 4).c_str(), nullptr, 16);
+                        p += 4;
+                        if (cp < 0x80) out += (char)cp;
+                        else if (cp < 0x800) { out += (char)(0xC0 | (cp >> 6)); out += (char)(0x80 | (cp & 0x3F)); }
+                        else { out += (char)(0xE0 | (cp >> 12)); out += (char)(0x80 | ((cp >> 6) & 0x3F)); out += (char)(0x80 | (cp & 0x3F)); }
+                        break;
+                    }
+                    default: out += e;
+                }
+            } else {
+                out += ch;
+            }
+        }
+        if (p >= end) return fail("unterminated string");
+        ++p;
+        return true;
+    }
+    bool parse(Json &v, int depth = 0) {
+        if (depth > 64) return fail("nesting too deep");
+        ws();
+        if (p >= end) return fail("unexpected end");
+        char c = *p;
+        if (c == '{') {
+            ++p;
+            v.type = Json::Object;
+            ws();
+            if (p < end && *p == '}') { ++p; return true; }
+            for (;;) {
+                ws();
+                std::string k;
+                if (!parse_string(k)) return false;
+                ws();
+                if (p >= end || *p != ':') return fail("expected ':'");
+                ++p;
+                v.obj.emplace_back(k, Json());
+                if (!parse(v.obj.back().second, depth + 1)) return false;
+                ws();
+                if (p < end && *p == ',') { ++p; continue; }
+                if (p < end && *p == '}') { ++p; return true; }
+                return fail("expected ',' or '}'");
+            }
+        }
+        if (c == '[') {
+            ++p;
+            v.type = Json::Array;
+            ws();
+            if (p < end && *p == ']') { ++p; return true; }
+            for (;;) {
+                v.arr.emplace_back();
+                if (!parse(v.arr.back(), depth + 1)) return false;
+                ws();
+                if (p < end && *p == ',') { ++p; continue; }
+                if (p < end && *p == ']') { ++p; return true; }
+                return fail("expected ',' or ']'");
+            }
+        }
+        if (c == '"') {
+            v.type = Json::String;
+            return parse_string(v.str);
+        }
+        if (!strncmp(p, "true", 4) && end - p >= 4) { p += 4; v.type = Json::Bool; v.b = true; return true; }
+        if (!strncmp(p, "false", 5) && end - p >= 5) { p += 5; v.type = Json::Bool; v.b = false; return true; }
+        if (!strncmp(p, "null", 4) && end - p >= 4) { p += 4; v.type = Json::Null; return true; }
+        char *q = nullptr;
+        std::string tok(p, std::min<size_t>((size_t)(end - p), 64));
+        double d = strtod(tok.c_str(), &q);
+        if (q == tok.c_str()) return fail("unexpected character");
+        p += (q - tok.c_str());
+        v.type = Json::Number;
+        v.num = d;
+        return true;
+    }
+};
+
+bool read_file(const std::string &path, std::vector<char> &out) {
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    fseek(f, 0, SEEK_END);
+    long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    out.resize(n > 0 ? (size_t)n : 0);
+    size_t got = n > 0 ? fread(out.data(), 1, (size_t)n, f) : 0;
+    fclose(f);
+    return got == out.size();
+}
+
+bool num(const Json *j, float *out) {
+    if (!j || j->type != Json::Number) return false;
+    *out = (float)j->num;
+    return true;
+}
+
+bool float3(const Json *j, float out[3]) {
+    if (!j || j->type != Json::Array || j->arr.size() != 3) return false;
+    for (int i = 0; i < 3; ++i)
+        if (!num(&j->arr[i], &out[i])) return false;
+    return true;
+}
+
+// ReadLMF (io/lantern_model_file.cpp:33-65) with bounds checks
+lt_status read_lmf(const std::string &path, uint8_t *vpp, std::vector<float> &pos, std::vector<uint32_t> &idx,
+                   std::vector<float> &nrm, std::string *err) {
+    std::vector<char> buf;
+    if (!read_file(path, buf)) {
+        *err = "cannot read LMF file " + path;
+        return LT_ERR_IO;
+    }
+    size_t off = 0;
+    auto take = [&](void *dst, size_t n) -> bool {
+        if (off + n > buf.size()) return false;
+        memcpy(dst, buf.data() + off, n);
+        off += n;
+        return true;
+    };
+    uint32_t magic = 0, flags = 0;
+    uint64_t n = 0;
+    if (!take(&magic, 4) || magic != (uint32_t)('L' | ('M' << 8) | ('F' << 16))) {
+        *err = path + ": not an LMF file";
+        return LT_ERR_PARSE;
+    }
+    if (!take(vpp, 1) || !take(&flags, 4) || !take(&n, 8) || n > (buf.size() / 12)) {
+        *err = path + ": truncated LMF header";
+        return LT_ERR_PARSE;
+    }
+    pos.resize(n * 3);
+    if (!take(pos.data(), n * 12)) { *err = path + ": truncated positions"; return LT_ERR_PARSE; }
+    uint64_t ni = 0;
+    if (!take(&ni, 8) || ni > buf.size() / 4) { *err = path + ": truncated index count"; return LT_ERR_PARSE; }
+    idx.resize(ni);
+    if (!take(idx.data(), ni * 4)) { *err = path + ": truncated indices"; return LT_ERR_PARSE; }
+    nrm.clear();
+    if (flags & 1u) {
+        uint64_t nn = 0;
+        if (!take(&nn, 8) || nn > buf.size() / 4) { *err = path + ": truncated normal count"; return LT_ERR_PARSE; }
+        nrm.resize(nn);
+        if (!take(nrm.data(), nn * 4)) { *err = path + ": truncated normals"; return LT_ERR_PARSE; }
+    }
+    return LT_OK;
+}
+
+}  // namespace
+
+lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorage *st, std::string *err) {
+    std::vector<char> text;
+    if (!read_file(path, text)) {
+        *err = std::string("cannot read scene file ") + path;
+        return LT_ERR_IO;
+    }
+    Parser ps{text.data(), text.data() + text.size(), ""};
+    Json root;
+    if (!ps.parse(root) || root.type != Json::Object) {
+        *err = std::string("scene JSON parse error: ") + (ps.err.empty() ? "not an object" : ps.err);
+        return LT_ERR_PARSE;
+    }
+    std::string dir(path);
+    size_t slash = dir.find_last_of('/');
+    dir = slash == std::string::npos ? std::string(".") : dir.substr(0, slash);
+
+    memset(desc, 0, sizeof *desc);
+    if (const Json *bg = root.get("background_color")) {
+        if (!float3(bg, desc->background)) { *err = "background_color must be 3 numbers"; return LT_ERR_PARSE; }
+    }
+    const Json *cam = root.get("camera");
+    if (!cam || cam->type != Json::Object) {
+        *err = "JSON parse error: \"camera\" is required";
+        return LT_ERR_PARSE;
+    }
+    lt_camera_desc &c = desc->camera;
+    c.phi = 0.785398163397448309616f;   // (float)M_PI_4, scene.cpp:229
+    c.theta = 0.0f;
+    c.radius = 10.0f;
+    c.fov = 0.785398163397448309616f;
+    float w = 0, h = 0;
+    if (!num(cam->get("client_width"), &w) || !num(cam->get("client_height"), &h) || w < 1 || h < 1) {
+        *err = "camera client_width and client_height are required";
+        return LT_ERR_PARSE;
+    }
+    c.width = (uint32_t)cam->get("client_width")->num;
+    c.height = (uint32_t)cam->get("client_height")->num;
+    num(cam->get("phi"), &c.phi);
+    num(cam->get("theta"), &c.theta);
+    num(cam->get("radius"), &c.radius);
+    num(cam->get("fov"), &c.fov);
+    if (const Json *t = cam->get("target")) float3(t, c.target);
+
+    std::map<std::string, int> medium_ix, material_ix;
+    if (const Json *media = root.get("media")) {
+        for (const Json &m : media->arr) {
+            const Json *name = m.get("name"), *type = m.get("type");
+            if (!name || !type) { *err = "medium needs name and type"; return LT_ERR_PARSE; }
+            lt_medium_desc md;
+            memset(&md, 0, sizeof md);
+            if (type->str == "henyey_greenstein") {
+                md.type = LT_MEDIUM_HG;
+                if (!float3(m.get("sigma_a"), md.sigma_a) || !float3(m.get("sigma_s"), md.sigma_s)) {
+                    *err = "henyey_greenstein medium needs sigma_a and sigma_s";
+                    return LT_ERR_PARSE;
+                }
+                num(m.get("g"), &md.g);
+            } else if (type->str == "non_scattering" || type->str == "isotropic_scattering") {
+                // Medium ctor (medium.h:19-23): sigma_a = -log(color) / distance;
+                // isotropic (isotropic_scattering_medium.h:22-25): sigma_s = 1 / distance
+                float col[3], at = 1.0f, sd = 1.0f;
+                if (!float3(m.get("absorption_color"), col) || !num(m.get("absorption_at_distance"), &at)) {
+                    *err = "medium needs absorption_color and absorption_at_distance";
+                    return LT_ERR_PARSE;
+                }
+                for (int k = 0; k < 3; ++k) md.sigma_a[k] = -logf(col[k]) / at;
+                if (type->str == "isotropic_scattering") {
+                    if (!num(m.get("scattering_distance"), &sd)) {
+                        *err = "isotropic_scattering medium needs scattering_distance";
+                        return LT_ERR_PARSE;
+                    }
+                    md.type = LT_MEDIUM_ISOTROPIC;
+                    for (int k = 0; k < 3; ++k) md.sigma_s[k] = 1 / sd;
+                } else {
+                    md.type = LT_MEDIUM_NON_SCATTERING;
+                }
+            } else {
+                continue;  // unknown medium types are ignored, as the reference does
+            }
+            medium_ix[name->str] = (int)st->media.size();
+            st->media.push_back(md);
+        }
+    }
+    std::map<std::string, const Json *> bsdfs;
+    if (const Json *b = root.get("bsdfs"))
+        for (const Json &x : b->arr)
+            if (const Json *n = x.get("name")) bsdfs[n->str] = &x;
+    if (const Json *mats = root.get("materials")) {
+        for (const Json &m : mats->arr) {
+            const Json *name = m.get("name"), *bn = m.get("bsdf");
+            if (!name || !bn) { *err = "material needs name and bsdf"; return LT_ERR_PARSE; }
+            auto it = bsdfs.find(bn->str);
+            if (it == bsdfs.end()) continue;  // scene.cpp:346-349 skips it
+            const Json &b = *it->second;
+            lt_material_desc md;
+            memset(&md, 0, sizeof md);
+            md.medium = -1;
+            const std::string type = b.get("type") ? b.get("type")->str : "";
+            if (type == "lambert") md.bsdf = LT_BSDF_LAMBERT;
+            else if (type == "mirror") md.bsdf = LT_BSDF_MIRROR;
+            else if (type == "ideal_specular_dielectric") {
+                md.bsdf = LT_BSDF_DIELECTRIC;
+                if (!num(b.get("ior"), &md.ior)) { *err = "dielectric needs ior"; return LT_ERR_PARSE; }
+            } else {
+                *err = "unknown bsdf type " + type;
+                return LT_ERR_PARSE;
+            }
+            const Json *alb = b.get("albedo");
+            const Json *at = alb ? alb->get("type") : nullptr;
+            if (!at || at->str != "constant") {
+                *err = "bsdf " + bn->str + ": only constant albedo textures are supported";
+                return LT_ERR_UNSUPPORTED;
+            }
+            if (!float3(alb->get("value"), md.albedo)) { *err = "constant albedo needs value"; return LT_ERR_PARSE; }
+            if (const Json *mn = m.get("medium")) {
+                auto mi = medium_ix.find(mn->str);
+                if (mi == medium_ix.end()) continue;  // scene.cpp:354-357 skips it
+                md.medium = mi->second;
+            }
+            material_ix[name->str] = (int)st->materials.size();
+            st->materials.push_back(md);
+        }
+    }
+    if (const Json *prims = root.get("primitives")) {
+        for (const Json &p : prims->arr) {
+            const Json *type = p.get("type");
+            const std::string pname = p.get("name") ? p.get("name")->str : "";
+            if (!type || type->str != "lmf") {
+                *err = "primitive " + pname + ": only lmf primitives are supported";
+                return LT_ERR_UNSUPPORTED;
+            }
+            const Json *fp = p.get("file_path");
+            if (!fp) { *err = "lmf primitive needs file_path"; return LT_ERR_PARSE; }
+            std::string file = fp->str;
+            if (file.empty() || file[0] != '/') file = dir + "/" + file;
+            uint8_t vpp = 0;
+            std::vector<float> pos, nrm;
+            std::vector<uint32_t> idx;
+            lt_status rs = read_lmf(file, &vpp, pos, idx, nrm, err);
+            if (rs != LT_OK) return rs;
+            if (vpp != 3) {
+                *err = file + ": only triangle LMF files are supported";
+                return LT_ERR_UNSUPPORTED;
+            }
+            const size_t nv = pos.size() / 3;
+            if (const Json *t = p.get("transform")) {
+                if (t->type != Json::Array || t->arr.size() != 16) { *err = "transform needs 16 numbers"; return LT_ERR_PARSE; }
+                float m[16];
+                for (int k = 0; k < 16; ++k)
+                    if (!num(&t->arr[k], &m[k])) { *err = "transform needs 16 numbers"; return LT_ERR_PARSE; }
+                // transform * float3a(p, 1) (scene.cpp:517-522; linearspace4.h:43-47,165)
+                for (size_t v = 0; v < nv; ++v) {
+                    float x = pos[3 * v], y = pos[3 * v + 1], z = pos[3 * v + 2];
+                    for (int r = 0; r < 3; ++r)
+                        pos[3 * v + r] = ((x * m[4 * r] + y * m[4 * r + 1]) + z * m[4 * r + 2]) + 1.0f * m[4 * r + 3];
+                }
+            }
+            const Json *mn = p.get("material");
+            auto mi = mn ? material_ix.find(mn->str) : material_ix.end();
+            if (mi == material_ix.end()) {
+                *err = "primitive " + pname + ": unknown material";
+                return LT_ERR_PARSE;
+            }
+            lt_mesh_desc md;
+            memset(&md, 0, sizeof md);
+            md.num_vertices = (uint32_t)nv;
+            md.num_triangles = (uint32_t)(idx.size() / 3);
+            md.material = mi->second;
+            if (const Json *em = p.get("emission")) {
+                md.emissive = 1;
+                if (!float3(em->get("color"), md.emission_color) || !num(em->get("radiant_power"), &md.radiant_power)) {
+                    *err = "emission needs color and radiant_power";
+                    return LT_ERR_PARSE;
+                }
+            }
+            st->floats.push_back(std::move(pos));
+            md.positions = st->floats.back().data();
+            if (nrm.size() == nv * 3 && nv) {
+                st->floats.push_back(std::move(nrm));
+                md.normals = st->floats.back().data();
+            }
+            st->uints.push_back(std::move(idx));
+            md.indices = st->uints.back().data();
+            st->meshes.push_back(md);
+        }
+    }
+    desc->materials = st->materials.data();
+    desc->num_materials = (uint32_t)st->materials.size();
+    desc->media = st->media.data();
+    desc->num_media = (uint32_t)st->media.size();
+    desc->meshes = st->meshes.data();
+    desc->num_meshes = (uint32_t)st->meshes.size();
+    return LT_OK;
+}
+
+}  // namespace lt

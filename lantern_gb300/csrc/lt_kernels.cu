@@ -1,0 +1,625 @@
+// lt_kernels.cu -- sm_103a kernels of the wavefront path tracer.
+//
+// Stages per wavefront iteration (one path segment for every live path):
+//   trace    closest hit of every queued path ray                 (rtcIntersect1, scene.cpp:116-121)
+//   shade    one bounce of RenderPixel (integrator.cpp:116-243): background, medium
+//            free flight, emission, light choice, BSDF sampling, roulette;
+//            emits up to two connection rays; finished paths are added to the
+//            film and their slot starts the next (pixel, frame) sample
+//   connect  closest hit of every connection ray, then the area-light pdf and
+//            MIS weight of SampleLi/PdfLi (area_light.cpp:18-110) and the film add
+//
+// Queues are compacted with warp ballots (one atomic per warp). Every random
+// number is drawn in shade, in the reference's order, so that a path's
+// decisions do not depend on when its connection rays are traced.
+#include <cuda_runtime.h>
+
+#include "lt_device.h"
+
+namespace lt {
+
+namespace {
+
+constexpr int kStack = 64;
+constexpr uint32_t kLobeNull = 0, kLobeSRefl = 1, kLobeSTrans = 2, kLobeDiffuse = 4, kLobeSpecular = 3;
+constexpr uint32_t kConnectBsdf = 0x80000000u;
+
+__device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
+
+__device__ __forceinline__ float safe_inv(float d) {
+    return 1.0f / (fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
+}
+
+// Embree's dot for the triangle test: x*x + (y*y + z*z)
+__device__ __forceinline__ float edot(v3 a, v3 b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+
+__device__ __forceinline__ float xorsign(float a, uint32_t s) { return __uint_as_float(__float_as_uint(a) ^ s); }
+
+struct Hit {
+    float t, u, v;
+    uint32_t prim;
+};
+
+// Moeller-Trumbore with Embree 3.5's acceptance rule
+// (kernels/geometry/triangle_intersector_moeller.h:75-112): Ng = cross(e2, e1),
+// |den| * tnear < T <= |den| * tfar; t, u, v by exact division.
+__device__ __forceinline__ void tri_test(const float4 *tri, v3 O, v3 D, float tnear, Hit &h) {
+    float4 a = ldg4(tri), b = ldg4(tri + 1), c = ldg4(tri + 2);
+    v3 v0 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
+    v3 Ng = cross(e2, e1);
+    v3 C = v0 - O;
+    v3 R = cross(C, D);
+    float den = edot(Ng, D);
+    float absden = fabsf(den);
+    uint32_t sgn = __float_as_uint(den) & 0x80000000u;
+    float U = xorsign(edot(R, e2), sgn);
+    float V = xorsign(edot(R, e1), sgn);
+    if (den != 0.0f && U >= 0.0f && V >= 0.0f && U + V <= absden) {
+        float T = xorsign(edot(Ng, C), sgn);
+        if (absden * tnear < T && T <= absden * h.t) {
+            h.t = __fdiv_rn(T, absden);
+            h.u = __fdiv_rn(U, absden);
+            h.v = __fdiv_rn(V, absden);
+            h.prim = __float_as_uint(a.w);
+        }
+    }
+}
+
+// Conservative slab test of one child box (far distance widened by 2*gamma(3)).
+__device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz, v3 O,
+                                     v3 inv, float tnear, float tfar, float &tentry) {
+    float tx0 = (lox - O.x) * inv.x, tx1 = (hix - O.x) * inv.x;
+    float ty0 = (loy - O.y) * inv.y, ty1 = (hiy - O.y) * inv.y;
+    float tz0 = (loz - O.z) * inv.z, tz1 = (hiz - O.z) * inv.z;
+    float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tnear));
+    float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar));
+    tentry = tmin;
+    return tmin <= tmax * 1.0000004f;
+}
+
+// Closest hit along O + t*D, t in (tnear, tfar]. Stack-based, nearer child first;
+// leaves are intersected as soon as their box is hit.
+__device__ Hit trace_closest(const DevScene &S, v3 O, v3 D, float tnear, float tfar) {
+    Hit h;
+    h.t = tfar;
+    h.u = h.v = 0.0f;
+    h.prim = kMiss;
+    v3 inv = mk(safe_inv(D.x), safe_inv(D.y), safe_inv(D.z));
+    int stack_node[kStack];
+    float stack_t[kStack];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        const float4 *n = S.nodes + 4 * node;
+        float4 n0 = ldg4(n), n1 = ldg4(n + 1), n2 = ldg4(n + 2), n3 = ldg4(n + 3);
+        float t0, t1;
+        bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, O, inv, tnear, h.t, t0);
+        bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, O, inv, tnear, h.t, t1);
+        int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
+        uint32_t c0 = __float_as_uint(n3.z), c1 = __float_as_uint(n3.w);
+        // leaves first, nearer one first
+        bool l0 = h0 && r0 < 0, l1 = h1 && r1 < 0;
+        if (l0 && l1 && t1 < t0) {
+            for (uint32_t k = 0; k < c1; ++k) tri_test(S.tris + 3 * ((uint32_t)~r1 + k), O, D, tnear, h);
+            for (uint32_t k = 0; k < c0; ++k) tri_test(S.tris + 3 * ((uint32_t)~r0 + k), O, D, tnear, h);
+        } else {
+            if (l0) for (uint32_t k = 0; k < c0; ++k) tri_test(S.tris + 3 * ((uint32_t)~r0 + k), O, D, tnear, h);
+            if (l1) for (uint32_t k = 0; k < c1; ++k) tri_test(S.tris + 3 * ((uint32_t)~r1 + k), O, D, tnear, h);
+        }
+        bool i0 = h0 && r0 >= 0 && t0 <= h.t * 1.0000004f;
+        bool i1 = h1 && r1 >= 0 && t1 <= h.t * 1.0000004f;
+        if (i0 && i1) {
+            int nearer = r0, farther = r1;
+            float tf = t1;
+            if (t1 < t0) { nearer = r1; farther = r0; tf = t0; }
+            if (sp < kStack) { stack_node[sp] = farther; stack_t[sp] = tf; ++sp; }
+            node = nearer;
+            continue;
+        }
+        if (i0) { node = r0; continue; }
+        if (i1) { node = r1; continue; }
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= h.t * 1.0000004f) { node = stack_node[sp]; found = true; break; }
+        }
+        if (!found) break;
+    }
+    return h;
+}
+
+__device__ __forceinline__ v3 interp_normal(const DevScene &S, uint32_t prim, float u, float v) {
+    uint32_t i0 = __ldg(S.tri_vidx + 3 * prim), i1 = __ldg(S.tri_vidx + 3 * prim + 1),
+             i2 = __ldg(S.tri_vidx + 3 * prim + 2);
+    v3 n0 = mk(__ldg(S.vnormal + 3 * i0), __ldg(S.vnormal + 3 * i0 + 1), __ldg(S.vnormal + 3 * i0 + 2));
+    v3 n1 = mk(__ldg(S.vnormal + 3 * i1), __ldg(S.vnormal + 3 * i1 + 1), __ldg(S.vnormal + 3 * i1 + 2));
+    v3 n2 = mk(__ldg(S.vnormal + 3 * i2), __ldg(S.vnormal + 3 * i2 + 1), __ldg(S.vnormal + 3 * i2 + 2));
+    float w = 1.0f - u - v;
+    return (n0 * w + n1 * u) + n2 * v;
+}
+
+// warp-aggregated slot reservation: returns this lane's index (valid if pred)
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t *counter, bool pred) {
+    unsigned mask = __ballot_sync(0xFFFFFFFFu, pred);
+    uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0;
+    int leader = mask ? __ffs(mask) - 1 : 0;
+    if (mask && lane == (uint32_t)leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ unsigned long long warp_reserve64(unsigned long long *counter, bool pred) {
+    unsigned mask = __ballot_sync(0xFFFFFFFFu, pred);
+    uint32_t lane = threadIdx.x & 31u;
+    unsigned long long base = 0;
+    int leader = mask ? __ffs(mask) - 1 : 0;
+    if (mask && lane == (uint32_t)leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+struct Path {
+    Pcg rng;
+    uint32_t pixel, frame;
+    v3 T, color;
+    uint32_t bounces, lobe;
+    int medium;
+    float iori;
+};
+
+// Start sample `item`: PinholeCamera::CalculateRayFromPixel (pinhole_camera.cpp:88-113)
+// with the sampler of (pixel, frame).
+__device__ __forceinline__ void start_path(const DevScene &S, const RenderArgs &a, unsigned long long item, Path &p,
+                                           v3 &org, v3 &dir, float &tnear) {
+    uint32_t npix = a.width * a.height;
+    p.frame = a.first_frame + (uint32_t)(item / npix);
+    p.pixel = (uint32_t)(item % npix);
+    uint32_t x = p.pixel % a.width, y = p.pixel / a.width;
+    p.rng = sampler_for(p.pixel, p.frame);
+    float u = tent_sample(S.filter, p.rng.next_float());
+    float v = tent_sample(S.filter, p.rng.next_float());
+    dir = camera_dir(S.cam, x, y, u, v);
+    org = S.cam.origin;
+    tnear = 0.0f;
+    p.T = mk(1.0f, 1.0f, 1.0f);
+    p.color = mk(0.0f, 0.0f, 0.0f);
+    p.bounces = 0;
+    p.lobe = kLobeNull;
+    p.medium = -1;
+    p.iori = 1.0f;
+}
+
+__device__ __forceinline__ void store_path(const PathState &ps, uint32_t cap, uint32_t slot, const Path &p) {
+    ps.rng[slot] = p.rng.state;
+    ps.pixel[slot] = p.pixel;
+    ps.frame[slot] = p.frame;
+    ps.T[slot] = p.T.x; ps.T[cap + slot] = p.T.y; ps.T[2 * cap + slot] = p.T.z;
+    ps.color[slot] = p.color.x; ps.color[cap + slot] = p.color.y; ps.color[2 * cap + slot] = p.color.z;
+    ps.bounces[slot] = p.bounces;
+    ps.flags[slot] = p.lobe | ((uint32_t)(p.medium + 1) << 8);
+    ps.iori[slot] = p.iori;
+}
+
+__device__ __forceinline__ void load_path(const PathState &ps, uint32_t cap, uint32_t slot, Path &p) {
+    p.rng.state = ps.rng[slot];
+    p.pixel = ps.pixel[slot];
+    p.frame = ps.frame[slot];
+    p.rng.inc = (uint64_t)p.frame | 1u;
+    p.T = mk(ps.T[slot], ps.T[cap + slot], ps.T[2 * cap + slot]);
+    p.color = mk(ps.color[slot], ps.color[cap + slot], ps.color[2 * cap + slot]);
+    p.bounces = ps.bounces[slot];
+    uint32_t fl = ps.flags[slot];
+    p.lobe = fl & 0xFFu;
+    p.medium = (int)((fl >> 8) & 0xFFFFu) - 1;
+    p.iori = ps.iori[slot];
+}
+
+__device__ __forceinline__ void write_ray(float4 *rays, uint32_t i, v3 o, float tnear, v3 d) {
+    rays[2 * i] = make_float4(o.x, o.y, o.z, tnear);
+    rays[2 * i + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+}
+
+// SurfaceInteraction (integrator/surface_interaction.h:14-30)
+struct Inter {
+    v3 P, N, wi, wo;
+    uint32_t lobe;
+    float iori, ioro;
+};
+
+// BSDF Sample (lambert_bsdf.h:34-37, mirror_bsdf.h:31-34, ideal_specular_dielectric.h:35-64)
+__device__ __forceinline__ void bsdf_sample(const MaterialInfo &m, Inter &it, Pcg &g) {
+    if (m.bsdf == LT_BSDF_LAMBERT) {
+        it.wi = cosine_hemisphere(it.N, g);
+        it.lobe = kLobeDiffuse;
+    } else if (m.bsdf == LT_BSDF_MIRROR) {
+        it.wi = it.N * (2.0f * dot(it.wo, it.N)) - it.wo;
+        it.lobe = kLobeSRefl;
+    } else {
+        float vdn = dot(it.wo, it.N);
+        float ioro = m.ior;
+        if (vdn < 0.0f) {
+            ioro = 1.0f;
+            it.N = -it.N;
+            vdn = -vdn;
+        }
+        float eta = it.iori / ioro;
+        float s2 = eta * eta * (1 - vdn * vdn);
+        float F;
+        if (s2 > 1.0f) {
+            F = 1.0f;
+        } else {
+            float ct = sqrtf(1.0f - s2);
+            float rperp = (it.iori * vdn - ioro * ct) / (it.iori * vdn + ioro * ct);
+            float rpar = (ioro * vdn - it.iori * ct) / (ioro * vdn + it.iori * ct);
+            F = 0.5f * (rperp * rperp + rpar * rpar);
+        }
+        float rnd = g.next_float();
+        if (rnd <= F) {
+            it.wi = it.N * (2.0f * dot(it.wo, it.N)) - it.wo;
+            it.lobe = kLobeSRefl;
+            it.ioro = it.iori;
+        } else {
+            it.wi = it.N * (eta * vdn - sqrtf(1.0f - s2)) - it.wo * eta;
+            it.lobe = kLobeSTrans;
+            it.ioro = ioro;
+        }
+    }
+}
+
+__device__ __forceinline__ v3 bsdf_eval(const MaterialInfo &m, const Inter &it) {
+    v3 alb = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
+    if (m.bsdf == LT_BSDF_LAMBERT) return (alb * kInvPi) * dot(it.wi, it.N);
+    return alb;
+}
+
+__device__ __forceinline__ float bsdf_pdf(const MaterialInfo &m, const Inter &it) {
+    if (m.bsdf == LT_BSDF_LAMBERT) return dot(it.wi, it.N) * kInvPi;
+    return 1.0f;
+}
+
+__device__ __forceinline__ void film_add(const FilmPtrs &f, uint32_t pixel, v3 c) {
+    if (c.x != 0.0f) atomicAdd(f.rgb + 3 * (size_t)pixel, c.x);
+    if (c.y != 0.0f) atomicAdd(f.rgb + 3 * (size_t)pixel + 1, c.y);
+    if (c.z != 0.0f) atomicAdd(f.rgb + 3 * (size_t)pixel + 2, c.z);
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void __launch_bounds__(128) k_intersect(DevScene S, const float4 *__restrict__ rays,
+                                                   float4 *__restrict__ hits, unsigned long long n) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        float4 a = ldg4(rays + 2 * i), b = ldg4(rays + 2 * i + 1);
+        Hit h = trace_closest(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
+        hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+    }
+}
+
+// Fill up to `capacity` slots with camera rays of the first work items.
+__global__ void __launch_bounds__(128) k_raygen(DevScene S, Wavefront W, RenderArgs A) {
+    unsigned long long first = A.total < W.capacity ? A.total : W.capacity;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < first; i += gridDim.x * blockDim.x) {
+        Path p;
+        v3 o, d;
+        float tn;
+        start_path(S, A, i, p, o, d, tn);
+        store_path(W.p, W.capacity, i, p);
+        W.queue[0][i] = i;
+        write_ray(W.ray[0], i, o, tn, d);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counters->count[0] = (uint32_t)first;
+        W.counters->count[1] = 0;
+        W.counters->ccount = 0;
+        W.counters->work_next = first;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_trace(DevScene S, Wavefront W, int cur) {
+    uint32_t n = W.counters->count[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counters->count[cur ^ 1] = 0;
+        W.counters->ccount = 0;
+        W.counters->main_rays += n;
+    }
+    const float4 *rays = W.ray[cur];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 a = ldg4(rays + 2 * i), b = ldg4(rays + 2 * i + 1);
+        Hit h = trace_closest(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
+        W.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+    }
+}
+
+// One iteration of the bounce loop of Integrator::RenderPixel (integrator.cpp:115-243).
+__global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderArgs A, FilmPtrs F, int cur) {
+    const uint32_t n = W.counters->count[cur];
+    const uint32_t cap = W.capacity;
+    const int nxt = cur ^ 1;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t q = base + threadIdx.x;
+        bool active = q < n;
+        uint32_t slot = 0;
+        Path p;
+        bool done = false, push = false;
+        v3 norg = mk(0, 0, 0), ndir = mk(0, 0, 0);
+        float ntnear = 0.0f;
+        // connection records (light sample, BSDF-MIS sample)
+        bool emit_l = false, emit_b = false;
+        v3 l_dir = mk(0, 0, 0), b_dir = mk(0, 0, 0), l_f = mk(0, 0, 0), b_f = mk(0, 0, 0), conn_org = mk(0, 0, 0);
+        float l_pdf = 0.0f, b_pdf = 0.0f;
+        uint32_t conn_light = 0;
+        v3 conn_T = mk(0, 0, 0);
+        if (active) {
+            slot = W.queue[cur][q];
+            load_path(W.p, cap, slot, p);
+            float4 hv = W.hits[q];
+            float4 r0 = W.ray[cur][2 * q], r1 = W.ray[cur][2 * q + 1];
+            uint32_t prim = __float_as_uint(hv.w);
+            float t = hv.x;
+            if (prim == kMiss) {
+                p.color = p.color + p.T * S.background;
+                done = true;
+            } else {
+                v3 origin = mk(r0.x, r0.y, r0.z);
+                v3 direction = normalize(mk(r1.x, r1.y, r1.z));
+                bool hit_surface = true;
+                if (p.medium >= 0) {
+                    const MediumInfo M = S.meds[p.medium];
+                    float dist;
+                    if (M.type == LT_MEDIUM_NON_SCATTERING) {
+                        // non_scattering_medium.h:20-39
+                        dist = t;
+                        v3 tr = mk(expf(-M.sigma_a[0] * dist), expf(-M.sigma_a[1] * dist), expf(-M.sigma_a[2] * dist));
+                        p.T = (p.T * 1.0f) * tr;
+                    } else if (M.type == LT_MEDIUM_ISOTROPIC) {
+                        // isotropic_scattering_medium.h:31-51
+                        dist = -logf(p.rng.next_float()) / M.sigma_s[0];
+                        if (dist >= t) dist = t;
+                        v3 tr = mk(expf(-M.sigma_a[0] * dist), expf(-M.sigma_a[1] * dist), expf(-M.sigma_a[2] * dist));
+                        p.T = (p.T * 1.0f) * tr;
+                    } else {
+                        // RGB sigma_s (extension): distance from the mean sigma_s,
+                        // weight = transmittance (x sigma_s on scatter) / pdf
+                        float sbar = M.sigma_s_mean;
+                        dist = -logf(p.rng.next_float()) / sbar;
+                        bool scat = dist < t;
+                        if (!scat) dist = t;
+                        v3 w = mk(expf(-(M.sigma_a[0] + M.sigma_s[0] - sbar) * dist),
+                                  expf(-(M.sigma_a[1] + M.sigma_s[1] - sbar) * dist),
+                                  expf(-(M.sigma_a[2] + M.sigma_s[2] - sbar) * dist));
+                        if (scat) w = w * (mk(M.sigma_s[0], M.sigma_s[1], M.sigma_s[2]) / sbar);
+                        p.T = p.T * w;
+                    }
+                    if (dist < t) {
+                        hit_surface = false;
+                        norg = origin + direction * dist;
+                        ndir = M.type == LT_MEDIUM_HG ? hg_sample(p.rng, direction, M.g) : uniform_sphere(p.rng);
+                        ntnear = 0.001f;
+                    }
+                }
+                if (hit_surface) {
+                    const GeomInfo G = S.geoms[__ldg(S.tri_geom + prim)];
+                    const MaterialInfo m = S.mats[G.material];
+                    if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0) {
+                        const LightInfo &L = S.lights[G.light];
+                        p.color = p.color + p.T * mk(L.radiance[0], L.radiance[1], L.radiance[2]);
+                    }
+                    Inter it;
+                    it.P = origin + direction * t;
+                    it.N = G.has_normals ? normalize(interp_normal(S, prim, hv.y, hv.z)) : normalize(mk(0, 0, 0));
+                    it.wo = -direction;
+                    it.ioro = 0.0f;
+                    it.iori = p.iori;
+                    it.lobe = p.lobe;
+                    it.wi = mk(0, 0, 0);
+                    // SampleOneLight (integrator.cpp:252-271), interaction by value
+                    uint32_t nl = S.num_lights;
+                    if (!(nl == 0 || (nl == 1 && G.light >= 0))) {
+                        int li;
+                        int guard = 0;
+                        do {
+                            li = (int)p.rng.next_discrete(nl);
+                        } while (li == G.light && ++guard < 1 << 20);
+                        const LightInfo &L = S.lights[li];
+                        v3 Le = mk(L.radiance[0], L.radiance[1], L.radiance[2]);
+                        Inter c = it;
+                        conn_org = it.P;
+                        conn_light = (uint32_t)li;
+                        conn_T = p.T;
+                        // EstimateDirect (integrator.cpp:273-315)
+                        if (m.bsdf == LT_BSDF_LAMBERT) {
+                            // AreaLight::SampleLi (area_light.cpp:18-36)
+                            float x, y;
+                            sample_disc(p.rng, L.sphere[3], x, y);
+                            v3 cdir = mk(L.sphere[0], L.sphere[1], L.sphere[2]) - c.P;
+                            float dist = length(cdir);
+                            v3 cn = normalize(cdir);
+                            v3 point = rotate_to_world(x, y, dist - L.sphere[3], cn);
+                            v3 ldir = normalize(point);
+                            c.wi = ldir;
+                            if (dot(ldir, c.N) > 0.0f && !is_black(Le)) {
+                                v3 f = bsdf_eval(m, c);
+                                float spdf = bsdf_pdf(m, c);
+                                if (spdf != 0.0f && !is_black(f)) {
+                                    emit_l = true;
+                                    l_dir = ldir;
+                                    l_f = f;
+                                    l_pdf = spdf;
+                                }
+                            }
+                        }
+                        bsdf_sample(m, c, p.rng);
+                        v3 f = bsdf_eval(m, c);
+                        float spdf = bsdf_pdf(m, c);
+                        // AreaLight::PdfLi horizon test (area_light.cpp:76-78)
+                        if (spdf != 0.0f && !is_black(f) && dot(c.wi, c.N) > 0.0f) {
+                            emit_b = true;
+                            b_dir = c.wi;
+                            b_f = f;
+                            b_pdf = spdf;
+                        }
+                    }
+                    // main path BSDF sample (integrator.cpp:199-209)
+                    bsdf_sample(m, it, p.rng);
+                    float pdf = bsdf_pdf(m, it);
+                    p.T = (p.T * bsdf_eval(m, it)) / pdf;
+                    if (it.lobe == kLobeSTrans) {
+                        it.iori = it.ioro;
+                        p.medium = m.medium;
+                    }
+                    p.iori = it.iori;
+                    p.lobe = it.lobe;
+                    norg = it.P;
+                    ndir = it.wi;
+                    ntnear = 0.001f;
+                }
+                // Russian roulette (integrator.cpp:235-242)
+                if (p.bounces > A.rr_depth) {
+                    float pr = fmaxf(p.T.x, fmaxf(p.T.y, p.T.z));
+                    if (p.rng.next_float() > pr) done = true;
+                    else p.T = p.T * (1 / pr);
+                }
+            }
+            if (!done) {
+                p.bounces++;
+                if (p.bounces >= A.max_depth) done = true;
+                else push = true;
+            }
+        }
+        // connection records
+        {
+            uint32_t idx = warp_reserve(&W.counters->ccount, emit_l);
+            if (emit_l) {
+                W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light));
+                W.cray[2 * idx + 1] = make_float4(l_dir.x, l_dir.y, l_dir.z, __uint_as_float(p.pixel));
+                W.crec[2 * idx] = make_float4(l_f.x, l_f.y, l_f.z, l_pdf);
+                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, 0.0f);
+            }
+            idx = warp_reserve(&W.counters->ccount, emit_b);
+            if (emit_b) {
+                W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z,
+                                              __uint_as_float(conn_light | kConnectBsdf));
+                W.cray[2 * idx + 1] = make_float4(b_dir.x, b_dir.y, b_dir.z, __uint_as_float(p.pixel));
+                W.crec[2 * idx] = make_float4(b_f.x, b_f.y, b_f.z, b_pdf);
+                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, 0.0f);
+            }
+        }
+        // finished paths: film write (integrator.cpp:245-249), then the slot takes
+        // the next work item
+        bool regen = false;
+        if (done) {
+            film_add(F, p.pixel, p.color);
+            atomicAdd(F.bounces + p.pixel, p.bounces);
+            atomicAdd(F.counts + p.pixel, 1u);
+        }
+        unsigned long long item = warp_reserve64(&W.counters->work_next, done);
+        if (done && item < A.total) {
+            start_path(S, A, item, p, norg, ndir, ntnear);
+            regen = true;
+        }
+        bool enqueue = push || regen;
+        uint32_t qi = warp_reserve(&W.counters->count[nxt], enqueue);
+        if (enqueue) {
+            W.queue[nxt][qi] = slot;
+            write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
+        }
+        if (active) store_path(W.p, cap, slot, p);
+    }
+}
+
+// Trace connection rays and add their MIS-weighted contributions
+// (EstimateDirect, integrator.cpp:281-312; SampleLi/PdfLi pdf, area_light.cpp:64-67,105-109).
+__global__ void __launch_bounds__(128) k_connect(DevScene S, Wavefront W, FilmPtrs F) {
+    const uint32_t n = W.counters->ccount;
+    uint32_t n_all = 0, n_bsdf = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 a = ldg4(W.cray + 2 * i), b = ldg4(W.cray + 2 * i + 1);
+        v3 org = mk(a.x, a.y, a.z), dir = mk(b.x, b.y, b.z);
+        uint32_t kl = __float_as_uint(a.w);
+        uint32_t pixel = __float_as_uint(b.w);
+        bool is_bsdf = (kl & kConnectBsdf) != 0;
+        n_all++;
+        n_bsdf += is_bsdf;
+        const LightInfo &L = S.lights[kl & ~kConnectBsdf];
+        Hit h = trace_closest(S, org, dir, 0.001f, __int_as_float(0x7f800000));
+        if (h.prim == kMiss || __ldg(S.tri_geom + h.prim) != (uint32_t)L.geom) continue;
+        v3 ip = org + normalize(dir) * h.t;
+        v3 dd = ip - org;
+        float d2 = dot(dd, dd);
+        v3 nrm = normalize(interp_normal(S, h.prim, h.u, h.v));
+        float cosl = is_bsdf ? dot(nrm, dir) : dot(nrm, -dir);
+        float lpdf = d2 / (fabsf(cosl) * L.area);
+        if (lpdf == 0.0f) continue;
+        float4 r0 = ldg4(W.crec + 2 * i), r1 = ldg4(W.crec + 2 * i + 1);
+        v3 f = mk(r0.x, r0.y, r0.z);
+        float spdf = r0.w;
+        v3 Le = mk(L.radiance[0], L.radiance[1], L.radiance[2]);
+        v3 c;
+        if (!is_bsdf) c = ((f * Le) * power_heuristic(lpdf, spdf)) / lpdf;
+        else c = ((f * Le) * power_heuristic(spdf, lpdf)) / spdf;
+        v3 T = mk(r1.x, r1.y, r1.z);
+        film_add(F, pixel, T * (c * (float)S.num_lights));
+    }
+    // tallies of connection rays by kind, one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) {
+        n_all += __shfl_xor_sync(0xFFFFFFFFu, n_all, o);
+        n_bsdf += __shfl_xor_sync(0xFFFFFFFFu, n_bsdf, o);
+    }
+    if ((threadIdx.x & 31u) == 0 && n_all) {
+        atomicAdd(&W.counters->bsdf_rays, (unsigned long long)n_bsdf);
+        atomicAdd(&W.counters->light_rays, (unsigned long long)(n_all - n_bsdf));
+    }
+}
+
+// counts += spp for every pixel (render with max_depth 0: the bounce loop never runs)
+__global__ void k_add_counts(FilmPtrs F, uint32_t npix, uint32_t spp) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x)
+        F.counts[i] += spp;
+}
+
+}  // namespace
+
+void query_launch_shape(int device, LaunchShape *out) {
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, device);
+    out->sms = prop.multiProcessorCount;
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
+    out->trace_blocks = out->sms * (b > 0 ? b : 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade, 128, 0);
+    out->shade_blocks = out->sms * (b > 0 ? b : 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_connect, 128, 0);
+    out->connect_blocks = out->sms * (b > 0 ? b : 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_intersect, 128, 0);
+    out->isect_blocks = out->sms * (b > 0 ? b : 1);
+}
+
+cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
+                             const LaunchShape &ls, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    unsigned long long need = (n + 127) / 128;
+    int blocks = (int)(need < (unsigned long long)ls.isect_blocks ? need : ls.isect_blocks);
+    k_intersect<<<blocks, 128, 0, st>>>(s, rays, hits, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st) {
+    k_add_counts<<<(npix + 255) / 256, 256, 0, st>>>(f, npix, spp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &,
+                             const LaunchShape &ls, cudaStream_t st) {
+    k_raygen<<<ls.shade_blocks, 128, 0, st>>>(s, w, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wave_stage(int stage, const DevScene &s, const Wavefront &w, const RenderArgs &a,
+                              const FilmPtrs &f, int cur, const LaunchShape &ls, cudaStream_t st) {
+    if (stage == kStageTrace) k_trace<<<ls.trace_blocks, 128, 0, st>>>(s, w, cur);
+    else if (stage == kStageShade) k_shade<<<ls.shade_blocks, 128, 0, st>>>(s, w, a, f, cur);
+    else k_connect<<<ls.connect_blocks, 128, 0, st>>>(s, w, f);
+    return cudaGetLastError();
+}
+
+}  // namespace lt

@@ -1,0 +1,191 @@
+"""ctypes binding of liblantern_gpu.so (include/lantern_gpu.h).
+
+The library is built in-tree by :mod:`lantern_gb300.build`. There is no CPU
+fallback: :func:`load` raises when the library cannot be built or loaded, and
+every C-ABI error is raised as :class:`LanternError` with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+LT_OK = 0
+STATUS = {0: "LT_OK", 1: "LT_ERR_INVALID", 2: "LT_ERR_CUDA", 3: "LT_ERR_OOM", 4: "LT_ERR_TIMEOUT",
+          5: "LT_ERR_IO", 6: "LT_ERR_PARSE", 7: "LT_ERR_UNSUPPORTED", 8: "LT_ERR_STATE"}
+BSDF_LAMBERT, BSDF_MIRROR, BSDF_DIELECTRIC = 0, 1, 2
+MEDIUM_NON_SCATTERING, MEDIUM_ISOTROPIC, MEDIUM_HG = 1, 2, 3
+MISS = 0xFFFFFFFF
+
+# exported symbols (include/lantern_gpu.h)
+SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error", "lt_set_stream", "lt_get_stream",
+           "lt_sync",
+           "lt_scene_create", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
+           "lt_render_stats_get", "lt_intersect"]
+
+
+class LanternError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("bsdf", C.c_int32), ("albedo", C.c_float * 3), ("ior", C.c_float), ("medium", C.c_int32)]
+
+
+class MediumDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("sigma_a", C.c_float * 3), ("sigma_s", C.c_float * 3), ("g", C.c_float)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("positions", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+                ("indices", C.POINTER(C.c_uint32)), ("num_vertices", C.c_uint32),
+                ("num_triangles", C.c_uint32), ("material", C.c_int32), ("emissive", C.c_int32),
+                ("emission_color", C.c_float * 3), ("radiant_power", C.c_float)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("phi", C.c_float), ("theta", C.c_float), ("radius", C.c_float), ("fov", C.c_float),
+                ("target", C.c_float * 3), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("camera", CameraDesc), ("background", C.c_float * 3),
+                ("materials", C.POINTER(MaterialDesc)), ("num_materials", C.c_uint32),
+                ("media", C.POINTER(MediumDesc)), ("num_media", C.c_uint32),
+                ("meshes", C.POINTER(MeshDesc)), ("num_meshes", C.c_uint32)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("num_triangles", C.c_uint32),
+                ("num_meshes", C.c_uint32), ("num_lights", C.c_uint32), ("num_bvh_nodes", C.c_uint32),
+                ("device_bytes", C.c_uint64), ("build_ms", C.c_float)]
+
+
+class Film(C.Structure):
+    _fields_ = [("rgb", C.c_void_p), ("bounces", C.c_void_p), ("counts", C.c_void_p),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("on_device", C.c_int32)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("first_frame", C.c_uint32), ("max_depth", C.c_uint32),
+                ("rr_depth", C.c_uint32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("main_rays", C.c_uint64), ("light_rays", C.c_uint64), ("bsdf_rays", C.c_uint64),
+                ("samples", C.c_uint64), ("iterations", C.c_uint32), ("kernel_launches", C.c_uint32),
+                ("gpu_ms", C.c_float), ("trace_ms", C.c_float), ("shade_ms", C.c_float),
+                ("connect_ms", C.c_float)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(build_if_needed: bool = True) -> C.CDLL:
+    """Load liblantern_gpu.so, building it first if it is missing or stale."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_needed and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(path):
+            raise LanternError(2, f"{path} is not built")
+        L = C.CDLL(path)
+        p = C.c_void_p
+        L.lt_abi_version.restype = C.c_int
+        L.lt_ctx_create.argtypes = [C.c_int, C.POINTER(p)]
+        L.lt_ctx_destroy.argtypes = [p]
+        L.lt_ctx_destroy.restype = None
+        L.lt_last_error.argtypes = [p]
+        L.lt_last_error.restype = C.c_char_p
+        L.lt_set_stream.argtypes = [p, p]
+        L.lt_get_stream.argtypes = [p]
+        L.lt_get_stream.restype = p
+        L.lt_sync.argtypes = [p]
+        L.lt_scene_create.argtypes = [p, C.POINTER(SceneDesc)]
+        L.lt_scene_load_json.argtypes = [p, C.c_char_p]
+        L.lt_scene_info_get.argtypes = [p, C.POINTER(SceneInfo)]
+        L.lt_scene_mesh_offsets.argtypes = [p, C.POINTER(C.c_uint32), C.c_uint32]
+        L.lt_render.argtypes = [p, C.POINTER(RenderParams), C.POINTER(Film)]
+        L.lt_render_stats_get.argtypes = [p, C.POINTER(RenderStats)]
+        L.lt_intersect.argtypes = [p, p, p, C.c_uint64, C.c_int32]
+        _lib = L
+        return L
+
+
+def check(L, ctx, status: int) -> None:
+    if status != LT_OK:
+        raise LanternError(status, L.lt_last_error(ctx).decode(errors="replace"))
+
+
+class Context:
+    """One lt_ctx: a CUDA device, its stream, one scene and the wavefront buffers."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = C.c_void_p()
+        st = self.L.lt_ctx_create(device, C.byref(h))
+        if st != LT_OK:
+            raise LanternError(st, self.L.lt_last_error(None).decode(errors="replace"))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        check(self.L, self.h, st)
+
+    def set_stream(self, stream_ptr: int | None):
+        """Issue work on this cudaStream_t (0 = CUDA's legacy default stream)."""
+        self._check(self.L.lt_set_stream(self.h, C.c_void_p(stream_ptr or 0)))
+
+    def get_stream(self) -> int:
+        return self.L.lt_get_stream(self.h) or 0
+
+    def sync(self):
+        self._check(self.L.lt_sync(self.h))
+
+    def load_scene_json(self, path: str):
+        self._check(self.L.lt_scene_load_json(self.h, os.path.abspath(path).encode()))
+
+    def create_scene(self, desc: SceneDesc):
+        self._check(self.L.lt_scene_create(self.h, C.byref(desc)))
+
+    def scene_info(self) -> SceneInfo:
+        info = SceneInfo()
+        self._check(self.L.lt_scene_info_get(self.h, C.byref(info)))
+        return info
+
+    def mesh_offsets(self):
+        info = self.scene_info()
+        arr = (C.c_uint32 * max(1, info.num_meshes))()
+        self._check(self.L.lt_scene_mesh_offsets(self.h, arr, len(arr)))
+        return list(arr)[:info.num_meshes]
+
+    def render(self, film: Film, spp: int, first_frame: int = 0, max_depth: int = 1500, rr_depth: int = 3):
+        prm = RenderParams(spp, first_frame, max_depth, rr_depth)
+        self._check(self.L.lt_render(self.h, C.byref(prm), C.byref(film)))
+
+    def stats(self) -> RenderStats:
+        s = RenderStats()
+        self._check(self.L.lt_render_stats_get(self.h, C.byref(s)))
+        return s
+
+    def intersect(self, rays_ptr: int, hits_ptr: int, n: int, on_device: bool):
+        self._check(self.L.lt_intersect(self.h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr), n, int(on_device)))

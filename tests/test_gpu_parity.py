@@ -1,0 +1,166 @@
+"""GPU path against the oracle, through the C ABI (liblantern_gpu.so).
+
+* Intersection (lt_intersect) against the oracle's Embree-semantics closest
+  hit: primitive bit-exact except exact ties, t within 1e-5 relative.
+* Rendering (lt_render) against the oracle with the same per-(pixel, frame)
+  sampler keying: the same paths are traced, so sample counts are exact and
+  colours agree pixel by pixel except where a transcendental function's last
+  bit (CUDA vs glibc sinf/cosf/logf/expf) sends a path elsewhere.
+"""
+import numpy as np
+import pytest
+import torch
+
+import lantern_gb300.scenes as S
+from lantern_gb300.integrator import FrameBuffer, Integrator, Scene, intersect, render_host
+from lantern_gb300.native import MISS, Context, LanternError
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _scene_rays(path, n, seed):
+    orc = O.OracleScene(path)
+    pos = []
+    for p in orc.json["primitives"]:
+        pos.append(O.read_lmf(__import__("os").path.join(__import__("os").path.dirname(path), p["file_path"]))["positions"])
+    allp = np.concatenate(pos)
+    lo, hi = allp.min(0), allp.max(0)
+    c, e = (lo + hi) / 2, (hi - lo) / 2
+    rays = S.random_rays(n, c - 0.6 * e, c + 0.6 * e, seed=seed)
+    return orc, rays
+
+
+def _compare_hits(gh, oh):
+    gprim = gh[:, 3].view(np.uint32)
+    oprim = oh[:, 3]
+    ot = oh[:, 0].view(np.float32)
+    gt = gh[:, 0]
+    hit = oprim != MISS
+    assert np.array_equal(gprim == MISS, oprim == MISS), "hit/miss differs"
+    diff = hit & (gprim != oprim)
+    # exact ties only: the oracle's t for the GPU's primitive equals the oracle's best t
+    assert np.all(gt[diff] == ot[diff]), f"{diff.sum()} primitive mismatches that are not ties"
+    rel = np.abs(gt[hit] - ot[hit]) / np.maximum(np.abs(ot[hit]), 1e-30)
+    assert rel.max(initial=0) <= 1e-5
+    return int(hit.sum()), int(diff.sum())
+
+
+@pytest.mark.parametrize("make", [
+    lambda: S.nine_spheres(width=64, height=64, name="isect_nine"),
+    lambda: S.displaced_icosphere_scene(width=64, height=64, levels=5, name="isect_ico5"),
+    lambda: S.tiny_scene(name="isect_tiny"),
+])
+def test_intersect_matches_oracle(ctx, scene_dir, make):
+    path = make().write(scene_dir)
+    ctx.load_scene_json(path)
+    orc, rays = _scene_rays(path, 1 << 16, seed=7)
+    oh = orc.intersect(rays)
+    gh = intersect(ctx, torch.from_numpy(rays).cuda()).cpu().numpy()
+    nhit, nties = _compare_hits(gh, oh)
+    assert nhit > 1000
+    # host-memory path gives the same answer
+    gh2 = intersect(ctx, rays)
+    assert np.array_equal(gh.view(np.uint32), gh2.view(np.uint32))
+
+
+def test_intersect_tnear_tfar_rule(ctx, scene_dir):
+    """Rays clipped exactly at, and one float short of, each hit distance (and
+    starting there) are accepted or rejected as the oracle's Embree rule says:
+    |den|*tnear < T <= |den|*tfar, evaluated in float."""
+    path = S.tiny_scene(name="isect_rule").write(scene_dir)
+    ctx.load_scene_json(path)
+    orc, rays = _scene_rays(path, 4096, seed=3)
+    oh = orc.intersect(rays)
+    hit = oh[:, 3] != MISS
+    t = oh[hit, 0].view(np.float32)
+    cases = []
+    for tfar in (t, np.nextafter(t, np.float32(0)), np.nextafter(t, np.float32(np.inf))):
+        r = rays[hit].copy()
+        r[:, 7] = tfar
+        cases.append(r)
+    r = rays[hit].copy()
+    r[:, 3] = t                      # tnear = hit distance: that hit is excluded
+    cases.append(r)
+    for r in cases:
+        _compare_hits(intersect(ctx, r), orc.intersect(r))
+    assert (intersect(ctx, cases[0])[:, 3].view(np.uint32) != MISS).mean() > 0.5
+
+
+@pytest.mark.parametrize("make,spp,depth", [
+    (lambda: S.tiny_scene(width=48, height=40, name="paths_tiny"), 6, 12),
+    (lambda: S.nine_spheres(width=64, height=64, name="paths_nine"), 4, 8),
+    (lambda: S.medium_sphere_scene(width=40, height=40, reference_expressible=True, name="paths_med_ref"), 4, 32),
+    (lambda: S.medium_sphere_scene(width=40, height=40, name="paths_med_hg"), 4, 32),
+])
+def test_render_matches_oracle_path_by_path(scene_dir, make, spp, depth):
+    path = make().write(scene_dir)
+    sc = Scene(0)
+    sc.LoadSceneFromJSON(path)
+    fb = FrameBuffer(sc.width, sc.height, "cuda:0")
+    Integrator(sc, fb, max_depth=depth, rr_depth=3).RenderFrame(spp)
+    torch.cuda.synchronize()
+    rgb = fb.ColorData.cpu().numpy()
+    ref = O.OracleScene(path).render(spp, max_depth=depth, rr_depth=3, keying=O.KEY_PIXEL)
+    assert np.array_equal(fb.ColorSampleCount.cpu().numpy(), ref["counts"].astype(np.int32))
+    close = np.isclose(rgb, ref["rgb"], rtol=2e-4, atol=1e-5).all(-1)
+    assert close.mean() > 0.97, close.mean()
+    same_b = fb.Bounces.cpu().numpy() == ref["bounces"].astype(np.int32)
+    assert same_b.mean() > 0.97
+    m_g, m_o = rgb.astype(np.float64).mean(), ref["rgb"].astype(np.float64).mean()
+    assert abs(m_g - m_o) <= 0.01 * abs(m_o) + 1e-6
+
+
+def test_render_is_additive_and_host_path_agrees(scene_dir):
+    path = S.tiny_scene(width=32, height=24, name="additive").write(scene_dir)
+    sc = Scene(0)
+    sc.LoadSceneFromJSON(path)
+    fb = FrameBuffer(sc.width, sc.height, "cuda:0")
+    it = Integrator(sc, fb, max_depth=10)
+    it.RenderFrame(2)
+    it.RenderFrame(3)
+    torch.cuda.synchronize()
+    one = FrameBuffer(sc.width, sc.height, "cuda:0")
+    Integrator(sc, one, max_depth=10).RenderFrame(5)
+    torch.cuda.synchronize()
+    assert torch.equal(fb.ColorSampleCount, one.ColorSampleCount)
+    assert torch.equal(fb.Bounces, one.Bounces)
+    assert torch.allclose(fb.ColorData, one.ColorData, rtol=1e-5, atol=1e-6)
+    host = render_host(sc.ctx, sc.width, sc.height, 5, max_depth=10)
+    assert np.array_equal(host["counts"].astype(np.int32), one.ColorSampleCount.cpu().numpy())
+    assert np.allclose(host["rgb"], one.ColorData.cpu().numpy(), rtol=1e-5, atol=1e-6)
+
+
+def test_max_depth_zero_counts_only(ctx, scene_dir):
+    path = S.tiny_scene(width=8, height=8, name="depth0").write(scene_dir)
+    ctx.load_scene_json(path)
+    film = render_host(ctx, 8, 8, 3, max_depth=0)
+    assert np.all(film["counts"] == 3) and np.all(film["rgb"] == 0) and np.all(film["bounces"] == 0)
+
+
+def test_errors_are_reported(ctx, scene_dir, tmp_path):
+    c = Context(0)
+    with pytest.raises(LanternError) as e:
+        render_host(c, 4, 4, 1)
+    assert e.value.status == 8  # LT_ERR_STATE: no scene yet
+    with pytest.raises(LanternError) as e:
+        c.load_scene_json(str(tmp_path / "missing.json"))
+    assert e.value.status == 5  # LT_ERR_IO
+    bad = tmp_path / "bad.json"
+    bad.write_text('{"camera": {"client_width": 4, ')
+    with pytest.raises(LanternError) as e:
+        c.load_scene_json(str(bad))
+    assert e.value.status == 6  # LT_ERR_PARSE
+    path = S.tiny_scene(width=8, height=8, name="err_size").write(scene_dir)
+    c.load_scene_json(path)
+    with pytest.raises(LanternError) as e:
+        render_host(c, 9, 8, 1)
+    assert e.value.status == 1  # LT_ERR_INVALID: film size
+    c.close()
