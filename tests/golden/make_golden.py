@@ -68,20 +68,33 @@ def film_tiny():
                         rays=np.uint64(r["rays"]))
 
 
-def c0_images():
-    path = S.nine_spheres(name="golden_c0").write(SCENES)
+def image_pair(scene, spp, depth, out_name):
+    """Two reference renders with independent streams (frames 0.. and 1000000..)."""
+    path = scene.write(SCENES)
     ref = O.ReferenceScene(path)
     imgs = {}
     for tag, first in (("a", 0), ("b", 1_000_000)):
         t = time.time()
-        r = ref.render(16, first_frame=first, max_depth=8, rr_depth=3)
+        r = ref.render(spp, first_frame=first, max_depth=depth, rr_depth=3)
         rgb = r["rgb"].astype(np.float64) + r["rgb_b"]
         cnt = (r["counts"] + r["counts_b"]).astype(np.float64)
         imgs[tag] = (rgb / cnt[..., None]).astype(np.float16)
         imgs[f"seconds_{tag}"] = np.float64(r["seconds"])
         imgs[f"rays_{tag}"] = np.uint64(r["rays"])
-        print(f"c0 {tag}: {time.time() - t:.1f}s, {r['rays']} rays")
-    np.savez_compressed(os.path.join(OUT, "reference_c0_images.npz"), **imgs)
+        print(f"{out_name} {tag}: {time.time() - t:.1f}s, {r['rays']} rays")
+    np.savez_compressed(os.path.join(OUT, out_name), **imgs)
+
+
+def c0_images():
+    # config 0: 256x256, 16 spp, max depth 8
+    image_pair(S.nine_spheres(name="golden_c0"), 16, 8, "reference_c0_images.npz")
+    # Lambert + mirror + dielectric spheres: 96x96, 64 spp, max depth 12
+    image_pair(S.tiny_scene(width=96, height=96, name="golden_tiny96"), 64, 12, "reference_tiny_images.npz")
+    # config 2 in the reference's terms (isotropic phase, scalar sigma_s): 128x128, 512 spp, depth 32
+    # (the medium's light paths are heavy-tailed: 512 spp keeps the standard error of
+    # the image mean near 0.2%)
+    image_pair(S.medium_sphere_scene(width=128, height=128, reference_expressible=True, name="golden_c2r"),
+               512, 32, "reference_c2r_images.npz")
 
 
 if __name__ == "__main__":
