@@ -157,6 +157,33 @@ typedef struct lt_render_params {
  * (integrator.cpp:84-89) keyed by pixel instead of tile. */
 lt_status lt_render(lt_ctx *ctx, const lt_render_params *params, lt_film *film);
 
+/* lt_render without any device or host allocation. No counterpart in the
+ * reference (its CPU integrator has nothing to allocate on a device).
+ *
+ * For callers that cannot have the library allocate GPU memory while they run:
+ * an application that gives the library a fixed memory budget up front and
+ * forbids allocations afterwards, or an interactive loop in which cudaMalloc /
+ * cudaFree (which can synchronise the whole device) would stall other work.
+ * The wavefront state lives in a fixed array inside liblantern_gpu.so of
+ * LT_NOALLOC_MAX_PATHS path slots (about 17.6 MB), reserved on every GPU that
+ * loads the library until the process exits. Same sampling, same film
+ * semantics and same result as lt_render; only the number of paths in flight
+ * is bounded.
+ *
+ * - film must be on the device (on_device = 1): host films need staging memory.
+ * - paths_in_flight: path slots to use, 1..LT_NOALLOC_MAX_PATHS; anything else
+ *   is rejected with LT_ERR_INVALID. More slots keep more of the GPU busy.
+ * - The first call on a device looks up the array's device address; make that
+ *   first call before any stream capture on that device.
+ * - All calls in the process share the one array per device: calls whose GPU
+ *   work overlaps (other threads, other contexts, other streams) race and
+ *   corrupt each other. Serialise them. The array keeps the last call's
+ *   contents; each call clears what it needs before use.
+ * - No per-stage timing is recorded (lt_render_stats: stage times are 0). */
+#define LT_NOALLOC_MAX_PATHS 65536
+lt_status lt_render_noalloc(lt_ctx *ctx, const lt_render_params *params, lt_film *film,
+                            uint32_t paths_in_flight);
+
 typedef struct lt_render_stats {
     uint64_t main_rays;      /* closest-hit queries of path segments */
     uint64_t light_rays;     /* light-sample connection rays (AreaLight::SampleLi) */

@@ -419,3 +419,103 @@ lt_status lt_scene_load_json(lt_ctx *c, const char *path) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ lt_render_noalloc
+// Same wavefront as lt_render, with its state carved out of the fixed device
+// array of lt_noalloc.cu instead of a cudaMalloc'd arena. Nothing here
+// allocates: no cudaMalloc / cudaFree / cudaMallocHost, no new CUDA events, no
+// staging buffers (the film must already be on the device).
+#include "lt_noalloc.h"
+
+static Wavefront carve_noalloc(char *a, uint32_t cap) {
+    size_t P = cap, off = 0;
+    auto take = [&](size_t n) { size_t o = off; off += (n + 255) & ~(size_t)255; return a + o; };
+    Wavefront w;
+    w.capacity = cap;
+    w.p.rng = (uint64_t *)take(8 * P);
+    w.p.pixel = (uint32_t *)take(4 * P);
+    w.p.frame = (uint32_t *)take(4 * P);
+    w.p.T = (float *)take(12 * P);
+    w.p.color = (float *)take(12 * P);
+    w.p.bounces = (uint32_t *)take(4 * P);
+    w.p.flags = (uint32_t *)take(4 * P);
+    w.p.iori = (float *)take(4 * P);
+    w.ray[0] = (float4 *)take(32 * P);
+    w.ray[1] = (float4 *)take(32 * P);
+    w.queue[0] = (uint32_t *)take(4 * P);
+    w.queue[1] = (uint32_t *)take(4 * P);
+    w.hits = (float4 *)take(16 * P);
+    w.cray = (float4 *)take(64 * P);
+    w.crec = (float4 *)take(64 * P);
+    w.counters = (WaveCounters *)take(sizeof(WaveCounters));
+    w.arena = nullptr;  // not owned: never freed
+    w.arena_bytes = off;
+    return w;
+}
+
+extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_film *film,
+                                       uint32_t paths_in_flight) {
+    if (!c || !p || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
+    if (paths_in_flight == 0 || paths_in_flight > LT_NOALLOC_MAX_PATHS)
+        return fail(c, LT_ERR_INVALID, "paths_in_flight = %u; lt_render_noalloc holds 1..%u paths", paths_in_flight,
+                    (unsigned)LT_NOALLOC_MAX_PATHS);
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "lt_render_noalloc without a scene");
+    const uint32_t W = c->host.camera.width, H = c->host.camera.height;
+    if (film->width != W || film->height != H)
+        return fail(c, LT_ERR_INVALID, "film is %ux%u, scene camera is %ux%u", film->width, film->height, W, H);
+    if (!film->on_device) return fail(c, LT_ERR_INVALID, "lt_render_noalloc needs a device film (on_device = 1)");
+    if (!film->rgb || !film->bounces || !film->counts) return fail(c, LT_ERR_INVALID, "film buffers missing");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    void *scratch = nullptr;
+    CUDA_TRY(c, noalloc_scratch(c->device, &scratch));
+    const size_t npix = (size_t)W * H;
+    FilmPtrs f;
+    f.rgb = film->rgb;
+    f.bounces = film->bounces;
+    f.counts = film->counts;
+    RenderArgs a;
+    a.width = W;
+    a.height = H;
+    a.first_frame = p->first_frame;
+    a.max_depth = p->max_depth;
+    a.rr_depth = p->rr_depth;
+    a.total = (unsigned long long)npix * p->spp;
+    c->stats = lt_render_stats{};
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    if (a.total > 0 && p->max_depth == 0) {
+        CUDA_TRY(c, launch_add_counts(f, (uint32_t)npix, p->spp, c->stream));
+        c->stats.kernel_launches = 1;
+    } else if (a.total > 0) {
+        uint32_t cap = (uint32_t)(a.total < paths_in_flight ? a.total : paths_in_flight);
+        Wavefront w = carve_noalloc((char *)scratch, cap);
+        // the array keeps the previous call's contents: the counters must start at zero
+        CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
+        CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
+        uint32_t launches = 1, iters = 0;
+        int cur = 0;
+        const int kBatch = 4;
+        const uint32_t limit = 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u;
+        for (;;) {
+            for (int k = 0; k < kBatch; ++k) {
+                for (int stage = 0; stage < 3; ++stage)
+                    CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
+                launches += 3;
+                cur ^= 1;
+                ++iters;
+            }
+            CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
+                                        c->stream));
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            if (c->counters_host->count[cur] == 0) break;
+            if (iters > limit) return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
+        }
+        c->stats.main_rays = c->counters_host->main_rays;
+        c->stats.light_rays = c->counters_host->light_rays;
+        c->stats.bsdf_rays = c->counters_host->bsdf_rays;
+        c->stats.iterations = iters;
+        c->stats.kernel_launches = launches;
+    }
+    c->stats.samples = a.total;
+    CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    return LT_OK;
+}

@@ -23,7 +23,8 @@ MISS = 0xFFFFFFFF
 SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error", "lt_set_stream", "lt_get_stream",
            "lt_sync",
            "lt_scene_create", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
-           "lt_render_stats_get", "lt_intersect"]
+           "lt_render_stats_get", "lt_intersect", "lt_render_noalloc"]
+NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 
 
 class LanternError(RuntimeError):
@@ -116,6 +117,7 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_render.argtypes = [p, C.POINTER(RenderParams), C.POINTER(Film)]
         L.lt_render_stats_get.argtypes = [p, C.POINTER(RenderStats)]
         L.lt_intersect.argtypes = [p, p, p, C.c_uint64, C.c_int32]
+        L.lt_render_noalloc.argtypes = [p, C.POINTER(RenderParams), C.POINTER(Film), C.c_uint32]
         _lib = L
         return L
 
@@ -181,6 +183,13 @@ class Context:
     def render(self, film: Film, spp: int, first_frame: int = 0, max_depth: int = 1500, rr_depth: int = 3):
         prm = RenderParams(spp, first_frame, max_depth, rr_depth)
         self._check(self.L.lt_render(self.h, C.byref(prm), C.byref(film)))
+
+    def render_noalloc(self, film: Film, spp: int, paths_in_flight: int, first_frame: int = 0,
+                       max_depth: int = 1500, rr_depth: int = 3):
+        """lt_render_noalloc: the same render with the library's fixed device
+        scratch, for callers that must not have the library allocate memory."""
+        prm = RenderParams(spp, first_frame, max_depth, rr_depth)
+        self._check(self.L.lt_render_noalloc(self.h, C.byref(prm), C.byref(film), paths_in_flight))
 
     def stats(self) -> RenderStats:
         s = RenderStats()
