@@ -195,6 +195,8 @@ def main():
     ap.add_argument("--workload", default="icosphere-1.3M")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--microbench", action=argparse.BooleanOptionalAction, default=True,
+                    help="also time lt_intersect on 16,777,216 random rays of the same mesh")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -287,6 +289,10 @@ def main():
         e2e = {"value": round(samples * world / e2e_s / 1e6, 3), "unit": "Msamples/s",
                "h2d_bytes_per_step": npix * 20, "d2h_bytes_per_step": npix * 20}
 
+    micro = None
+    if args.microbench and args.workload == "icosphere-1.3M":
+        micro = microbench(scene, path, local)
+
     line = None
     if rank == 0:
         peak, peak_kind = _peaks()
@@ -316,11 +322,57 @@ def main():
                            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1
                            else "single GPU"},
                 "mrays": round(mrays, 2), "gpu_launches": launches,
-                "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu}
+                "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "intersect_microbench": micro}
         print(json.dumps(line))
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def microbench(scene, path, local, n=1 << 24):
+    """lt_intersect on n rays: origins uniform in the mesh bounds, directions
+    uniform on the sphere (seed 2), tnear 0, tfar inf. Device Mrays/s over 5
+    launches (inputs 512 MiB, larger than L2), plus the oracle's BVH2 on a
+    bounded CPU sample with all host cores."""
+    import numpy as np
+    import torch
+    import lantern_gb300.scenes as S
+    from lantern_gb300.integrator import intersect
+    with open(path) as fh:
+        j = json.load(fh)
+    lo, hi = np.full(3, np.inf), np.full(3, -np.inf)
+    from oracle import oracle as O
+    for p in j["primitives"]:
+        if p["name"].startswith("ico_"):
+            pos = O.read_lmf(os.path.join(os.path.dirname(path), p["file_path"]))["positions"]
+            lo, hi = np.minimum(lo, pos.min(0)), np.maximum(hi, pos.max(0))
+    rays = S.random_rays(n, lo, hi, seed=2)
+    dr = torch.from_numpy(rays).to(f"cuda:{local}")
+    intersect(scene.ctx, dr)  # warm-up
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    ms = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        hits = intersect(scene.ctx, dr)
+        e1.record(st)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+    hit_frac = float((hits[:, 3].view(torch.int32) != -1).float().mean())
+    out = {"rays": n, "mrays": round(5 * n / (ms / 1e3) / 1e6, 1), "hit_fraction": round(hit_frac, 4)}
+    try:
+        orc = O.OracleScene(path)
+        sample = rays[: 1 << 18]
+        t0 = time.perf_counter()
+        orc.intersect(sample, threads=os.cpu_count())
+        dt = time.perf_counter() - t0
+        out["cpu_oracle_mrays"] = round(sample.shape[0] / dt / 1e6, 2)
+        out["cpu_oracle_sample"] = f"{sample.shape[0]} rays, {os.cpu_count()} threads, oracle BVH2"
+    except Exception as e:
+        out["cpu_oracle_error"] = str(e)[:200]
+    return out
 
 
 def cpu_baseline(path, rp):

@@ -37,6 +37,7 @@ struct lt_ctx {
     // wavefront
     Wavefront wave;
     WaveCounters *counters_host = nullptr;  // pinned
+    uint32_t *isect_fetch = nullptr;        // device ray counter of lt_intersect
 
     // scratch for host-memory calls
     void *scratch = nullptr;
@@ -101,6 +102,7 @@ lt_status lt_ctx_create(int device, lt_ctx **out) {
     e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->counters_host, sizeof(WaveCounters));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->isect_fetch, 256);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e != cudaSuccess) {
@@ -121,6 +123,7 @@ void lt_ctx_destroy(lt_ctx *c) {
     free_wave(c);
     if (c->scratch) cudaFree(c->scratch);
     if (c->counters_host) cudaFreeHost(c->counters_host);
+    if (c->isect_fetch) cudaFree(c->isect_fetch);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (cudaEvent_t e : c->stage_events) cudaEventDestroy(e);
@@ -187,6 +190,9 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     if ((st = upload(c, h.materials, &d.mats)) != LT_OK) return st;
     if ((st = upload(c, h.media, &d.meds)) != LT_OK) return st;
     if ((st = upload(c, h.lights, &d.lights)) != LT_OK) return st;
+    const float *ltris = nullptr;
+    if ((st = upload(c, h.light_tris, &ltris)) != LT_OK) return st;
+    d.light_tris = (const float4 *)ltris;
     d.num_lights = (uint32_t)h.lights.size();
     d.num_tris = (uint32_t)h.tri_geom.size();
     d.background = h.background;
@@ -394,7 +400,8 @@ lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, 
     if (on_device) {
         if (((uintptr_t)rays & 15u) || ((uintptr_t)hits & 15u))
             return fail(c, LT_ERR_INVALID, "rays and hits must be 16-byte aligned");
-        CUDA_TRY(c, launch_intersect(c->dev, (const float4 *)rays, (float4 *)hits, n, c->shape, c->stream));
+        CUDA_TRY(c, launch_intersect(c->dev, (const float4 *)rays, (float4 *)hits, n, c->isect_fetch, c->shape,
+                                     c->stream));
         return LT_OK;
     }
     lt_status st = ensure_scratch(c, n * 48);
@@ -402,7 +409,7 @@ lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, 
     float4 *dr = (float4 *)c->scratch;
     float4 *dh = dr + 2 * n;
     CUDA_TRY(c, cudaMemcpyAsync(dr, rays, n * 32, cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, launch_intersect(c->dev, dr, dh, n, c->shape, c->stream));
+    CUDA_TRY(c, launch_intersect(c->dev, dr, dh, n, c->isect_fetch, c->shape, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(hits, dh, n * 16, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return LT_OK;

@@ -21,6 +21,7 @@ struct DevScene {
     const MaterialInfo *mats;
     const MediumInfo *meds;
     const LightInfo *lights;
+    const float4 *light_tris;   // emissive meshes' triangles, 3 float4 each
     uint32_t num_lights;
     uint32_t num_tris;
     v3 background;
@@ -46,6 +47,9 @@ struct WaveCounters {
     uint32_t error;              // nonzero: a device-side bound was exceeded
     unsigned long long work_next; // next (pixel, frame) work item
     unsigned long long main_rays, light_rays, bsdf_rays;
+    uint32_t trace_fetch;         // persistent-thread ray counters, zeroed by the
+    uint32_t connect_fetch;       // kernel that runs before each consumer
+    unsigned long long light_traversals;  // connection rays that needed an occlusion query
 };
 
 struct Wavefront {
@@ -82,7 +86,7 @@ struct LaunchShape {
 // launchers (lt_kernels.cu)
 void query_launch_shape(int device, LaunchShape *out);
 cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
-                             const LaunchShape &ls, cudaStream_t st);
+                             uint32_t *fetch, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st);
 cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
                              const LaunchShape &ls, cudaStream_t st);

@@ -77,55 +77,104 @@ __device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy,
     return tmin <= tmax * 1.0000004f;
 }
 
-// Closest hit along O + t*D, t in (tnear, tfar]. Stack-based, nearer child first;
-// leaves are intersected as soon as their box is hit.
-__device__ Hit trace_closest(const DevScene &S, v3 O, v3 D, float tnear, float tfar) {
+// ------------------------------------------------------------------ traversal
+// Persistent "while-while" traversal (Aila & Laine, "Understanding the
+// efficiency of ray traversal on GPUs", HPG 2009): a warp walks inner nodes
+// until every lane holds a leaf (one leaf per lane is postponed so that lanes
+// keep descending), then all lanes test triangles together. A lane whose ray is
+// done fetches the next one from a global counter; a warp leaves the loop early
+// when fewer than kFetchThreshold lanes are still working so that idle lanes
+// refill. Stack entries are node refs (inner >= 0, leaf < 0); the bottom entry
+// is kSentinel. Box tests widen the far distance by 2*gamma(3) so no hit is lost.
+constexpr int kSentinel = 0x76543210;
+constexpr int kFetchThreshold = 20;
+
+struct Trav {
+    v3 O, D, inv;
+    float tnear;
     Hit h;
-    h.t = tfar;
-    h.u = h.v = 0.0f;
-    h.prim = kMiss;
-    v3 inv = mk(safe_inv(D.x), safe_inv(D.y), safe_inv(D.z));
-    int stack_node[kStack];
-    float stack_t[kStack];
-    int sp = 0;
-    int node = 0;
-    for (;;) {
-        const float4 *n = S.nodes + 4 * node;
-        float4 n0 = ldg4(n), n1 = ldg4(n + 1), n2 = ldg4(n + 2), n3 = ldg4(n + 3);
-        float t0, t1;
-        bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, O, inv, tnear, h.t, t0);
-        bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, O, inv, tnear, h.t, t1);
-        int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
-        uint32_t c0 = __float_as_uint(n3.z), c1 = __float_as_uint(n3.w);
-        // leaves first, nearer one first
-        bool l0 = h0 && r0 < 0, l1 = h1 && r1 < 0;
-        if (l0 && l1 && t1 < t0) {
-            for (uint32_t k = 0; k < c1; ++k) tri_test(S.tris + 3 * ((uint32_t)~r1 + k), O, D, tnear, h);
-            for (uint32_t k = 0; k < c0; ++k) tri_test(S.tris + 3 * ((uint32_t)~r0 + k), O, D, tnear, h);
-        } else {
-            if (l0) for (uint32_t k = 0; k < c0; ++k) tri_test(S.tris + 3 * ((uint32_t)~r0 + k), O, D, tnear, h);
-            if (l1) for (uint32_t k = 0; k < c1; ++k) tri_test(S.tris + 3 * ((uint32_t)~r1 + k), O, D, tnear, h);
+    int node, leaf, sp;
+    bool any;                // occlusion query: stop at the first hit not on `skip_geom`
+    uint32_t skip_geom;
+    int stack[kStack];
+};
+
+__device__ __forceinline__ void trav_start(Trav &r, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip_geom) {
+    r.O = O;
+    r.D = D;
+    r.inv = mk(safe_inv(D.x), safe_inv(D.y), safe_inv(D.z));
+    r.tnear = tnear;
+    r.h.t = tfar;
+    r.h.u = r.h.v = 0.0f;
+    r.h.prim = kMiss;
+    r.node = 0;
+    r.leaf = 0;
+    r.sp = 0;
+    r.stack[0] = kSentinel;
+    r.any = any;
+    r.skip_geom = skip_geom;
+}
+
+// Advances the ray until it is finished (r.node == kSentinel) or the warp
+// should refill idle lanes.
+__device__ __forceinline__ void traverse(const DevScene &S, Trav &r) {
+    while (r.node != kSentinel) {
+        while ((unsigned)r.node < (unsigned)kSentinel) {
+            const float4 *n = S.nodes + 4 * r.node;
+            float4 n0 = ldg4(n), n1 = ldg4(n + 1), n2 = ldg4(n + 2), n3 = ldg4(n + 3);
+            float t0, t1;
+            bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r.O, r.inv, r.tnear, r.h.t, t0);
+            bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r.O, r.inv, r.tnear, r.h.t, t1);
+            int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+            if (!h0 && !h1) {
+                r.node = r.stack[r.sp--];
+            } else {
+                r.node = h0 ? c0 : c1;
+                if (h0 && h1) {
+                    int far = c1;
+                    if (t1 < t0) { far = c0; r.node = c1; }
+                    r.stack[++r.sp] = far;
+                }
+            }
+            if (r.node < 0 && r.leaf >= 0) {  // postpone the first leaf, keep descending
+                r.leaf = r.node;
+                r.node = r.stack[r.sp--];
+            }
+            if (!__any_sync(__activemask(), r.leaf >= 0)) break;
         }
-        bool i0 = h0 && r0 >= 0 && t0 <= h.t * 1.0000004f;
-        bool i1 = h1 && r1 >= 0 && t1 <= h.t * 1.0000004f;
-        if (i0 && i1) {
-            int nearer = r0, farther = r1;
-            float tf = t1;
-            if (t1 < t0) { nearer = r1; farther = r0; tf = t0; }
-            if (sp < kStack) { stack_node[sp] = farther; stack_t[sp] = tf; ++sp; }
-            node = nearer;
-            continue;
+        while (r.leaf < 0) {
+            uint32_t code = ~(uint32_t)r.leaf;
+            uint32_t first = code >> kLeafBits, count = code & ((1u << kLeafBits) - 1u);
+            for (uint32_t k = 0; k < count; ++k) {
+                const float4 *tri = S.tris + 3 * (first + k);
+                if (!r.any) {
+                    tri_test(tri, r.O, r.D, r.tnear, r.h);
+                } else {
+                    Hit c = r.h;
+                    tri_test(tri, r.O, r.D, r.tnear, c);
+                    if (c.prim != kMiss && __ldg(S.tri_geom + c.prim) != r.skip_geom) {
+                        r.h.prim = c.prim;  // occluded
+                        r.node = kSentinel;
+                        r.leaf = 0;
+                        return;
+                    }
+                }
+            }
+            r.leaf = r.node;
+            if (r.node < 0) r.node = r.stack[r.sp--];
         }
-        if (i0) { node = r0; continue; }
-        if (i1) { node = r1; continue; }
-        bool found = false;
-        while (sp > 0) {
-            --sp;
-            if (stack_t[sp] <= h.t * 1.0000004f) { node = stack_node[sp]; found = true; break; }
-        }
-        if (!found) break;
+        if (__popc(__activemask()) < kFetchThreshold) return;
     }
-    return h;
+}
+
+// Warp-aggregated fetch of the next work index for the lanes that ask.
+__device__ __forceinline__ uint32_t fetch_next(uint32_t *counter) {
+    unsigned m = __activemask();
+    int leader = __ffs(m) - 1;
+    uint32_t lane = threadIdx.x & 31u, base = 0;
+    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
 }
 
 __device__ __forceinline__ v3 interp_normal(const DevScene &S, uint32_t prim, float u, float v) {
@@ -285,13 +334,21 @@ __device__ __forceinline__ void film_add(const FilmPtrs &f, uint32_t pixel, v3 c
 }
 
 // ------------------------------------------------------------------ kernels
+// Closest hits of n rays (lt_intersect). Persistent: rays are fetched from *fetch.
 __global__ void __launch_bounds__(128) k_intersect(DevScene S, const float4 *__restrict__ rays,
-                                                   float4 *__restrict__ hits, unsigned long long n) {
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        float4 a = ldg4(rays + 2 * i), b = ldg4(rays + 2 * i + 1);
-        Hit h = trace_closest(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
-        hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+                                                   float4 *__restrict__ hits, uint32_t n, uint32_t *fetch) {
+    Trav r;
+    r.node = kSentinel;
+    uint32_t idx = 0;
+    for (;;) {
+        if (r.node == kSentinel) {
+            idx = fetch_next(fetch);
+            if (idx >= n) break;
+            float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
+            trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
+        }
+        traverse(S, r);
+        if (r.node == kSentinel) hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
     }
 }
 
@@ -312,21 +369,32 @@ __global__ void __launch_bounds__(128) k_raygen(DevScene S, Wavefront W, RenderA
         W.counters->count[1] = 0;
         W.counters->ccount = 0;
         W.counters->work_next = first;
+        W.counters->trace_fetch = 0;
     }
 }
 
+// Closest hit of every queued path ray. Persistent: entries are fetched from
+// counters->trace_fetch (zeroed by the kernel before).
 __global__ void __launch_bounds__(128) k_trace(DevScene S, Wavefront W, int cur) {
-    uint32_t n = W.counters->count[cur];
+    const uint32_t n = W.counters->count[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters->count[cur ^ 1] = 0;
         W.counters->ccount = 0;
         W.counters->main_rays += n;
     }
     const float4 *rays = W.ray[cur];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 a = ldg4(rays + 2 * i), b = ldg4(rays + 2 * i + 1);
-        Hit h = trace_closest(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
-        W.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+    Trav r;
+    r.node = kSentinel;
+    uint32_t idx = 0;
+    for (;;) {
+        if (r.node == kSentinel) {
+            idx = fetch_next(&W.counters->trace_fetch);
+            if (idx >= n) break;
+            float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
+            trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
+        }
+        traverse(S, r);
+        if (r.node == kSentinel) W.hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
     }
 }
 
@@ -335,6 +403,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
     const uint32_t n = W.counters->count[cur];
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->connect_fetch = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         uint32_t q = base + threadIdx.x;
         bool active = q < n;
@@ -527,47 +596,95 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
     }
 }
 
-// Trace connection rays and add their MIS-weighted contributions
-// (EstimateDirect, integrator.cpp:281-312; SampleLi/PdfLi pdf, area_light.cpp:64-67,105-109).
+// Connection rays and their MIS-weighted contributions (EstimateDirect,
+// integrator.cpp:281-312; SampleLi/PdfLi, area_light.cpp:58-67,100-109).
+//
+// The reference takes the closest hit in the whole scene and keeps it if it
+// lies on the chosen light. The same answer (up to exact distance ties between
+// the light and an occluder) comes cheaper in two steps: the closest hit among
+// the light's own triangles first -- a ray that misses the light contributes
+// nothing and is never traversed -- then an occlusion query up to that distance
+// that ignores the light's own geometry. Lights with more than kLightBrute
+// triangles use the full closest-hit query instead.
+constexpr uint32_t kLightBrute = 16;
+
+__device__ __forceinline__ void resolve_connection(const DevScene &S, const Wavefront &W, const FilmPtrs &F,
+                                                   uint32_t idx, uint32_t kl, uint32_t pixel, const Trav &r,
+                                                   const Hit &lh) {
+    const bool is_bsdf = (kl & kConnectBsdf) != 0;
+    const LightInfo &L = S.lights[kl & ~kConnectBsdf];
+    Hit h;
+    if (r.any) {
+        if (r.h.prim != kMiss) return;  // occluded
+        h = lh;
+    } else {
+        if (r.h.prim == kMiss || __ldg(S.tri_geom + r.h.prim) != (uint32_t)L.geom) return;
+        h = r.h;
+    }
+    v3 org = r.O, dir = r.D;
+    v3 ip = org + normalize(dir) * h.t;
+    v3 dd = ip - org;
+    float d2 = dot(dd, dd);
+    v3 nrm = normalize(interp_normal(S, h.prim, h.u, h.v));
+    float cosl = is_bsdf ? dot(nrm, dir) : dot(nrm, -dir);
+    float lpdf = d2 / (fabsf(cosl) * L.area);
+    if (lpdf == 0.0f) return;
+    float4 r0 = ldg4(W.crec + 2 * idx), r1 = ldg4(W.crec + 2 * idx + 1);
+    v3 f = mk(r0.x, r0.y, r0.z);
+    float spdf = r0.w;
+    v3 Le = mk(L.radiance[0], L.radiance[1], L.radiance[2]);
+    v3 c;
+    if (!is_bsdf) c = ((f * Le) * power_heuristic(lpdf, spdf)) / lpdf;
+    else c = ((f * Le) * power_heuristic(spdf, lpdf)) / spdf;
+    v3 T = mk(r1.x, r1.y, r1.z);
+    film_add(F, pixel, T * (c * (float)S.num_lights));
+}
+
 __global__ void __launch_bounds__(128) k_connect(DevScene S, Wavefront W, FilmPtrs F) {
     const uint32_t n = W.counters->ccount;
-    uint32_t n_all = 0, n_bsdf = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 a = ldg4(W.cray + 2 * i), b = ldg4(W.cray + 2 * i + 1);
-        v3 org = mk(a.x, a.y, a.z), dir = mk(b.x, b.y, b.z);
-        uint32_t kl = __float_as_uint(a.w);
-        uint32_t pixel = __float_as_uint(b.w);
-        bool is_bsdf = (kl & kConnectBsdf) != 0;
-        n_all++;
-        n_bsdf += is_bsdf;
-        const LightInfo &L = S.lights[kl & ~kConnectBsdf];
-        Hit h = trace_closest(S, org, dir, 0.001f, __int_as_float(0x7f800000));
-        if (h.prim == kMiss || __ldg(S.tri_geom + h.prim) != (uint32_t)L.geom) continue;
-        v3 ip = org + normalize(dir) * h.t;
-        v3 dd = ip - org;
-        float d2 = dot(dd, dd);
-        v3 nrm = normalize(interp_normal(S, h.prim, h.u, h.v));
-        float cosl = is_bsdf ? dot(nrm, dir) : dot(nrm, -dir);
-        float lpdf = d2 / (fabsf(cosl) * L.area);
-        if (lpdf == 0.0f) continue;
-        float4 r0 = ldg4(W.crec + 2 * i), r1 = ldg4(W.crec + 2 * i + 1);
-        v3 f = mk(r0.x, r0.y, r0.z);
-        float spdf = r0.w;
-        v3 Le = mk(L.radiance[0], L.radiance[1], L.radiance[2]);
-        v3 c;
-        if (!is_bsdf) c = ((f * Le) * power_heuristic(lpdf, spdf)) / lpdf;
-        else c = ((f * Le) * power_heuristic(spdf, lpdf)) / spdf;
-        v3 T = mk(r1.x, r1.y, r1.z);
-        film_add(F, pixel, T * (c * (float)S.num_lights));
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
+    uint32_t n_all = 0, n_bsdf = 0, n_trav = 0;
+    Trav r;
+    r.node = kSentinel;
+    Hit lh;
+    uint32_t idx = 0, kl = 0, pixel = 0;
+    bool pending = false;
+    for (;;) {
+        if (r.node == kSentinel) {
+            idx = fetch_next(&W.counters->connect_fetch);
+            if (idx >= n) break;
+            float4 a = ldg4(W.cray + 2 * idx), b = ldg4(W.cray + 2 * idx + 1);
+            v3 org = mk(a.x, a.y, a.z), dir = mk(b.x, b.y, b.z);
+            kl = __float_as_uint(a.w);
+            pixel = __float_as_uint(b.w);
+            n_all++;
+            n_bsdf += (kl & kConnectBsdf) != 0;
+            const LightInfo &L = S.lights[kl & ~kConnectBsdf];
+            if (L.tri_count <= kLightBrute) {
+                lh.t = __int_as_float(0x7f800000);
+                lh.u = lh.v = 0.0f;
+                lh.prim = kMiss;
+                for (uint32_t k = 0; k < L.tri_count; ++k)
+                    tri_test(S.light_tris + 3 * (L.tri_first + k), org, dir, 0.001f, lh);
+                if (lh.prim == kMiss) continue;  // misses the light: no contribution, no traversal
+                trav_start(r, org, dir, 0.001f, lh.t, true, (uint32_t)L.geom);
+            } else {
+                trav_start(r, org, dir, 0.001f, __int_as_float(0x7f800000), false, 0);
+            }
+            n_trav++;
+            pending = true;
+        }
+        traverse(S, r);
+        if (r.node == kSentinel && pending) {
+            resolve_connection(S, W, F, idx, kl, pixel, r, lh);
+            pending = false;
+        }
     }
-    // tallies of connection rays by kind, one atomic per warp
-    for (int o = 16; o > 0; o >>= 1) {
-        n_all += __shfl_xor_sync(0xFFFFFFFFu, n_all, o);
-        n_bsdf += __shfl_xor_sync(0xFFFFFFFFu, n_bsdf, o);
-    }
-    if ((threadIdx.x & 31u) == 0 && n_all) {
+    // tallies of connection rays by kind, one atomic per lane with work
+    if (n_all) {
         atomicAdd(&W.counters->bsdf_rays, (unsigned long long)n_bsdf);
         atomicAdd(&W.counters->light_rays, (unsigned long long)(n_all - n_bsdf));
+        atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
     }
 }
 
@@ -595,12 +712,19 @@ void query_launch_shape(int device, LaunchShape *out) {
 }
 
 cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
-                             const LaunchShape &ls, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
-    unsigned long long need = (n + 127) / 128;
-    int blocks = (int)(need < (unsigned long long)ls.isect_blocks ? need : ls.isect_blocks);
-    k_intersect<<<blocks, 128, 0, st>>>(s, rays, hits, n);
-    return cudaGetLastError();
+                             uint32_t *fetch, const LaunchShape &ls, cudaStream_t st) {
+    const unsigned long long kChunk = 1ull << 30;
+    for (unsigned long long off = 0; off < n; off += kChunk) {
+        uint32_t m = (uint32_t)(n - off < kChunk ? n - off : kChunk);
+        cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+        unsigned long long need = (m + 127) / 128;
+        int blocks = (int)(need < (unsigned long long)ls.isect_blocks ? need : ls.isect_blocks);
+        k_intersect<<<blocks, 128, 0, st>>>(s, rays + 2 * off, hits + off, m, fetch);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st) {

@@ -88,12 +88,13 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
         ntri += d->meshes[g].num_triangles;
         nvert += d->meshes[g].num_vertices;
     }
-    if (ntri >= 0x7FFFFFFFu || nvert >= 0xFFFFFFFFu) {
-        *err = "scene too large for 32-bit triangle indices";
+    if (ntri >= (1u << (31 - kLeafBits)) || nvert >= 0xFFFFFFFFu) {
+        *err = "scene too large: at most 2^28 triangles";
         return LT_ERR_INVALID;
     }
     s->geoms.clear();
     s->lights.clear();
+    s->light_tris.clear();
     s->tri_v0e1e2.assign(ntri * 9, 0.0f);
     s->tri_geom.assign(ntri, 0);
     s->tri_vidx.assign(ntri * 3, 0);
@@ -146,6 +147,14 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
             // AreaLight ctor (area_light.h:16-21): color * radiantPower * (float)M_1_PI / area
             v3 rad = ((ld3(m.emission_color) * m.radiant_power) * kInvPi) / area;
             li.radiance[0] = rad.x; li.radiance[1] = rad.y; li.radiance[2] = rad.z;
+            li.tri_first = (uint32_t)(s->light_tris.size() / 12);
+            li.tri_count = m.num_triangles;
+            for (uint32_t t = 0; t < m.num_triangles; ++t) {
+                const float *d = &s->tri_v0e1e2[9 * (t0 + t)];
+                const float row[12] = {d[0], d[1], d[2], bits_to_float((uint32_t)(t0 + t)),
+                                       d[3], d[4], d[5], 0.0f, d[6], d[7], d[8], 0.0f};
+                s->light_tris.insert(s->light_tris.end(), row, row + 12);
+            }
             gi.light = (int32_t)s->lights.size();
             s->lights.push_back(li);
         }
@@ -316,7 +325,7 @@ void build_bvh(HostScene *s) {
     s->nodes.clear();
     s->nodes.reserve(tn.size() / 2 + 1);
     auto child_ref = [&](int32_t c, int32_t assigned) -> int32_t {
-        return tn[c].left < 0 ? ~(int32_t)tn[c].first : assigned;
+        return tn[c].left < 0 ? leaf_ref(tn[c].first, tn[c].count) : assigned;
     };
     auto set_box = [&](BvhNode &g, int k, const Box &b) {
         if (k == 0) {
@@ -332,8 +341,8 @@ void build_bvh(HostScene *s) {
         memset(&g, 0, sizeof g);
         set_box(g, 0, tn[0].box);
         set_box(g, 1, tn[0].box);
-        g.ref[0] = ~(int32_t)tn[0].first;
-        g.ref[1] = ~(int32_t)tn[0].first;
+        g.ref[0] = leaf_ref(tn[0].first, tn[0].count);
+        g.ref[1] = leaf_ref(0, 0);
         g.count[0] = tn[0].count;
         g.count[1] = 0;
         s->nodes.push_back(g);

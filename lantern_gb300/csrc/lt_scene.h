@@ -40,7 +40,8 @@ struct alignas(16) MediumInfo {
 struct alignas(16) LightInfo {
     int32_t geom;
     float area;
-    float pad[2];
+    uint32_t tri_first;   // first of the light's triangles in HostScene::light_tris
+    uint32_t tri_count;
     float radiance[4];
     float sphere[4];     // bounding sphere centre, radius
 };
@@ -48,7 +49,11 @@ struct alignas(16) LightInfo {
 // BVH2 node for the device, 64 bytes (four float4):
 //  [0] c0.lo.x c0.hi.x c0.lo.y c0.hi.y   [1] c1.lo.x c1.hi.x c1.lo.y c1.hi.y
 //  [2] c0.lo.z c0.hi.z c1.lo.z c1.hi.z   [3] c0 ref, c1 ref, c0 count, c1 count
-// ref >= 0: inner node index; ref < 0: leaf, first triangle (leaf order) = ~ref.
+// ref >= 0: inner node index; ref < 0: leaf, ~ref = (first triangle in leaf
+// order) << 3 | triangle count.
+constexpr uint32_t kLeafBits = 3;
+inline int32_t leaf_ref(uint32_t first, uint32_t count) { return ~(int32_t)((first << kLeafBits) | count); }
+
 struct alignas(16) BvhNode {
     float a[4], b[4], c[4];
     int32_t ref[2];
@@ -71,6 +76,7 @@ struct HostScene {
     // BVH
     std::vector<BvhNode> nodes;
     std::vector<float> leaf_tris;    // 12 floats per triangle in leaf order: v0,prim | e1,0 | e2,0
+    std::vector<float> light_tris;   // the emissive meshes' triangles, same 12-float layout
     uint32_t max_depth = 0;          // deepest leaf (the traversal stack holds 64)
     float build_ms = 0.0f;
 };
