@@ -165,7 +165,7 @@ lt_status lt_render(lt_ctx *ctx, const lt_render_params *params, lt_film *film);
  * forbids allocations afterwards, or an interactive loop in which cudaMalloc /
  * cudaFree (which can synchronise the whole device) would stall other work.
  * The wavefront state lives in a fixed array inside liblantern_gpu.so of
- * LT_NOALLOC_MAX_PATHS path slots (about 17.6 MB), reserved on every GPU that
+ * LT_NOALLOC_MAX_PATHS path slots (about 20.5 MB), reserved on every GPU that
  * loads the library until the process exits. Same sampling, same film
  * semantics and same result as lt_render; only the number of paths in flight
  * is bounded.

@@ -237,39 +237,43 @@ static lt_status ensure_scratch(lt_ctx *c, size_t bytes) {
     return LT_OK;
 }
 
-// Carves the wavefront buffers for `cap` path slots out of one allocation.
+// Lays the wavefront buffers for `cap` entries out from `base` (each array
+// 256-byte aligned); returns the bytes used. With base == nullptr it only sizes.
+static size_t carve_wave(char *base, uint32_t cap, Wavefront *w) {
+    size_t P = cap, off = 0;
+    auto take = [&](size_t n) { char *p = base + off; off += (n + 255) & ~(size_t)255; return p; };
+    w->capacity = cap;
+    for (int k = 0; k < 2; ++k) {
+        PathState &s = w->p[k];
+        s.rng = (uint64_t *)take(8 * P);
+        s.pixel = (uint32_t *)take(4 * P);
+        s.frame = (uint32_t *)take(4 * P);
+        s.T = (float *)take(12 * P);
+        s.color = (float *)take(12 * P);
+        s.bounces = (uint32_t *)take(4 * P);
+        s.flags = (uint32_t *)take(4 * P);
+        s.iori = (float *)take(4 * P);
+    }
+    w->ray[0] = (float4 *)take(32 * P);
+    w->ray[1] = (float4 *)take(32 * P);
+    w->hits = (float4 *)take(16 * P);
+    w->cray = (float4 *)take(64 * P);
+    w->crec = (float4 *)take(64 * P);
+    w->counters = (WaveCounters *)take(sizeof(WaveCounters));
+    return off;
+}
+
+// Sizes the context's wavefront arena for `cap` entries (one allocation, reused).
 static lt_status ensure_wave(lt_ctx *c, uint32_t cap) {
     if (c->wave.capacity >= cap && c->wave.arena) return LT_OK;
     free_wave(c);
-    size_t P = cap;
-    size_t bytes = 0;
-    auto take = [&](size_t n) { size_t o = bytes; bytes += (n + 255) & ~(size_t)255; return o; };
-    size_t o_rng = take(8 * P), o_pix = take(4 * P), o_frame = take(4 * P), o_T = take(12 * P),
-           o_col = take(12 * P), o_b = take(4 * P), o_fl = take(4 * P), o_ior = take(4 * P),
-           o_r0 = take(32 * P), o_r1 = take(32 * P), o_q0 = take(4 * P), o_q1 = take(4 * P),
-           o_hit = take(16 * P), o_cray = take(64 * P), o_crec = take(64 * P), o_cnt = take(sizeof(WaveCounters));
+    Wavefront sizing;
+    size_t bytes = carve_wave(nullptr, cap, &sizing);
     char *a = nullptr;
     CUDA_TRY(c, cudaMalloc((void **)&a, bytes));
-    Wavefront &w = c->wave;
-    w.arena = a;
-    w.arena_bytes = bytes;
-    w.capacity = cap;
-    w.p.rng = (uint64_t *)(a + o_rng);
-    w.p.pixel = (uint32_t *)(a + o_pix);
-    w.p.frame = (uint32_t *)(a + o_frame);
-    w.p.T = (float *)(a + o_T);
-    w.p.color = (float *)(a + o_col);
-    w.p.bounces = (uint32_t *)(a + o_b);
-    w.p.flags = (uint32_t *)(a + o_fl);
-    w.p.iori = (float *)(a + o_ior);
-    w.ray[0] = (float4 *)(a + o_r0);
-    w.ray[1] = (float4 *)(a + o_r1);
-    w.queue[0] = (uint32_t *)(a + o_q0);
-    w.queue[1] = (uint32_t *)(a + o_q1);
-    w.hits = (float4 *)(a + o_hit);
-    w.cray = (float4 *)(a + o_cray);
-    w.crec = (float4 *)(a + o_crec);
-    w.counters = (WaveCounters *)(a + o_cnt);
+    carve_wave(a, cap, &c->wave);
+    c->wave.arena = a;
+    c->wave.arena_bytes = bytes;
     return LT_OK;
 }
 
@@ -435,28 +439,9 @@ lt_status lt_scene_load_json(lt_ctx *c, const char *path) {
 #include "lt_noalloc.h"
 
 static Wavefront carve_noalloc(char *a, uint32_t cap) {
-    size_t P = cap, off = 0;
-    auto take = [&](size_t n) { size_t o = off; off += (n + 255) & ~(size_t)255; return a + o; };
     Wavefront w;
-    w.capacity = cap;
-    w.p.rng = (uint64_t *)take(8 * P);
-    w.p.pixel = (uint32_t *)take(4 * P);
-    w.p.frame = (uint32_t *)take(4 * P);
-    w.p.T = (float *)take(12 * P);
-    w.p.color = (float *)take(12 * P);
-    w.p.bounces = (uint32_t *)take(4 * P);
-    w.p.flags = (uint32_t *)take(4 * P);
-    w.p.iori = (float *)take(4 * P);
-    w.ray[0] = (float4 *)take(32 * P);
-    w.ray[1] = (float4 *)take(32 * P);
-    w.queue[0] = (uint32_t *)take(4 * P);
-    w.queue[1] = (uint32_t *)take(4 * P);
-    w.hits = (float4 *)take(16 * P);
-    w.cray = (float4 *)take(64 * P);
-    w.crec = (float4 *)take(64 * P);
-    w.counters = (WaveCounters *)take(sizeof(WaveCounters));
+    w.arena_bytes = carve_wave(a, cap, &w);
     w.arena = nullptr;  // not owned: never freed
-    w.arena_bytes = off;
     return w;
 }
 
@@ -495,6 +480,9 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
     } else if (a.total > 0) {
         uint32_t cap = (uint32_t)(a.total < paths_in_flight ? a.total : paths_in_flight);
         Wavefront w = carve_noalloc((char *)scratch, cap);
+        if (w.arena_bytes > kNoAllocScratchBytes)
+            return fail(c, LT_ERR_INVALID, "internal: wavefront needs %zu bytes, fixed scratch holds %zu", w.arena_bytes,
+                        kNoAllocScratchBytes);
         // the array keeps the previous call's contents: the counters must start at zero
         CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
         CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));

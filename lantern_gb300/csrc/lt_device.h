@@ -29,7 +29,10 @@ struct DevScene {
     TentFilter filter;
 };
 
-// Path state, structure of arrays over `capacity` path slots.
+// Path state, structure of arrays over `capacity` entries. It is kept in
+// queue order: shade reads entry q of the current buffer and writes the
+// surviving path to its compacted position in the other one, so every access
+// is coalesced.
 struct PathState {
     uint64_t *rng;     // PCG32 state (increment = frame | 1)
     uint32_t *pixel;
@@ -54,9 +57,8 @@ struct WaveCounters {
 
 struct Wavefront {
     uint32_t capacity = 0;
-    PathState p{};
+    PathState p[2] = {};                    // ping-pong, in queue order
     float4 *ray[2] = {nullptr, nullptr};    // 2 float4 per entry: (org, tnear) (dir, tfar)
-    uint32_t *queue[2] = {nullptr, nullptr};
     float4 *hits = nullptr;                 // (t, u, v, prim bits)
     float4 *cray = nullptr;                 // 2 float4 per record: (org, kind|light) (dir, pixel)
     float4 *crec = nullptr;                 // 2 float4 per record: (f, bsdf pdf) (throughput, -)

@@ -23,6 +23,9 @@ namespace {
 constexpr int kStack = 64;
 constexpr uint32_t kLobeNull = 0, kLobeSRefl = 1, kLobeSTrans = 2, kLobeDiffuse = 4, kLobeSpecular = 3;
 constexpr uint32_t kConnectBsdf = 0x80000000u;
+// Lights with at most this many triangles are tested triangle by triangle
+// before a connection ray is traced.
+constexpr uint32_t kLightBrute = 16;
 
 __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
 
@@ -185,6 +188,20 @@ __device__ __forceinline__ v3 interp_normal(const DevScene &S, uint32_t prim, fl
     v3 n2 = mk(__ldg(S.vnormal + 3 * i2), __ldg(S.vnormal + 3 * i2 + 1), __ldg(S.vnormal + 3 * i2 + 2));
     float w = 1.0f - u - v;
     return (n0 * w + n1 * u) + n2 * v;
+}
+
+// Distance to the closest of the light's own triangles along (org, dir), t in
+// (0.001, inf): 0 when the ray misses the light, -1 when the light has more
+// than kLightBrute triangles and was not tested. `out` (optional) gets the hit.
+__device__ __forceinline__ float light_distance(const DevScene &S, const LightInfo &L, v3 org, v3 dir, Hit *out) {
+    if (L.tri_count > kLightBrute) return -1.0f;
+    Hit lh;
+    lh.t = __int_as_float(0x7f800000);
+    lh.u = lh.v = 0.0f;
+    lh.prim = kMiss;
+    for (uint32_t k = 0; k < L.tri_count; ++k) tri_test(S.light_tris + 3 * (L.tri_first + k), org, dir, 0.001f, lh);
+    if (out) *out = lh;
+    return lh.prim == kMiss ? 0.0f : lh.t;
 }
 
 // warp-aggregated slot reservation: returns this lane's index (valid if pred)
@@ -360,8 +377,7 @@ __global__ void __launch_bounds__(128) k_raygen(DevScene S, Wavefront W, RenderA
         v3 o, d;
         float tn;
         start_path(S, A, i, p, o, d, tn);
-        store_path(W.p, W.capacity, i, p);
-        W.queue[0][i] = i;
+        store_path(W.p[0], W.capacity, i, p);
         write_ray(W.ray[0], i, o, tn, d);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -399,15 +415,17 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, Wavefront W, int cur)
 }
 
 // One iteration of the bounce loop of Integrator::RenderPixel (integrator.cpp:115-243).
-__global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderArgs A, FilmPtrs F, int cur) {
+// Occupancy hint: at most 64 registers (8 blocks of 128 threads per SM), so that
+// more warps hide the latency of the scattered normal / material loads.
+__global__ void __launch_bounds__(128, 8) k_shade(DevScene S, Wavefront W, RenderArgs A, FilmPtrs F, int cur) {
     const uint32_t n = W.counters->count[cur];
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->connect_fetch = 0;
+    uint32_t n_ref_rays = 0, n_ref_rays_b = 0;  // connection rays the reference would trace
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         uint32_t q = base + threadIdx.x;
         bool active = q < n;
-        uint32_t slot = 0;
         Path p;
         bool done = false, push = false;
         v3 norg = mk(0, 0, 0), ndir = mk(0, 0, 0);
@@ -415,12 +433,11 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
         // connection records (light sample, BSDF-MIS sample)
         bool emit_l = false, emit_b = false;
         v3 l_dir = mk(0, 0, 0), b_dir = mk(0, 0, 0), l_f = mk(0, 0, 0), b_f = mk(0, 0, 0), conn_org = mk(0, 0, 0);
-        float l_pdf = 0.0f, b_pdf = 0.0f;
+        float l_pdf = 0.0f, b_pdf = 0.0f, l_tl = 0.0f, b_tl = 0.0f;
         uint32_t conn_light = 0;
         v3 conn_T = mk(0, 0, 0);
         if (active) {
-            slot = W.queue[cur][q];
-            load_path(W.p, cap, slot, p);
+            load_path(W.p[cur], cap, q, p);
             float4 hv = W.hits[q];
             float4 r0 = W.ray[cur][2 * q], r1 = W.ray[cur][2 * q + 1];
             uint32_t prim = __float_as_uint(hv.w);
@@ -506,14 +523,20 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
                             v3 point = rotate_to_world(x, y, dist - L.sphere[3], cn);
                             v3 ldir = normalize(point);
                             c.wi = ldir;
-                            if (dot(ldir, c.N) > 0.0f && !is_black(Le)) {
+                            if (dot(ldir, c.N) > 0.0f) {
+                                n_ref_rays++;  // the reference traces this ray (area_light.cpp:58)
                                 v3 f = bsdf_eval(m, c);
                                 float spdf = bsdf_pdf(m, c);
-                                if (spdf != 0.0f && !is_black(f)) {
-                                    emit_l = true;
-                                    l_dir = ldir;
-                                    l_f = f;
-                                    l_pdf = spdf;
+                                if (!is_black(Le) && spdf != 0.0f && !is_black(f)) {
+                                    // a ray that misses the light's own triangles cannot contribute
+                                    float tl = light_distance(S, L, c.P, ldir, nullptr);
+                                    if (tl != 0.0f) {
+                                        emit_l = true;
+                                        l_dir = ldir;
+                                        l_f = f;
+                                        l_pdf = spdf;
+                                        l_tl = tl;
+                                    }
                                 }
                             }
                         }
@@ -522,10 +545,15 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
                         float spdf = bsdf_pdf(m, c);
                         // AreaLight::PdfLi horizon test (area_light.cpp:76-78)
                         if (spdf != 0.0f && !is_black(f) && dot(c.wi, c.N) > 0.0f) {
-                            emit_b = true;
-                            b_dir = c.wi;
-                            b_f = f;
-                            b_pdf = spdf;
+                            n_ref_rays_b++;  // the reference traces this ray (area_light.cpp:100)
+                            float tl = light_distance(S, L, c.P, c.wi, nullptr);
+                            if (tl != 0.0f) {
+                                emit_b = true;
+                                b_dir = c.wi;
+                                b_f = f;
+                                b_pdf = spdf;
+                                b_tl = tl;
+                            }
                         }
                     }
                     // main path BSDF sample (integrator.cpp:199-209)
@@ -562,7 +590,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
                 W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light));
                 W.cray[2 * idx + 1] = make_float4(l_dir.x, l_dir.y, l_dir.z, __uint_as_float(p.pixel));
                 W.crec[2 * idx] = make_float4(l_f.x, l_f.y, l_f.z, l_pdf);
-                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, 0.0f);
+                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, l_tl);
             }
             idx = warp_reserve(&W.counters->ccount, emit_b);
             if (emit_b) {
@@ -570,11 +598,11 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
                                               __uint_as_float(conn_light | kConnectBsdf));
                 W.cray[2 * idx + 1] = make_float4(b_dir.x, b_dir.y, b_dir.z, __uint_as_float(p.pixel));
                 W.crec[2 * idx] = make_float4(b_f.x, b_f.y, b_f.z, b_pdf);
-                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, 0.0f);
+                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, b_tl);
             }
         }
-        // finished paths: film write (integrator.cpp:245-249), then the slot takes
-        // the next work item
+        // finished paths: film write (integrator.cpp:245-249); the thread then
+        // starts the next work item in their place
         bool regen = false;
         if (done) {
             film_add(F, p.pixel, p.color);
@@ -589,10 +617,18 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
         bool enqueue = push || regen;
         uint32_t qi = warp_reserve(&W.counters->count[nxt], enqueue);
         if (enqueue) {
-            W.queue[nxt][qi] = slot;
             write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
+            store_path(W.p[nxt], cap, qi, p);
         }
-        if (active) store_path(W.p, cap, slot, p);
+    }
+    // ray tallies in the reference's terms (every SampleLi / PdfLi trace), one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) {
+        n_ref_rays += __shfl_xor_sync(0xFFFFFFFFu, n_ref_rays, o);
+        n_ref_rays_b += __shfl_xor_sync(0xFFFFFFFFu, n_ref_rays_b, o);
+    }
+    if ((threadIdx.x & 31u) == 0 && (n_ref_rays | n_ref_rays_b)) {
+        atomicAdd(&W.counters->light_rays, (unsigned long long)n_ref_rays);
+        atomicAdd(&W.counters->bsdf_rays, (unsigned long long)n_ref_rays_b);
     }
 }
 
@@ -601,22 +637,19 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, Wavefront W, RenderAr
 //
 // The reference takes the closest hit in the whole scene and keeps it if it
 // lies on the chosen light. The same answer (up to exact distance ties between
-// the light and an occluder) comes cheaper in two steps: the closest hit among
-// the light's own triangles first -- a ray that misses the light contributes
-// nothing and is never traversed -- then an occlusion query up to that distance
-// that ignores the light's own geometry. Lights with more than kLightBrute
-// triangles use the full closest-hit query instead.
-constexpr uint32_t kLightBrute = 16;
-
+// the light and an occluder) comes cheaper in two steps: k_shade finds the
+// closest hit among the light's own triangles and emits only rays that reach
+// the light, with that distance; here an occlusion query up to the distance,
+// ignoring the light's own geometry, decides the rest. Lights with more than
+// kLightBrute triangles (distance -1 in the record) use a full closest-hit query.
 __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wavefront &W, const FilmPtrs &F,
-                                                   uint32_t idx, uint32_t kl, uint32_t pixel, const Trav &r,
-                                                   const Hit &lh) {
+                                                   uint32_t idx, uint32_t kl, uint32_t pixel, const Trav &r) {
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
     const LightInfo &L = S.lights[kl & ~kConnectBsdf];
     Hit h;
     if (r.any) {
         if (r.h.prim != kMiss) return;  // occluded
-        h = lh;
+        light_distance(S, L, r.O, r.D, &h);  // the same light hit k_shade found
     } else {
         if (r.h.prim == kMiss || __ldg(S.tri_geom + r.h.prim) != (uint32_t)L.geom) return;
         h = r.h;
@@ -643,49 +676,27 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 __global__ void __launch_bounds__(128) k_connect(DevScene S, Wavefront W, FilmPtrs F) {
     const uint32_t n = W.counters->ccount;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
-    uint32_t n_all = 0, n_bsdf = 0, n_trav = 0;
+    uint32_t n_trav = 0;
     Trav r;
     r.node = kSentinel;
-    Hit lh;
     uint32_t idx = 0, kl = 0, pixel = 0;
-    bool pending = false;
     for (;;) {
         if (r.node == kSentinel) {
             idx = fetch_next(&W.counters->connect_fetch);
             if (idx >= n) break;
             float4 a = ldg4(W.cray + 2 * idx), b = ldg4(W.cray + 2 * idx + 1);
-            v3 org = mk(a.x, a.y, a.z), dir = mk(b.x, b.y, b.z);
+            float tl = ldg4(W.crec + 2 * idx + 1).w;
             kl = __float_as_uint(a.w);
             pixel = __float_as_uint(b.w);
-            n_all++;
-            n_bsdf += (kl & kConnectBsdf) != 0;
             const LightInfo &L = S.lights[kl & ~kConnectBsdf];
-            if (L.tri_count <= kLightBrute) {
-                lh.t = __int_as_float(0x7f800000);
-                lh.u = lh.v = 0.0f;
-                lh.prim = kMiss;
-                for (uint32_t k = 0; k < L.tri_count; ++k)
-                    tri_test(S.light_tris + 3 * (L.tri_first + k), org, dir, 0.001f, lh);
-                if (lh.prim == kMiss) continue;  // misses the light: no contribution, no traversal
-                trav_start(r, org, dir, 0.001f, lh.t, true, (uint32_t)L.geom);
-            } else {
-                trav_start(r, org, dir, 0.001f, __int_as_float(0x7f800000), false, 0);
-            }
+            if (tl > 0.0f) trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, tl, true, (uint32_t)L.geom);
+            else trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, __int_as_float(0x7f800000), false, 0);
             n_trav++;
-            pending = true;
         }
         traverse(S, r);
-        if (r.node == kSentinel && pending) {
-            resolve_connection(S, W, F, idx, kl, pixel, r, lh);
-            pending = false;
-        }
+        if (r.node == kSentinel) resolve_connection(S, W, F, idx, kl, pixel, r);
     }
-    // tallies of connection rays by kind, one atomic per lane with work
-    if (n_all) {
-        atomicAdd(&W.counters->bsdf_rays, (unsigned long long)n_bsdf);
-        atomicAdd(&W.counters->light_rays, (unsigned long long)(n_all - n_bsdf));
-        atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
-    }
+    if (n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
 }
 
 // counts += spp for every pixel (render with max_depth 0: the bounce loop never runs)
