@@ -116,6 +116,13 @@ typedef struct lt_scene_desc {
  * sphere and radiance the way AddLMF and AreaLight's constructor do. */
 lt_status lt_scene_create(lt_ctx *ctx, const lt_scene_desc *desc);
 
+/* Which builder lt_scene_create uses for the BVH (rtcCommitScene's job):
+ * LT_BVH_GPU (default) -- binned SAH (32 bins, <= 4 triangles per leaf) built
+ * level by level on the device; LT_BVH_HOST -- the same algorithm on the host
+ * CPU. Both make the same splits. */
+enum { LT_BVH_GPU = 0, LT_BVH_HOST = 1 };
+lt_status lt_set_bvh_builder(lt_ctx *ctx, int32_t builder);
+
 /* Scene::LoadSceneFromJSON (scene.h:71): reads a Lantern scene JSON and the
  * LMF files it names (triangle LMF, transform, constant albedo, media,
  * emission), then lt_scene_create. */

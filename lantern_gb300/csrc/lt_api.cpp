@@ -16,6 +16,7 @@
 
 #include "lantern_gpu.h"
 #include "lt_device.h"
+#include "lt_bvh_gpu.h"
 #include "lt_scene.h"
 
 using namespace lt;
@@ -33,6 +34,8 @@ struct lt_ctx {
     DevScene dev{};
     std::vector<void *> scene_allocs;
     uint64_t scene_bytes = 0;
+    uint32_t num_nodes = 0;
+    int32_t bvh_builder = LT_BVH_GPU;
 
     // wavefront
     Wavefront wave;
@@ -141,6 +144,13 @@ lt_status lt_set_stream(lt_ctx *c, void *stream) {
 
 void *lt_get_stream(const lt_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+lt_status lt_set_bvh_builder(lt_ctx *c, int32_t builder) {
+    if (!c) return LT_ERR_INVALID;
+    if (builder != LT_BVH_GPU && builder != LT_BVH_HOST) return fail(c, LT_ERR_INVALID, "unknown BVH builder %d", builder);
+    c->bvh_builder = builder;
+    return LT_OK;
+}
+
 lt_status lt_sync(lt_ctx *c) {
     if (!c) return LT_ERR_INVALID;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -171,18 +181,44 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     std::string err;
     lt_status st = build_host_scene(desc, &c->host, &err);
     if (st != LT_OK) return fail(c, st, "%s", err.c_str());
-    build_bvh(&c->host);
-    if (c->host.max_depth >= 64)
-        return fail(c, LT_ERR_UNSUPPORTED, "BVH depth %u exceeds the traversal stack", c->host.max_depth);
     HostScene &h = c->host;
     DevScene &d = c->dev;
-    const float *nodes = nullptr, *tris = nullptr;
-    std::vector<float> nodes_f(h.nodes.size() * 16);
-    memcpy(nodes_f.data(), h.nodes.data(), nodes_f.size() * sizeof(float));
-    if ((st = upload(c, nodes_f, &nodes)) != LT_OK) return st;
-    if ((st = upload(c, h.leaf_tris, &tris)) != LT_OK) return st;
-    d.nodes = (const float4 *)nodes;
-    d.tris = (const float4 *)tris;
+    const size_t ntri = h.tri_geom.size();
+    if (c->bvh_builder == LT_BVH_GPU && ntri > 4) {
+        // binned-SAH build on the device from the triangles in global order
+        const float *tri = nullptr;
+        if ((st = upload(c, h.tri_v0e1e2, &tri)) != LT_OK) return st;
+        GpuBvh gb;
+        cudaError_t e = build_bvh_gpu(tri, (uint32_t)ntri, &gb, c->stream);
+        cudaFree((void *)tri);
+        c->scene_allocs.pop_back();
+        c->scene_bytes -= h.tri_v0e1e2.size() * sizeof(float);
+        if (e != cudaSuccess)
+            return fail(c, e == cudaErrorMemoryAllocation ? LT_ERR_OOM : LT_ERR_CUDA, "GPU BVH build: %s",
+                        cudaGetErrorString(e));
+        c->scene_allocs.push_back(gb.nodes);
+        c->scene_allocs.push_back(gb.leaf_tris);
+        c->scene_bytes += (uint64_t)gb.num_nodes * 64 + (uint64_t)ntri * 48;
+        d.nodes = (const float4 *)gb.nodes;
+        d.tris = (const float4 *)gb.leaf_tris;
+        h.nodes.clear();
+        h.leaf_tris.clear();
+        h.max_depth = gb.max_depth;
+        h.build_ms = gb.build_ms;
+        c->num_nodes = gb.num_nodes;
+    } else {
+        build_bvh(&c->host);
+        const float *nodes = nullptr, *tris = nullptr;
+        std::vector<float> nodes_f(h.nodes.size() * 16);
+        memcpy(nodes_f.data(), h.nodes.data(), nodes_f.size() * sizeof(float));
+        if ((st = upload(c, nodes_f, &nodes)) != LT_OK) return st;
+        if ((st = upload(c, h.leaf_tris, &tris)) != LT_OK) return st;
+        d.nodes = (const float4 *)nodes;
+        d.tris = (const float4 *)tris;
+        c->num_nodes = (uint32_t)h.nodes.size();
+    }
+    if (h.max_depth >= 64)
+        return fail(c, LT_ERR_UNSUPPORTED, "BVH depth %u exceeds the traversal stack", h.max_depth);
     if ((st = upload(c, h.tri_geom, &d.tri_geom)) != LT_OK) return st;
     if ((st = upload(c, h.tri_vidx, &d.tri_vidx)) != LT_OK) return st;
     if ((st = upload(c, h.vnormal, &d.vnormal)) != LT_OK) return st;
@@ -211,7 +247,7 @@ lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) {
     out->num_triangles = (uint32_t)c->host.tri_geom.size();
     out->num_meshes = (uint32_t)c->host.geoms.size();
     out->num_lights = (uint32_t)c->host.lights.size();
-    out->num_bvh_nodes = (uint32_t)c->host.nodes.size();
+    out->num_bvh_nodes = c->num_nodes;
     out->device_bytes = c->scene_bytes;
     out->build_ms = c->host.build_ms;
     return LT_OK;

@@ -52,7 +52,7 @@ struct alignas(16) LightInfo {
 // ref >= 0: inner node index; ref < 0: leaf, ~ref = (first triangle in leaf
 // order) << 3 | triangle count.
 constexpr uint32_t kLeafBits = 3;
-inline int32_t leaf_ref(uint32_t first, uint32_t count) { return ~(int32_t)((first << kLeafBits) | count); }
+LT_HD int32_t leaf_ref(uint32_t first, uint32_t count) { return ~(int32_t)((first << kLeafBits) | count); }
 
 struct alignas(16) BvhNode {
     float a[4], b[4], c[4];

@@ -23,7 +23,8 @@ MISS = 0xFFFFFFFF
 SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error", "lt_set_stream", "lt_get_stream",
            "lt_sync",
            "lt_scene_create", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
-           "lt_render_stats_get", "lt_intersect", "lt_render_noalloc"]
+           "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder"]
+BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 
 
@@ -118,6 +119,7 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_render_stats_get.argtypes = [p, C.POINTER(RenderStats)]
         L.lt_intersect.argtypes = [p, p, p, C.c_uint64, C.c_int32]
         L.lt_render_noalloc.argtypes = [p, C.POINTER(RenderParams), C.POINTER(Film), C.c_uint32]
+        L.lt_set_bvh_builder.argtypes = [p, C.c_int32]
         _lib = L
         return L
 
@@ -162,6 +164,10 @@ class Context:
 
     def sync(self):
         self._check(self.L.lt_sync(self.h))
+
+    def set_bvh_builder(self, builder: int):
+        """BVH_GPU (default) or BVH_HOST for the next scene load."""
+        self._check(self.L.lt_set_bvh_builder(self.h, builder))
 
     def load_scene_json(self, path: str):
         self._check(self.L.lt_scene_load_json(self.h, os.path.abspath(path).encode()))

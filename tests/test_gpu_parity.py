@@ -164,3 +164,26 @@ def test_errors_are_reported(ctx, scene_dir, tmp_path):
         render_host(c, 9, 8, 1)
     assert e.value.status == 1  # LT_ERR_INVALID: film size
     c.close()
+
+
+@pytest.mark.parametrize("make", [
+    lambda: S.nine_spheres(width=64, height=64, name="isect_nine"),
+    lambda: S.displaced_icosphere_scene(width=64, height=64, levels=6, name="isect_ico6"),
+])
+def test_gpu_bvh_build_matches_host_build(scene_dir, make):
+    """The device builder makes the host builder's splits: same node count and
+    depth, and closest hits identical to the oracle's."""
+    from lantern_gb300.native import BVH_GPU, BVH_HOST
+    path = make().write(scene_dir)
+    orc, rays = _scene_rays(path, 1 << 15, seed=11)
+    oh = orc.intersect(rays)
+    infos = {}
+    for builder in (BVH_HOST, BVH_GPU):
+        c = Context(0)
+        c.set_bvh_builder(builder)
+        c.load_scene_json(path)
+        infos[builder] = c.scene_info()
+        _compare_hits(intersect(c, rays), oh)
+        c.close()
+    assert infos[BVH_GPU].num_bvh_nodes == infos[BVH_HOST].num_bvh_nodes
+    assert infos[BVH_GPU].num_triangles == infos[BVH_HOST].num_triangles
