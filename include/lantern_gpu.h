@@ -134,6 +134,7 @@ typedef struct lt_scene_info {
     uint32_t num_bvh_nodes;
     uint64_t device_bytes;    /* scene + BVH bytes on the device */
     float build_ms;           /* BVH build time */
+    uint32_t num_media;
 } lt_scene_info;
 lt_status lt_scene_info_get(lt_ctx *ctx, lt_scene_info *out);
 
@@ -204,6 +205,45 @@ typedef struct lt_render_stats {
     float connect_ms;        /* ... in the connection trace + resolve kernel */
 } lt_render_stats;
 lt_status lt_render_stats_get(lt_ctx *ctx, lt_render_stats *out);
+
+/* ---------------------------------------------------------------- differentiable rendering */
+/* Extension with no counterpart in the reference: gradients of an image loss
+ * with respect to per-triangle albedo, per-triangle emission and per-medium
+ * sigma_a / sigma_s, by path replay (each sample is re-traced from its
+ * (pixel, frame) seed; no path is stored).
+ *
+ * The differentiable estimator is the render loop with per-triangle albedo and
+ * emission (emission counts on emissive meshes only), the RGB medium form
+ * (distance sampled with the mean of the detached sigma_s; isotropic media
+ * sample with the detached sigma_s[0]), and the roulette probability taken from
+ * a throughput computed with the detached parameter copies. With the detached
+ * copies equal to the parameters it traces the same paths as lt_render.
+ * All arrays are device memory. */
+typedef struct lt_diff_params {
+    const float *albedo;            /* num_triangles * 3 */
+    const float *emission;          /* num_triangles * 3 (radiance) */
+    const float *sigma_a;           /* num_media * 3 */
+    const float *sigma_s;           /* num_media * 3 */
+    const float *albedo_detached;   /* sampling copies; NULL = the parameters themselves */
+    const float *sigma_a_detached;
+    const float *sigma_s_detached;
+} lt_diff_params;
+
+/* The scene's own values as parameters, into HOST arrays of num_triangles*3
+ * (albedo, emission) and num_media*3 (sigma_a, sigma_s). */
+lt_status lt_diff_defaults(lt_ctx *ctx, float *albedo, float *emission, float *sigma_a, float *sigma_s);
+
+/* Forward render of the differentiable estimator into a device film
+ * (additive, as lt_render). */
+lt_status lt_render_diff(lt_ctx *ctx, const lt_render_params *params, const lt_diff_params *dp, lt_film *film);
+
+/* Adjoint: given d_loss_d_film (W*H*3, derivative of the loss with respect to
+ * the film's colour sums) adds d loss / d parameter to the four gradient arrays
+ * (same shapes as the parameters; not cleared). crop = {x0, y0, x1, y1} limits
+ * the pixels whose samples are replayed, or NULL for the whole film. */
+lt_status lt_render_adjoint(lt_ctx *ctx, const lt_render_params *params, const lt_diff_params *dp,
+                            const float *d_loss_d_film, float *grad_albedo, float *grad_emission,
+                            float *grad_sigma_a, float *grad_sigma_s, const uint32_t *crop);
 
 /* ---------------------------------------------------------------- rays */
 typedef struct lt_ray { float org[3]; float tnear; float dir[3]; float tfar; } lt_ray; /* 32 B */

@@ -248,6 +248,7 @@ lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) {
     out->num_meshes = (uint32_t)c->host.geoms.size();
     out->num_lights = (uint32_t)c->host.lights.size();
     out->num_bvh_nodes = c->num_nodes;
+    out->num_media = (uint32_t)c->host.media.size();
     out->device_bytes = c->scene_bytes;
     out->build_ms = c->host.build_ms;
     return LT_OK;
@@ -452,6 +453,93 @@ lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, 
     CUDA_TRY(c, launch_intersect(c->dev, dr, dh, n, c->isect_fetch, c->shape, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(hits, dh, n * 16, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return LT_OK;
+}
+
+lt_status lt_diff_defaults(lt_ctx *c, float *albedo, float *emission, float *sigma_a, float *sigma_s) {
+    if (!c) return LT_ERR_INVALID;
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
+    const HostScene &h = c->host;
+    for (size_t t = 0; t < h.tri_geom.size(); ++t) {
+        const GeomInfo &g = h.geoms[h.tri_geom[t]];
+        const MaterialInfo &m = h.materials[g.material];
+        for (int k = 0; k < 3; ++k) {
+            if (albedo) albedo[3 * t + k] = m.albedo[k];
+            if (emission) emission[3 * t + k] = g.light >= 0 ? h.lights[g.light].radiance[k] : 0.0f;
+        }
+    }
+    for (size_t i = 0; i < h.media.size(); ++i)
+        for (int k = 0; k < 3; ++k) {
+            if (sigma_a) sigma_a[3 * i + k] = h.media[i].sigma_a[k];
+            if (sigma_s) sigma_s[3 * i + k] = h.media[i].sigma_s[k];
+        }
+    return LT_OK;
+}
+
+static lt_status diff_setup(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, DiffParams *P,
+                            RenderArgs *a) {
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
+    if (!dp->albedo || !dp->emission || (c->host.media.size() && (!dp->sigma_a || !dp->sigma_s)))
+        return fail(c, LT_ERR_INVALID, "differentiable parameters missing");
+    P->albedo = dp->albedo;
+    P->emission = dp->emission;
+    P->sigma_a = dp->sigma_a;
+    P->sigma_s = dp->sigma_s;
+    P->albedo_s = dp->albedo_detached ? dp->albedo_detached : dp->albedo;
+    P->sigma_a_s = dp->sigma_a_detached ? dp->sigma_a_detached : dp->sigma_a;
+    P->sigma_s_s = dp->sigma_s_detached ? dp->sigma_s_detached : dp->sigma_s;
+    a->width = c->host.camera.width;
+    a->height = c->host.camera.height;
+    a->first_frame = p->first_frame;
+    a->max_depth = p->max_depth;
+    a->rr_depth = p->rr_depth;
+    a->total = (unsigned long long)a->width * a->height * p->spp;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    return LT_OK;
+}
+
+lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, lt_film *film) {
+    if (!c || !p || !dp || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
+    DiffParams P;
+    RenderArgs a;
+    lt_status st = diff_setup(c, p, dp, &P, &a);
+    if (st != LT_OK) return st;
+    if (!film->on_device || film->width != a.width || film->height != a.height)
+        return fail(c, LT_ERR_INVALID, "lt_render_diff needs a device film of the camera's size");
+    FilmPtrs f{film->rgb, film->bounces, film->counts};
+    c->stats = lt_render_stats{};
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    CUDA_TRY(c, launch_diff_forward(c->dev, P, a, f, c->shape, c->stream));
+    CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    c->stats.samples = a.total;
+    c->stats.kernel_launches = 1;
+    return LT_OK;
+}
+
+lt_status lt_render_adjoint(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, const float *dI,
+                            float *g_albedo, float *g_emission, float *g_sigma_a, float *g_sigma_s,
+                            const uint32_t *crop) {
+    if (!c || !p || !dp || !dI || !g_albedo || !g_emission) return fail(c, LT_ERR_INVALID, "NULL argument");
+    DiffParams P;
+    RenderArgs a;
+    lt_status st = diff_setup(c, p, dp, &P, &a);
+    if (st != LT_OK) return st;
+    if (c->host.media.size() && (!g_sigma_a || !g_sigma_s)) return fail(c, LT_ERR_INVALID, "medium gradients missing");
+    DiffGrads G{dI, g_albedo, g_emission, g_sigma_a, g_sigma_s, 0, 0, a.width, a.height};
+    if (crop) {
+        if (crop[0] > crop[2] || crop[1] > crop[3] || crop[2] > a.width || crop[3] > a.height)
+            return fail(c, LT_ERR_INVALID, "crop outside the film");
+        G.x0 = crop[0];
+        G.y0 = crop[1];
+        G.x1 = crop[2];
+        G.y1 = crop[3];
+    }
+    c->stats = lt_render_stats{};
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    CUDA_TRY(c, launch_diff_adjoint(c->dev, P, a, G, (uint32_t)c->host.media.size(), c->shape, c->stream));
+    CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    c->stats.samples = a.total;
+    c->stats.kernel_launches = 1;
     return LT_OK;
 }
 

@@ -83,6 +83,23 @@ struct RenderArgs {
 struct LaunchShape {
     int sms = 0;
     int trace_blocks = 0, shade_blocks = 0, connect_blocks = 0, isect_blocks = 0;
+    int diff_blocks = 0;
+};
+
+// Parameters of the differentiable render (device arrays): per-triangle RGB
+// albedo and emission, per-medium RGB sigma_a / sigma_s, and the detached
+// copies that drive sampling (roulette throughput, medium distances).
+struct DiffParams {
+    const float *albedo, *emission, *sigma_a, *sigma_s;
+    const float *albedo_s, *sigma_a_s, *sigma_s_s;
+};
+
+// Adjoint inputs/outputs: d loss / d film colour sum per pixel (W*H*3), the
+// gradient arrays (accumulated), and the pixel rectangle [x0, x1) x [y0, y1).
+struct DiffGrads {
+    const float *dI;
+    float *albedo, *emission, *sigma_a, *sigma_s;
+    uint32_t x0, y0, x1, y1;
 };
 
 // launchers (lt_kernels.cu)
@@ -90,6 +107,10 @@ void query_launch_shape(int device, LaunchShape *out);
 cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
                              uint32_t *fetch, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st);
+cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
+                                const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const RenderArgs &a, const DiffGrads &g,
+                                uint32_t num_media, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
                              const LaunchShape &ls, cudaStream_t st);
 enum WaveStage { kStageTrace = 0, kStageShade = 1, kStageConnect = 2 };

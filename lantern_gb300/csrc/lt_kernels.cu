@@ -705,6 +705,288 @@ __global__ void k_add_counts(FilmPtrs F, uint32_t npix, uint32_t spp) {
         F.counts[i] += spp;
 }
 
+// ------------------------------------------------------------------ differentiable rendering
+// Extension with no reference counterpart: gradients of an image loss with
+// respect to per-triangle albedo, per-triangle emission and per-medium
+// sigma_a / sigma_s, by path replay (Vicini, Speierer, Jakob, "Path Replay
+// Backpropagation", SIGGRAPH 2021). The estimator is the render loop above with
+// three changes that make it a smooth function of the parameters: albedo and
+// emission come from per-triangle arrays, media use the RGB form (distance
+// sampled with the mean of a detached sigma_s, weight = transmittance x sigma_s
+// / pdf), and the roulette probability comes from a detached throughput Ts
+// computed with the detached parameter copies. At the detached values the
+// paths are the same as a plain render's; finite differences that keep the
+// detached copies fixed differentiate the same function as the adjoint.
+//
+// One thread replays one (pixel, frame) sample from its seed: pass 1 collects
+// the path's radiance I, pass 2 replays it again and, at every factor w that
+// depends on a parameter, adds delta * (I - C) * dlog(w)/dtheta, where C is the
+// radiance collected before w applies; every emission term e adds
+// delta * T * de/dtheta.
+
+constexpr int kMediaAcc = 4;  // media whose gradients are summed in registers
+
+__device__ __forceinline__ Hit trace_all(const DevScene &S, v3 O, v3 D, float tnear, float tfar, bool any,
+                                         uint32_t skip_geom) {
+    Trav r;
+    trav_start(r, O, D, tnear, tfar, any, skip_geom);
+    do {
+        traverse(S, r);
+    } while (r.node != kSentinel);
+    return r.h;
+}
+
+// Is the closest hit along (P, dir) on light L? On success h is the light hit.
+__device__ __forceinline__ bool diff_light_visible(const DevScene &S, const LightInfo &L, v3 P, v3 dir, Hit &h) {
+    float tl = light_distance(S, L, P, dir, &h);
+    if (tl == 0.0f) return false;
+    if (tl > 0.0f) return trace_all(S, P, dir, 0.001f, tl, true, (uint32_t)L.geom).prim == kMiss;
+    h = trace_all(S, P, dir, 0.001f, __int_as_float(0x7f800000), false, 0);
+    return h.prim != kMiss && __ldg(S.tri_geom + h.prim) == (uint32_t)L.geom;
+}
+
+__device__ __forceinline__ void add3(float *g, v3 v) {
+    if (v.x != 0.0f) atomicAdd(g, v.x);
+    if (v.y != 0.0f) atomicAdd(g + 1, v.y);
+    if (v.z != 0.0f) atomicAdd(g + 2, v.z);
+}
+
+__device__ __forceinline__ void add_medium(const DiffGrads &G, float *acc, int mi, v3 ga, v3 gs) {
+    if (mi < kMediaAcc) {
+        acc[6 * mi] += ga.x; acc[6 * mi + 1] += ga.y; acc[6 * mi + 2] += ga.z;
+        acc[6 * mi + 3] += gs.x; acc[6 * mi + 4] += gs.y; acc[6 * mi + 5] += gs.z;
+    } else {
+        add3(G.sigma_a + 3 * mi, ga);
+        add3(G.sigma_s + 3 * mi, gs);
+    }
+}
+
+template <bool kGrad>
+__device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads &G, const RenderArgs &A,
+                        unsigned long long item, v3 I, v3 delta, float *macc, uint32_t &bounces_out) {
+    Path p;
+    v3 org, dir;
+    float tnear;
+    start_path(S, A, item, p, org, dir, tnear);
+    v3 Ts = p.T;
+    v3 C = mk(0, 0, 0);
+    const float inf = __int_as_float(0x7f800000);
+    uint32_t bounces = 0;
+    for (; bounces < A.max_depth; ++bounces) {
+        Hit h = trace_all(S, org, dir, tnear, inf, false, 0);
+        if (h.prim == kMiss) {
+            C = C + p.T * S.background;
+            break;
+        }
+        const uint32_t prim = h.prim;
+        v3 origin = org, direction = normalize(dir);
+        bool hit_surface = true;
+        if (p.medium >= 0) {
+            const int mi = p.medium;
+            const MediumInfo M = S.meds[mi];
+            v3 sa = ld3(P.sigma_a + 3 * mi), ss = ld3(P.sigma_s + 3 * mi);
+            v3 sa_d = ld3(P.sigma_a_s + 3 * mi), ss_d = ld3(P.sigma_s_s + 3 * mi);
+            float dist;
+            bool scat = false;
+            v3 w, ws;
+            if (M.type == LT_MEDIUM_NON_SCATTERING) {
+                dist = h.t;
+                w = mk(expf(-sa.x * dist), expf(-sa.y * dist), expf(-sa.z * dist));
+                ws = mk(expf(-sa_d.x * dist), expf(-sa_d.y * dist), expf(-sa_d.z * dist));
+            } else {
+                float sbar = M.type == LT_MEDIUM_ISOTROPIC ? ss_d.x : (ss_d.x + ss_d.y + ss_d.z) / 3.0f;
+                dist = -logf(p.rng.next_float()) / sbar;
+                scat = dist < h.t;
+                if (!scat) dist = h.t;
+                w = mk(expf(-(sa.x + ss.x - sbar) * dist), expf(-(sa.y + ss.y - sbar) * dist),
+                       expf(-(sa.z + ss.z - sbar) * dist));
+                ws = mk(expf(-(sa_d.x + ss_d.x - sbar) * dist), expf(-(sa_d.y + ss_d.y - sbar) * dist),
+                        expf(-(sa_d.z + ss_d.z - sbar) * dist));
+                if (scat) {
+                    w = w * (ss / sbar);
+                    ws = ws * (ss_d / sbar);
+                }
+            }
+            if (kGrad) {
+                v3 R = (I - C) * delta;
+                v3 ga = R * (-dist);
+                v3 gs = mk(0, 0, 0);
+                if (M.type != LT_MEDIUM_NON_SCATTERING)
+                    gs = mk(R.x * (-dist + (scat ? 1.0f / ss.x : 0.0f)), R.y * (-dist + (scat ? 1.0f / ss.y : 0.0f)),
+                            R.z * (-dist + (scat ? 1.0f / ss.z : 0.0f)));
+                add_medium(G, macc, mi, ga, gs);
+            }
+            p.T = p.T * w;
+            Ts = Ts * ws;
+            if (scat) {
+                hit_surface = false;
+                org = origin + direction * dist;
+                dir = M.type == LT_MEDIUM_HG ? hg_sample(p.rng, direction, M.g) : uniform_sphere(p.rng);
+                tnear = 0.001f;
+            }
+        }
+        if (hit_surface) {
+            const GeomInfo Gi = S.geoms[__ldg(S.tri_geom + prim)];
+            const MaterialInfo m = S.mats[Gi.material];
+            const v3 alb = ld3(P.albedo + 3 * prim), alb_d = ld3(P.albedo_s + 3 * prim);
+            if ((bounces == 0 || (p.lobe & kLobeSpecular) != 0) && Gi.light >= 0) {
+                C = C + p.T * ld3(P.emission + 3 * prim);
+                if (kGrad) add3(G.emission + 3 * prim, p.T * delta);
+            }
+            Inter it;
+            it.P = origin + direction * h.t;
+            it.N = Gi.has_normals ? normalize(interp_normal(S, prim, h.u, h.v)) : normalize(mk(0, 0, 0));
+            it.wo = -direction;
+            it.ioro = 0.0f;
+            it.iori = p.iori;
+            it.lobe = p.lobe;
+            it.wi = mk(0, 0, 0);
+            const uint32_t nl = S.num_lights;
+            if (!(nl == 0 || (nl == 1 && Gi.light >= 0))) {
+                int li;
+                int guard = 0;
+                do {
+                    li = (int)p.rng.next_discrete(nl);
+                } while (li == Gi.light && ++guard < 1 << 20);
+                const LightInfo &L = S.lights[li];
+                const float fn = (float)nl;
+                Inter c = it;
+                if (m.bsdf == LT_BSDF_LAMBERT) {
+                    float x, y;
+                    sample_disc(p.rng, L.sphere[3], x, y);
+                    v3 cdir = mk(L.sphere[0], L.sphere[1], L.sphere[2]) - c.P;
+                    float dl = length(cdir);
+                    v3 point = rotate_to_world(x, y, dl - L.sphere[3], normalize(cdir));
+                    v3 ldir = normalize(point);
+                    c.wi = ldir;
+                    float cosl = dot(ldir, c.N);
+                    Hit lh;
+                    if (cosl > 0.0f && diff_light_visible(S, L, c.P, ldir, lh)) {
+                        float spdf = cosl * kInvPi;
+                        v3 ip = c.P + normalize(ldir) * lh.t;
+                        v3 dd = ip - c.P;
+                        float lpdf = dot(dd, dd) / (fabsf(dot(normalize(interp_normal(S, lh.prim, lh.u, lh.v)), -ldir)) * L.area);
+                        if (lpdf != 0.0f && spdf != 0.0f) {
+                            v3 Li = ld3(P.emission + 3 * lh.prim);
+                            v3 f = (alb * kInvPi) * cosl;
+                            float wgt = power_heuristic(lpdf, spdf);
+                            C = C + p.T * ((((f * Li) * wgt) / lpdf) * fn);
+                            if (kGrad) {
+                                v3 Td = p.T * delta;
+                                add3(G.albedo + 3 * prim, Td * (Li * (fn * (cosl * kInvPi) * wgt / lpdf)));
+                                add3(G.emission + 3 * lh.prim, Td * (f * (fn * wgt / lpdf)));
+                            }
+                        }
+                    }
+                }
+                bsdf_sample(m, c, p.rng);
+                float spdf = bsdf_pdf(m, c);
+                float cosb = dot(c.wi, c.N);
+                Hit bh;
+                if (spdf != 0.0f && cosb > 0.0f && diff_light_visible(S, L, c.P, c.wi, bh)) {
+                    v3 ip = c.P + normalize(c.wi) * bh.t;
+                    v3 dd = ip - c.P;
+                    float lpdf = dot(dd, dd) / (fabsf(dot(normalize(interp_normal(S, bh.prim, bh.u, bh.v)), c.wi)) * L.area);
+                    if (lpdf != 0.0f) {
+                        v3 Le = ld3(P.emission + 3 * bh.prim);
+                        float dfa = m.bsdf == LT_BSDF_LAMBERT ? kInvPi * cosb : 1.0f;  // f = albedo * dfa
+                        v3 f = m.bsdf == LT_BSDF_LAMBERT ? (alb * kInvPi) * cosb : alb;
+                        float wgt = power_heuristic(spdf, lpdf);
+                        C = C + p.T * ((((f * Le) * wgt) / spdf) * fn);
+                        if (kGrad) {
+                            v3 Td = p.T * delta;
+                            add3(G.albedo + 3 * prim, Td * (Le * (fn * dfa * wgt / spdf)));
+                            add3(G.emission + 3 * bh.prim, Td * (f * (fn * wgt / spdf)));
+                        }
+                    }
+                }
+            }
+            bsdf_sample(m, it, p.rng);
+            float pdf = bsdf_pdf(m, it);
+            v3 f = m.bsdf == LT_BSDF_LAMBERT ? (alb * kInvPi) * dot(it.wi, it.N) : alb;
+            v3 fs = m.bsdf == LT_BSDF_LAMBERT ? (alb_d * kInvPi) * dot(it.wi, it.N) : alb_d;
+            if (kGrad) {
+                v3 R = (I - C) * delta;
+                add3(G.albedo + 3 * prim, mk(alb.x > 0.0f ? R.x / alb.x : 0.0f, alb.y > 0.0f ? R.y / alb.y : 0.0f,
+                                             alb.z > 0.0f ? R.z / alb.z : 0.0f));
+            }
+            p.T = (p.T * f) / pdf;
+            Ts = (Ts * fs) / pdf;
+            if (it.lobe == kLobeSTrans) {
+                it.iori = it.ioro;
+                p.medium = m.medium;
+            }
+            p.iori = it.iori;
+            p.lobe = it.lobe;
+            org = it.P;
+            dir = it.wi;
+            tnear = 0.001f;
+        }
+        if (bounces > A.rr_depth) {
+            float pr = fmaxf(Ts.x, fmaxf(Ts.y, Ts.z));  // detached roulette probability
+            if (p.rng.next_float() > pr) break;
+            p.T = p.T * (1 / pr);
+            Ts = Ts * (1 / pr);
+        }
+    }
+    bounces_out = bounces;
+    return C;
+}
+
+// One thread per pixel, samples in frame order: the film is the same on every
+// run (finite differences of the loss see no summation-order noise).
+__global__ void __launch_bounds__(128) k_diff_forward(DevScene S, DiffParams P, RenderArgs A, FilmPtrs F) {
+    DiffGrads G{};
+    float macc[1];
+    const uint32_t npix = A.width * A.height;
+    const uint32_t spp = (uint32_t)(A.total / npix);
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
+        v3 sum = mk(0, 0, 0);
+        uint32_t bsum = 0;
+        for (uint32_t s = 0; s < spp; ++s) {
+            uint32_t b = 0;
+            sum = sum + diff_path<false>(S, P, G, A, (unsigned long long)s * npix + pixel, mk(0, 0, 0),
+                                         mk(0, 0, 0), macc, b);
+            bsum += b;
+        }
+        F.rgb[3 * (size_t)pixel] += sum.x;
+        F.rgb[3 * (size_t)pixel + 1] += sum.y;
+        F.rgb[3 * (size_t)pixel + 2] += sum.z;
+        F.bounces[pixel] += bsum;
+        F.counts[pixel] += spp;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, RenderArgs A, DiffGrads G,
+                                                     uint32_t num_media) {
+    float macc[6 * kMediaAcc];
+    for (int k = 0; k < 6 * kMediaAcc; ++k) macc[k] = 0.0f;
+    const uint32_t npix = A.width * A.height;
+    const uint32_t spp = (uint32_t)(A.total / npix);
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
+        uint32_t x = pixel % A.width, y = pixel / A.width;
+        if (x < G.x0 || x >= G.x1 || y < G.y0 || y >= G.y1) continue;
+        v3 delta = ld3(G.dI + 3 * (size_t)pixel);
+        if (is_black(delta)) continue;
+        for (uint32_t s = 0; s < spp; ++s) {
+            unsigned long long item = (unsigned long long)s * npix + pixel;
+            uint32_t b = 0;
+            v3 I = diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, b);
+            diff_path<true>(S, P, G, A, item, I, delta, macc, b);
+        }
+    }
+    // medium gradients: warp sums, one atomic per warp and component
+    for (int k = 0; k < 6 * kMediaAcc; ++k) {
+        if (k / 6 >= (int)num_media) break;
+        float v = macc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        if ((threadIdx.x & 31u) == 0 && v != 0.0f) {
+            int mi = k / 6, c = k % 6;
+            atomicAdd(c < 3 ? G.sigma_a + 3 * mi + c : G.sigma_s + 3 * mi + (c - 3), v);
+        }
+    }
+}
+
 }  // namespace
 
 void query_launch_shape(int device, LaunchShape *out) {
@@ -720,6 +1002,22 @@ void query_launch_shape(int device, LaunchShape *out) {
     out->connect_blocks = out->sms * (b > 0 ? b : 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_intersect, 128, 0);
     out->isect_blocks = out->sms * (b > 0 ? b : 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_diff_adjoint, 128, 0);
+    out->diff_blocks = out->sms * (b > 0 ? b : 1);
+}
+
+cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
+                                const LaunchShape &ls, cudaStream_t st) {
+    if (a.total == 0) return cudaSuccess;
+    k_diff_forward<<<ls.diff_blocks, 128, 0, st>>>(s, p, a, f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const RenderArgs &a, const DiffGrads &g,
+                                uint32_t num_media, const LaunchShape &ls, cudaStream_t st) {
+    if (a.total == 0) return cudaSuccess;
+    k_diff_adjoint<<<ls.diff_blocks, 128, 0, st>>>(s, p, a, g, num_media);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,

@@ -1,0 +1,131 @@
+"""Differentiable rendering: a torch.autograd.Function over lt_render_diff /
+lt_render_adjoint (path-replay backpropagation in liblantern_gpu.so).
+
+Parameters are CUDA tensors: per-triangle RGB albedo (T, 3), per-triangle RGB
+emission (T, 3; only emissive meshes' triangles emit), per-medium RGB sigma_a
+and sigma_s (M, 3). The forward pass renders the image (colour sum / spp); the
+backward pass replays every sample from its (pixel, frame) seed and returns the
+gradients of the loss with respect to all four tensors. Nothing per path is
+stored between the two passes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import native
+from .native import Context, Film, RenderParams
+
+
+class DiffParams(C.Structure):
+    _fields_ = [("albedo", C.c_void_p), ("emission", C.c_void_p), ("sigma_a", C.c_void_p),
+                ("sigma_s", C.c_void_p), ("albedo_detached", C.c_void_p), ("sigma_a_detached", C.c_void_p),
+                ("sigma_s_detached", C.c_void_p)]
+
+
+def _bind(L):
+    if getattr(L, "_diff_bound", False):
+        return
+    p = C.c_void_p
+    L.lt_diff_defaults.argtypes = [p, p, p, p, p]
+    L.lt_render_diff.argtypes = [p, C.POINTER(RenderParams), C.POINTER(DiffParams), C.POINTER(Film)]
+    L.lt_render_adjoint.argtypes = [p, C.POINTER(RenderParams), C.POINTER(DiffParams), p, p, p, p, p,
+                                    C.POINTER(C.c_uint32)]
+    L._diff_bound = True
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return None if t is None else t.data_ptr()
+
+
+def _dev(t: torch.Tensor, device) -> torch.Tensor:
+    return t.detach().to(device=device, dtype=torch.float32).contiguous()
+
+
+class DiffScene:
+    """A loaded scene plus the sizes of its differentiable parameters."""
+
+    def __init__(self, path: str, device: int = 0):
+        self.ctx = Context(device)
+        _bind(self.ctx.L)
+        self.ctx.load_scene_json(path)
+        info = self.ctx.scene_info()
+        self.width, self.height = info.width, info.height
+        self.num_triangles, self.num_media = info.num_triangles, info.num_media
+        self.device = torch.device(f"cuda:{device}")
+
+    def defaults(self):
+        """The scene's own values: (albedo, emission, sigma_a, sigma_s) CUDA tensors."""
+        T, M = self.num_triangles, max(self.num_media, 1)
+        a, e = np.zeros((T, 3), np.float32), np.zeros((T, 3), np.float32)
+        sa, ss = np.zeros((M, 3), np.float32), np.zeros((M, 3), np.float32)
+        native.check(self.ctx.L, self.ctx.h, self.ctx.L.lt_diff_defaults(
+            self.ctx.h, a.ctypes.data, e.ctypes.data, sa.ctypes.data, ss.ctypes.data))
+        return tuple(torch.from_numpy(x).to(self.device) for x in (a, e, sa, ss))
+
+    def _params(self, albedo, emission, sigma_a, sigma_s, detached=None):
+        keep = [_dev(albedo, self.device), _dev(emission, self.device), _dev(sigma_a, self.device),
+                _dev(sigma_s, self.device)]
+        det = [None, None, None]
+        if detached is not None:
+            det = [None if d is None else _dev(d, self.device) for d in detached]
+        keep += det
+        return keep, DiffParams(*[_ptr(k) for k in keep])
+
+    def render(self, albedo, emission, sigma_a, sigma_s, spp: int, first_frame: int = 0, max_depth: int = 8,
+               rr_depth: int = 3, detached=None):
+        """Film (rgb sum, bounces, counts) of the differentiable estimator.
+        `detached` = (albedo, sigma_a, sigma_s) sampling copies, or None."""
+        keep, dp = self._params(albedo, emission, sigma_a, sigma_s, detached)
+        rgb = torch.zeros((self.height, self.width, 3), dtype=torch.float32, device=self.device)
+        b = torch.zeros((self.height, self.width), dtype=torch.int32, device=self.device)
+        n = torch.zeros_like(b)
+        film = Film(rgb.data_ptr(), b.data_ptr(), n.data_ptr(), self.width, self.height, 1)
+        self.ctx.set_stream(torch.cuda.current_stream(self.device).cuda_stream)
+        prm = RenderParams(spp, first_frame, max_depth, rr_depth)
+        native.check(self.ctx.L, self.ctx.h, self.ctx.L.lt_render_diff(self.ctx.h, C.byref(prm), C.byref(dp),
+                                                                         C.byref(film)))
+        del keep
+        return rgb, b, n
+
+    def adjoint(self, albedo, emission, sigma_a, sigma_s, d_loss_d_sum: torch.Tensor, spp: int,
+                first_frame: int = 0, max_depth: int = 8, rr_depth: int = 3, detached=None, crop=None):
+        keep, dp = self._params(albedo, emission, sigma_a, sigma_s, detached)
+        grads = [torch.zeros_like(k) for k in keep[:4]]
+        dI = _dev(d_loss_d_sum, self.device)
+        crop_arr = None if crop is None else (C.c_uint32 * 4)(*crop)
+        self.ctx.set_stream(torch.cuda.current_stream(self.device).cuda_stream)
+        prm = RenderParams(spp, first_frame, max_depth, rr_depth)
+        native.check(self.ctx.L, self.ctx.h, self.ctx.L.lt_render_adjoint(
+            self.ctx.h, C.byref(prm), C.byref(dp), dI.data_ptr(), *[g.data_ptr() for g in grads], crop_arr))
+        del keep
+        return grads
+
+
+class RenderImage(torch.autograd.Function):
+    """image = render(albedo, emission, sigma_a, sigma_s); backward by path replay."""
+
+    @staticmethod
+    def forward(ctx, albedo, emission, sigma_a, sigma_s, scene: DiffScene, spp: int, first_frame: int,
+                max_depth: int, rr_depth: int):
+        rgb, _, _ = scene.render(albedo, emission, sigma_a, sigma_s, spp, first_frame, max_depth, rr_depth)
+        ctx.scene = scene
+        ctx.cfg = (spp, first_frame, max_depth, rr_depth)
+        ctx.save_for_backward(albedo, emission, sigma_a, sigma_s)
+        return rgb / spp
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        albedo, emission, sigma_a, sigma_s = ctx.saved_tensors
+        spp, first_frame, max_depth, rr_depth = ctx.cfg
+        g = ctx.scene.adjoint(albedo, emission, sigma_a, sigma_s, grad_image.contiguous() / spp, spp,
+                              first_frame, max_depth, rr_depth)
+        return g[0], g[1], g[2], g[3], None, None, None, None, None
+
+
+def render_image(scene: DiffScene, albedo, emission, sigma_a, sigma_s, spp: int, first_frame: int = 0,
+                 max_depth: int = 8, rr_depth: int = 3) -> torch.Tensor:
+    return RenderImage.apply(albedo, emission, sigma_a, sigma_s, scene, spp, first_frame, max_depth, rr_depth)

@@ -64,7 +64,7 @@ class SceneDesc(C.Structure):
 class SceneInfo(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("num_triangles", C.c_uint32),
                 ("num_meshes", C.c_uint32), ("num_lights", C.c_uint32), ("num_bvh_nodes", C.c_uint32),
-                ("device_bytes", C.c_uint64), ("build_ms", C.c_float)]
+                ("device_bytes", C.c_uint64), ("build_ms", C.c_float), ("num_media", C.c_uint32)]
 
 
 class Film(C.Structure):

@@ -390,6 +390,34 @@ def medium_sphere_scene(width=512, height=512, spp=256, max_depth=32, rr_depth=3
     return sc
 
 
+def differentiable_scene(width=512, height=512, spp=32, max_depth=8, rr_depth=3, slices=64, stacks=32,
+                         name="diff_scene") -> Scene:
+    """Config 3: the nine-sphere scene plus a dielectric sphere (IOR 1.33,
+    radius 0.6, to the right of the grid) holding the config-2 medium
+    (RGB sigma_s, sigma_a, HG g = 0.3)."""
+    sc = nine_spheres(width=width, height=height, spp=spp, max_depth=max_depth, rr_depth=rr_depth, seed=0,
+                      slices=slices, stacks=stacks, name=name)
+    sc.media.append({"name": "fog", "type": "henyey_greenstein", "sigma_a": [0.05, 0.1, 0.2],
+                     "sigma_s": [2.0, 1.5, 1.0], "g": 0.3})
+    sc.bsdfs.append({"name": "water", "type": "ideal_specular_dielectric",
+                     "albedo": {"type": "constant", "value": [1.0, 1.0, 1.0]}, "ior": 1.33})
+    sc.materials.append({"name": "water", "bsdf": "water", "medium": "fog"})
+    p, n, i = uv_sphere(0.6, slices, stacks, center=(2.4, 0.6, 0.0))
+    sc.meshes.append(Mesh("fog_ball", p, n, i, "water"))
+    return sc
+
+
+def differentiable_targets(num_triangles: int, seed: int = 3):
+    """Config 3 parameters: true per-triangle albedo U(0.2, 0.9) (seed 3) and the
+    config-2 medium; initial guess albedo 0.5 and sigma_s = sigma_a = 1."""
+    rng = np.random.default_rng(seed)
+    true = {"albedo": rng.uniform(0.2, 0.9, size=(num_triangles, 3)).astype(F32),
+            "sigma_a": np.array([[0.05, 0.1, 0.2]], F32), "sigma_s": np.array([[2.0, 1.5, 1.0]], F32)}
+    init = {"albedo": np.full((num_triangles, 3), 0.5, F32),
+            "sigma_a": np.ones((1, 3), F32), "sigma_s": np.ones((1, 3), F32)}
+    return true, init
+
+
 def tiny_scene(width=32, height=32, spp=4, max_depth=8, rr_depth=3, name="tiny") -> Scene:
     """Smallest scene with every reference material: three low-poly spheres
     (Lambert, mirror, dielectric) over the ground, under the light."""
