@@ -234,16 +234,22 @@ typedef struct lt_diff_params {
 lt_status lt_diff_defaults(lt_ctx *ctx, float *albedo, float *emission, float *sigma_a, float *sigma_s);
 
 /* Forward render of the differentiable estimator into a device film
- * (additive, as lt_render). */
-lt_status lt_render_diff(lt_ctx *ctx, const lt_render_params *params, const lt_diff_params *dp, lt_film *film);
+ * (additive, as lt_render). sample_radiance (device, optional): receives every
+ * sample's radiance, 3 floats at ((frame - first_frame) * W * H + pixel); with
+ * it the adjoint replays each path once instead of twice. */
+lt_status lt_render_diff(lt_ctx *ctx, const lt_render_params *params, const lt_diff_params *dp, lt_film *film,
+                         float *sample_radiance);
 
 /* Adjoint: given d_loss_d_film (W*H*3, derivative of the loss with respect to
  * the film's colour sums) adds d loss / d parameter to the four gradient arrays
  * (same shapes as the parameters; not cleared). crop = {x0, y0, x1, y1} limits
- * the pixels whose samples are replayed, or NULL for the whole film. */
+ * the pixels whose samples are replayed, or NULL for the whole film.
+ * sample_radiance: from lt_render_diff with the same parameters and render
+ * params, or NULL (each path is then replayed twice). */
 lt_status lt_render_adjoint(lt_ctx *ctx, const lt_render_params *params, const lt_diff_params *dp,
                             const float *d_loss_d_film, float *grad_albedo, float *grad_emission,
-                            float *grad_sigma_a, float *grad_sigma_s, const uint32_t *crop);
+                            float *grad_sigma_a, float *grad_sigma_s, const uint32_t *crop,
+                            const float *sample_radiance);
 
 /* ---------------------------------------------------------------- rays */
 typedef struct lt_ray { float org[3]; float tnear; float dir[3]; float tfar; } lt_ray; /* 32 B */

@@ -498,7 +498,8 @@ static lt_status diff_setup(lt_ctx *c, const lt_render_params *p, const lt_diff_
     return LT_OK;
 }
 
-lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, lt_film *film) {
+lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, lt_film *film,
+                         float *sample_radiance) {
     if (!c || !p || !dp || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     DiffParams P;
     RenderArgs a;
@@ -509,7 +510,7 @@ lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_par
     FilmPtrs f{film->rgb, film->bounces, film->counts};
     c->stats = lt_render_stats{};
     CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-    CUDA_TRY(c, launch_diff_forward(c->dev, P, a, f, c->shape, c->stream));
+    CUDA_TRY(c, launch_diff_forward(c->dev, P, a, f, sample_radiance, c->shape, c->stream));
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     c->stats.samples = a.total;
     c->stats.kernel_launches = 1;
@@ -518,14 +519,14 @@ lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_par
 
 lt_status lt_render_adjoint(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, const float *dI,
                             float *g_albedo, float *g_emission, float *g_sigma_a, float *g_sigma_s,
-                            const uint32_t *crop) {
+                            const uint32_t *crop, const float *sample_radiance) {
     if (!c || !p || !dp || !dI || !g_albedo || !g_emission) return fail(c, LT_ERR_INVALID, "NULL argument");
     DiffParams P;
     RenderArgs a;
     lt_status st = diff_setup(c, p, dp, &P, &a);
     if (st != LT_OK) return st;
     if (c->host.media.size() && (!g_sigma_a || !g_sigma_s)) return fail(c, LT_ERR_INVALID, "medium gradients missing");
-    DiffGrads G{dI, g_albedo, g_emission, g_sigma_a, g_sigma_s, 0, 0, a.width, a.height};
+    DiffGrads G{dI, g_albedo, g_emission, g_sigma_a, g_sigma_s, 0, 0, a.width, a.height, sample_radiance};
     if (crop) {
         if (crop[0] > crop[2] || crop[1] > crop[3] || crop[2] > a.width || crop[3] > a.height)
             return fail(c, LT_ERR_INVALID, "crop outside the film");

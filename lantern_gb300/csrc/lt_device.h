@@ -100,6 +100,7 @@ struct DiffGrads {
     const float *dI;
     float *albedo, *emission, *sigma_a, *sigma_s;
     uint32_t x0, y0, x1, y1;
+    const float *sample_I;  // per-sample radiance from the forward pass, or null (replay twice)
 };
 
 // launchers (lt_kernels.cu)
@@ -108,7 +109,7 @@ cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits
                              uint32_t *fetch, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st);
 cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
-                                const LaunchShape &ls, cudaStream_t st);
+                                float *sample_I, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const RenderArgs &a, const DiffGrads &g,
                                 uint32_t num_media, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,

@@ -751,6 +751,35 @@ __device__ __forceinline__ void add3(float *g, v3 v) {
     if (v.z != 0.0f) atomicAdd(g + 2, v.z);
 }
 
+// Per-thread sums of gradient terms keyed by triangle (direct mapped). A
+// pixel's samples keep hitting the same few triangles, so most additions stay
+// in the thread; the atomics happen when an entry is evicted and at the end.
+template <int N> struct GradCache {
+    uint32_t key[N];
+    v3 val[N];
+    __device__ __forceinline__ void init() {
+        for (int i = 0; i < N; ++i) key[i] = kMiss;
+    }
+    __device__ __forceinline__ void add(float *base, uint32_t prim, v3 v) {
+        int s = (int)(prim % N);
+        if (key[s] == prim) {
+            val[s] = val[s] + v;
+            return;
+        }
+        if (key[s] != kMiss) add3(base + 3 * key[s], val[s]);
+        key[s] = prim;
+        val[s] = v;
+    }
+    __device__ __forceinline__ void flush(float *base) {
+        for (int i = 0; i < N; ++i) {
+            if (key[i] != kMiss) add3(base + 3 * key[i], val[i]);
+            key[i] = kMiss;
+        }
+    }
+};
+using AlbedoCache = GradCache<4>;
+using EmissionCache = GradCache<2>;
+
 __device__ __forceinline__ void add_medium(const DiffGrads &G, float *acc, int mi, v3 ga, v3 gs) {
     if (mi < kMediaAcc) {
         acc[6 * mi] += ga.x; acc[6 * mi + 1] += ga.y; acc[6 * mi + 2] += ga.z;
@@ -763,7 +792,8 @@ __device__ __forceinline__ void add_medium(const DiffGrads &G, float *acc, int m
 
 template <bool kGrad>
 __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads &G, const RenderArgs &A,
-                        unsigned long long item, v3 I, v3 delta, float *macc, uint32_t &bounces_out) {
+                        unsigned long long item, v3 I, v3 delta, float *macc, AlbedoCache &ca, EmissionCache &ce,
+                        uint32_t &bounces_out) {
     Path p;
     v3 org, dir;
     float tnear;
@@ -831,7 +861,7 @@ __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads 
             const v3 alb = ld3(P.albedo + 3 * prim), alb_d = ld3(P.albedo_s + 3 * prim);
             if ((bounces == 0 || (p.lobe & kLobeSpecular) != 0) && Gi.light >= 0) {
                 C = C + p.T * ld3(P.emission + 3 * prim);
-                if (kGrad) add3(G.emission + 3 * prim, p.T * delta);
+                if (kGrad) ce.add(G.emission, prim, p.T * delta);
             }
             Inter it;
             it.P = origin + direction * h.t;
@@ -873,8 +903,8 @@ __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads 
                             C = C + p.T * ((((f * Li) * wgt) / lpdf) * fn);
                             if (kGrad) {
                                 v3 Td = p.T * delta;
-                                add3(G.albedo + 3 * prim, Td * (Li * (fn * (cosl * kInvPi) * wgt / lpdf)));
-                                add3(G.emission + 3 * lh.prim, Td * (f * (fn * wgt / lpdf)));
+                                ca.add(G.albedo, prim, Td * (Li * (fn * (cosl * kInvPi) * wgt / lpdf)));
+                                ce.add(G.emission, lh.prim, Td * (f * (fn * wgt / lpdf)));
                             }
                         }
                     }
@@ -895,8 +925,8 @@ __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads 
                         C = C + p.T * ((((f * Le) * wgt) / spdf) * fn);
                         if (kGrad) {
                             v3 Td = p.T * delta;
-                            add3(G.albedo + 3 * prim, Td * (Le * (fn * dfa * wgt / spdf)));
-                            add3(G.emission + 3 * bh.prim, Td * (f * (fn * wgt / spdf)));
+                            ca.add(G.albedo, prim, Td * (Le * (fn * dfa * wgt / spdf)));
+                            ce.add(G.emission, bh.prim, Td * (f * (fn * wgt / spdf)));
                         }
                     }
                 }
@@ -907,7 +937,7 @@ __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads 
             v3 fs = m.bsdf == LT_BSDF_LAMBERT ? (alb_d * kInvPi) * dot(it.wi, it.N) : alb_d;
             if (kGrad) {
                 v3 R = (I - C) * delta;
-                add3(G.albedo + 3 * prim, mk(alb.x > 0.0f ? R.x / alb.x : 0.0f, alb.y > 0.0f ? R.y / alb.y : 0.0f,
+                ca.add(G.albedo, prim, mk(alb.x > 0.0f ? R.x / alb.x : 0.0f, alb.y > 0.0f ? R.y / alb.y : 0.0f,
                                              alb.z > 0.0f ? R.z / alb.z : 0.0f));
             }
             p.T = (p.T * f) / pdf;
@@ -935,9 +965,14 @@ __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads 
 
 // One thread per pixel, samples in frame order: the film is the same on every
 // run (finite differences of the loss see no summation-order noise).
-__global__ void __launch_bounds__(128) k_diff_forward(DevScene S, DiffParams P, RenderArgs A, FilmPtrs F) {
+// sample_I (optional): each sample's radiance, 3 floats at (frame index * W*H + pixel),
+// so that the adjoint need not replay the path a first time.
+__global__ void __launch_bounds__(128) k_diff_forward(DevScene S, DiffParams P, RenderArgs A, FilmPtrs F,
+                                                     float *sample_I) {
     DiffGrads G{};
     float macc[1];
+    AlbedoCache ca;
+    EmissionCache ce;
     const uint32_t npix = A.width * A.height;
     const uint32_t spp = (uint32_t)(A.total / npix);
     for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
@@ -945,8 +980,14 @@ __global__ void __launch_bounds__(128) k_diff_forward(DevScene S, DiffParams P, 
         uint32_t bsum = 0;
         for (uint32_t s = 0; s < spp; ++s) {
             uint32_t b = 0;
-            sum = sum + diff_path<false>(S, P, G, A, (unsigned long long)s * npix + pixel, mk(0, 0, 0),
-                                         mk(0, 0, 0), macc, b);
+            unsigned long long item = (unsigned long long)s * npix + pixel;
+            v3 c = diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
+            if (sample_I) {
+                sample_I[3 * item] = c.x;
+                sample_I[3 * item + 1] = c.y;
+                sample_I[3 * item + 2] = c.z;
+            }
+            sum = sum + c;
             bsum += b;
         }
         F.rgb[3 * (size_t)pixel] += sum.x;
@@ -961,6 +1002,10 @@ __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, 
                                                      uint32_t num_media) {
     float macc[6 * kMediaAcc];
     for (int k = 0; k < 6 * kMediaAcc; ++k) macc[k] = 0.0f;
+    AlbedoCache ca;
+    EmissionCache ce;
+    ca.init();
+    ce.init();
     const uint32_t npix = A.width * A.height;
     const uint32_t spp = (uint32_t)(A.total / npix);
     for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
@@ -971,10 +1016,13 @@ __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, 
         for (uint32_t s = 0; s < spp; ++s) {
             unsigned long long item = (unsigned long long)s * npix + pixel;
             uint32_t b = 0;
-            v3 I = diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, b);
-            diff_path<true>(S, P, G, A, item, I, delta, macc, b);
+            v3 I = G.sample_I ? ld3(G.sample_I + 3 * item)
+                              : diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
+            diff_path<true>(S, P, G, A, item, I, delta, macc, ca, ce, b);
         }
     }
+    ca.flush(G.albedo);
+    ce.flush(G.emission);
     // medium gradients: warp sums, one atomic per warp and component
     for (int k = 0; k < 6 * kMediaAcc; ++k) {
         if (k / 6 >= (int)num_media) break;
@@ -1007,9 +1055,9 @@ void query_launch_shape(int device, LaunchShape *out) {
 }
 
 cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
-                                const LaunchShape &ls, cudaStream_t st) {
+                                float *sample_I, const LaunchShape &ls, cudaStream_t st) {
     if (a.total == 0) return cudaSuccess;
-    k_diff_forward<<<ls.diff_blocks, 128, 0, st>>>(s, p, a, f);
+    k_diff_forward<<<ls.diff_blocks, 128, 0, st>>>(s, p, a, f, sample_I);
     return cudaGetLastError();
 }
 

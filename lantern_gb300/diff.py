@@ -31,9 +31,9 @@ def _bind(L):
         return
     p = C.c_void_p
     L.lt_diff_defaults.argtypes = [p, p, p, p, p]
-    L.lt_render_diff.argtypes = [p, C.POINTER(RenderParams), C.POINTER(DiffParams), C.POINTER(Film)]
+    L.lt_render_diff.argtypes = [p, C.POINTER(RenderParams), C.POINTER(DiffParams), C.POINTER(Film), p]
     L.lt_render_adjoint.argtypes = [p, C.POINTER(RenderParams), C.POINTER(DiffParams), p, p, p, p, p,
-                                    C.POINTER(C.c_uint32)]
+                                    C.POINTER(C.c_uint32), p]
     L._diff_bound = True
 
 
@@ -76,23 +76,29 @@ class DiffScene:
         return keep, DiffParams(*[_ptr(k) for k in keep])
 
     def render(self, albedo, emission, sigma_a, sigma_s, spp: int, first_frame: int = 0, max_depth: int = 8,
-               rr_depth: int = 3, detached=None):
-        """Film (rgb sum, bounces, counts) of the differentiable estimator.
+               rr_depth: int = 3, detached=None, keep_samples: bool = False):
+        """Film (rgb sum, bounces, counts) of the differentiable estimator, and
+        with keep_samples every sample's radiance (for the adjoint).
         `detached` = (albedo, sigma_a, sigma_s) sampling copies, or None."""
         keep, dp = self._params(albedo, emission, sigma_a, sigma_s, detached)
         rgb = torch.zeros((self.height, self.width, 3), dtype=torch.float32, device=self.device)
         b = torch.zeros((self.height, self.width), dtype=torch.int32, device=self.device)
         n = torch.zeros_like(b)
+        samples = (torch.empty((spp, self.height, self.width, 3), dtype=torch.float32, device=self.device)
+                   if keep_samples else None)
         film = Film(rgb.data_ptr(), b.data_ptr(), n.data_ptr(), self.width, self.height, 1)
         self.ctx.set_stream(torch.cuda.current_stream(self.device).cuda_stream)
         prm = RenderParams(spp, first_frame, max_depth, rr_depth)
         native.check(self.ctx.L, self.ctx.h, self.ctx.L.lt_render_diff(self.ctx.h, C.byref(prm), C.byref(dp),
-                                                                         C.byref(film)))
+                                                                         C.byref(film), _ptr(samples)))
         del keep
+        if keep_samples:
+            return rgb, b, n, samples
         return rgb, b, n
 
     def adjoint(self, albedo, emission, sigma_a, sigma_s, d_loss_d_sum: torch.Tensor, spp: int,
-                first_frame: int = 0, max_depth: int = 8, rr_depth: int = 3, detached=None, crop=None):
+                first_frame: int = 0, max_depth: int = 8, rr_depth: int = 3, detached=None, crop=None,
+                samples: Optional[torch.Tensor] = None):
         keep, dp = self._params(albedo, emission, sigma_a, sigma_s, detached)
         grads = [torch.zeros_like(k) for k in keep[:4]]
         dI = _dev(d_loss_d_sum, self.device)
@@ -100,7 +106,8 @@ class DiffScene:
         self.ctx.set_stream(torch.cuda.current_stream(self.device).cuda_stream)
         prm = RenderParams(spp, first_frame, max_depth, rr_depth)
         native.check(self.ctx.L, self.ctx.h, self.ctx.L.lt_render_adjoint(
-            self.ctx.h, C.byref(prm), C.byref(dp), dI.data_ptr(), *[g.data_ptr() for g in grads], crop_arr))
+            self.ctx.h, C.byref(prm), C.byref(dp), dI.data_ptr(), *[g.data_ptr() for g in grads], crop_arr,
+            _ptr(samples)))
         del keep
         return grads
 
@@ -111,18 +118,19 @@ class RenderImage(torch.autograd.Function):
     @staticmethod
     def forward(ctx, albedo, emission, sigma_a, sigma_s, scene: DiffScene, spp: int, first_frame: int,
                 max_depth: int, rr_depth: int):
-        rgb, _, _ = scene.render(albedo, emission, sigma_a, sigma_s, spp, first_frame, max_depth, rr_depth)
+        rgb, _, _, samples = scene.render(albedo, emission, sigma_a, sigma_s, spp, first_frame, max_depth, rr_depth,
+                                          keep_samples=True)
         ctx.scene = scene
         ctx.cfg = (spp, first_frame, max_depth, rr_depth)
-        ctx.save_for_backward(albedo, emission, sigma_a, sigma_s)
+        ctx.save_for_backward(albedo, emission, sigma_a, sigma_s, samples)
         return rgb / spp
 
     @staticmethod
     def backward(ctx, grad_image):
-        albedo, emission, sigma_a, sigma_s = ctx.saved_tensors
+        albedo, emission, sigma_a, sigma_s, samples = ctx.saved_tensors
         spp, first_frame, max_depth, rr_depth = ctx.cfg
         g = ctx.scene.adjoint(albedo, emission, sigma_a, sigma_s, grad_image.contiguous() / spp, spp,
-                              first_frame, max_depth, rr_depth)
+                              first_frame, max_depth, rr_depth, samples=samples)
         return g[0], g[1], g[2], g[3], None, None, None, None, None
 
 

@@ -1087,3 +1087,49 @@ void orc_camera_ray(const orc_scene *s, uint32_t x, uint32_t y, float u, float v
     out_dir[2] = dot(view, s->mz);
     out_org[0] = s->origin.x; out_org[1] = s->origin.y; out_org[2] = s->origin.z;
 }
+
+/* ------------------------------------------------------------------ accessors */
+/* Read-only views of the loaded scene for the differentiable reference
+ * (oracle/lt_diff_ref.cpp). */
+void orc_camera_info(const orc_scene *s, float cam[14], uint32_t *w, uint32_t *h) {
+    const v3 *v[4] = {&s->origin, &s->mx, &s->my, &s->mz};
+    for (int i = 0; i < 4; ++i) {
+        cam[3 * i] = v[i]->x; cam[3 * i + 1] = v[i]->y; cam[3 * i + 2] = v[i]->z;
+    }
+    cam[12] = s->tanx;
+    cam[13] = s->tany;
+    *w = s->width;
+    *h = s->height;
+}
+void orc_background_info(const orc_scene *s, float rgb[3]) {
+    rgb[0] = s->background.x; rgb[1] = s->background.y; rgb[2] = s->background.z;
+}
+int orc_num_lights(const orc_scene *s) { return s->nlights; }
+int orc_num_media(const orc_scene *s) { return s->nmeds; }
+int orc_light_geom(const orc_scene *s, int i) { return s->lights[i].geom; }
+uint32_t orc_tri_geom(const orc_scene *s, uint32_t prim) { return s->tri_geom[prim]; }
+void orc_geom_info(const orc_scene *s, uint32_t g, int *material, int *light, int *has_normals) {
+    *material = s->geoms[g].material;
+    *light = s->geoms[g].light;
+    *has_normals = s->geoms[g].has_normals;
+}
+void orc_material_info(const orc_scene *s, int m, int *bsdf, float albedo[3], float *ior, int *medium) {
+    const material *M = &s->mats[m];
+    *bsdf = M->bsdf;
+    albedo[0] = M->albedo.x; albedo[1] = M->albedo.y; albedo[2] = M->albedo.z;
+    *ior = M->ior;
+    *medium = M->medium;
+}
+void orc_medium_info(const orc_scene *s, int m, int *type, float sa[3], float ss[3], float *g) {
+    const medium *M = &s->meds[m];
+    *type = M->type;
+    sa[0] = M->sigma_a.x; sa[1] = M->sigma_a.y; sa[2] = M->sigma_a.z;
+    ss[0] = M->sigma_s.x; ss[1] = M->sigma_s.y; ss[2] = M->sigma_s.z;
+    *g = M->g;
+}
+void orc_tri_normals(const orc_scene *s, uint32_t prim, float n[9]) {
+    for (int j = 0; j < 3; ++j) {
+        const float *p = s->vnormal + 3 * (size_t)s->tri_vidx[3 * (size_t)prim + j];
+        n[3 * j] = p[0]; n[3 * j + 1] = p[1]; n[3 * j + 2] = p[2];
+    }
+}

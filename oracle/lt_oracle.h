@@ -99,6 +99,30 @@ void orc_render(const orc_scene *s, const orc_render_opts *o, uint32_t first_fra
 void orc_render_path(const orc_scene *s, const orc_render_opts *o, uint32_t x, uint32_t y,
                      uint32_t frame, float color[3], uint32_t *bounces);
 
+/* Read-only scene views for the differentiable reference (lt_diff_ref.cpp).
+ * cam = origin, mx, my, mz (3 floats each), tanx, tany. */
+void orc_camera_info(const orc_scene *s, float cam[14], uint32_t *w, uint32_t *h);
+void orc_background_info(const orc_scene *s, float rgb[3]);
+int orc_num_lights(const orc_scene *s);
+int orc_num_media(const orc_scene *s);
+int orc_light_geom(const orc_scene *s, int i);
+uint32_t orc_tri_geom(const orc_scene *s, uint32_t prim);
+void orc_geom_info(const orc_scene *s, uint32_t g, int *material, int *light, int *has_normals);
+void orc_material_info(const orc_scene *s, int m, int *bsdf, float albedo[3], float *ior, int *medium);
+void orc_medium_info(const orc_scene *s, int m, int *type, float sa[3], float ss[3], float *g);
+void orc_tri_normals(const orc_scene *s, uint32_t prim, float n[9]);
+
+/* Differentiable estimator and its gradient (oracle/lt_diff_ref.cpp), in
+ * double (fp64 != 0) or float. Parameters as for lt_render_diff (host arrays,
+ * detached copies = the parameters). dI: d loss / d film colour sum (W*H*3).
+ * crop = x0, y0, x1, y1. Outputs: film colour sums of the crop's pixels (W*H*3,
+ * other pixels untouched) and gradients (accumulated, double). */
+void orc_diff_render(const orc_scene *s, int fp64, const float *albedo, const float *emission,
+                     const float *sigma_a, const float *sigma_s, uint32_t spp, uint32_t first_frame,
+                     uint32_t max_depth, uint32_t rr_depth, const uint32_t crop[4], const float *dI,
+                     double *rgb, double *g_albedo, double *g_emission, double *g_sigma_a, double *g_sigma_s,
+                     int threads);
+
 /* Building blocks, exported for golden-vector checks against the reference. */
 void orc_pcg_stream(uint64_t seed, uint64_t seq, uint32_t n, uint32_t *out_uint, float *out_float);
 uint32_t orc_tile_seed(uint32_t tile, uint32_t frame);

@@ -42,17 +42,25 @@ _ref = None
 
 
 def build_oracle(force: bool = False) -> str:
-    """Compile oracle/lt_oracle.c into oracle/_build/liboracle.so."""
+    """Compile oracle/lt_oracle.c (C) and oracle/lt_diff_ref.cpp (C++) into
+    oracle/_build/liboracle.so."""
     src = os.path.join(HERE, "lt_oracle.c")
+    cpp = os.path.join(HERE, "lt_diff_ref.cpp")
     hdr = os.path.join(HERE, "lt_oracle.h")
     os.makedirs(BUILD, exist_ok=True)
     if (not force and os.path.exists(ORACLE_SO)
-            and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+            and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(f) for f in (src, cpp, hdr))):
         return ORACLE_SO
-    tmp = ORACLE_SO + f".{os.getpid()}.tmp"
-    subprocess.check_call(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
-                           "-o", tmp, src, "-lm", "-lpthread"])
+    pid = os.getpid()
+    obj_c, obj_cpp = os.path.join(BUILD, f"lt_oracle.{pid}.o"), os.path.join(BUILD, f"lt_diff_ref.{pid}.o")
+    flags = ["-O2", "-ffp-contract=off", "-fPIC"]
+    subprocess.check_call(["gcc", "-std=c11"] + flags + ["-c", src, "-o", obj_c])
+    subprocess.check_call(["g++", "-std=c++17"] + flags + ["-c", cpp, "-o", obj_cpp])
+    tmp = ORACLE_SO + f".{pid}.tmp"
+    subprocess.check_call(["g++", "-shared", "-o", tmp, obj_c, obj_cpp, "-lm", "-lpthread"])
     os.replace(tmp, ORACLE_SO)
+    for o in (obj_c, obj_cpp):
+        os.remove(o)
     return ORACLE_SO
 
 
@@ -101,6 +109,9 @@ def lib():
             L.orc_filter_sample.argtypes = [f32]
             L.orc_filter_sample.restype = f32
             L.orc_camera_ray.argtypes = [p, u32, u32, f32, f32, fp, fp]
+            dp = C.POINTER(C.c_double)
+            L.orc_diff_render.argtypes = [p, C.c_int, fp, fp, fp, fp, u32, u32, u32, u32, up, fp, dp, dp, dp, dp, dp,
+                                          C.c_int]
             _lib = L
     return _lib
 
@@ -262,6 +273,65 @@ class OracleScene:
         lib().orc_intersect(self.h, fptr(rays), uptr(hits), n, int(use_bvh), uptr(cnt),
                             threads or os.cpu_count())
         return (hits, cnt) if counters else hits
+
+    def diff_defaults(self):
+        """The scene's own (albedo, emission, sigma_a, sigma_s) as parameter arrays."""
+        L = lib()
+        L.orc_tri_geom.restype = C.c_uint32
+        L.orc_tri_geom.argtypes = [C.c_void_p, C.c_uint32]
+        L.orc_geom_info.argtypes = [C.c_void_p, C.c_uint32] + [C.POINTER(C.c_int)] * 3
+        L.orc_material_info.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), C.POINTER(C.c_int)]
+        L.orc_medium_info.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                      C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_num_media.argtypes = [C.c_void_p]
+        T = self.num_triangles
+        albedo, emission = np.zeros((T, 3), np.float32), np.zeros((T, 3), np.float32)
+        geoms = {}
+        for t in range(T):
+            g = L.orc_tri_geom(self.h, t)
+            if g not in geoms:
+                mat, light, hn = C.c_int(), C.c_int(), C.c_int()
+                L.orc_geom_info(self.h, g, C.byref(mat), C.byref(light), C.byref(hn))
+                b, ior, med = C.c_int(), C.c_float(), C.c_int()
+                alb = (C.c_float * 3)()
+                L.orc_material_info(self.h, mat.value, C.byref(b), alb, C.byref(ior), C.byref(med))
+                rad = np.zeros(3, np.float32)
+                if light.value >= 0:
+                    area, sph = C.c_float(), (C.c_float * 4)()
+                    r3 = (C.c_float * 3)()
+                    L.orc_light_info(self.h, light.value, C.byref(area), sph, r3)
+                    rad = np.array(list(r3), np.float32)
+                geoms[g] = (np.array(list(alb), np.float32), rad)
+            albedo[t], emission[t] = geoms[g]
+        M = max(L.orc_num_media(self.h), 1)
+        sa, ss = np.zeros((M, 3), np.float32), np.zeros((M, 3), np.float32)
+        for m in range(L.orc_num_media(self.h)):
+            ty, g = C.c_int(), C.c_float()
+            a3, s3 = (C.c_float * 3)(), (C.c_float * 3)()
+            L.orc_medium_info(self.h, m, C.byref(ty), a3, s3, C.byref(g))
+            sa[m], ss[m] = list(a3), list(s3)
+        return albedo, emission, sa, ss
+
+    def diff_render(self, albedo, emission, sigma_a, sigma_s, spp: int, max_depth: int = 8, rr_depth: int = 3,
+                    first_frame: int = 0, crop=None, dI=None, fp64: bool = True, threads: int = 0):
+        """Differentiable estimator and its gradient on the host (lt_diff_ref.cpp):
+        returns (film colour sums float64 (H, W, 3), dict of float64 gradients)."""
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
+        albedo, emission, sigma_a, sigma_s = f(albedo), f(emission), f(sigma_a), f(sigma_s)
+        if crop is None:
+            crop = (0, 0, self.width, self.height)
+        crop_a = np.asarray(crop, dtype=np.uint32)
+        rgb = np.zeros((self.height, self.width, 3), np.float64)
+        g = {k: np.zeros(v.shape, np.float64) for k, v in
+             (("albedo", albedo), ("emission", emission), ("sigma_a", sigma_a), ("sigma_s", sigma_s))}
+        dptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        dI_a = None if dI is None else f(dI)
+        lib().orc_diff_render(self.h, int(fp64), fptr(albedo), fptr(emission), fptr(sigma_a), fptr(sigma_s), spp,
+                              first_frame, max_depth, rr_depth, uptr(crop_a), fptr(dI_a), dptr(rgb),
+                              dptr(g["albedo"]), dptr(g["emission"]), dptr(g["sigma_a"]), dptr(g["sigma_s"]),
+                              threads or os.cpu_count())
+        return rgb, g
 
     def render(self, frames: int, first_frame: int = 0, max_depth: int = 1500, rr_depth: int = 3,
                keying: int = KEY_PIXEL, threads: int = 0, two_films: bool = False):

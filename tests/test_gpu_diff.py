@@ -84,3 +84,32 @@ def test_adjoint_matches_finite_differences(scene_dir):
         if abs(ad - fd) > 0.02 * max(abs(fd), abs(ad)):
             bad.append((k, i, ad, fd))
     assert not bad, bad[:10]
+
+
+def test_adjoint_crop_matches_fp64_host_reference(scene_dir):
+    """GPU adjoint of the samples of a 32x32 crop against the same gradient from
+    the host restatement in double precision (oracle/lt_diff_ref.cpp)."""
+    from oracle import oracle as O
+    path = _small(scene_dir)
+    ds = DiffScene(path)
+    orc = O.OracleScene(path)
+    a0, e0, sa0, ss0 = ds.defaults()
+    true, init = S.differentiable_targets(ds.num_triangles)
+    spp, depth, crop = 8, 6, (16, 8, 48, 40)
+    e_np = e0.cpu().numpy()
+    tgt, _ = orc.diff_render(true["albedo"], e_np, true["sigma_a"], true["sigma_s"], spp, max_depth=depth)
+    cur, _ = orc.diff_render(init["albedo"], e_np, init["sigma_a"], init["sigma_s"], spp, max_depth=depth)
+    dI = (2.0 * (cur - tgt) / spp / spp).astype(np.float32)  # d/d(film sum) of sum((img - target)^2)
+    _, g64 = orc.diff_render(init["albedo"], e_np, init["sigma_a"], init["sigma_s"], spp, max_depth=depth,
+                             crop=crop, dI=dI, fp64=True)
+    dev = ds.device
+    g = ds.adjoint(torch.from_numpy(init["albedo"]).to(dev), e0, torch.from_numpy(init["sigma_a"]).to(dev),
+                   torch.from_numpy(init["sigma_s"]).to(dev), torch.from_numpy(dI).to(dev), spp, 0, depth, 3,
+                   crop=crop)
+    torch.cuda.synchronize()
+    for name, gg in zip(("albedo", "emission", "sigma_a", "sigma_s"), g):
+        ref = g64[name].reshape(-1)
+        got = gg.detach().cpu().numpy().astype(np.float64).reshape(-1)
+        assert np.linalg.norm(ref) > 0, name
+        rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert rel < 2e-3, (name, rel)
