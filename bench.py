@@ -197,6 +197,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--microbench", action=argparse.BooleanOptionalAction, default=True,
                     help="also time lt_intersect on 16,777,216 random rays of the same mesh")
+    ap.add_argument("--adjoint", action=argparse.BooleanOptionalAction, default=True,
+                    help="also time the path-replay adjoint on the differentiable config")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -292,6 +294,7 @@ def main():
     micro = None
     if args.microbench and args.workload == "icosphere-1.3M":
         micro = microbench(scene, path, local)
+    adjoint = adjoint_bench(local) if args.adjoint else None
 
     line = None
     if rank == 0:
@@ -323,11 +326,60 @@ def main():
                            else "single GPU"},
                 "mrays": round(mrays, 2), "gpu_launches": launches,
                 "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-                "intersect_microbench": micro}
+                "intersect_microbench": micro, "adjoint": adjoint}
         print(json.dumps(line))
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def adjoint_bench(local):
+    """Differentiable workload: nine spheres + HG medium sphere, 512x512, 32 spp,
+    depth 8. Times the plain forward render (wavefront), the differentiable
+    forward that keeps per-sample radiance, and the path-replay adjoint of the
+    L2 loss to the true-parameter image; grads/s = full gradients per second."""
+    import torch
+    import lantern_gb300.scenes as S
+    from lantern_gb300.diff import DiffScene, render_image
+    from lantern_gb300.integrator import FrameBuffer, Integrator, Scene
+    path = S.ensure_written(S.differentiable_scene(), SCENES)
+    ds = DiffScene(path, local)
+    a0, e0, sa0, ss0 = ds.defaults()
+    true, init = S.differentiable_targets(ds.num_triangles)
+    dev = ds.device
+    sc = Scene(local)
+    sc.LoadSceneFromJSON(path)
+    fb = FrameBuffer(sc.width, sc.height, f"cuda:{local}")
+    it = Integrator(sc, fb, max_depth=8, rr_depth=3)
+    th = [torch.from_numpy(init["albedo"]).to(dev), e0, torch.from_numpy(init["sigma_a"]).to(dev),
+          torch.from_numpy(init["sigma_s"]).to(dev)]
+    with torch.no_grad():
+        target = render_image(ds, torch.from_numpy(true["albedo"]).to(dev), e0,
+                              torch.from_numpy(true["sigma_a"]).to(dev), torch.from_numpy(true["sigma_s"]).to(dev),
+                              32, 0, 8, 3)
+
+    def timed(f, n=3):
+        f()
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream()
+        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0_.record(st)
+        for _ in range(n):
+            f()
+        e1_.record(st)
+        e1_.synchronize()
+        return e0_.elapsed_time(e1_) / n
+
+    fwd = timed(lambda: it.RenderFrame(32))
+    out = {}
+    dfw = timed(lambda: out.update(r=ds.render(*th, 32, 0, 8, 3, keep_samples=True)))
+    rgb, _, _, samples = out["r"]
+    dI = (2.0 * (rgb / 32 - target) / 32).contiguous()
+    adj = timed(lambda: ds.adjoint(*th, dI, 32, 0, 8, 3, samples=samples))
+    nparams = 6 * ds.num_triangles + 6 * ds.num_media
+    return {"config": "differentiable scene 512x512, 32 spp, depth 8", "parameters": nparams,
+            "forward_ms": round(fwd, 3), "diff_forward_ms": round(dfw, 3), "adjoint_ms": round(adj, 3),
+            "adjoint_over_forward": round(adj / fwd, 3), "grads_per_s": round(1e3 / adj, 2)}
 
 
 def microbench(scene, path, local, n=1 << 24):

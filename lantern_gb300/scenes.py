@@ -392,9 +392,9 @@ def medium_sphere_scene(width=512, height=512, spp=256, max_depth=32, rr_depth=3
 
 def differentiable_scene(width=512, height=512, spp=32, max_depth=8, rr_depth=3, slices=64, stacks=32,
                          name="diff_scene") -> Scene:
-    """Config 3: the nine-sphere scene plus a dielectric sphere (IOR 1.33,
-    radius 0.6, to the right of the grid) holding the config-2 medium
-    (RGB sigma_s, sigma_a, HG g = 0.3)."""
+    """Differentiable workload: the nine-sphere scene plus a dielectric sphere
+    (IOR 1.33, radius 0.6, to the right of the grid) holding the RGB
+    Henyey-Greenstein fog of the medium workload (sigma_s, sigma_a, g = 0.3)."""
     sc = nine_spheres(width=width, height=height, spp=spp, max_depth=max_depth, rr_depth=rr_depth, seed=0,
                       slices=slices, stacks=stacks, name=name)
     sc.media.append({"name": "fog", "type": "henyey_greenstein", "sigma_a": [0.05, 0.1, 0.2],
@@ -408,8 +408,8 @@ def differentiable_scene(width=512, height=512, spp=32, max_depth=8, rr_depth=3,
 
 
 def differentiable_targets(num_triangles: int, seed: int = 3):
-    """Config 3 parameters: true per-triangle albedo U(0.2, 0.9) (seed 3) and the
-    config-2 medium; initial guess albedo 0.5 and sigma_s = sigma_a = 1."""
+    """Differentiable workload parameters: true per-triangle albedo U(0.2, 0.9)
+    (seed 3) and the fog's own coefficients; initial guess albedo 0.5 and sigma_s = sigma_a = 1."""
     rng = np.random.default_rng(seed)
     true = {"albedo": rng.uniform(0.2, 0.9, size=(num_triangles, 3)).astype(F32),
             "sigma_a": np.array([[0.05, 0.1, 0.2]], F32), "sigma_s": np.array([[2.0, 1.5, 1.0]], F32)}
