@@ -198,7 +198,11 @@ def main():
     ap.add_argument("--microbench", action=argparse.BooleanOptionalAction, default=True,
                     help="also time lt_intersect on 16,777,216 random rays of the same mesh")
     ap.add_argument("--adjoint", action=argparse.BooleanOptionalAction, default=True,
-                    help="also time the path-replay adjoint on the differentiable config")
+                    help="also time the path-replay adjoint on the differentiable workload")
+    ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8],
+                    help="BVH width of the traversal (lt_tuning.bvh_width)")
+    ap.add_argument("--batch", action=argparse.BooleanOptionalAction, default=True,
+                    help="also time the 64-scene batch: one lt_render_batch vs one lt_render per scene")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -229,6 +233,7 @@ def main():
         path = os.path.join(SCENES, f"{sc.name}.json")
     scene = Scene(local)
     scene.LoadSceneFromJSON(path)
+    scene.ctx.set_tuning(bvh_width=args.bvh_width)
     info = scene.info()
     fb = FrameBuffer(scene.width, scene.height, f"cuda:{local}")
     integ = Integrator(scene, fb, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
@@ -295,6 +300,7 @@ def main():
     if args.microbench and args.workload == "icosphere-1.3M":
         micro = microbench(scene, path, local)
     adjoint = adjoint_bench(local) if args.adjoint else None
+    batch = batch_bench(local) if args.batch else None
 
     line = None
     if rank == 0:
@@ -322,11 +328,12 @@ def main():
                 "config": {"workload": args.workload, "width": scene.width, "height": scene.height, "spp": spp,
                            "max_depth": rp["max_depth"], "rr_depth": rp["rr_depth"],
                            "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
+                           "bvh_width": args.bvh_width,
                            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1
                            else "single GPU"},
                 "mrays": round(mrays, 2), "gpu_launches": launches,
                 "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-                "intersect_microbench": micro, "adjoint": adjoint}
+                "intersect_microbench": micro, "adjoint": adjoint, "batch": batch}
         print(json.dumps(line))
     if dist:
         dist.barrier()
@@ -380,6 +387,104 @@ def adjoint_bench(local):
     return {"config": "differentiable scene 512x512, 32 spp, depth 8", "parameters": nparams,
             "forward_ms": round(fwd, 3), "diff_forward_ms": round(dfw, 3), "adjoint_ms": round(adj, 3),
             "adjoint_over_forward": round(adj / fwd, 3), "grads_per_s": round(1e3 / adj, 2)}
+
+
+def batch_bench(local, count=64, reps=3):
+    """Batched workload: 64 seeded scenes (seed 5; 128^2..1024^2, 1k..500k
+    triangles, 4/16/64 spp, 30% with the fog medium; depth 10). Times every
+    scene rendered by its own Integrator.RenderFrame (lt_render, one after the
+    other: the sequential baseline, with the default and with the tuned launch
+    configuration) against one RenderBatch (lt_render_batch: one captured
+    graph launch) after lt_autotune_batch. Device time on the stream, best of
+    `reps`; films accumulate across repetitions (additive, like RenderFrame)."""
+    import torch
+    import lantern_gb300.scenes as S
+    from lantern_gb300.integrator import FrameBuffer, Integrator, RenderBatch, Scene
+    gen = S.batch_scenes(count=count)
+    sdir = os.path.join(SCENES, "batch")
+    scenes = []
+    for sc in gen:
+        s = Scene(local)
+        s.LoadSceneFromJSON(S.ensure_written(sc, sdir))
+        scenes.append(s)
+    fbs = [FrameBuffer(s.width, s.height, f"cuda:{local}") for s in scenes]
+    spps = [sc.render["spp"] for sc in gen]
+    depth = [sc.render["max_depth"] for sc in gen]
+    samples = sum(s.width * s.height * n for s, n in zip(scenes, spps))
+    stream = torch.cuda.current_stream()
+
+    def integrators():
+        return [Integrator(s, fb, max_depth=d, rr_depth=3) for s, fb, d in zip(scenes, fbs, depth)]
+
+    def sequential():
+        for it, n in zip(integrators(), spps):
+            it.RenderFrame(n)
+
+    def batched():
+        RenderBatch(integrators(), spps)
+
+    def timed(f):
+        f()
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            f()
+            e1.record(stream)
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    seq_default = timed(sequential)
+    owner = scenes[0].ctx
+    owner.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    tune = owner.autotune_batch([s.ctx for s in scenes], [(n, 0, d, 3) for n, d in zip(spps, depth)], spp_cap=1)
+    tune_s = time.perf_counter() - t0
+    bat = timed(batched)
+    st = owner.stats()
+    tuned = tune.as_dict()
+    for s in scenes[1:]:
+        s.ctx.set_tuning(**{k: v for k, v in tuned.items() if k != "ms"})
+    seq_tuned = timed(sequential)
+    seq = min(seq_default, seq_tuned)
+
+    # the scenes marked for the adjoint: differentiable forward (keeping every
+    # sample's radiance) and the adjoint of loss = sum(image^2), per scene vs batched
+    from lantern_gb300.diff import DiffScene, adjoint_batch, render_batch
+    marked = [k for k, sc in enumerate(gen) if sc.render.get("adjoint")]
+    dss = [DiffScene(ctx=scenes[k].ctx) for k in marked]
+    prm = [ds.defaults() for ds in dss]
+    asp = [spps[k] for k in marked]
+    adep = [depth[k] for k in marked]
+
+    def adj_sequential():
+        for ds, p, n, d in zip(dss, prm, asp, adep):
+            rgb, _, _, smp = ds.render(*p, n, 0, d, 3, keep_samples=True)
+            ds.adjoint(*p, (2.0 * rgb / n) / n, n, 0, d, 3, samples=smp)
+            del smp
+
+    def adj_batched():
+        outs = render_batch(dss, prm, asp, 0, adep, 3, keep_samples=True)
+        adjoint_batch(dss, prm, [(2.0 * o[0] / n) / n for o, n in zip(outs, asp)], asp, 0, adep, 3,
+                      samples=[o[3] for o in outs])
+
+    adj_samples = sum(ds.width * ds.height * n for ds, n in zip(dss, asp))
+    adj_seq = timed(adj_sequential)
+    adj_bat = timed(adj_batched)
+    return {"workload": f"{count} scenes (seed 5): 128^2-1024^2, 1k-500k triangles, 4/16/64 spp, 30% medium; "
+                        f"{len(marked)} also run the adjoint",
+            "samples": samples, "triangles": sum(s.info().num_triangles for s in scenes),
+            "sequential_ms": round(seq_default, 2), "sequential_tuned_ms": round(seq_tuned, 2),
+            "batched_ms": round(bat, 2), "batched_msamples_per_s": round(samples / bat / 1e3, 2),
+            "speedup_vs_sequential": round(seq / bat, 3), "tuning": tuned, "tune_s": round(tune_s, 2),
+            "batched_iterations": st.iterations, "batched_kernel_launches": st.kernel_launches,
+            "adjoint_scenes": len(marked), "adjoint_samples": adj_samples,
+            "adjoint_sequential_ms": round(adj_seq, 2), "adjoint_batched_ms": round(adj_bat, 2),
+            "adjoint_speedup": round(adj_seq / adj_bat, 3),
+            "total_sequential_ms": round(seq + adj_seq, 2), "total_batched_ms": round(bat + adj_bat, 2),
+            "total_speedup": round((seq + adj_seq) / (bat + adj_bat), 3)}
 
 
 def microbench(scene, path, local, n=1 << 24):

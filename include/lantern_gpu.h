@@ -206,6 +206,68 @@ typedef struct lt_render_stats {
 } lt_render_stats;
 lt_status lt_render_stats_get(lt_ctx *ctx, lt_render_stats *out);
 
+/* ---------------------------------------------------------------- resolve */
+/* The visualizer's final pass into a headless buffer (the window, swapchain and
+ * GLSL pass are not part of this library). Per pixel, as
+ * visualizer.cpp:352-364 and final_resolve_ps.glsl:24-43 compute it:
+ *   c = exp2f(exposure_stops) * (ColorData / ColorSampleCount, 1)   (visualizer.cpp:1308)
+ *   LT_TONEMAP_CLAMP:  c = clamp(c, 0, 1)
+ *   LT_TONEMAP_FILMIC: x = max(0, c - 0.004); c = clamp(x(6.2x + 0.5) / (x(6.2x + 1.7) + 0.06), 0, 1); alpha = 1
+ * rgba (4 floats per pixel) and rgba8 (4 bytes per pixel, round(c * 255) as
+ * the swapchain's UNORM format stores it) may each be NULL; both are device
+ * pointers when film->on_device, else host memory. spp (optional, host)
+ * receives the minimum, maximum and sum of the sample counts. A pixel with no
+ * samples divides by zero as the reference does. */
+enum { LT_TONEMAP_CLAMP = 0, LT_TONEMAP_FILMIC = 1 };
+typedef struct lt_spp_range { uint32_t min_spp, max_spp; uint64_t sum_spp; } lt_spp_range;
+lt_status lt_resolve(lt_ctx *ctx, const lt_film *film, int32_t tonemap, float exposure_stops, float *rgba,
+                     uint8_t *rgba8, lt_spp_range *spp);
+
+/* ---------------------------------------------------------------- batching and tuning */
+/* Extension with no counterpart in the reference, whose integrator renders one
+ * scene per Integrator (integrator.cpp:28-43): the wavefront's launch
+ * configuration, and many scenes rendered together in one captured loop. */
+typedef struct lt_tuning {
+    uint32_t paths_in_flight;  /* wavefront path slots; 0 = min(samples, 2,097,152) */
+    uint32_t trace_threads;    /* threads per block of the path-segment trace kernel: 64, 128 or 256 */
+    uint32_t shade_threads;    /* ... of the shade kernel (and camera-ray generation) */
+    uint32_t connect_threads;  /* ... of the connection kernel */
+    uint32_t loop_iterations;  /* wavefront iterations per body of lt_render_batch's loop: 2, 4 or 8 */
+    uint32_t bvh_width;        /* children per BVH node: 2 (BVH2) or 8 (compressed 8-wide, built on demand) */
+    float ms;                  /* lt_autotune_batch: device time of the chosen tuning on its sample */
+} lt_tuning;
+/* The context's tuning; it applies to lt_render, lt_render_batch and the
+ * tuner's starting point. Zero fields of lt_set_tuning keep their defaults
+ * (0 paths = automatic, 128 threads, 2 iterations, width 2). Width 8 builds
+ * the scene's compressed 8-wide BVH from its BVH2 (Ylitie, Karras, Laine, HPG
+ * 2017 node layout); lt_scene_create then builds it for every new scene. */
+lt_status lt_get_tuning(const lt_ctx *ctx, lt_tuning *out);
+lt_status lt_set_tuning(lt_ctx *ctx, const lt_tuning *t);
+
+/* Renders scenes[i] (contexts that hold a scene, all on ctx's device; ctx may
+ * be one of them) with params[i] into films[i], as n lt_render calls would,
+ * but together: the work items of all scenes form one sequence over one
+ * wavefront owned by ctx, so that paths of every scene share each launch. The
+ * iteration loop is captured once into a CUDA graph (a while node whose
+ * condition kernel stops when no path is left) and the whole batch runs as one
+ * graph launch on ctx's stream; the graph is kept and reused while the
+ * wavefront and tuning stay the same.
+ * - films must be on the device (on_device = 1), of each camera's size, and
+ *   must not overlap;
+ * - n <= LT_MAX_BATCH; each scene may have at most 1,048,576 lights and 8,190 media;
+ * - returns after the batch has finished (the film writes are complete). */
+#define LT_MAX_BATCH 2048
+lt_status lt_render_batch(lt_ctx *ctx, lt_ctx *const *scenes, const lt_render_params *params, lt_film *films,
+                          uint32_t n);
+
+/* Autotuner: renders the batch (into scratch films, spp capped at spp_cap) under
+ * candidate tunings -- BVH width, paths in flight, threads per block of each
+ * stage, iterations per loop body -- by coordinate descent from ctx's tuning,
+ * keeps the fastest in ctx and returns it in *best (may be NULL). Trying width
+ * 8 builds the 8-wide BVH of every scene of the batch. */
+lt_status lt_autotune_batch(lt_ctx *ctx, lt_ctx *const *scenes, const lt_render_params *params, uint32_t n,
+                            uint32_t spp_cap, lt_tuning *best);
+
 /* ---------------------------------------------------------------- differentiable rendering */
 /* Extension with no counterpart in the reference: gradients of an image loss
  * with respect to per-triangle albedo, per-triangle emission and per-medium
@@ -250,6 +312,30 @@ lt_status lt_render_adjoint(lt_ctx *ctx, const lt_render_params *params, const l
                             const float *d_loss_d_film, float *grad_albedo, float *grad_emission,
                             float *grad_sigma_a, float *grad_sigma_s, const uint32_t *crop,
                             const float *sample_radiance);
+
+/* Batched forms of lt_render_diff and lt_render_adjoint: each job names a
+ * scene (a context holding one, on ctx's device), its render params and
+ * differentiable parameters; all jobs' pixels run in one persistent launch on
+ * ctx's stream (warps take 32 consecutive pixels at a time from a shared
+ * counter, so scenes of any size and spp fill the GPU together). Per job the
+ * results are those of the single-scene call over the whole film (no crop).
+ * - lt_render_diff_batch: film (device, additive) and sample_radiance
+ *   (optional, as lt_render_diff's) are outputs;
+ * - lt_render_adjoint_batch: d_loss_d_film and sample_radiance (optional) are
+ *   inputs, the four gradient arrays outputs (accumulated; sigma arrays may be
+ *   NULL for scenes without media). Jobs must not share gradient arrays.
+ * n <= LT_MAX_BATCH. The calls return once the work is queued. */
+typedef struct lt_diff_job {
+    lt_ctx *scene;
+    lt_render_params params;
+    lt_diff_params dp;
+    lt_film film;
+    float *sample_radiance;
+    const float *d_loss_d_film;
+    float *grad_albedo, *grad_emission, *grad_sigma_a, *grad_sigma_s;
+} lt_diff_job;
+lt_status lt_render_diff_batch(lt_ctx *ctx, const lt_diff_job *jobs, uint32_t n);
+lt_status lt_render_adjoint_batch(lt_ctx *ctx, const lt_diff_job *jobs, uint32_t n);
 
 /* ---------------------------------------------------------------- rays */
 typedef struct lt_ray { float org[3]; float tnear; float dir[3]; float tfar; } lt_ray; /* 32 B */

@@ -7,7 +7,9 @@
 // batch until no path is left.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -30,6 +32,8 @@ struct lt_ctx {
 
     // scene
     bool has_scene = false;
+    bool has_bvh8 = false;
+    uint32_t bvh8_depth = 0;
     HostScene host;
     DevScene dev{};
     std::vector<void *> scene_allocs;
@@ -45,6 +49,18 @@ struct lt_ctx {
     // scratch for host-memory calls
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+
+    // launch configuration (lt_set_tuning / lt_autotune_batch); shape is the
+    // single-scene instantiation's, batch_shape the batched one's
+    lt_tuning tuning{};
+    LaunchShape batch_shape;
+
+    // batched rendering: the scene table (pinned host copy + device copy) and
+    // the captured loop, rebuilt when its key changes
+    SceneTable *table_host = nullptr, *table_dev = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<uintptr_t> graph_key;
 
     lt_render_stats stats{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -79,12 +95,41 @@ static void free_scene(lt_ctx *c) {
     c->scene_allocs.clear();
     c->scene_bytes = 0;
     c->has_scene = false;
+    c->has_bvh8 = false;
     c->dev = DevScene{};
 }
 
+static void free_graph(lt_ctx *c) {
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->graph_exec = nullptr;
+    c->graph = nullptr;
+    c->graph_key.clear();
+}
+
 static void free_wave(lt_ctx *c) {
+    free_graph(c);  // its kernels point into the arena
     if (c->wave.arena) cudaFree(c->wave.arena);
     c->wave = Wavefront{};
+}
+
+static void default_tuning(lt_tuning *t) {
+    *t = lt_tuning{};
+    t->trace_threads = t->shade_threads = t->connect_threads = 128;
+    t->loop_iterations = 2;
+    t->bvh_width = 2;
+}
+
+// Block counts of both kernel instantiations for the tuning's thread counts.
+static void apply_tuning(lt_ctx *c) {
+    for (LaunchShape *ls : {&c->shape, &c->batch_shape}) {
+        ls->bvh_width = (int)c->tuning.bvh_width;
+        ls->trace_threads = (int)c->tuning.trace_threads;
+        ls->shade_threads = (int)c->tuning.shade_threads;
+        ls->connect_threads = (int)c->tuning.connect_threads;
+    }
+    query_launch_shape(c->device, false, &c->shape);
+    query_launch_shape(c->device, true, &c->batch_shape);
 }
 
 extern "C" {
@@ -113,7 +158,8 @@ lt_status lt_ctx_create(int device, lt_ctx **out) {
         return fail(nullptr, LT_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
     }
     c->stream = c->own_stream;
-    query_launch_shape(device, &c->shape);
+    default_tuning(&c->tuning);
+    apply_tuning(c);
     *out = c;
     return LT_OK;
 }
@@ -124,6 +170,8 @@ void lt_ctx_destroy(lt_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_scene(c);
     free_wave(c);
+    if (c->table_dev) cudaFree(c->table_dev);
+    if (c->table_host) cudaFreeHost(c->table_host);
     if (c->scratch) cudaFree(c->scratch);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->isect_fetch) cudaFree(c->isect_fetch);
@@ -168,6 +216,43 @@ static lt_status upload(lt_ctx *c, const std::vector<T> &v, const T **dst) {
     c->scene_bytes += bytes;
     if (bytes) CUDA_TRY(c, cudaMemcpyAsync(p, v.data(), bytes, cudaMemcpyHostToDevice, c->stream));
     *dst = (const T *)p;
+    return LT_OK;
+}
+
+// Builds the compressed 8-wide BVH of the context's scene from its BVH2 (read
+// back from the device when the GPU built it) and uploads it.
+static lt_status ensure_bvh8(lt_ctx *c) {
+    if (c->has_bvh8) return LT_OK;
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
+    HostScene &h = c->host;
+    std::vector<BvhNode> nodes = h.nodes;
+    std::vector<float> tris = h.leaf_tris;
+    if (nodes.empty()) {
+        nodes.resize(c->num_nodes);
+        tris.resize(12 * h.tri_geom.size());
+        CUDA_TRY(c, cudaMemcpyAsync(nodes.data(), c->dev.nodes, nodes.size() * sizeof(BvhNode),
+                                    cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(tris.data(), c->dev.tris, tris.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    std::vector<Bvh8Node> n8;
+    std::vector<float> t8;
+    const uint32_t depth = build_bvh8(nodes, tris, &n8, &t8);
+    if (2 * depth + 2 > 64)
+        return fail(c, LT_ERR_UNSUPPORTED, "8-wide BVH depth %u exceeds the traversal stack", depth);
+    std::vector<float> nf(n8.size() * 20);
+    memcpy(nf.data(), n8.data(), nf.size() * sizeof(float));
+    const float *d_nodes = nullptr, *d_tris = nullptr;
+    lt_status st = upload(c, nf, &d_nodes);
+    if (st == LT_OK) st = upload(c, t8, &d_tris);
+    if (st != LT_OK) return st;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->dev.nodes8 = (const float4 *)d_nodes;
+    c->dev.tris8 = (const float4 *)d_tris;
+    c->dev.num_nodes8 = (uint32_t)n8.size();
+    c->bvh8_depth = depth;
+    c->has_bvh8 = true;
     return LT_OK;
 }
 
@@ -219,6 +304,9 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     }
     if (h.max_depth >= 64)
         return fail(c, LT_ERR_UNSUPPORTED, "BVH depth %u exceeds the traversal stack", h.max_depth);
+    if (h.lights.size() > kMaxLights || h.media.size() > kMaxMedia)
+        return fail(c, LT_ERR_UNSUPPORTED, "%zu lights / %zu media: at most %u and %u", h.lights.size(),
+                    h.media.size(), kMaxLights, kMaxMedia);
     if ((st = upload(c, h.tri_geom, &d.tri_geom)) != LT_OK) return st;
     if ((st = upload(c, h.tri_vidx, &d.tri_vidx)) != LT_OK) return st;
     if ((st = upload(c, h.vnormal, &d.vnormal)) != LT_OK) return st;
@@ -236,6 +324,7 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     d.filter = h.filter;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->has_scene = true;
+    if (c->tuning.bvh_width == 8) return ensure_bvh8(c);
     return LT_OK;
 }
 
@@ -314,9 +403,19 @@ static lt_status ensure_wave(lt_ctx *c, uint32_t cap) {
     return LT_OK;
 }
 
-static uint32_t default_capacity(unsigned long long total) {
-    const unsigned long long kMax = 1ull << 21;  // 2M path slots, ~560 MB
-    return (uint32_t)(total < kMax ? total : kMax);
+// Paths in flight for `total` work items: the tuning's count, else 2M path
+// slots (~650 MB), and never more than the work.
+static uint32_t capacity_for(const lt_ctx *c, unsigned long long total) {
+    const unsigned long long cap = c->tuning.paths_in_flight ? c->tuning.paths_in_flight : 1ull << 21;
+    return (uint32_t)(total < cap ? total : cap);
+}
+
+// The context's arena laid out for `cap` entries (cap <= the arena's capacity).
+static Wavefront wave_view(const lt_ctx *c, uint32_t cap) {
+    Wavefront w;
+    w.arena_bytes = carve_wave((char *)c->wave.arena, cap, &w);
+    w.arena = c->wave.arena;
+    return w;
 }
 
 extern "C" {
@@ -359,10 +458,12 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
         CUDA_TRY(c, launch_add_counts(f, (uint32_t)npix, p->spp, c->stream));
         c->stats.kernel_launches = 1;
     } else if (a.total > 0) {
-        lt_status st = ensure_wave(c, default_capacity(a.total));
+        const uint32_t cap = capacity_for(c, a.total);
+        lt_status st = ensure_wave(c, cap);
         if (st != LT_OK) return st;
-        CUDA_TRY(c, cudaMemsetAsync(c->wave.counters, 0, sizeof(WaveCounters), c->stream));
-        CUDA_TRY(c, launch_wave_init(c->dev, c->wave, a, f, c->shape, c->stream));
+        const Wavefront w = wave_view(c, cap);
+        CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
+        CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
         uint32_t launches = 1, iters = 0;
         size_t nev = 0;
         c->stage_of_event.clear();
@@ -378,17 +479,17 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
                     }
                     CUDA_TRY(c, cudaEventRecord(c->stage_events[nev++], c->stream));
                     c->stage_of_event.push_back(stage);
-                    CUDA_TRY(c, launch_wave_stage(stage, c->dev, c->wave, a, f, cur, c->shape, c->stream));
+                    CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
                 }
                 launches += 3;
                 cur ^= 1;
                 ++iters;
             }
-            CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, c->wave.counters, sizeof(WaveCounters),
+            CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters),
                                         cudaMemcpyDeviceToHost, c->stream));
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
             if (c->counters_host->count[cur] == 0) break;
-            if (iters > 4u * (p->max_depth + 8u) * (uint32_t)((a.total + c->wave.capacity - 1) / c->wave.capacity) + 64u)
+            if (iters > 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u)
                 return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
         }
         c->stats.main_rays = c->counters_host->main_rays;
@@ -638,4 +739,408 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
     c->stats.samples = a.total;
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     return LT_OK;
+}
+
+// ------------------------------------------------------------------ tuning
+extern "C" lt_status lt_get_tuning(const lt_ctx *c, lt_tuning *out) {
+    if (!c || !out) return LT_ERR_INVALID;
+    *out = c->tuning;
+    return LT_OK;
+}
+
+static bool valid_threads(uint32_t t) { return t == 64 || t == 128 || t == 256; }
+
+extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) {
+    if (!c || !t) return fail(c, LT_ERR_INVALID, "NULL argument");
+    lt_tuning n;
+    default_tuning(&n);
+    n.paths_in_flight = t->paths_in_flight;
+    if (t->trace_threads) n.trace_threads = t->trace_threads;
+    if (t->shade_threads) n.shade_threads = t->shade_threads;
+    if (t->connect_threads) n.connect_threads = t->connect_threads;
+    if (t->loop_iterations) n.loop_iterations = t->loop_iterations;
+    if (t->bvh_width) n.bvh_width = t->bvh_width;
+    n.ms = t->ms;
+    if (!valid_threads(n.trace_threads) || !valid_threads(n.shade_threads) || !valid_threads(n.connect_threads))
+        return fail(c, LT_ERR_INVALID, "threads per block must be 64, 128 or 256");
+    if (n.loop_iterations != 2 && n.loop_iterations != 4 && n.loop_iterations != 8)
+        return fail(c, LT_ERR_INVALID, "loop_iterations must be 2, 4 or 8");
+    if (n.bvh_width != 2 && n.bvh_width != 8)
+        return fail(c, LT_ERR_UNSUPPORTED, "BVH width %u: the widths built are 2 and 8", n.bvh_width);
+    if (n.paths_in_flight && (n.paths_in_flight < 1024 || n.paths_in_flight > (1u << 24)))
+        return fail(c, LT_ERR_INVALID, "paths_in_flight %u outside 1024..16777216", n.paths_in_flight);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (n.bvh_width == 8 && c->has_scene) {
+        lt_status st = ensure_bvh8(c);
+        if (st != LT_OK) return st;
+    }
+    c->tuning = n;
+    apply_tuning(c);
+    return LT_OK;
+}
+
+// ------------------------------------------------------------------ lt_render_batch
+// Captures the batched loop for wavefront `w`: memset(counters), camera rays,
+// then a while node whose body runs loop_iterations (trace, shade, connect)
+// iterations and the condition kernel. Captured on the context's own stream in
+// thread-local mode, so other threads' CUDA calls are not affected.
+static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
+    std::vector<uintptr_t> key = {(uintptr_t)c->wave.arena, w.capacity, (uintptr_t)c->table_dev,
+                                  (uintptr_t)c->batch_shape.trace_threads, (uintptr_t)c->batch_shape.trace_blocks,
+                                  (uintptr_t)c->batch_shape.shade_threads, (uintptr_t)c->batch_shape.shade_blocks,
+                                  (uintptr_t)c->batch_shape.connect_threads, (uintptr_t)c->batch_shape.connect_blocks,
+                                  c->tuning.loop_iterations};
+    if (c->graph_exec && key == c->graph_key) return LT_OK;
+    free_graph(c);
+    cudaStream_t cs = c->own_stream;
+    CUDA_TRY(c, cudaGraphCreate(&c->graph, 0));
+    cudaGraphConditionalHandle h;
+    CUDA_TRY(c, cudaGraphConditionalHandleCreate(&h, c->graph, 1, cudaGraphCondAssignDefault));
+
+    // prologue, then the while node appended to the capture
+    CUDA_TRY(c, cudaStreamBeginCaptureToGraph(cs, c->graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};  // the rest zero
+    cudaError_t e = cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), cs);
+    if (e == cudaSuccess) e = launch_batch_init(c->table_dev, w, c->batch_shape, cs);
+    if (e == cudaSuccess) {
+        cudaStreamCaptureStatus status;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t ndeps = 0;
+        e = cudaStreamGetCaptureInfo(cs, &status, nullptr, nullptr, &deps, nullptr, &ndeps);
+        if (e == cudaSuccess) {
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t cond;
+            e = cudaGraphAddNode(&cond, c->graph, deps, nullptr, ndeps, &cp);
+            if (e == cudaSuccess)
+                e = cudaStreamUpdateCaptureDependencies(cs, &cond, nullptr, 1, cudaStreamSetCaptureDependencies);
+        }
+    }
+    cudaGraph_t captured = nullptr;
+    cudaError_t e_end = cudaStreamEndCapture(cs, &captured);
+    CUDA_TRY(c, e);
+    CUDA_TRY(c, e_end);
+
+    // loop body
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CUDA_TRY(c, cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int cur = 0;
+    for (uint32_t k = 0; k < c->tuning.loop_iterations && e == cudaSuccess; ++k) {
+        for (int stage = 0; stage < 3 && e == cudaSuccess; ++stage)
+            e = launch_batch_stage(stage, c->table_dev, w, cur, c->batch_shape, cs);
+        cur ^= 1;
+    }
+    if (e == cudaSuccess) e = launch_loop_condition(w, c->table_dev, h, cur, c->tuning.loop_iterations, cs);
+    e_end = cudaStreamEndCapture(cs, &captured);
+    CUDA_TRY(c, e);
+    CUDA_TRY(c, e_end);
+    CUDA_TRY(c, cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+    c->graph_key = key;
+    return LT_OK;
+}
+
+// The scene table's host and device copies; waits until the previous
+// batch's table upload (from the pinned host copy) has completed.
+static lt_status ensure_table(lt_ctx *c) {
+    if (!c->table_host) {
+        CUDA_TRY(c, cudaMallocHost((void **)&c->table_host, sizeof(SceneTable)));
+        CUDA_TRY(c, cudaMalloc((void **)&c->table_dev, sizeof(SceneTable)));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return LT_OK;
+}
+
+extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_render_params *params,
+                                     lt_film *films, uint32_t n) {
+    if (!c || (n && (!scenes || !params || !films))) return fail(c, LT_ERR_INVALID, "NULL argument");
+    if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u scenes; a batch holds at most %u", n, LT_MAX_BATCH);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    lt_status st0 = ensure_table(c);
+    if (st0 != LT_OK) return st0;
+    SceneTable &T = *c->table_host;
+    uint32_t count = 0, max_depth = 0, launches = 0;
+    unsigned long long total = 0;
+    c->stats = lt_render_stats{};
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    for (uint32_t i = 0; i < n; ++i) {
+        const lt_ctx *s = scenes[i];
+        const lt_render_params &p = params[i];
+        const lt_film &f = films[i];
+        if (!s || !s->has_scene) return fail(c, LT_ERR_STATE, "batch scene %u: no scene", i);
+        if (s->device != c->device) return fail(c, LT_ERR_INVALID, "batch scene %u is on another device", i);
+        if (c->tuning.bvh_width == 8 && !s->has_bvh8) {
+            lt_status sb = ensure_bvh8(const_cast<lt_ctx *>(s));
+            if (sb != LT_OK) return fail(c, sb, "batch scene %u: %s", i, s->error.c_str());
+        }
+        const uint32_t W = s->host.camera.width, H = s->host.camera.height;
+        if (!f.on_device || f.width != W || f.height != H || !f.rgb || !f.bounces || !f.counts)
+            return fail(c, LT_ERR_INVALID, "batch film %u: needs device buffers of %ux%u", i, W, H);
+        const unsigned long long items = (unsigned long long)W * H * p.spp;
+        if (items == 0) continue;
+        FilmPtrs fp{f.rgb, f.bounces, f.counts};
+        if (p.max_depth == 0) {  // the bounce loop never runs
+            CUDA_TRY(c, launch_add_counts(fp, W * H, p.spp, c->stream));
+            ++launches;
+            continue;
+        }
+        SceneSlot &slot = T.slots[count];
+        slot.s = s->dev;
+        slot.a = RenderArgs{W, H, p.first_frame, p.max_depth, p.rr_depth, items};
+        slot.f = fp;
+        T.begin[count] = total;
+        total += items;
+        if (p.max_depth > max_depth) max_depth = p.max_depth;
+        ++count;
+    }
+    c->stats.samples = total;
+    if (count) {
+        const uint32_t cap = capacity_for(c, total);
+        lt_status st = ensure_wave(c, cap);
+        if (st != LT_OK) return st;
+        const Wavefront w = wave_view(c, cap);
+        T.count = count;
+        T.pad = 0;
+        T.total = total;
+        T.iteration_limit = 4ull * (max_depth + 8ull) * ((total + cap - 1) / cap) + 64ull;
+        CUDA_TRY(c, cudaMemcpyAsync(c->table_dev, c->table_host, offsetof(SceneTable, slots), cudaMemcpyHostToDevice,
+                                    c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->slots, T.slots, count * sizeof(SceneSlot), cudaMemcpyHostToDevice,
+                                    c->stream));
+        if ((st = build_batch_graph(c, w)) != LT_OK) return st;
+        CUDA_TRY(c, cudaGraphLaunch(c->graph_exec, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        const WaveCounters &k = *c->counters_host;
+        if (k.error == 2) return fail(c, LT_ERR_TIMEOUT, "batched wavefront did not drain in %llu iterations", k.iterations);
+        c->stats.main_rays = k.main_rays;
+        c->stats.light_rays = k.light_rays;
+        c->stats.bsdf_rays = k.bsdf_rays;
+        c->stats.iterations = (uint32_t)k.iterations;
+        launches += 1 + 3 * (uint32_t)k.iterations + (uint32_t)(k.iterations / c->tuning.loop_iterations);
+    } else {
+        CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    c->stats.kernel_launches = launches;
+    return LT_OK;
+}
+
+// ------------------------------------------------------------------ lt_autotune_batch
+extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_render_params *params, uint32_t n,
+                                       uint32_t spp_cap, lt_tuning *best) {
+    if (!c || !n || !scenes || !params) return fail(c, LT_ERR_INVALID, "NULL argument or empty batch");
+    if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u scenes; a batch holds at most %u", n, LT_MAX_BATCH);
+    if (spp_cap == 0) spp_cap = 1;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    // scratch films, one per scene, and the capped render parameters
+    std::vector<lt_render_params> prm(params, params + n);
+    std::vector<size_t> off(n);
+    size_t bytes = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!scenes[i] || !scenes[i]->has_scene) return fail(c, LT_ERR_STATE, "batch scene %u: no scene", i);
+        if (prm[i].spp > spp_cap) prm[i].spp = spp_cap;
+        off[i] = bytes;
+        bytes += ((size_t)scenes[i]->host.camera.width * scenes[i]->host.camera.height * 20 + 255) & ~(size_t)255;
+    }
+    lt_status st = ensure_scratch(c, bytes);
+    if (st != LT_OK) return st;
+    std::vector<lt_film> films(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t W = scenes[i]->host.camera.width, H = scenes[i]->host.camera.height;
+        char *b = (char *)c->scratch + off[i];
+        films[i].rgb = (float *)b;
+        films[i].bounces = (uint32_t *)(b + (size_t)W * H * 12);
+        films[i].counts = films[i].bounces + (size_t)W * H;
+        films[i].width = W;
+        films[i].height = H;
+        films[i].on_device = 1;
+    }
+    auto measure = [&](const lt_tuning &t, float *ms) -> lt_status {
+        lt_status s2 = lt_set_tuning(c, &t);
+        if (s2 != LT_OK) return s2;
+        float best_ms = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {  // the first run also captures the graph
+            CUDA_TRY(c, cudaMemsetAsync(c->scratch, 0, bytes, c->stream));
+            if ((s2 = lt_render_batch(c, scenes, prm.data(), films.data(), n)) != LT_OK) return s2;
+            float m = 0.0f;
+            CUDA_TRY(c, cudaEventElapsedTime(&m, c->ev0, c->ev1));
+            if (rep > 0 && m < best_ms) best_ms = m;
+        }
+        *ms = best_ms;
+        return LT_OK;
+    };
+    lt_tuning cur = c->tuning;
+    float cur_ms = 0.0f;
+    if ((st = measure(cur, &cur_ms)) != LT_OK) return st;
+    const uint32_t widths[] = {2, 8};
+    const uint32_t paths[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
+    const uint32_t threads[] = {64, 128, 256};
+    const uint32_t iters[] = {2, 4, 8};
+    for (int coord = 0; coord < 6; ++coord) {
+        const uint32_t *vals = coord == 0 ? widths : coord == 1 ? paths : coord == 5 ? iters : threads;
+        const int nv = coord == 0 ? 2 : coord == 1 ? 4 : 3;
+        for (int v = 0; v < nv; ++v) {
+            lt_tuning t = cur;
+            uint32_t *field = coord == 0   ? &t.bvh_width
+                              : coord == 1 ? &t.paths_in_flight
+                              : coord == 2 ? &t.trace_threads
+                              : coord == 3 ? &t.shade_threads
+                              : coord == 4 ? &t.connect_threads
+                                           : &t.loop_iterations;
+            if (*field == vals[v]) continue;
+            *field = vals[v];
+            float ms = 0.0f;
+            if ((st = measure(t, &ms)) != LT_OK) return st;
+            if (ms < cur_ms) {
+                cur = t;
+                cur_ms = ms;
+            }
+        }
+    }
+    cur.ms = cur_ms;
+    if ((st = lt_set_tuning(c, &cur)) != LT_OK) return st;
+    if (best) *best = c->tuning;
+    return LT_OK;
+}
+
+// ------------------------------------------------------------------ lt_resolve
+extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap, float exposure_stops, float *rgba,
+                                uint8_t *rgba8, lt_spp_range *spp) {
+    if (!c || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
+    if (tonemap != LT_TONEMAP_CLAMP && tonemap != LT_TONEMAP_FILMIC)
+        return fail(c, LT_ERR_INVALID, "unknown tone mapper %d", tonemap);
+    if (!film->rgb || !film->counts) return fail(c, LT_ERR_INVALID, "film buffers missing");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const size_t npix = (size_t)film->width * film->height;
+    if (npix > 0xFFFFFFFFull) return fail(c, LT_ERR_INVALID, "film too large");
+    const float exposure = exp2f(exposure_stops);
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    // scratch: [stats][film rgb, counts when on the host][outputs when on the host]
+    const bool host = !film->on_device;
+    size_t need = al(sizeof(SppStats));
+    if (host) need += al(npix * 12) + al(npix * 4) + (rgba ? al(npix * 16) : 0) + (rgba8 ? al(npix * 4) : 0);
+    lt_status st = ensure_scratch(c, need);
+    if (st != LT_OK) return st;
+    char *s = (char *)c->scratch;
+    SppStats *d_stats = (SppStats *)s;
+    s += al(sizeof(SppStats));
+    const float *d_rgb = film->rgb;
+    const uint32_t *d_counts = film->counts;
+    float4 *d_out = (float4 *)rgba;
+    uchar4 *d_out8 = (uchar4 *)rgba8;
+    if (host) {
+        float *r = (float *)s;
+        s += al(npix * 12);
+        uint32_t *n = (uint32_t *)s;
+        s += al(npix * 4);
+        CUDA_TRY(c, cudaMemcpyAsync(r, film->rgb, npix * 12, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(n, film->counts, npix * 4, cudaMemcpyHostToDevice, c->stream));
+        d_rgb = r;
+        d_counts = n;
+        if (rgba) { d_out = (float4 *)s; s += al(npix * 16); }
+        if (rgba8) { d_out8 = (uchar4 *)s; s += al(npix * 4); }
+    } else if (((uintptr_t)rgba & 15u) || ((uintptr_t)rgba8 & 3u)) {
+        return fail(c, LT_ERR_INVALID, "rgba must be 16-byte and rgba8 4-byte aligned");
+    }
+    CUDA_TRY(c, launch_resolve(d_rgb, d_counts, (uint32_t)npix, tonemap, exposure, d_out, d_out8, d_stats,
+                               c->shape.sms, c->stream));
+    if (host) {
+        if (rgba) CUDA_TRY(c, cudaMemcpyAsync(rgba, d_out, npix * 16, cudaMemcpyDeviceToHost, c->stream));
+        if (rgba8) CUDA_TRY(c, cudaMemcpyAsync(rgba8, d_out8, npix * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (spp || host) {
+        SppStats h{};
+        CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, d_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        memcpy(&h, c->counters_host, sizeof h);
+        if (spp) {
+            spp->min_spp = h.min_spp;
+            spp->max_spp = h.max_spp;
+            spp->sum_spp = h.sum_spp;
+        }
+    }
+    return LT_OK;
+}
+
+// ------------------------------------------------------------------ batched differentiable rendering
+static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool adjoint) {
+    if (!c || (n && !jobs)) return fail(c, LT_ERR_INVALID, "NULL argument");
+    if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u jobs; a batch holds at most %u", n, LT_MAX_BATCH);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    lt_status st = ensure_table(c);
+    if (st != LT_OK) return st;
+    SceneTable &T = *c->table_host;
+    uint32_t count = 0;
+    unsigned long long pixels = 0, samples = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const lt_diff_job &j = jobs[i];
+        const lt_ctx *s = j.scene;
+        if (!s || !s->has_scene) return fail(c, LT_ERR_STATE, "job %u: no scene", i);
+        if (s->device != c->device) return fail(c, LT_ERR_INVALID, "job %u is on another device", i);
+        const HostScene &h = s->host;
+        const uint32_t W = h.camera.width, H = h.camera.height;
+        const bool media = !h.media.empty();
+        if (!j.dp.albedo || !j.dp.emission || (media && (!j.dp.sigma_a || !j.dp.sigma_s)))
+            return fail(c, LT_ERR_INVALID, "job %u: differentiable parameters missing", i);
+        if (!adjoint && (!j.film.on_device || j.film.width != W || j.film.height != H || !j.film.rgb ||
+                         !j.film.bounces || !j.film.counts))
+            return fail(c, LT_ERR_INVALID, "job %u: needs a device film of %ux%u", i, W, H);
+        if (adjoint && (!j.d_loss_d_film || !j.grad_albedo || !j.grad_emission ||
+                        (media && (!j.grad_sigma_a || !j.grad_sigma_s))))
+            return fail(c, LT_ERR_INVALID, "job %u: adjoint inputs or gradient arrays missing", i);
+        if ((unsigned long long)W * H * j.params.spp == 0) continue;
+        SceneSlot &sl = T.slots[count];
+        DiffSlot &d = T.diff[count];
+        sl.s = s->dev;
+        sl.a = RenderArgs{W, H, j.params.first_frame, j.params.max_depth, j.params.rr_depth,
+                          (unsigned long long)W * H * j.params.spp};
+        sl.f = FilmPtrs{j.film.rgb, j.film.bounces, j.film.counts};
+        d.p.albedo = j.dp.albedo;
+        d.p.emission = j.dp.emission;
+        d.p.sigma_a = j.dp.sigma_a;
+        d.p.sigma_s = j.dp.sigma_s;
+        d.p.albedo_s = j.dp.albedo_detached ? j.dp.albedo_detached : j.dp.albedo;
+        d.p.sigma_a_s = j.dp.sigma_a_detached ? j.dp.sigma_a_detached : j.dp.sigma_a;
+        d.p.sigma_s_s = j.dp.sigma_s_detached ? j.dp.sigma_s_detached : j.dp.sigma_s;
+        d.g = DiffGrads{j.d_loss_d_film, j.grad_albedo, j.grad_emission, j.grad_sigma_a, j.grad_sigma_s,
+                        0, 0, W, H, adjoint ? j.sample_radiance : nullptr};
+        d.sample_I = adjoint ? nullptr : j.sample_radiance;
+        d.num_media = (uint32_t)h.media.size();
+        T.pbegin[count] = pixels;
+        pixels += (unsigned long long)W * H;
+        samples += sl.a.total;
+        ++count;
+    }
+    c->stats = lt_render_stats{};
+    c->stats.samples = samples;
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    if (count) {
+        T.count = count;
+        T.pad = 0;
+        T.total = 0;
+        T.iteration_limit = 0;
+        T.total_pixels = pixels;
+        T.fetch = 0;
+        CUDA_TRY(c, cudaMemcpyAsync(c->table_dev, c->table_host, offsetof(SceneTable, slots),
+                                    cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->slots, T.slots, count * sizeof(SceneSlot), cudaMemcpyHostToDevice,
+                                    c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->diff, T.diff, count * sizeof(DiffSlot), cudaMemcpyHostToDevice,
+                                    c->stream));
+        CUDA_TRY(c, launch_diff_batch(adjoint, c->table_dev, c->shape, c->stream));
+        c->stats.kernel_launches = 1;
+    }
+    CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    return LT_OK;
+}
+
+extern "C" lt_status lt_render_diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n) {
+    return diff_batch(c, jobs, n, false);
+}
+
+extern "C" lt_status lt_render_adjoint_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n) {
+    return diff_batch(c, jobs, n, true);
 }

@@ -22,8 +22,11 @@ struct DevScene {
     const MediumInfo *meds;
     const LightInfo *lights;
     const float4 *light_tris;   // emissive meshes' triangles, 3 float4 each
+    const float4 *nodes8;       // compressed 8-wide BVH (Bvh8Node, 5 float4 each), or null
+    const float4 *tris8;        // triangles in 8-wide leaf order, 3 float4 each
     uint32_t num_lights;
     uint32_t num_tris;
+    uint32_t num_nodes8;
     v3 background;
     Camera cam;
     TentFilter filter;
@@ -53,6 +56,7 @@ struct WaveCounters {
     uint32_t trace_fetch;         // persistent-thread ray counters, zeroed by the
     uint32_t connect_fetch;       // kernel that runs before each consumer
     unsigned long long light_traversals;  // connection rays that needed an occlusion query
+    unsigned long long iterations;        // wavefront iterations of a captured loop
 };
 
 struct Wavefront {
@@ -80,10 +84,16 @@ struct RenderArgs {
     unsigned long long total;  // width * height * spp
 };
 
+// Grid and block sizes of the stage kernels. The threads per block are chosen
+// (64, 128 or 256; the autotuner may change them); the block counts follow from
+// the occupancy of the kernel at that size (persistent grids: one full wave).
 struct LaunchShape {
     int sms = 0;
+    int bvh_width = 2;  // 2: BVH2 traversal; 8: compressed 8-wide traversal
+    int trace_threads = 128, shade_threads = 128, connect_threads = 128;
     int trace_blocks = 0, shade_blocks = 0, connect_blocks = 0, isect_blocks = 0;
     int diff_blocks = 0;
+    int diff_fwd_batch_blocks = 0, diff_adj_batch_blocks = 0;
 };
 
 // Parameters of the differentiable render (device arrays): per-triangle RGB
@@ -103,8 +113,58 @@ struct DiffGrads {
     const float *sample_I;  // per-sample radiance from the forward pass, or null (replay twice)
 };
 
+// Limits of the bit fields that carry a scene slot, a light and a medium index
+// in the path flags and connection records.
+constexpr uint32_t kMaxBatchScenes = 2048;
+constexpr uint32_t kMaxLights = 1u << 20;
+constexpr uint32_t kMaxMedia = 8190;
+
+// One scene of a batched render.
+struct SceneSlot {
+    DevScene s;
+    RenderArgs a;
+    FilmPtrs f;
+};
+
+// The scenes of a batch as the kernels read them (device memory, rewritten
+// before each batched render). The work items of all scenes form one
+// sequence: slot i owns [begin[i], begin[i] + slots[i].a.total).
+// Differentiable parameters and outputs of one slot of a batched
+// differentiable render (whole film: the crop is the full image).
+struct DiffSlot {
+    DiffParams p;
+    DiffGrads g;
+    float *sample_I;  // forward: per-sample radiance out, or null
+    uint32_t num_media;
+};
+
+struct SceneTable {
+    uint32_t count;
+    uint32_t pad;
+    unsigned long long total;            // work items of all slots (wavefront)
+    unsigned long long iteration_limit;  // a captured loop stops here (counters->error = 2)
+    unsigned long long total_pixels;     // pixels of all slots (differentiable kernels)
+    unsigned long long fetch;            // pixel counter of the differentiable kernels, 0 on upload
+    unsigned long long begin[kMaxBatchScenes];
+    unsigned long long pbegin[kMaxBatchScenes];
+    SceneSlot slots[kMaxBatchScenes];
+    DiffSlot diff[kMaxBatchScenes];
+};
+
+// Sample-count range of a film (lt_resolve), reduced on the device.
+struct SppStats {
+    uint32_t min_spp, max_spp;
+    unsigned long long sum_spp;
+};
+
+// launcher (lt_resolve.cu): tonemap 0 = clamp, 1 = filmic; out / out8 / stats may be null
+cudaError_t launch_resolve(const float *rgb, const uint32_t *counts, uint32_t npix, int tonemap, float exposure,
+                           float4 *out, uchar4 *out8, SppStats *stats, int sms, cudaStream_t st);
+
 // launchers (lt_kernels.cu)
-void query_launch_shape(int device, LaunchShape *out);
+// Fills the block counts of *out for its thread counts; `batch` selects the
+// ManyScenes instantiations of the stage kernels.
+void query_launch_shape(int device, bool batch, LaunchShape *out);
 cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
                              uint32_t *fetch, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st);
@@ -117,5 +177,16 @@ cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const Render
 enum WaveStage { kStageTrace = 0, kStageShade = 1, kStageConnect = 2 };
 cudaError_t launch_wave_stage(int stage, const DevScene &s, const Wavefront &w, const RenderArgs &a,
                               const FilmPtrs &f, int cur, const LaunchShape &ls, cudaStream_t st);
+// batched render over a scene table (lt_render_batch)
+cudaError_t launch_batch_init(const SceneTable *t, const Wavefront &w, const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_batch_stage(int stage, const SceneTable *t, const Wavefront &w, int cur, const LaunchShape &ls,
+                               cudaStream_t st);
+// Condition kernel of a captured loop: counters->iterations += iters; the
+// while node `h` continues while queue `cur` holds paths and the iteration
+// limit of `t` is not reached.
+// batched differentiable forward (adjoint false) or adjoint over t's slots and diff entries
+cudaError_t launch_diff_batch(bool adjoint, SceneTable *t, const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_loop_condition(const Wavefront &w, const SceneTable *t, cudaGraphConditionalHandle h, int cur,
+                                  uint32_t iters, cudaStream_t st);
 
 }  // namespace lt

@@ -99,10 +99,10 @@ struct Trav {
     int node, leaf, sp;
     bool any;                // occlusion query: stop at the first hit not on `skip_geom`
     uint32_t skip_geom;
-    int stack[kStack];
 };
 
-__device__ __forceinline__ void trav_start(Trav &r, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip_geom) {
+__device__ __forceinline__ void trav_start(Trav &r, int *stack, v3 O, v3 D, float tnear, float tfar, bool any,
+                                           uint32_t skip_geom) {
     r.O = O;
     r.D = D;
     r.inv = mk(safe_inv(D.x), safe_inv(D.y), safe_inv(D.z));
@@ -113,14 +113,23 @@ __device__ __forceinline__ void trav_start(Trav &r, v3 O, v3 D, float tnear, flo
     r.node = 0;
     r.leaf = 0;
     r.sp = 0;
-    r.stack[0] = kSentinel;
+    stack[0] = kSentinel;
     r.any = any;
     r.skip_geom = skip_geom;
 }
 
+// The arrays one traversal reads: nodes, leaf-ordered triangles, triangle -> mesh.
+struct Geo {
+    const float4 *nodes, *tris;
+    const uint32_t *tri_geom;
+    uint32_t num_nodes, num_tris;  // bounds of the 8-wide traversal's indices
+};
+
+__device__ __forceinline__ Geo geo_of(const DevScene &S) { return Geo{S.nodes, S.tris, S.tri_geom, 0u, 0u}; }
+
 // Advances the ray until it is finished (r.node == kSentinel) or the warp
 // should refill idle lanes.
-__device__ __forceinline__ void traverse(const DevScene &S, Trav &r) {
+__device__ __forceinline__ void traverse(const Geo &S, Trav &r, int *stack) {
     while (r.node != kSentinel) {
         while ((unsigned)r.node < (unsigned)kSentinel) {
             const float4 *n = S.nodes + 4 * r.node;
@@ -130,18 +139,18 @@ __device__ __forceinline__ void traverse(const DevScene &S, Trav &r) {
             bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r.O, r.inv, r.tnear, r.h.t, t1);
             int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
             if (!h0 && !h1) {
-                r.node = r.stack[r.sp--];
+                r.node = stack[r.sp--];
             } else {
                 r.node = h0 ? c0 : c1;
                 if (h0 && h1) {
                     int far = c1;
                     if (t1 < t0) { far = c0; r.node = c1; }
-                    r.stack[++r.sp] = far;
+                    stack[++r.sp] = far;
                 }
             }
             if (r.node < 0 && r.leaf >= 0) {  // postpone the first leaf, keep descending
                 r.leaf = r.node;
-                r.node = r.stack[r.sp--];
+                r.node = stack[r.sp--];
             }
             if (!__any_sync(__activemask(), r.leaf >= 0)) break;
         }
@@ -164,11 +173,190 @@ __device__ __forceinline__ void traverse(const DevScene &S, Trav &r) {
                 }
             }
             r.leaf = r.node;
-            if (r.node < 0) r.node = r.stack[r.sp--];
+            if (r.node < 0) r.node = stack[r.sp--];
         }
         if (__popc(__activemask()) < kFetchThreshold) return;
     }
 }
+
+// ------------------------------------------------------------------ 8-wide traversal
+// Compressed 8-wide BVH (Bvh8Node, lt_scene.h), traversed as in Ylitie,
+// Karras and Laine (HPG 2017): the ray keeps a node group -- the children of
+// one visited node that its box tests hit, as a base index and a hit mask --
+// and a triangle group (base triangle index, 24-bit hit mask); the rest waits
+// on a stack of such groups. Inner-child hits sit in bits 24-31 at position
+// 24 + (slot ^ octant), so taking the highest bit first visits the children
+// roughly front to back. Triangle groups are postponed (pushed) while fewer
+// than a fifth of the warp's active lanes have triangles to test and the lane
+// still has nodes to visit. Box planes are p + q * cell, the float expression
+// the builder checked to enclose each child.
+constexpr int kStack8 = 64;  // groups; the builder keeps 2 * depth + 2 within it
+
+struct Trav8 {
+    v3 O, D, inv;
+    float tnear;
+    Hit h;
+    bool any;
+    uint32_t skip_geom;
+    uint32_t oct;    // bit c: D[c] < 0
+    uint2 ngroup;    // (base child, hits << 24 | imask)
+    uint2 tgroup;    // (base triangle, hits in bits 0-23)
+    int sp;
+    bool done;
+};
+
+__device__ __forceinline__ void trav8_start(Trav8 &r, v3 O, v3 D, float tnear, float tfar, bool any,
+                                            uint32_t skip_geom) {
+    r.O = O;
+    r.D = D;
+    r.inv = mk(safe_inv(D.x), safe_inv(D.y), safe_inv(D.z));
+    r.tnear = tnear;
+    r.h.t = tfar;
+    r.h.u = r.h.v = 0.0f;
+    r.h.prim = kMiss;
+    r.any = any;
+    r.skip_geom = skip_geom;
+    r.oct = (D.x < 0.0f ? 1u : 0u) | (D.y < 0.0f ? 2u : 0u) | (D.z < 0.0f ? 4u : 0u);
+    r.ngroup = make_uint2(0u, (1u << (24u + r.oct)) | 1u);  // the root: node 0 in slot 0
+    r.tgroup = make_uint2(0u, 0u);
+    r.sp = 0;
+    r.done = false;
+}
+
+__device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) { return (float)((w >> (8u * k)) & 0xFFu); }
+
+// Box tests of the 8 children of node `idx`; returns the hit mask (inner
+// children in bits 24-31, leaf triangles in bits 0-23) and the node's bases.
+__device__ __forceinline__ uint32_t node8_hits(const float4 *nodes, uint32_t idx, const Trav8 &r,
+                                               uint32_t &base_child, uint32_t &base_tri, uint32_t &imask) {
+    const float4 *n = nodes + 5 * (size_t)idx;
+    const float4 w0 = ldg4(n), w1 = ldg4(n + 1), w2 = ldg4(n + 2), w3 = ldg4(n + 3), w4 = ldg4(n + 4);
+    const uint32_t eb = __float_as_uint(w0.w);
+    imask = eb >> 24;
+    base_child = __float_as_uint(w1.x);
+    base_tri = __float_as_uint(w1.y);
+    const float cx = __uint_as_float((eb & 0xFFu) << 23), cy = __uint_as_float(((eb >> 8) & 0xFFu) << 23),
+                cz = __uint_as_float(((eb >> 16) & 0xFFu) << 23);
+    // t of plane p + q * cell along each axis: q * (cell * inv) + (p - O) * inv
+    const float sx = cx * r.inv.x, sy = cy * r.inv.y, sz = cz * r.inv.z;
+    const float ox = (w0.x - r.O.x) * r.inv.x, oy = (w0.y - r.O.y) * r.inv.y, oz = (w0.z - r.O.z) * r.inv.z;
+    // near / far plane words per axis from the direction signs
+    const bool nx = r.inv.x < 0.0f, ny = r.inv.y < 0.0f, nz = r.inv.z < 0.0f;
+    const uint32_t lx0 = __float_as_uint(w2.x), lx1 = __float_as_uint(w2.y), ly0 = __float_as_uint(w2.z),
+                   ly1 = __float_as_uint(w2.w), lz0 = __float_as_uint(w3.x), lz1 = __float_as_uint(w3.y),
+                   hx0 = __float_as_uint(w3.z), hx1 = __float_as_uint(w3.w), hy0 = __float_as_uint(w4.x),
+                   hy1 = __float_as_uint(w4.y), hz0 = __float_as_uint(w4.z), hz1 = __float_as_uint(w4.w);
+    const uint32_t nx0 = nx ? hx0 : lx0, nx1 = nx ? hx1 : lx1, fx0 = nx ? lx0 : hx0, fx1 = nx ? lx1 : hx1;
+    const uint32_t ny0 = ny ? hy0 : ly0, ny1 = ny ? hy1 : ly1, fy0 = ny ? ly0 : hy0, fy1 = ny ? ly1 : hy1;
+    const uint32_t nz0 = nz ? hz0 : lz0, nz1 = nz ? hz1 : lz1, fz0 = nz ? lz0 : hz0, fz1 = nz ? lz1 : hz1;
+    const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
+    uint32_t hits = 0;
+#pragma unroll
+    for (uint32_t s = 0; s < 8; ++s) {
+        const uint32_t k = s & 3u;
+        const uint32_t meta = ((s < 4 ? meta0 : meta1) >> (8u * k)) & 0xFFu;
+        const float tx0 = fmaf(byte_f(s < 4 ? nx0 : nx1, k), sx, ox), tx1 = fmaf(byte_f(s < 4 ? fx0 : fx1, k), sx, ox);
+        const float ty0 = fmaf(byte_f(s < 4 ? ny0 : ny1, k), sy, oy), ty1 = fmaf(byte_f(s < 4 ? fy0 : fy1, k), sy, oy);
+        const float tz0 = fmaf(byte_f(s < 4 ? nz0 : nz1, k), sz, oz), tz1 = fmaf(byte_f(s < 4 ? fz0 : fz1, k), sz, oz);
+        const float tmin = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, r.tnear));
+        const float tmax = fminf(fminf(tx1, ty1), fminf(tz1, r.h.t));
+        if (meta != 0u && tmin <= tmax * 1.0000004f) {
+            if (imask & (1u << s)) hits |= 1u << (24u + (s ^ r.oct));
+            else hits |= (meta >> 5) << (meta & 31u);
+        }
+    }
+    return hits;
+}
+
+__device__ __forceinline__ void traverse8(const Geo &g, Trav8 &r, uint2 *stack) {
+    while (!r.done) {
+        if (r.ngroup.y > 0x00FFFFFFu) {
+            // next inner child of the node group
+            const uint32_t b = 31u - __clz(r.ngroup.y);
+            const uint32_t slot = (b - 24u) ^ r.oct;
+            const uint32_t imask = r.ngroup.y & 0xFFu;
+            const uint32_t idx = r.ngroup.x + __popc(imask & ((1u << slot) - 1u));
+            r.ngroup.y &= ~(1u << b);
+            if (r.ngroup.y > 0x00FFFFFFu && r.sp < kStack8) stack[r.sp++] = r.ngroup;
+            if (idx < g.num_nodes) {
+                uint32_t bc, bt, im;
+                const uint32_t hits = node8_hits(g.nodes, idx, r, bc, bt, im);
+                r.ngroup = make_uint2(bc, (hits & 0xFF000000u) | im);
+                r.tgroup = make_uint2(bt, hits & 0x00FFFFFFu);
+            } else {  // malformed tree: skip the subtree rather than read out of bounds
+                r.ngroup = make_uint2(0u, 0u);
+                r.tgroup = make_uint2(0u, 0u);
+            }
+        } else {
+            r.tgroup = r.ngroup;  // a triangle group from the stack (or nothing)
+            r.ngroup = make_uint2(0u, 0u);
+        }
+        // triangles, unless too few lanes have some and this lane can visit nodes instead
+        {
+            const unsigned act = __activemask();
+            const unsigned want = __ballot_sync(act, r.tgroup.y != 0u);
+            if (r.tgroup.y != 0u && r.ngroup.y > 0x00FFFFFFu && 5 * __popc(want) < __popc(act) &&
+                r.sp < kStack8) {
+                stack[r.sp++] = r.tgroup;
+                r.tgroup.y = 0u;
+            }
+        }
+        while (r.tgroup.y != 0u) {
+            const uint32_t t = __ffs(r.tgroup.y) - 1u;
+            r.tgroup.y &= r.tgroup.y - 1u;
+            if (r.tgroup.x + t >= g.num_tris) continue;
+            const float4 *tri = g.tris + 3 * (size_t)(r.tgroup.x + t);
+            if (!r.any) {
+                tri_test(tri, r.O, r.D, r.tnear, r.h);
+            } else {
+                Hit c = r.h;
+                tri_test(tri, r.O, r.D, r.tnear, c);
+                if (c.prim != kMiss && __ldg(g.tri_geom + c.prim) != r.skip_geom) {
+                    r.h.prim = c.prim;  // occluded
+                    r.done = true;
+                    return;
+                }
+            }
+        }
+        if (r.ngroup.y <= 0x00FFFFFFu) {
+            if (r.sp == 0) {
+                r.done = true;
+                return;
+            }
+            r.ngroup = stack[--r.sp];
+        }
+        if (__popc(__activemask()) < kFetchThreshold) return;
+    }
+}
+
+// Traversal policies: the BVH2 (while-while, Trav) and the compressed 8-wide BVH (Trav8).
+struct Bvh2 {
+    using State = Trav;
+    using Entry = int;
+    static constexpr int kDepth = kStack;
+    __device__ static Geo geo(const DevScene &S) { return geo_of(S); }
+    __device__ static void start(State &r, Entry *st, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip) {
+        trav_start(r, st, O, D, tnear, tfar, any, skip);
+    }
+    __device__ static void run(const Geo &g, State &r, Entry *st) { traverse(g, r, st); }
+    __device__ static bool done(const State &r) { return r.node == kSentinel; }
+    __device__ static void idle(State &r) { r.node = kSentinel; }
+};
+
+struct Bvh8 {
+    using State = Trav8;
+    using Entry = uint2;
+    static constexpr int kDepth = kStack8;
+    __device__ static Geo geo(const DevScene &S) {
+        return Geo{S.nodes8, S.tris8, S.tri_geom, S.num_nodes8, S.num_tris};
+    }
+    __device__ static void start(State &r, Entry *, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip) {
+        trav8_start(r, O, D, tnear, tfar, any, skip);
+    }
+    __device__ static void run(const Geo &g, State &r, Entry *st) { traverse8(g, r, st); }
+    __device__ static bool done(const State &r) { return r.done; }
+    __device__ static void idle(State &r) { r.done = true; }
+};
 
 // Warp-aggregated fetch of the next work index for the lanes that ask.
 __device__ __forceinline__ uint32_t fetch_next(uint32_t *counter) {
@@ -232,7 +420,16 @@ struct Path {
     uint32_t bounces, lobe;
     int medium;
     float iori;
+    uint32_t scene;  // slot of a batched render, 0 otherwise
 };
+
+// Path flags: bits 0-7 sampled lobe, 8-20 medium index + 1, 21-31 scene slot.
+constexpr uint32_t kFlagMediumShift = 8, kFlagMediumMask = 0x1FFFu, kFlagSceneShift = 21;
+// Connection record word: bits 0-19 light index, 20-30 scene slot, bit 31 BSDF sample.
+constexpr uint32_t kConnLightMask = 0xFFFFFu, kConnSceneShift = 20, kConnSceneMask = 0x7FFu;
+static_assert(kMaxBatchScenes <= kConnSceneMask + 1 && kMaxBatchScenes <= (1u << (32 - kFlagSceneShift)),
+              "scene slot field too narrow");
+static_assert(kMaxLights <= kConnLightMask + 1 && kMaxMedia < kFlagMediumMask, "light / medium field too narrow");
 
 // Start sample `item`: PinholeCamera::CalculateRayFromPixel (pinhole_camera.cpp:88-113)
 // with the sampler of (pixel, frame).
@@ -254,6 +451,7 @@ __device__ __forceinline__ void start_path(const DevScene &S, const RenderArgs &
     p.lobe = kLobeNull;
     p.medium = -1;
     p.iori = 1.0f;
+    p.scene = 0;
 }
 
 __device__ __forceinline__ void store_path(const PathState &ps, uint32_t cap, uint32_t slot, const Path &p) {
@@ -263,7 +461,7 @@ __device__ __forceinline__ void store_path(const PathState &ps, uint32_t cap, ui
     ps.T[slot] = p.T.x; ps.T[cap + slot] = p.T.y; ps.T[2 * cap + slot] = p.T.z;
     ps.color[slot] = p.color.x; ps.color[cap + slot] = p.color.y; ps.color[2 * cap + slot] = p.color.z;
     ps.bounces[slot] = p.bounces;
-    ps.flags[slot] = p.lobe | ((uint32_t)(p.medium + 1) << 8);
+    ps.flags[slot] = p.lobe | ((uint32_t)(p.medium + 1) << kFlagMediumShift) | (p.scene << kFlagSceneShift);
     ps.iori[slot] = p.iori;
 }
 
@@ -277,7 +475,8 @@ __device__ __forceinline__ void load_path(const PathState &ps, uint32_t cap, uin
     p.bounces = ps.bounces[slot];
     uint32_t fl = ps.flags[slot];
     p.lobe = fl & 0xFFu;
-    p.medium = (int)((fl >> 8) & 0xFFFFu) - 1;
+    p.medium = (int)((fl >> kFlagMediumShift) & kFlagMediumMask) - 1;
+    p.scene = fl >> kFlagSceneShift;
     p.iori = ps.iori[slot];
 }
 
@@ -350,33 +549,83 @@ __device__ __forceinline__ void film_add(const FilmPtrs &f, uint32_t pixel, v3 c
     if (c.z != 0.0f) atomicAdd(f.rgb + 3 * (size_t)pixel + 2, c.z);
 }
 
+// ------------------------------------------------------------------ scene sources
+// The wavefront kernels are instantiated for two sources of scene data.
+// OneScene keeps the scene, its render arguments and its film in the kernel
+// parameters (lt_render). ManyScenes reads them per path from a batch's scene
+// table in device memory (lt_render_batch): the work items of all scenes form
+// one sequence, slot i owning [begin[i], begin[i] + slots[i].a.total), and every
+// path carries its slot in its flags and connection records.
+struct OneScene {
+    static constexpr bool kMany = false;
+    DevScene s;
+    RenderArgs a;
+    FilmPtrs f;
+    __device__ __forceinline__ const DevScene &scene(uint32_t) const { return s; }
+    __device__ __forceinline__ const RenderArgs &args(uint32_t) const { return a; }
+    __device__ __forceinline__ const FilmPtrs &film(uint32_t) const { return f; }
+    __device__ __forceinline__ unsigned long long total() const { return a.total; }
+    __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
+        local = item;
+        return 0;
+    }
+};
+
+struct ManyScenes {
+    static constexpr bool kMany = true;
+    const SceneTable *t;
+    __device__ __forceinline__ const DevScene &scene(uint32_t i) const { return t->slots[i].s; }
+    __device__ __forceinline__ const RenderArgs &args(uint32_t i) const { return t->slots[i].a; }
+    __device__ __forceinline__ const FilmPtrs &film(uint32_t i) const { return t->slots[i].f; }
+    __device__ __forceinline__ unsigned long long total() const { return t->total; }
+    // the slot that owns work item `item`: the last i with begin[i] <= item
+    __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
+        uint32_t lo = 0, hi = t->count;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (t->begin[mid] <= item) lo = mid;
+            else hi = mid;
+        }
+        local = item - t->begin[lo];
+        return lo;
+    }
+};
+
 // ------------------------------------------------------------------ kernels
 // Closest hits of n rays (lt_intersect). Persistent: rays are fetched from *fetch.
+template <class B>
 __global__ void __launch_bounds__(128) k_intersect(DevScene S, const float4 *__restrict__ rays,
                                                    float4 *__restrict__ hits, uint32_t n, uint32_t *fetch) {
-    Trav r;
-    r.node = kSentinel;
+    const Geo g = B::geo(S);
+    typename B::State r;
+    typename B::Entry stack[B::kDepth];
+    B::idle(r);
     uint32_t idx = 0;
     for (;;) {
-        if (r.node == kSentinel) {
+        if (B::done(r)) {
             idx = fetch_next(fetch);
             if (idx >= n) break;
             float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
-            trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
+            B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
         }
-        traverse(S, r);
-        if (r.node == kSentinel) hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
+        B::run(g, r, stack);
+        if (B::done(r)) hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
     }
 }
 
 // Fill up to `capacity` slots with camera rays of the first work items.
-__global__ void __launch_bounds__(128) k_raygen(DevScene S, Wavefront W, RenderArgs A) {
-    unsigned long long first = A.total < W.capacity ? A.total : W.capacity;
+template <class Src>
+__global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
+    const unsigned long long total = src.total();
+    unsigned long long first = total < W.capacity ? total : W.capacity;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < first; i += gridDim.x * blockDim.x) {
         Path p;
         v3 o, d;
         float tn;
-        start_path(S, A, i, p, o, d, tn);
+        unsigned long long local;
+        const uint32_t sid = src.locate(i, local);
+        start_path(src.scene(sid), src.args(sid), local, p, o, d, tn);
+        p.scene = sid;
         store_path(W.p[0], W.capacity, i, p);
         write_ray(W.ray[0], i, o, tn, d);
     }
@@ -391,7 +640,8 @@ __global__ void __launch_bounds__(128) k_raygen(DevScene S, Wavefront W, RenderA
 
 // Closest hit of every queued path ray. Persistent: entries are fetched from
 // counters->trace_fetch (zeroed by the kernel before).
-__global__ void __launch_bounds__(128) k_trace(DevScene S, Wavefront W, int cur) {
+template <class Src, class B>
+__global__ void __launch_bounds__(256) k_trace(Src src, Wavefront W, int cur) {
     const uint32_t n = W.counters->count[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters->count[cur ^ 1] = 0;
@@ -399,25 +649,29 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, Wavefront W, int cur)
         W.counters->main_rays += n;
     }
     const float4 *rays = W.ray[cur];
-    Trav r;
-    r.node = kSentinel;
+    Geo g = B::geo(src.scene(0));
+    typename B::State r;
+    typename B::Entry stack[B::kDepth];
+    B::idle(r);
     uint32_t idx = 0;
     for (;;) {
-        if (r.node == kSentinel) {
+        if (B::done(r)) {
             idx = fetch_next(&W.counters->trace_fetch);
             if (idx >= n) break;
+            if (Src::kMany) g = B::geo(src.scene(W.p[cur].flags[idx] >> kFlagSceneShift));
             float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
-            trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
+            B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
         }
-        traverse(S, r);
-        if (r.node == kSentinel) W.hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
+        B::run(g, r, stack);
+        if (B::done(r)) W.hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
     }
 }
 
 // One iteration of the bounce loop of Integrator::RenderPixel (integrator.cpp:115-243).
-// Occupancy hint: at most 64 registers (8 blocks of 128 threads per SM), so that
-// more warps hide the latency of the scattered normal / material loads.
-__global__ void __launch_bounds__(128, 8) k_shade(DevScene S, Wavefront W, RenderArgs A, FilmPtrs F, int cur) {
+// Occupancy hint: at most 64 registers (1024 threads per SM), so that more
+// warps hide the latency of the scattered normal / material loads.
+template <class Src>
+__global__ void __launch_bounds__(256, 4) k_shade(Src src, Wavefront W, int cur) {
     const uint32_t n = W.counters->count[cur];
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;
@@ -438,6 +692,8 @@ __global__ void __launch_bounds__(128, 8) k_shade(DevScene S, Wavefront W, Rende
         v3 conn_T = mk(0, 0, 0);
         if (active) {
             load_path(W.p[cur], cap, q, p);
+            const DevScene &S = src.scene(p.scene);
+            const RenderArgs &A = src.args(p.scene);
             float4 hv = W.hits[q];
             float4 r0 = W.ray[cur][2 * q], r1 = W.ray[cur][2 * q + 1];
             uint32_t prim = __float_as_uint(hv.w);
@@ -585,6 +841,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(DevScene S, Wavefront W, Rende
         }
         // connection records
         {
+            conn_light |= p.scene << kConnSceneShift;
             uint32_t idx = warp_reserve(&W.counters->ccount, emit_l);
             if (emit_l) {
                 W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light));
@@ -605,13 +862,17 @@ __global__ void __launch_bounds__(128, 8) k_shade(DevScene S, Wavefront W, Rende
         // starts the next work item in their place
         bool regen = false;
         if (done) {
+            const FilmPtrs &F = src.film(p.scene);
             film_add(F, p.pixel, p.color);
             atomicAdd(F.bounces + p.pixel, p.bounces);
             atomicAdd(F.counts + p.pixel, 1u);
         }
         unsigned long long item = warp_reserve64(&W.counters->work_next, done);
-        if (done && item < A.total) {
-            start_path(S, A, item, p, norg, ndir, ntnear);
+        if (done && item < src.total()) {
+            unsigned long long local;
+            const uint32_t sid = src.locate(item, local);
+            start_path(src.scene(sid), src.args(sid), local, p, norg, ndir, ntnear);
+            p.scene = sid;
             regen = true;
         }
         bool enqueue = push || regen;
@@ -642,10 +903,11 @@ __global__ void __launch_bounds__(128, 8) k_shade(DevScene S, Wavefront W, Rende
 // the light, with that distance; here an occlusion query up to the distance,
 // ignoring the light's own geometry, decides the rest. Lights with more than
 // kLightBrute triangles (distance -1 in the record) use a full closest-hit query.
+template <class State>
 __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wavefront &W, const FilmPtrs &F,
-                                                   uint32_t idx, uint32_t kl, uint32_t pixel, const Trav &r) {
+                                                   uint32_t idx, uint32_t kl, uint32_t pixel, const State &r) {
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
-    const LightInfo &L = S.lights[kl & ~kConnectBsdf];
+    const LightInfo &L = S.lights[kl & kConnLightMask];
     Hit h;
     if (r.any) {
         if (r.h.prim != kMiss) return;  // occluded
@@ -673,30 +935,51 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     film_add(F, pixel, T * (c * (float)S.num_lights));
 }
 
-__global__ void __launch_bounds__(128) k_connect(DevScene S, Wavefront W, FilmPtrs F) {
+template <class Src, class B>
+__global__ void __launch_bounds__(256) k_connect(Src src, Wavefront W) {
     const uint32_t n = W.counters->ccount;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
     uint32_t n_trav = 0;
-    Trav r;
-    r.node = kSentinel;
+    Geo g = B::geo(src.scene(0));
+    typename B::State r;
+    typename B::Entry stack[B::kDepth];
+    B::idle(r);
     uint32_t idx = 0, kl = 0, pixel = 0;
     for (;;) {
-        if (r.node == kSentinel) {
+        if (B::done(r)) {
             idx = fetch_next(&W.counters->connect_fetch);
             if (idx >= n) break;
             float4 a = ldg4(W.cray + 2 * idx), b = ldg4(W.cray + 2 * idx + 1);
             float tl = ldg4(W.crec + 2 * idx + 1).w;
             kl = __float_as_uint(a.w);
             pixel = __float_as_uint(b.w);
-            const LightInfo &L = S.lights[kl & ~kConnectBsdf];
-            if (tl > 0.0f) trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, tl, true, (uint32_t)L.geom);
-            else trav_start(r, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, __int_as_float(0x7f800000), false, 0);
+            const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
+            if (Src::kMany) g = B::geo(S);
+            const LightInfo &L = S.lights[kl & kConnLightMask];
+            if (tl > 0.0f) B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, tl, true, (uint32_t)L.geom);
+            else B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, __int_as_float(0x7f800000), false, 0);
             n_trav++;
         }
-        traverse(S, r);
-        if (r.node == kSentinel) resolve_connection(S, W, F, idx, kl, pixel, r);
+        B::run(g, r, stack);
+        if (B::done(r)) {
+            const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
+            resolve_connection(src.scene(sid), W, src.film(sid), idx, kl, pixel, r);
+        }
     }
     if (n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
+}
+
+// While-node condition of a captured wavefront loop (one thread): continue
+// while queue `cur` holds paths; give up with error 2 at the iteration limit.
+__global__ void k_loop_condition(WaveCounters *c, const SceneTable *t, cudaGraphConditionalHandle h, int cur,
+                                 uint32_t iters) {
+    c->iterations += iters;
+    unsigned int more = c->count[cur] != 0u;
+    if (more && c->iterations >= t->iteration_limit) {
+        c->error = 2;
+        more = 0;
+    }
+    cudaGraphSetConditional(h, more);
 }
 
 // counts += spp for every pixel (render with max_depth 0: the bounce loop never runs)
@@ -728,10 +1011,12 @@ constexpr int kMediaAcc = 4;  // media whose gradients are summed in registers
 
 __device__ __forceinline__ Hit trace_all(const DevScene &S, v3 O, v3 D, float tnear, float tfar, bool any,
                                          uint32_t skip_geom) {
+    const Geo g = geo_of(S);
     Trav r;
-    trav_start(r, O, D, tnear, tfar, any, skip_geom);
+    int stack[kStack];
+    trav_start(r, stack, O, D, tnear, tfar, any, skip_geom);
     do {
-        traverse(S, r);
+        traverse(g, r, stack);
     } while (r.node != kSentinel);
     return r.h;
 }
@@ -967,35 +1252,62 @@ __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads 
 // run (finite differences of the loss see no summation-order noise).
 // sample_I (optional): each sample's radiance, 3 floats at (frame index * W*H + pixel),
 // so that the adjoint need not replay the path a first time.
+// All spp samples of one pixel: film sums (deterministic, no atomics) and,
+// optionally, every sample's radiance.
+__device__ __forceinline__ void diff_forward_pixel(const DevScene &S, const DiffParams &P, const RenderArgs &A,
+                                                   const FilmPtrs &F, float *sample_I, uint32_t pixel,
+                                                   AlbedoCache &ca, EmissionCache &ce) {
+    const DiffGrads G{};
+    float macc[1];
+    const uint32_t npix = A.width * A.height;
+    const uint32_t spp = (uint32_t)(A.total / npix);
+    v3 sum = mk(0, 0, 0);
+    uint32_t bsum = 0;
+    for (uint32_t s = 0; s < spp; ++s) {
+        uint32_t b = 0;
+        unsigned long long item = (unsigned long long)s * npix + pixel;
+        v3 c = diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
+        if (sample_I) {
+            sample_I[3 * item] = c.x;
+            sample_I[3 * item + 1] = c.y;
+            sample_I[3 * item + 2] = c.z;
+        }
+        sum = sum + c;
+        bsum += b;
+    }
+    F.rgb[3 * (size_t)pixel] += sum.x;
+    F.rgb[3 * (size_t)pixel + 1] += sum.y;
+    F.rgb[3 * (size_t)pixel + 2] += sum.z;
+    F.bounces[pixel] += bsum;
+    F.counts[pixel] += spp;
+}
+
+// Gradient terms of all spp samples of one pixel (inside G's crop).
+__device__ __forceinline__ void diff_adjoint_pixel(const DevScene &S, const DiffParams &P, const RenderArgs &A,
+                                                   const DiffGrads &G, uint32_t pixel, float *macc,
+                                                   AlbedoCache &ca, EmissionCache &ce) {
+    const uint32_t npix = A.width * A.height;
+    const uint32_t spp = (uint32_t)(A.total / npix);
+    uint32_t x = pixel % A.width, y = pixel / A.width;
+    if (x < G.x0 || x >= G.x1 || y < G.y0 || y >= G.y1) return;
+    v3 delta = ld3(G.dI + 3 * (size_t)pixel);
+    if (is_black(delta)) return;
+    for (uint32_t s = 0; s < spp; ++s) {
+        unsigned long long item = (unsigned long long)s * npix + pixel;
+        uint32_t b = 0;
+        v3 I = G.sample_I ? ld3(G.sample_I + 3 * item)
+                          : diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
+        diff_path<true>(S, P, G, A, item, I, delta, macc, ca, ce, b);
+    }
+}
+
 __global__ void __launch_bounds__(128) k_diff_forward(DevScene S, DiffParams P, RenderArgs A, FilmPtrs F,
                                                      float *sample_I) {
-    DiffGrads G{};
-    float macc[1];
     AlbedoCache ca;
     EmissionCache ce;
     const uint32_t npix = A.width * A.height;
-    const uint32_t spp = (uint32_t)(A.total / npix);
-    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
-        v3 sum = mk(0, 0, 0);
-        uint32_t bsum = 0;
-        for (uint32_t s = 0; s < spp; ++s) {
-            uint32_t b = 0;
-            unsigned long long item = (unsigned long long)s * npix + pixel;
-            v3 c = diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
-            if (sample_I) {
-                sample_I[3 * item] = c.x;
-                sample_I[3 * item + 1] = c.y;
-                sample_I[3 * item + 2] = c.z;
-            }
-            sum = sum + c;
-            bsum += b;
-        }
-        F.rgb[3 * (size_t)pixel] += sum.x;
-        F.rgb[3 * (size_t)pixel + 1] += sum.y;
-        F.rgb[3 * (size_t)pixel + 2] += sum.z;
-        F.bounces[pixel] += bsum;
-        F.counts[pixel] += spp;
-    }
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x)
+        diff_forward_pixel(S, P, A, F, sample_I, pixel, ca, ce);
 }
 
 __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, RenderArgs A, DiffGrads G,
@@ -1007,20 +1319,8 @@ __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, 
     ca.init();
     ce.init();
     const uint32_t npix = A.width * A.height;
-    const uint32_t spp = (uint32_t)(A.total / npix);
-    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
-        uint32_t x = pixel % A.width, y = pixel / A.width;
-        if (x < G.x0 || x >= G.x1 || y < G.y0 || y >= G.y1) continue;
-        v3 delta = ld3(G.dI + 3 * (size_t)pixel);
-        if (is_black(delta)) continue;
-        for (uint32_t s = 0; s < spp; ++s) {
-            unsigned long long item = (unsigned long long)s * npix + pixel;
-            uint32_t b = 0;
-            v3 I = G.sample_I ? ld3(G.sample_I + 3 * item)
-                              : diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
-            diff_path<true>(S, P, G, A, item, I, delta, macc, ca, ce, b);
-        }
-    }
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x)
+        diff_adjoint_pixel(S, P, A, G, pixel, macc, ca, ce);
     ca.flush(G.albedo);
     ce.flush(G.emission);
     // medium gradients: warp sums, one atomic per warp and component
@@ -1035,23 +1335,122 @@ __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, 
     }
 }
 
+// ---- batched differentiable rendering (lt_render_diff_batch / lt_render_adjoint_batch)
+// The pixels of all slots form one sequence (slot i owns [pbegin[i],
+// pbegin[i] + width * height)); warps take 32 consecutive pixels at a time
+// from t->fetch, so scenes of any size and spp share one persistent launch.
+
+// The slot that owns global pixel gp: the last i with pbegin[i] <= gp.
+__device__ __forceinline__ uint32_t locate_pixel(const SceneTable *t, unsigned long long gp, uint32_t &pixel) {
+    uint32_t lo = 0, hi = t->count;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (t->pbegin[mid] <= gp) lo = mid;
+        else hi = mid;
+    }
+    pixel = (uint32_t)(gp - t->pbegin[lo]);
+    return lo;
+}
+
+// Next 32-pixel chunk for the calling warp (all lanes call it together).
+__device__ __forceinline__ unsigned long long fetch_chunk(unsigned long long *fetch) {
+    unsigned long long base = 0;
+    if ((threadIdx.x & 31u) == 0) base = atomicAdd(fetch, 32ull);
+    return __shfl_sync(0xFFFFFFFFu, base, 0);
+}
+
+__global__ void __launch_bounds__(128) k_diff_forward_batch(SceneTable *t) {
+    AlbedoCache ca;
+    EmissionCache ce;
+    const unsigned long long total = t->total_pixels;
+    for (;;) {
+        const unsigned long long base = fetch_chunk(&t->fetch);
+        if (base >= total) break;
+        const unsigned long long gp = base + (threadIdx.x & 31u);
+        if (gp < total) {
+            uint32_t pixel;
+            const uint32_t sid = locate_pixel(t, gp, pixel);
+            const SceneSlot &sl = t->slots[sid];
+            const DiffSlot &d = t->diff[sid];
+            diff_forward_pixel(sl.s, d.p, sl.a, sl.f, d.sample_I, pixel, ca, ce);
+        }
+    }
+}
+
+// Adds a thread's cached gradient terms to slot d's arrays and clears them.
+__device__ __forceinline__ void flush_diff_slot(const DiffSlot &d, float *macc, AlbedoCache &ca, EmissionCache &ce) {
+    ca.flush(d.g.albedo);
+    ce.flush(d.g.emission);
+    for (int k = 0; k < 6 * kMediaAcc; ++k) {
+        if (k / 6 >= (int)d.num_media) break;
+        if (macc[k] != 0.0f) {
+            int mi = k / 6, c = k % 6;
+            atomicAdd(c < 3 ? d.g.sigma_a + 3 * mi + c : d.g.sigma_s + 3 * mi + (c - 3), macc[k]);
+        }
+        macc[k] = 0.0f;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_diff_adjoint_batch(SceneTable *t) {
+    float macc[6 * kMediaAcc];
+    for (int k = 0; k < 6 * kMediaAcc; ++k) macc[k] = 0.0f;
+    AlbedoCache ca;
+    EmissionCache ce;
+    ca.init();
+    ce.init();
+    uint32_t held = 0xFFFFFFFFu;  // slot whose gradients the caches hold
+    const unsigned long long total = t->total_pixels;
+    for (;;) {
+        const unsigned long long base = fetch_chunk(&t->fetch);
+        if (base >= total) break;
+        const unsigned long long gp = base + (threadIdx.x & 31u);
+        if (gp < total) {
+            uint32_t pixel;
+            const uint32_t sid = locate_pixel(t, gp, pixel);
+            if (sid != held) {
+                if (held != 0xFFFFFFFFu) flush_diff_slot(t->diff[held], macc, ca, ce);
+                held = sid;
+            }
+            const SceneSlot &sl = t->slots[sid];
+            const DiffSlot &d = t->diff[sid];
+            diff_adjoint_pixel(sl.s, d.p, sl.a, d.g, pixel, macc, ca, ce);
+        }
+    }
+    if (held != 0xFFFFFFFFu) flush_diff_slot(t->diff[held], macc, ca, ce);
+}
+
 }  // namespace
 
-void query_launch_shape(int device, LaunchShape *out) {
+template <class F>
+static int blocks_for(F kernel, int threads, int sms) {
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, 0);
+    return sms * (b > 0 ? b : 1);
+}
+
+void query_launch_shape(int device, bool batch, LaunchShape *out) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, device);
-    out->sms = prop.multiProcessorCount;
-    int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace, 128, 0);
-    out->trace_blocks = out->sms * (b > 0 ? b : 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade, 128, 0);
-    out->shade_blocks = out->sms * (b > 0 ? b : 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_connect, 128, 0);
-    out->connect_blocks = out->sms * (b > 0 ? b : 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_intersect, 128, 0);
-    out->isect_blocks = out->sms * (b > 0 ? b : 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_diff_adjoint, 128, 0);
-    out->diff_blocks = out->sms * (b > 0 ? b : 1);
+    const int sms = prop.multiProcessorCount;
+    out->sms = sms;
+    const bool w8 = out->bvh_width == 8;
+    if (batch) {
+        out->trace_blocks = w8 ? blocks_for(k_trace<ManyScenes, Bvh8>, out->trace_threads, sms)
+                               : blocks_for(k_trace<ManyScenes, Bvh2>, out->trace_threads, sms);
+        out->shade_blocks = blocks_for(k_shade<ManyScenes>, out->shade_threads, sms);
+        out->connect_blocks = w8 ? blocks_for(k_connect<ManyScenes, Bvh8>, out->connect_threads, sms)
+                                 : blocks_for(k_connect<ManyScenes, Bvh2>, out->connect_threads, sms);
+    } else {
+        out->trace_blocks = w8 ? blocks_for(k_trace<OneScene, Bvh8>, out->trace_threads, sms)
+                               : blocks_for(k_trace<OneScene, Bvh2>, out->trace_threads, sms);
+        out->shade_blocks = blocks_for(k_shade<OneScene>, out->shade_threads, sms);
+        out->connect_blocks = w8 ? blocks_for(k_connect<OneScene, Bvh8>, out->connect_threads, sms)
+                                 : blocks_for(k_connect<OneScene, Bvh2>, out->connect_threads, sms);
+    }
+    out->isect_blocks = w8 ? blocks_for(k_intersect<Bvh8>, 128, sms) : blocks_for(k_intersect<Bvh2>, 128, sms);
+    out->diff_blocks = blocks_for(k_diff_adjoint, 128, sms);
+    out->diff_fwd_batch_blocks = blocks_for(k_diff_forward_batch, 128, sms);
+    out->diff_adj_batch_blocks = blocks_for(k_diff_adjoint_batch, 128, sms);
 }
 
 cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
@@ -1068,6 +1467,12 @@ cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const Re
     return cudaGetLastError();
 }
 
+cudaError_t launch_diff_batch(bool adjoint, SceneTable *t, const LaunchShape &ls, cudaStream_t st) {
+    if (adjoint) k_diff_adjoint_batch<<<ls.diff_adj_batch_blocks, 128, 0, st>>>(t);
+    else k_diff_forward_batch<<<ls.diff_fwd_batch_blocks, 128, 0, st>>>(t);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
                              uint32_t *fetch, const LaunchShape &ls, cudaStream_t st) {
     const unsigned long long kChunk = 1ull << 30;
@@ -1077,7 +1482,8 @@ cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits
         if (e != cudaSuccess) return e;
         unsigned long long need = (m + 127) / 128;
         int blocks = (int)(need < (unsigned long long)ls.isect_blocks ? need : ls.isect_blocks);
-        k_intersect<<<blocks, 128, 0, st>>>(s, rays + 2 * off, hits + off, m, fetch);
+        if (ls.bvh_width == 8) k_intersect<Bvh8><<<blocks, 128, 0, st>>>(s, rays + 2 * off, hits + off, m, fetch);
+        else k_intersect<Bvh2><<<blocks, 128, 0, st>>>(s, rays + 2 * off, hits + off, m, fetch);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -1089,17 +1495,46 @@ cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cu
     return cudaGetLastError();
 }
 
-cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &,
-                             const LaunchShape &ls, cudaStream_t st) {
-    k_raygen<<<ls.shade_blocks, 128, 0, st>>>(s, w, a);
+template <class Src>
+static cudaError_t stage(int stage, const Src &src, const Wavefront &w, int cur, const LaunchShape &ls,
+                         cudaStream_t st) {
+    const bool w8 = ls.bvh_width == 8;
+    if (stage == kStageTrace) {
+        if (w8) k_trace<Src, Bvh8><<<ls.trace_blocks, ls.trace_threads, 0, st>>>(src, w, cur);
+        else k_trace<Src, Bvh2><<<ls.trace_blocks, ls.trace_threads, 0, st>>>(src, w, cur);
+    } else if (stage == kStageShade) {
+        k_shade<Src><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(src, w, cur);
+    } else {
+        if (w8) k_connect<Src, Bvh8><<<ls.connect_blocks, ls.connect_threads, 0, st>>>(src, w);
+        else k_connect<Src, Bvh2><<<ls.connect_blocks, ls.connect_threads, 0, st>>>(src, w);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_wave_stage(int stage, const DevScene &s, const Wavefront &w, const RenderArgs &a,
+cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
+                             const LaunchShape &ls, cudaStream_t st) {
+    k_raygen<OneScene><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(OneScene{s, a, f}, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wave_stage(int st_, const DevScene &s, const Wavefront &w, const RenderArgs &a,
                               const FilmPtrs &f, int cur, const LaunchShape &ls, cudaStream_t st) {
-    if (stage == kStageTrace) k_trace<<<ls.trace_blocks, 128, 0, st>>>(s, w, cur);
-    else if (stage == kStageShade) k_shade<<<ls.shade_blocks, 128, 0, st>>>(s, w, a, f, cur);
-    else k_connect<<<ls.connect_blocks, 128, 0, st>>>(s, w, f);
+    return stage(st_, OneScene{s, a, f}, w, cur, ls, st);
+}
+
+cudaError_t launch_batch_init(const SceneTable *t, const Wavefront &w, const LaunchShape &ls, cudaStream_t st) {
+    k_raygen<ManyScenes><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(ManyScenes{t}, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_stage(int st_, const SceneTable *t, const Wavefront &w, int cur, const LaunchShape &ls,
+                               cudaStream_t st) {
+    return stage(st_, ManyScenes{t}, w, cur, ls, st);
+}
+
+cudaError_t launch_loop_condition(const Wavefront &w, const SceneTable *t, cudaGraphConditionalHandle h, int cur,
+                                  uint32_t iters, cudaStream_t st) {
+    k_loop_condition<<<1, 1, 0, st>>>(w.counters, t, h, cur, iters);
     return cudaGetLastError();
 }
 

@@ -60,6 +60,29 @@ struct alignas(16) BvhNode {
     uint32_t count[2];
 };
 
+// Compressed 8-wide node, 80 bytes (five 16-byte words), after Ylitie, Karras
+// and Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed
+// Wide BVHs" (HPG 2017): child boxes quantised to 8 bits per plane on a grid
+// with origin p and per-axis power-of-two cell size 2^(e - 127).
+//  [0] p.x p.y p.z | e.x e.y e.z imask        imask bit s: slot s is an inner node
+//  [1] base_child base_tri | meta[0..7]       inner children: nodes base_child + rank among
+//                                             inner slots; leaves: triangles base_tri + (meta & 31),
+//                                             count = popcount(meta >> 5) (1..3, unary)
+//  [2] qlo.x[8] qlo.y[8]  [3] qlo.z[8] qhi.x[8]  [4] qhi.y[8] qhi.z[8]
+// Slot s holds the child that lies furthest along the octant direction whose
+// negative axes are the bits of s, so a ray whose direction has sign bits o
+// meets the children roughly in decreasing order of (s ^ o).
+struct alignas(16) Bvh8Node {
+    float p[3];
+    uint8_t e[3];
+    uint8_t imask;
+    uint32_t base_child, base_tri;
+    uint8_t meta[8];
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(Bvh8Node) == 80, "Bvh8Node is five 16-byte words");
+
 struct HostScene {
     Camera camera;
     TentFilter filter;
@@ -87,6 +110,15 @@ lt_status build_host_scene(const lt_scene_desc *desc, HostScene *out, std::strin
 // Binned-SAH BVH2 (32 bins, at most 4 triangles per leaf) over the scene's
 // triangles; fills nodes and leaf_tris.
 void build_bvh(HostScene *s);
+
+// Collapses a BVH2 (nodes in BvhNode layout, triangles in leaf order) into
+// compressed 8-wide nodes: every wide node takes the BVH2 children of one node
+// and keeps opening its largest-area inner child while the children fit in 8
+// slots (a leaf needs one slot per 3 triangles); children are placed by octant,
+// boxes quantised conservatively. tris8 receives the triangles in wide-leaf
+// order (same 12-float layout). Returns the depth of the wide tree.
+uint32_t build_bvh8(const std::vector<BvhNode> &nodes, const std::vector<float> &leaf_tris,
+                    std::vector<Bvh8Node> *out, std::vector<float> *tris8);
 
 // Scene::ParseJSON subset (scene.cpp:154-446) into a description whose
 // arrays live in `storage`.

@@ -26,10 +26,18 @@ class DiffParams(C.Structure):
                 ("sigma_s_detached", C.c_void_p)]
 
 
+class DiffJob(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("params", RenderParams), ("dp", DiffParams), ("film", Film),
+                ("sample_radiance", C.c_void_p), ("d_loss_d_film", C.c_void_p), ("grad_albedo", C.c_void_p),
+                ("grad_emission", C.c_void_p), ("grad_sigma_a", C.c_void_p), ("grad_sigma_s", C.c_void_p)]
+
+
 def _bind(L):
     if getattr(L, "_diff_bound", False):
         return
     p = C.c_void_p
+    L.lt_render_diff_batch.argtypes = [p, C.POINTER(DiffJob), C.c_uint32]
+    L.lt_render_adjoint_batch.argtypes = [p, C.POINTER(DiffJob), C.c_uint32]
     L.lt_diff_defaults.argtypes = [p, p, p, p, p]
     L.lt_render_diff.argtypes = [p, C.POINTER(RenderParams), C.POINTER(DiffParams), C.POINTER(Film), p]
     L.lt_render_adjoint.argtypes = [p, C.POINTER(RenderParams), C.POINTER(DiffParams), p, p, p, p, p,
@@ -48,10 +56,14 @@ def _dev(t: torch.Tensor, device) -> torch.Tensor:
 class DiffScene:
     """A loaded scene plus the sizes of its differentiable parameters."""
 
-    def __init__(self, path: str, device: int = 0):
-        self.ctx = Context(device)
+    def __init__(self, path: Optional[str] = None, device: int = 0, ctx: Optional[Context] = None):
+        """Loads the scene JSON at `path` into a new context, or uses `ctx`, a
+        context that already holds the scene."""
+        self.ctx = ctx or Context(device)
+        device = self.ctx.device
         _bind(self.ctx.L)
-        self.ctx.load_scene_json(path)
+        if ctx is None:
+            self.ctx.load_scene_json(path)
         info = self.ctx.scene_info()
         self.width, self.height = info.width, info.height
         self.num_triangles, self.num_media = info.num_triangles, info.num_media
@@ -137,3 +149,63 @@ class RenderImage(torch.autograd.Function):
 def render_image(scene: DiffScene, albedo, emission, sigma_a, sigma_s, spp: int, first_frame: int = 0,
                  max_depth: int = 8, rr_depth: int = 3) -> torch.Tensor:
     return RenderImage.apply(albedo, emission, sigma_a, sigma_s, scene, spp, first_frame, max_depth, rr_depth)
+
+
+def _batch_call(fn, owner: DiffScene, jobs):
+    arr = (DiffJob * len(jobs))(*jobs)
+    owner.ctx.set_stream(torch.cuda.current_stream(owner.device).cuda_stream)
+    native.check(owner.ctx.L, owner.ctx.h, fn(owner.ctx.h, arr, len(jobs)))
+
+
+def render_batch(scenes, params, spp, first_frame=0, max_depth: int = 8, rr_depth: int = 3,
+                 keep_samples: bool = False):
+    """lt_render_diff_batch: the differentiable forward render of several
+    scenes in one launch. scenes: DiffScenes (the first one's context runs the
+    launch); params: per scene (albedo, emission, sigma_a, sigma_s); spp,
+    first_frame, max_depth, rr_depth: one value or one per scene. Returns per
+    scene (rgb, bounces, counts[, samples]) as DiffScene.render does."""
+    n = len(scenes)
+    per = lambda v: list(v) if isinstance(v, (list, tuple)) else [v] * n
+    spp, first_frame, max_depth, rr_depth = per(spp), per(first_frame), per(max_depth), per(rr_depth)
+    jobs, keep, out = [], [], []
+    for k, sc in enumerate(scenes):
+        kp, dp = sc._params(*params[k])
+        rgb = torch.zeros((sc.height, sc.width, 3), dtype=torch.float32, device=sc.device)
+        b = torch.zeros((sc.height, sc.width), dtype=torch.int32, device=sc.device)
+        cnt = torch.zeros_like(b)
+        smp = (torch.empty((spp[k], sc.height, sc.width, 3), dtype=torch.float32, device=sc.device)
+               if keep_samples else None)
+        film = Film(rgb.data_ptr(), b.data_ptr(), cnt.data_ptr(), sc.width, sc.height, 1)
+        jobs.append(DiffJob(sc.ctx.h.value, RenderParams(spp[k], first_frame[k], max_depth[k], rr_depth[k]), dp,
+                            film, _ptr(smp), None, None, None, None, None))
+        keep.append(kp)
+        out.append((rgb, b, cnt, smp) if keep_samples else (rgb, b, cnt))
+    _batch_call(scenes[0].ctx.L.lt_render_diff_batch, scenes[0], jobs)
+    del keep
+    return out
+
+
+def adjoint_batch(scenes, params, d_loss_d_sum, spp, first_frame=0, max_depth: int = 8, rr_depth: int = 3,
+                  samples=None):
+    """lt_render_adjoint_batch: per scene the gradients (albedo, emission,
+    sigma_a, sigma_s) of the loss whose derivative with respect to the film
+    colour sums is d_loss_d_sum[k], in one launch. samples: per-scene
+    per-sample radiance from render_batch(keep_samples=True), or None."""
+    n = len(scenes)
+    per = lambda v: list(v) if isinstance(v, (list, tuple)) else [v] * n
+    spp, first_frame, max_depth, rr_depth = per(spp), per(first_frame), per(max_depth), per(rr_depth)
+    samples = samples if samples is not None else [None] * n
+    jobs, keep, grads = [], [], []
+    for k, sc in enumerate(scenes):
+        kp, dp = sc._params(*params[k])
+        g = [torch.zeros_like(x) for x in kp[:4]]
+        dI = _dev(d_loss_d_sum[k], sc.device)
+        film = Film(None, None, None, sc.width, sc.height, 1)
+        jobs.append(DiffJob(sc.ctx.h.value, RenderParams(spp[k], first_frame[k], max_depth[k], rr_depth[k]), dp,
+                            film, _ptr(samples[k]), dI.data_ptr(), *[x.data_ptr() for x in g]))
+        keep.append((kp, dI))
+        grads.append(g)
+    _batch_call(scenes[0].ctx.L.lt_render_adjoint_batch, scenes[0], jobs)
+    torch.cuda.current_stream(scenes[0].device).synchronize()
+    del keep
+    return grads

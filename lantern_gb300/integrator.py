@@ -117,3 +117,21 @@ def intersect(ctx: Context, rays, on_device: Optional[bool] = None):
     ctx.intersect(rays.ctypes.data, hits.ctypes.data, rays.shape[0], False)
     return hits
 
+
+
+def RenderBatch(integrators, frames=1, owner: Optional[Context] = None):
+    """RenderFrame(frames[i]) of every integrator, done together by
+    lt_render_batch: all scenes' samples share one wavefront and one captured
+    loop. `owner` holds that wavefront (default: the first integrator's scene
+    context). Each integrator's frame number advances as RenderFrame's would."""
+    if isinstance(frames, int):
+        frames = [frames] * len(integrators)
+    if not integrators:
+        return
+    owner = owner or integrators[0].scene.ctx
+    owner.set_stream(torch.cuda.current_stream(integrators[0].frame_buffer.ColorData.device).cuda_stream)
+    owner.render_batch([it.scene.ctx for it in integrators],
+                       [(f, it.frame_number, it.max_depth, it.rr_depth) for it, f in zip(integrators, frames)],
+                       [it.frame_buffer.film() for it in integrators])
+    for it, f in zip(integrators, frames):
+        it.frame_number += f

@@ -23,9 +23,13 @@ MISS = 0xFFFFFFFF
 SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error", "lt_set_stream", "lt_get_stream",
            "lt_sync",
            "lt_scene_create", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
-           "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder"]
+           "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
+           "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
+           "lt_render_diff_batch", "lt_render_adjoint_batch"]
 BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
+MAX_BATCH = 2048  # LT_MAX_BATCH
+TONEMAP_CLAMP, TONEMAP_FILMIC = 0, 1
 
 
 class LanternError(RuntimeError):
@@ -84,6 +88,19 @@ class RenderStats(C.Structure):
                 ("connect_ms", C.c_float)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("paths_in_flight", C.c_uint32), ("trace_threads", C.c_uint32), ("shade_threads", C.c_uint32),
+                ("connect_threads", C.c_uint32), ("loop_iterations", C.c_uint32), ("bvh_width", C.c_uint32),
+                ("ms", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class SppRange(C.Structure):
+    _fields_ = [("min_spp", C.c_uint32), ("max_spp", C.c_uint32), ("sum_spp", C.c_uint64)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -120,6 +137,12 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_intersect.argtypes = [p, p, p, C.c_uint64, C.c_int32]
         L.lt_render_noalloc.argtypes = [p, C.POINTER(RenderParams), C.POINTER(Film), C.c_uint32]
         L.lt_set_bvh_builder.argtypes = [p, C.c_int32]
+        L.lt_get_tuning.argtypes = [p, C.POINTER(Tuning)]
+        L.lt_set_tuning.argtypes = [p, C.POINTER(Tuning)]
+        L.lt_render_batch.argtypes = [p, C.POINTER(p), C.POINTER(RenderParams), C.POINTER(Film), C.c_uint32]
+        L.lt_autotune_batch.argtypes = [p, C.POINTER(p), C.POINTER(RenderParams), C.c_uint32, C.c_uint32,
+                                        C.POINTER(Tuning)]
+        L.lt_resolve.argtypes = [p, C.POINTER(Film), C.c_int32, C.c_float, p, p, C.POINTER(SppRange)]
         _lib = L
         return L
 
@@ -204,3 +227,42 @@ class Context:
 
     def intersect(self, rays_ptr: int, hits_ptr: int, n: int, on_device: bool):
         self._check(self.L.lt_intersect(self.h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr), n, int(on_device)))
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        self._check(self.L.lt_get_tuning(self.h, C.byref(t)))
+        return t
+
+    def set_tuning(self, **fields):
+        """lt_set_tuning with the given fields changed from the current tuning."""
+        t = self.tuning()
+        for k, v in fields.items():
+            setattr(t, k, v)
+        self._check(self.L.lt_set_tuning(self.h, C.byref(t)))
+
+    @staticmethod
+    def _batch_args(scenes, params):
+        n = len(scenes)
+        hs = (C.c_void_p * n)(*[s.h.value for s in scenes])
+        ps = (RenderParams * n)(*[RenderParams(*p) for p in params])
+        return n, hs, ps
+
+    def render_batch(self, scenes, params, films):
+        """lt_render_batch: scenes = Contexts holding a scene, params = (spp,
+        first_frame, max_depth, rr_depth) per scene, films = device Films."""
+        n, hs, ps = self._batch_args(scenes, params)
+        fs = (Film * n)(*films)
+        self._check(self.L.lt_render_batch(self.h, hs, ps, fs, n))
+
+    def resolve(self, film: Film, tonemap: int, exposure_stops: float, rgba_ptr: int | None,
+                rgba8_ptr: int | None) -> SppRange:
+        r = SppRange()
+        self._check(self.L.lt_resolve(self.h, C.byref(film), tonemap, exposure_stops, C.c_void_p(rgba_ptr or 0),
+                                      C.c_void_p(rgba8_ptr or 0), C.byref(r)))
+        return r
+
+    def autotune_batch(self, scenes, params, spp_cap: int = 1) -> Tuning:
+        n, hs, ps = self._batch_args(scenes, params)
+        t = Tuning()
+        self._check(self.L.lt_autotune_batch(self.h, hs, ps, n, spp_cap, C.byref(t)))
+        return t

@@ -418,6 +418,74 @@ def differentiable_targets(num_triangles: int, seed: int = 3):
     return true, init
 
 
+def batch_scenes(count: int = 64, seed: int = 5, max_depth: int = 10, rr_depth: int = 3, max_resolution: int = 1024,
+                 max_triangles: int = 500_000, name: str = "batch"):
+    """The batched workload: `count` scenes with sizes drawn per scene from one
+    generator seeded `seed`:
+
+    * resolution from {128, 256, 512, 1024}^2 (capped at max_resolution);
+    * triangle target log-uniform in [1,000, max_triangles], met as closely as
+      1-4 displaced icospheres of one subdivision level (20 * 4^L triangles
+      each, at most max_triangles in all) allow, on the ground quad under the
+      area light;
+    * spp from {4, 16, 64};
+    * 30% of the scenes also hold the dielectric fog ball of the medium
+      workload (RGB sigma_s, sigma_a, Henyey-Greenstein g = 0.3);
+    * every second scene is marked for the adjoint (``render["adjoint"]``).
+
+    Sphere materials: Lambert (60%), mirror (20%), dielectric IOR 1.5 (20%)."""
+    rng = np.random.default_rng(seed)
+    bases = {}
+    scenes = []
+    for s in range(count):
+        res = int(min(rng.choice([128, 256, 512, 1024]), max_resolution))
+        target = float(np.exp(rng.uniform(np.log(1000.0), np.log(max_triangles))))
+        spp = int(rng.choice([4, 16, 64]))
+        medium = bool(rng.uniform() < 0.3)
+        level, k = min(((lv, kk) for lv in range(1, 9) for kk in range(1, 5) if kk * 20 * 4 ** lv <= max_triangles),
+                       key=lambda c: abs(np.log(c[1] * 20 * 4 ** c[0] / target)))
+        theta = float(rng.uniform(-0.6, 0.6))
+        sc = Scene(res, res,
+                   camera={"phi": 1.1, "theta": theta, "radius": 6.0, "fov": 0.785398,
+                           "target": [0.0, 0.6, 0.0]},
+                   render={"spp": spp, "max_depth": max_depth, "rr_depth": rr_depth,
+                           "adjoint": s % 2 == 1, "target_triangles": int(target)},
+                   name=f"{name}{s:03d}")
+        if level not in bases:
+            bases[level] = icosphere(level)
+        v, f = bases[level]
+        for j in range(k):
+            cx = (j - (k - 1) / 2.0) * 1.3
+            radius = float(rng.uniform(0.45, 0.6))
+            d = fbm(v * 2.0, 4, seed * 1000 + s * 8 + j)
+            r = radius * (1.0 + 0.08 * d)
+            pos = (v * r[:, None] + np.array([cx, radius + 0.05, 0.0])[None, :]).astype(F32)
+            idx = f.astype(np.uint32)
+            u = rng.uniform()
+            bn = f"s{j}"
+            if u < 0.6:
+                sc.bsdfs.append(_lambert(bn, rng.uniform(0.2, 0.9, 3)))
+            elif u < 0.8:
+                sc.bsdfs.append({"name": bn, "type": "mirror",
+                                 "albedo": {"type": "constant", "value": [0.95, 0.95, 0.95]}})
+            else:
+                sc.bsdfs.append({"name": bn, "type": "ideal_specular_dielectric",
+                                 "albedo": {"type": "constant", "value": [0.98, 0.98, 0.98]}, "ior": 1.5})
+            sc.materials.append({"name": bn, "bsdf": bn})
+            sc.meshes.append(Mesh(bn, pos, vertex_normals(pos, idx), idx, bn))
+        if medium:
+            sc.media.append({"name": "fog", "type": "henyey_greenstein", "sigma_a": [0.05, 0.1, 0.2],
+                             "sigma_s": [2.0, 1.5, 1.0], "g": 0.3})
+            sc.bsdfs.append({"name": "water", "type": "ideal_specular_dielectric",
+                             "albedo": {"type": "constant", "value": [1.0, 1.0, 1.0]}, "ior": 1.33})
+            sc.materials.append({"name": "water", "bsdf": "water", "medium": "fog"})
+            p, n, i = uv_sphere(0.6, 64, 32, center=(0.0, 0.6, 1.4))
+            sc.meshes.append(Mesh("fog_ball", p, n, i, "water"))
+        _ground_and_light(sc)
+        scenes.append(sc)
+    return scenes
+
+
 def tiny_scene(width=32, height=32, spp=4, max_depth=8, rr_depth=3, name="tiny") -> Scene:
     """Smallest scene with every reference material: three low-poly spheres
     (Lambert, mirror, dielectric) over the ground, under the light."""

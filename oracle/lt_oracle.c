@@ -1133,3 +1133,38 @@ void orc_tri_normals(const orc_scene *s, uint32_t prim, float n[9]) {
         n[3 * j] = p[0]; n[3 * j + 1] = p[1]; n[3 * j + 2] = p[2];
     }
 }
+
+/* ---------------------------------------------------------------- resolve */
+/* visualizer.cpp:352-364 divides the colour sum by the count; the shader
+ * (final_resolve_ps.glsl:24-43) scales by the exposure constant exp2f(stops)
+ * (visualizer.cpp:1308) and tone maps. GLSL clamp(x, 0, 1) = min(max(x, 0), 1). */
+static float clamp01f(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+static float filmicf(float c) {
+    float x = fmaxf(0.0f, c - 0.004f);
+    return clamp01f((x * (6.2f * x + 0.5f)) / (x * (6.2f * x + 1.7f) + 0.06f));
+}
+
+void orc_resolve(const float *rgb, const uint32_t *counts, uint64_t npix, int tonemap, float exposure_stops,
+                 float *rgba, uint8_t *rgba8, uint32_t spp_minmax[2], uint64_t *spp_sum) {
+    const float e = exp2f(exposure_stops);
+    uint32_t lo = 0xFFFFFFFFu, hi = 0;
+    uint64_t sum = 0;
+    for (uint64_t i = 0; i < npix; ++i) {
+        const float n = (float)counts[i];
+        float c[4] = {e * (rgb[3 * i] / n), e * (rgb[3 * i + 1] / n), e * (rgb[3 * i + 2] / n), e * 1.0f};
+        for (int k = 0; k < 4; ++k) c[k] = tonemap == 1 ? (k == 3 ? 1.0f : filmicf(c[k])) : clamp01f(c[k]);
+        for (int k = 0; k < 4; ++k) {
+            if (rgba) rgba[4 * i + k] = c[k];
+            if (rgba8) rgba8[4 * i + k] = (uint8_t)lrintf(c[k] * 255.0f);
+        }
+        if (counts[i] < lo) lo = counts[i];
+        if (counts[i] > hi) hi = counts[i];
+        sum += counts[i];
+    }
+    if (spp_minmax) {
+        spp_minmax[0] = lo;
+        spp_minmax[1] = hi;
+    }
+    if (spp_sum) *spp_sum = sum;
+}

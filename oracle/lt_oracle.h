@@ -123,6 +123,13 @@ void orc_diff_render(const orc_scene *s, int fp64, const float *albedo, const fl
                      double *rgb, double *g_albedo, double *g_emission, double *g_sigma_a, double *g_sigma_s,
                      int threads);
 
+/* Final resolve (visualizer.cpp:352-364, final_resolve_ps.glsl:24-43): per
+ * pixel c = exp2f(exposure_stops) * (rgb / count, 1), tone mapped by clamp
+ * (tonemap 0) or the filmic curve (1); rgba8 = round(c * 255). Either output
+ * may be NULL; spp_minmax / spp_sum (optional) get the sample-count range. */
+void orc_resolve(const float *rgb, const uint32_t *counts, uint64_t npix, int tonemap, float exposure_stops,
+                 float *rgba, uint8_t *rgba8, uint32_t spp_minmax[2], uint64_t *spp_sum);
+
 /* Building blocks, exported for golden-vector checks against the reference. */
 void orc_pcg_stream(uint64_t seed, uint64_t seq, uint32_t n, uint32_t *out_uint, float *out_float);
 uint32_t orc_tile_seed(uint32_t tile, uint32_t frame);

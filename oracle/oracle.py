@@ -112,6 +112,8 @@ def lib():
             dp = C.POINTER(C.c_double)
             L.orc_diff_render.argtypes = [p, C.c_int, fp, fp, fp, fp, u32, u32, u32, u32, up, fp, dp, dp, dp, dp, dp,
                                           C.c_int]
+            L.orc_resolve.argtypes = [fp, up, u64, C.c_int, f32, fp, C.POINTER(C.c_uint8), up,
+                                      C.POINTER(C.c_uint64)]
             _lib = L
     return _lib
 
@@ -401,3 +403,19 @@ class ReferenceScene:
                                      C.byref(rays))
         return {"rgb": rgb_a, "bounces": b_a, "counts": c_a, "rgb_b": rgb_b, "bounces_b": b_b,
                 "counts_b": c_b, "seconds": secs, "rays": rays.value}
+
+
+def resolve(rgb, counts, tonemap: int, exposure_stops: float):
+    """orc_resolve on (H, W, 3) float32 colour sums and (H, W) counts:
+    returns (rgba float32 (H, W, 4), rgba8 uint8 (H, W, 4), (min, max, sum) spp)."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    counts = np.ascontiguousarray(counts, dtype=np.uint32)
+    h, w = counts.shape
+    out = np.empty((h, w, 4), np.float32)
+    out8 = np.empty((h, w, 4), np.uint8)
+    mm = np.zeros(2, np.uint32)
+    sm = C.c_uint64(0)
+    L = lib()
+    L.orc_resolve(fptr(rgb), uptr(counts), h * w, tonemap, C.c_float(exposure_stops), fptr(out),
+                  out8.ctypes.data_as(C.POINTER(C.c_uint8)), uptr(mm), C.byref(sm))
+    return out, out8, (int(mm[0]), int(mm[1]), int(sm.value))

@@ -53,12 +53,21 @@ def _compare_hits(gh, oh):
     return int(hit.sum()), int(diff.sum())
 
 
+@pytest.fixture(params=[2, 8], ids=["bvh2", "bvh8"])
+def width(request, ctx):
+    """BVH width of the traversal (lt_tuning.bvh_width); the shared context is
+    set back to 2 afterwards."""
+    ctx.set_tuning(bvh_width=request.param)
+    yield request.param
+    ctx.set_tuning(bvh_width=2)
+
+
 @pytest.mark.parametrize("make", [
     lambda: S.nine_spheres(width=64, height=64, name="isect_nine"),
     lambda: S.displaced_icosphere_scene(width=64, height=64, levels=5, name="isect_ico5"),
     lambda: S.tiny_scene(name="isect_tiny"),
 ])
-def test_intersect_matches_oracle(ctx, scene_dir, make):
+def test_intersect_matches_oracle(ctx, width, scene_dir, make):
     path = make().write(scene_dir)
     ctx.load_scene_json(path)
     orc, rays = _scene_rays(path, 1 << 16, seed=7)
@@ -71,7 +80,7 @@ def test_intersect_matches_oracle(ctx, scene_dir, make):
     assert np.array_equal(gh.view(np.uint32), gh2.view(np.uint32))
 
 
-def test_intersect_tnear_tfar_rule(ctx, scene_dir):
+def test_intersect_tnear_tfar_rule(ctx, width, scene_dir):
     """Rays clipped exactly at, and one float short of, each hit distance (and
     starting there) are accepted or rejected as the oracle's Embree rule says:
     |den|*tnear < T <= |den|*tfar, evaluated in float."""
@@ -100,10 +109,12 @@ def test_intersect_tnear_tfar_rule(ctx, scene_dir):
     (lambda: S.medium_sphere_scene(width=40, height=40, reference_expressible=True, name="paths_med_ref"), 4, 32),
     (lambda: S.medium_sphere_scene(width=40, height=40, name="paths_med_hg"), 4, 32),
 ])
-def test_render_matches_oracle_path_by_path(scene_dir, make, spp, depth):
+@pytest.mark.parametrize("bvh_width", [2, 8])
+def test_render_matches_oracle_path_by_path(scene_dir, make, spp, depth, bvh_width):
     path = make().write(scene_dir)
     sc = Scene(0)
     sc.LoadSceneFromJSON(path)
+    sc.ctx.set_tuning(bvh_width=bvh_width)
     fb = FrameBuffer(sc.width, sc.height, "cuda:0")
     Integrator(sc, fb, max_depth=depth, rr_depth=3).RenderFrame(spp)
     torch.cuda.synchronize()
