@@ -200,9 +200,9 @@ typedef struct lt_render_stats {
     uint32_t iterations;     /* wavefront iterations */
     uint32_t kernel_launches;
     float gpu_ms;            /* device time of the last lt_render */
-    float trace_ms;          /* device time in the path-segment trace kernel */
+    float trace_ms;          /* device time in the trace kernel (path rays + connection rays) */
     float shade_ms;          /* ... in the shade kernel (incl. camera-ray generation) */
-    float connect_ms;        /* ... in the connection trace + resolve kernel */
+    uint64_t light_traversals; /* connection rays traced (the rest were resolved against the light alone) */
 } lt_render_stats;
 lt_status lt_render_stats_get(lt_ctx *ctx, lt_render_stats *out);
 
@@ -229,9 +229,8 @@ lt_status lt_resolve(lt_ctx *ctx, const lt_film *film, int32_t tonemap, float ex
  * configuration, and many scenes rendered together in one captured loop. */
 typedef struct lt_tuning {
     uint32_t paths_in_flight;  /* wavefront path slots; 0 = min(samples, 2,097,152) */
-    uint32_t trace_threads;    /* threads per block of the path-segment trace kernel: 64, 128 or 256 */
+    uint32_t trace_threads;    /* threads per block of the trace kernel: 64, 128 or 256 */
     uint32_t shade_threads;    /* ... of the shade kernel (and camera-ray generation) */
-    uint32_t connect_threads;  /* ... of the connection kernel */
     uint32_t loop_iterations;  /* wavefront iterations per body of lt_render_batch's loop: 2, 4 or 8 */
     uint32_t bvh_width;        /* children per BVH node: 2 (BVH2) or 8 (compressed 8-wide, built on demand) */
     float ms;                  /* lt_autotune_batch: device time of the chosen tuning on its sample */

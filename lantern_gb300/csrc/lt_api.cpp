@@ -115,7 +115,7 @@ static void free_wave(lt_ctx *c) {
 
 static void default_tuning(lt_tuning *t) {
     *t = lt_tuning{};
-    t->trace_threads = t->shade_threads = t->connect_threads = 128;
+    t->trace_threads = t->shade_threads = 128;
     t->loop_iterations = 2;
     t->bvh_width = 2;
 }
@@ -126,7 +126,6 @@ static void apply_tuning(lt_ctx *c) {
         ls->bvh_width = (int)c->tuning.bvh_width;
         ls->trace_threads = (int)c->tuning.trace_threads;
         ls->shade_threads = (int)c->tuning.shade_threads;
-        ls->connect_threads = (int)c->tuning.connect_threads;
     }
     query_launch_shape(c->device, false, &c->shape);
     query_launch_shape(c->device, true, &c->batch_shape);
@@ -471,7 +470,7 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
         const int kBatch = 4;
         for (;;) {
             for (int k = 0; k < kBatch; ++k) {
-                for (int stage = 0; stage < 3; ++stage) {
+                for (int stage = 0; stage < kStages; ++stage) {
                     if (nev == c->stage_events.size()) {
                         cudaEvent_t e;
                         CUDA_TRY(c, cudaEventCreate(&e));
@@ -481,14 +480,15 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
                     c->stage_of_event.push_back(stage);
                     CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
                 }
-                launches += 3;
+                launches += kStages;
                 cur ^= 1;
                 ++iters;
             }
             CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters),
                                         cudaMemcpyDeviceToHost, c->stream));
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-            if (c->counters_host->count[cur] == 0) break;
+            // done when no path ray is queued and the last shade emitted no connection
+            if (c->counters_host->count[cur] == 0 && c->counters_host->ccount[cur ^ 1] == 0) break;
             if (iters > 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u)
                 return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
         }
@@ -504,15 +504,15 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
         }
         CUDA_TRY(c, cudaEventRecord(c->stage_events[nev], c->stream));
         CUDA_TRY(c, cudaEventSynchronize(c->stage_events[nev]));
-        float acc[3] = {0, 0, 0};
+        float acc[kStages] = {0, 0};
         for (size_t i = 0; i < nev; ++i) {
             float ms = 0.0f;
             CUDA_TRY(c, cudaEventElapsedTime(&ms, c->stage_events[i], c->stage_events[i + 1]));
             acc[c->stage_of_event[i]] += ms;
         }
-        c->stats.trace_ms = acc[0];
-        c->stats.shade_ms = acc[1];
-        c->stats.connect_ms = acc[2];
+        c->stats.trace_ms = acc[kStageTrace];
+        c->stats.shade_ms = acc[kStageShade];
+        c->stats.light_traversals = c->counters_host->light_traversals;
     }
     c->stats.samples = a.total;
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -718,16 +718,16 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
         const uint32_t limit = 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u;
         for (;;) {
             for (int k = 0; k < kBatch; ++k) {
-                for (int stage = 0; stage < 3; ++stage)
+                for (int stage = 0; stage < kStages; ++stage)
                     CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
-                launches += 3;
+                launches += kStages;
                 cur ^= 1;
                 ++iters;
             }
             CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
                                         c->stream));
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-            if (c->counters_host->count[cur] == 0) break;
+            if (c->counters_host->count[cur] == 0 && c->counters_host->ccount[cur ^ 1] == 0) break;
             if (iters > limit) return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
         }
         c->stats.main_rays = c->counters_host->main_rays;
@@ -757,11 +757,10 @@ extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) {
     n.paths_in_flight = t->paths_in_flight;
     if (t->trace_threads) n.trace_threads = t->trace_threads;
     if (t->shade_threads) n.shade_threads = t->shade_threads;
-    if (t->connect_threads) n.connect_threads = t->connect_threads;
     if (t->loop_iterations) n.loop_iterations = t->loop_iterations;
     if (t->bvh_width) n.bvh_width = t->bvh_width;
     n.ms = t->ms;
-    if (!valid_threads(n.trace_threads) || !valid_threads(n.shade_threads) || !valid_threads(n.connect_threads))
+    if (!valid_threads(n.trace_threads) || !valid_threads(n.shade_threads))
         return fail(c, LT_ERR_INVALID, "threads per block must be 64, 128 or 256");
     if (n.loop_iterations != 2 && n.loop_iterations != 4 && n.loop_iterations != 8)
         return fail(c, LT_ERR_INVALID, "loop_iterations must be 2, 4 or 8");
@@ -788,8 +787,7 @@ static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
     std::vector<uintptr_t> key = {(uintptr_t)c->wave.arena, w.capacity, (uintptr_t)c->table_dev,
                                   (uintptr_t)c->batch_shape.trace_threads, (uintptr_t)c->batch_shape.trace_blocks,
                                   (uintptr_t)c->batch_shape.shade_threads, (uintptr_t)c->batch_shape.shade_blocks,
-                                  (uintptr_t)c->batch_shape.connect_threads, (uintptr_t)c->batch_shape.connect_blocks,
-                                  c->tuning.loop_iterations};
+                                  (uintptr_t)c->batch_shape.bvh_width, c->tuning.loop_iterations};
     if (c->graph_exec && key == c->graph_key) return LT_OK;
     free_graph(c);
     cudaStream_t cs = c->own_stream;
@@ -827,7 +825,7 @@ static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
     CUDA_TRY(c, cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int cur = 0;
     for (uint32_t k = 0; k < c->tuning.loop_iterations && e == cudaSuccess; ++k) {
-        for (int stage = 0; stage < 3 && e == cudaSuccess; ++stage)
+        for (int stage = 0; stage < kStages && e == cudaSuccess; ++stage)
             e = launch_batch_stage(stage, c->table_dev, w, cur, c->batch_shape, cs);
         cur ^= 1;
     }
@@ -919,7 +917,8 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
         c->stats.light_rays = k.light_rays;
         c->stats.bsdf_rays = k.bsdf_rays;
         c->stats.iterations = (uint32_t)k.iterations;
-        launches += 1 + 3 * (uint32_t)k.iterations + (uint32_t)(k.iterations / c->tuning.loop_iterations);
+        launches += 1 + kStages * (uint32_t)k.iterations + (uint32_t)(k.iterations / c->tuning.loop_iterations);
+        c->stats.light_traversals = k.light_traversals;
     } else {
         CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -979,8 +978,8 @@ extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const l
     const uint32_t paths[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
     const uint32_t threads[] = {64, 128, 256};
     const uint32_t iters[] = {2, 4, 8};
-    for (int coord = 0; coord < 6; ++coord) {
-        const uint32_t *vals = coord == 0 ? widths : coord == 1 ? paths : coord == 5 ? iters : threads;
+    for (int coord = 0; coord < 5; ++coord) {
+        const uint32_t *vals = coord == 0 ? widths : coord == 1 ? paths : coord == 4 ? iters : threads;
         const int nv = coord == 0 ? 2 : coord == 1 ? 4 : 3;
         for (int v = 0; v < nv; ++v) {
             lt_tuning t = cur;
@@ -988,7 +987,6 @@ extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const l
                               : coord == 1 ? &t.paths_in_flight
                               : coord == 2 ? &t.trace_threads
                               : coord == 3 ? &t.shade_threads
-                              : coord == 4 ? &t.connect_threads
                                            : &t.loop_iterations;
             if (*field == vals[v]) continue;
             *field = vals[v];

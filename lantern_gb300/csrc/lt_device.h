@@ -48,13 +48,12 @@ struct PathState {
 };
 
 struct WaveCounters {
-    uint32_t count[2];           // queue lengths (ping-pong)
-    uint32_t ccount;             // connection records this iteration
-    uint32_t error;              // nonzero: a device-side bound was exceeded
+    uint32_t count[2];           // path-ray queue lengths (ping-pong by iteration parity)
+    uint32_t ccount[2];          // connection records written by k_shade(parity)
     unsigned long long work_next; // next (pixel, frame) work item
     unsigned long long main_rays, light_rays, bsdf_rays;
-    uint32_t trace_fetch;         // persistent-thread ray counters, zeroed by the
-    uint32_t connect_fetch;       // kernel that runs before each consumer
+    uint32_t trace_fetch;         // k_trace's persistent-thread counter, zeroed by the launch before
+    uint32_t error;               // nonzero: a device-side bound was exceeded
     unsigned long long light_traversals;  // connection rays that needed an occlusion query
     unsigned long long iterations;        // wavefront iterations of a captured loop
 };
@@ -90,8 +89,8 @@ struct RenderArgs {
 struct LaunchShape {
     int sms = 0;
     int bvh_width = 2;  // 2: BVH2 traversal; 8: compressed 8-wide traversal
-    int trace_threads = 128, shade_threads = 128, connect_threads = 128;
-    int trace_blocks = 0, shade_blocks = 0, connect_blocks = 0, isect_blocks = 0;
+    int trace_threads = 128, shade_threads = 128;
+    int trace_blocks = 0, shade_blocks = 0, isect_blocks = 0;
     int diff_blocks = 0;
     int diff_fwd_batch_blocks = 0, diff_adj_batch_blocks = 0;
 };
@@ -174,7 +173,10 @@ cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const Re
                                 uint32_t num_media, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
                              const LaunchShape &ls, cudaStream_t st);
-enum WaveStage { kStageTrace = 0, kStageShade = 1, kStageConnect = 2 };
+// Per wavefront iteration: k_trace (path rays of this iteration + connection
+// rays of the previous shade), then k_shade.
+enum WaveStage { kStageTrace = 0, kStageShade = 1 };
+constexpr int kStages = 2;
 cudaError_t launch_wave_stage(int stage, const DevScene &s, const Wavefront &w, const RenderArgs &a,
                               const FilmPtrs &f, int cur, const LaunchShape &ls, cudaStream_t st);
 // batched render over a scene table (lt_render_batch)
@@ -182,8 +184,8 @@ cudaError_t launch_batch_init(const SceneTable *t, const Wavefront &w, const Lau
 cudaError_t launch_batch_stage(int stage, const SceneTable *t, const Wavefront &w, int cur, const LaunchShape &ls,
                                cudaStream_t st);
 // Condition kernel of a captured loop: counters->iterations += iters; the
-// while node `h` continues while queue `cur` holds paths and the iteration
-// limit of `t` is not reached.
+// while node `h` continues while path queue `cur` or the connection records
+// of parity cur ^ 1 are not empty and the iteration limit of `t` is not reached.
 // batched differentiable forward (adjoint false) or adjoint over t's slots and diff entries
 cudaError_t launch_diff_batch(bool adjoint, SceneTable *t, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_loop_condition(const Wavefront &w, const SceneTable *t, cudaGraphConditionalHandle h, int cur,

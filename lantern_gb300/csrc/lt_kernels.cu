@@ -1,13 +1,14 @@
 // lt_kernels.cu -- sm_103a kernels of the wavefront path tracer.
 //
 // Stages per wavefront iteration (one path segment for every live path):
-//   trace    closest hit of every queued path ray                 (rtcIntersect1, scene.cpp:116-121)
+//   trace    closest hit of every queued path ray (rtcIntersect1, scene.cpp:116-121),
+//            and in the same persistent launch the connection rays that the
+//            previous shade emitted: occlusion query, area-light pdf and MIS
+//            weight of SampleLi/PdfLi (area_light.cpp:18-110), film add
 //   shade    one bounce of RenderPixel (integrator.cpp:116-243): background, medium
 //            free flight, emission, light choice, BSDF sampling, roulette;
 //            emits up to two connection rays; finished paths are added to the
 //            film and their slot starts the next (pixel, frame) sample
-//   connect  closest hit of every connection ray, then the area-light pdf and
-//            MIS weight of SampleLi/PdfLi (area_light.cpp:18-110) and the film add
 //
 // Queues are compacted with warp ballots (one atomic per warp). Every random
 // number is drawn in shade, in the reference's order, so that a path's
@@ -223,7 +224,11 @@ __device__ __forceinline__ void trav8_start(Trav8 &r, v3 O, v3 D, float tnear, f
     r.done = false;
 }
 
-__device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) { return (float)((w >> (8u * k)) & 0xFFu); }
+// float(byte k of w), exactly: the byte placed under the exponent of 2^23 by
+// one byte permute, minus 2^23 (avoids the slower integer-to-float conversion).
+__device__ __forceinline__ float byte_f(uint32_t w, uint32_t k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k)) - 8388608.0f;
+}
 
 // Box tests of the 8 children of node `idx`; returns the hit mask (inner
 // children in bits 24-31, leaf triangles in bits 0-23) and the node's bases.
@@ -632,38 +637,9 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters->count[0] = (uint32_t)first;
         W.counters->count[1] = 0;
-        W.counters->ccount = 0;
+        W.counters->ccount[0] = W.counters->ccount[1] = 0;
         W.counters->work_next = first;
         W.counters->trace_fetch = 0;
-    }
-}
-
-// Closest hit of every queued path ray. Persistent: entries are fetched from
-// counters->trace_fetch (zeroed by the kernel before).
-template <class Src, class B>
-__global__ void __launch_bounds__(256) k_trace(Src src, Wavefront W, int cur) {
-    const uint32_t n = W.counters->count[cur];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        W.counters->count[cur ^ 1] = 0;
-        W.counters->ccount = 0;
-        W.counters->main_rays += n;
-    }
-    const float4 *rays = W.ray[cur];
-    Geo g = B::geo(src.scene(0));
-    typename B::State r;
-    typename B::Entry stack[B::kDepth];
-    B::idle(r);
-    uint32_t idx = 0;
-    for (;;) {
-        if (B::done(r)) {
-            idx = fetch_next(&W.counters->trace_fetch);
-            if (idx >= n) break;
-            if (Src::kMany) g = B::geo(src.scene(W.p[cur].flags[idx] >> kFlagSceneShift));
-            float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
-            B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
-        }
-        B::run(g, r, stack);
-        if (B::done(r)) W.hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
     }
 }
 
@@ -675,7 +651,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(Src src, Wavefront W, int cur)
     const uint32_t n = W.counters->count[cur];
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->connect_fetch = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
     uint32_t n_ref_rays = 0, n_ref_rays_b = 0;  // connection rays the reference would trace
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         uint32_t q = base + threadIdx.x;
@@ -842,14 +818,14 @@ __global__ void __launch_bounds__(256, 4) k_shade(Src src, Wavefront W, int cur)
         // connection records
         {
             conn_light |= p.scene << kConnSceneShift;
-            uint32_t idx = warp_reserve(&W.counters->ccount, emit_l);
+            uint32_t idx = warp_reserve(&W.counters->ccount[cur], emit_l);
             if (emit_l) {
                 W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light));
                 W.cray[2 * idx + 1] = make_float4(l_dir.x, l_dir.y, l_dir.z, __uint_as_float(p.pixel));
                 W.crec[2 * idx] = make_float4(l_f.x, l_f.y, l_f.z, l_pdf);
                 W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, l_tl);
             }
-            idx = warp_reserve(&W.counters->ccount, emit_b);
+            idx = warp_reserve(&W.counters->ccount[cur], emit_b);
             if (emit_b) {
                 W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z,
                                               __uint_as_float(conn_light | kConnectBsdf));
@@ -935,35 +911,62 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     film_add(F, pixel, T * (c * (float)S.num_lights));
 }
 
+// Path rays of iteration `cur` (closest hit into W.hits) and, in the same
+// persistent launch, the connection records that the previous k_shade wrote
+// (parity cur ^ 1; occlusion query or closest hit, then resolve_connection).
+// Both come from one launch of k_shade, so one traversal kernel serves them:
+// items [0, n) are path rays, [n, n + nc) connection records, fetched from
+// counters->trace_fetch (zeroed by the launch before). Path rays come first so
+// that the short connection queries fill the tail.
 template <class Src, class B>
-__global__ void __launch_bounds__(256) k_connect(Src src, Wavefront W) {
-    const uint32_t n = W.counters->ccount;
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
-    uint32_t n_trav = 0;
+__global__ void __launch_bounds__(256) k_trace(Src src, Wavefront W, int cur) {
+    const uint32_t n = W.counters->count[cur];
+    const uint32_t nc = W.counters->ccount[cur ^ 1];
+    const uint32_t total = n + nc;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counters->count[cur ^ 1] = 0;  // filled by the next k_shade
+        W.counters->ccount[cur] = 0;
+        W.counters->main_rays += n;
+    }
+    const float4 *rays = W.ray[cur];
     Geo g = B::geo(src.scene(0));
     typename B::State r;
     typename B::Entry stack[B::kDepth];
     B::idle(r);
-    uint32_t idx = 0, kl = 0, pixel = 0;
+    uint32_t idx = 0, kl = 0, pixel = 0, n_trav = 0;
     for (;;) {
         if (B::done(r)) {
-            idx = fetch_next(&W.counters->connect_fetch);
-            if (idx >= n) break;
-            float4 a = ldg4(W.cray + 2 * idx), b = ldg4(W.cray + 2 * idx + 1);
-            float tl = ldg4(W.crec + 2 * idx + 1).w;
-            kl = __float_as_uint(a.w);
-            pixel = __float_as_uint(b.w);
-            const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
-            if (Src::kMany) g = B::geo(S);
-            const LightInfo &L = S.lights[kl & kConnLightMask];
-            if (tl > 0.0f) B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, tl, true, (uint32_t)L.geom);
-            else B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, __int_as_float(0x7f800000), false, 0);
-            n_trav++;
+            idx = fetch_next(&W.counters->trace_fetch);
+            if (idx >= total) break;
+            if (idx < n) {
+                if (Src::kMany) g = B::geo(src.scene(W.p[cur].flags[idx] >> kFlagSceneShift));
+                float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
+                B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
+            } else {
+                const uint32_t c = idx - n;
+                float4 a = ldg4(W.cray + 2 * c), b = ldg4(W.cray + 2 * c + 1);
+                float tl = ldg4(W.crec + 2 * c + 1).w;
+                kl = __float_as_uint(a.w);
+                pixel = __float_as_uint(b.w);
+                const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
+                if (Src::kMany) g = B::geo(S);
+                const LightInfo &L = S.lights[kl & kConnLightMask];
+                if (tl > 0.0f)
+                    B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, tl, true, (uint32_t)L.geom);
+                else
+                    B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, __int_as_float(0x7f800000),
+                             false, 0);
+                n_trav++;
+            }
         }
         B::run(g, r, stack);
         if (B::done(r)) {
-            const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
-            resolve_connection(src.scene(sid), W, src.film(sid), idx, kl, pixel, r);
+            if (idx < n) {
+                W.hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
+            } else {
+                const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
+                resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, pixel, r);
+            }
         }
     }
     if (n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
@@ -974,7 +977,7 @@ __global__ void __launch_bounds__(256) k_connect(Src src, Wavefront W) {
 __global__ void k_loop_condition(WaveCounters *c, const SceneTable *t, cudaGraphConditionalHandle h, int cur,
                                  uint32_t iters) {
     c->iterations += iters;
-    unsigned int more = c->count[cur] != 0u;
+    unsigned int more = c->count[cur] != 0u || c->ccount[cur ^ 1] != 0u;
     if (more && c->iterations >= t->iteration_limit) {
         c->error = 2;
         more = 0;
@@ -1438,14 +1441,10 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
         out->trace_blocks = w8 ? blocks_for(k_trace<ManyScenes, Bvh8>, out->trace_threads, sms)
                                : blocks_for(k_trace<ManyScenes, Bvh2>, out->trace_threads, sms);
         out->shade_blocks = blocks_for(k_shade<ManyScenes>, out->shade_threads, sms);
-        out->connect_blocks = w8 ? blocks_for(k_connect<ManyScenes, Bvh8>, out->connect_threads, sms)
-                                 : blocks_for(k_connect<ManyScenes, Bvh2>, out->connect_threads, sms);
     } else {
         out->trace_blocks = w8 ? blocks_for(k_trace<OneScene, Bvh8>, out->trace_threads, sms)
                                : blocks_for(k_trace<OneScene, Bvh2>, out->trace_threads, sms);
         out->shade_blocks = blocks_for(k_shade<OneScene>, out->shade_threads, sms);
-        out->connect_blocks = w8 ? blocks_for(k_connect<OneScene, Bvh8>, out->connect_threads, sms)
-                                 : blocks_for(k_connect<OneScene, Bvh2>, out->connect_threads, sms);
     }
     out->isect_blocks = w8 ? blocks_for(k_intersect<Bvh8>, 128, sms) : blocks_for(k_intersect<Bvh2>, 128, sms);
     out->diff_blocks = blocks_for(k_diff_adjoint, 128, sms);
@@ -1502,11 +1501,8 @@ static cudaError_t stage(int stage, const Src &src, const Wavefront &w, int cur,
     if (stage == kStageTrace) {
         if (w8) k_trace<Src, Bvh8><<<ls.trace_blocks, ls.trace_threads, 0, st>>>(src, w, cur);
         else k_trace<Src, Bvh2><<<ls.trace_blocks, ls.trace_threads, 0, st>>>(src, w, cur);
-    } else if (stage == kStageShade) {
-        k_shade<Src><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(src, w, cur);
     } else {
-        if (w8) k_connect<Src, Bvh8><<<ls.connect_blocks, ls.connect_threads, 0, st>>>(src, w);
-        else k_connect<Src, Bvh2><<<ls.connect_blocks, ls.connect_threads, 0, st>>>(src, w);
+        k_shade<Src><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(src, w, cur);
     }
     return cudaGetLastError();
 }

@@ -85,13 +85,12 @@ class RenderStats(C.Structure):
     _fields_ = [("main_rays", C.c_uint64), ("light_rays", C.c_uint64), ("bsdf_rays", C.c_uint64),
                 ("samples", C.c_uint64), ("iterations", C.c_uint32), ("kernel_launches", C.c_uint32),
                 ("gpu_ms", C.c_float), ("trace_ms", C.c_float), ("shade_ms", C.c_float),
-                ("connect_ms", C.c_float)]
+                ("light_traversals", C.c_uint64)]
 
 
 class Tuning(C.Structure):
     _fields_ = [("paths_in_flight", C.c_uint32), ("trace_threads", C.c_uint32), ("shade_threads", C.c_uint32),
-                ("connect_threads", C.c_uint32), ("loop_iterations", C.c_uint32), ("bvh_width", C.c_uint32),
-                ("ms", C.c_float)]
+                ("loop_iterations", C.c_uint32), ("bvh_width", C.c_uint32), ("ms", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

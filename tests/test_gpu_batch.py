@@ -107,12 +107,11 @@ def test_generated_batch_with_tuning(scene_dir):
     assert t.trace_threads in (64, 128, 256) and t.loop_iterations in (2, 4, 8) and t.ms > 0
     assert owner.tuning().as_dict() == t.as_dict()
     # a tuning that differs from the default in every field still gives the same image
-    owner.set_tuning(paths_in_flight=4096, trace_threads=64, shade_threads=256, connect_threads=64,
-                     loop_iterations=8, bvh_width=8)
+    owner.set_tuning(paths_in_flight=4096, trace_threads=64, shade_threads=256, loop_iterations=8, bvh_width=8)
     _check_batch(scenes, [sc.render["spp"] // 4 + 1 for sc in gen], [sc.render["max_depth"] for sc in gen],
                  list(range(len(gen))))
     st = owner.stats()
-    assert st.iterations > 0 and st.kernel_launches > 3 * st.iterations
+    assert st.iterations > 0 and st.kernel_launches > 2 * st.iterations
 
 
 def test_diff_batch_equals_individual(scene_dir):
