@@ -125,7 +125,9 @@ lt_status lt_set_bvh_builder(lt_ctx *ctx, int32_t builder);
 
 /* Scene::LoadSceneFromJSON (scene.h:71): reads a Lantern scene JSON and the
  * LMF files it names (triangle LMF, transform, constant albedo, media,
- * emission), then lt_scene_create. */
+ * emission), generates its "grid" and "geosphere" primitives as CreateGrid /
+ * CreateGeosphere do (geometry_generator.cpp:214-356,515-566; scene.cpp:408-426),
+ * then lt_scene_create. */
 lt_status lt_scene_load_json(lt_ctx *ctx, const char *path);
 
 typedef struct lt_scene_info {

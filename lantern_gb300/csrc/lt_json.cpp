@@ -5,7 +5,8 @@
 // orbiting pinhole camera with the reference's defaults, lambert / mirror /
 // ideal_specular_dielectric BSDFs with constant albedo, non_scattering and
 // isotropic_scattering media (plus the henyey_greenstein extension), materials,
-// and "lmf" primitives with an optional row-major 4x4 transform and emission.
+// and "lmf", "grid" and "geosphere" primitives with an optional row-major 4x4
+// transform and emission.
 // Numbers are read as double and narrowed to float, as nlohmann's get<float>()
 // does. Unlike the reference, which prints and skips a primitive it cannot
 // load, every problem here is returned as an error.
@@ -167,6 +168,82 @@ bool float3(const Json *j, float out[3]) {
 }
 
 // ReadLMF (io/lantern_model_file.cpp:33-65) with bounds checks
+// CreateGrid (geometry_generator.cpp:515-566): m rows of n vertices in the xz
+// plane, row i at z = -(depth/2 - i * dz), normals +y, two triangles per cell.
+void make_grid(float width, float depth, uint32_t m, uint32_t n, std::vector<float> &pos, std::vector<float> &nrm,
+               std::vector<uint32_t> &idx) {
+    const float half_w = 0.5f * width, half_d = 0.5f * depth;
+    const float dx = width / (float)(n - 1), dz = depth / (float)(m - 1);
+    pos.resize(3 * (size_t)m * n);
+    nrm.resize(3 * (size_t)m * n);
+    for (uint32_t i = 0; i < m; ++i) {
+        const float z = half_d - (float)i * dz;
+        for (uint32_t j = 0; j < n; ++j) {
+            const float x = -half_w + (float)j * dx;
+            float *p = &pos[3 * ((size_t)i * n + j)], *q = &nrm[3 * ((size_t)i * n + j)];
+            p[0] = x; p[1] = 0.0f; p[2] = -z;
+            q[0] = 0.0f; q[1] = 1.0f; q[2] = 0.0f;
+        }
+    }
+    idx.clear();
+    idx.reserve(6 * (size_t)(m - 1) * (n - 1));
+    for (uint32_t i = 0; i + 1 < m; ++i)
+        for (uint32_t j = 0; j + 1 < n; ++j) {
+            const uint32_t a = i * n + j, b = (i + 1) * n + j;
+            idx.insert(idx.end(), {a, a + 1, b, b, a + 1, b + 1});
+        }
+}
+
+// CreateGeosphere (geometry_generator.cpp:306-356) with Subdivide (:214-283):
+// the icosahedron below, each subdivision replacing every triangle by four with
+// six fresh vertices (no sharing), then every vertex projected to the sphere:
+// n = v * (1 / sqrt(dot(v, v))), position = radius * n, normal = n.
+void make_geosphere(float radius, uint32_t subdivisions, std::vector<float> &pos, std::vector<float> &nrm,
+                    std::vector<uint32_t> &idx) {
+    const float X = 0.525731f, Z = 0.850651f;
+    const float base[12][3] = {{-X, 0.0f, -Z}, {X, 0.0f, -Z}, {-X, 0.0f, Z}, {X, 0.0f, Z},
+                               {0.0f, Z, -X},  {0.0f, Z, X},  {0.0f, -Z, -X}, {0.0f, -Z, X},
+                               {Z, X, 0.0f},   {-Z, X, 0.0f}, {Z, -X, 0.0f},  {-Z, -X, 0.0f}};
+    const uint32_t tri[60] = {1, 4, 0, 4, 9, 0, 4, 5, 9, 8, 5, 4, 1, 8, 4, 1, 10, 8, 10, 3, 8, 8, 3, 5, 3, 2, 5,
+                              3, 7, 2, 3, 10, 7, 10, 6, 7, 6, 11, 7, 6, 0, 11, 6, 1, 0, 10, 1, 6, 11, 0, 9, 2, 11, 9,
+                              5, 2, 9, 11, 2, 7};
+    pos.assign(&base[0][0], &base[0][0] + 36);
+    idx.assign(tri, tri + 60);
+    for (uint32_t s = 0; s < subdivisions; ++s) {
+        std::vector<float> p2;
+        std::vector<uint32_t> i2;
+        const size_t nt = idx.size() / 3;
+        p2.reserve(18 * nt);
+        i2.reserve(12 * nt);
+        for (size_t t = 0; t < nt; ++t) {
+            const float *v0 = &pos[3 * (size_t)idx[3 * t]], *v1 = &pos[3 * (size_t)idx[3 * t + 1]],
+                        *v2 = &pos[3 * (size_t)idx[3 * t + 2]];
+            float m0[3], m1[3], m2[3];
+            for (int c = 0; c < 3; ++c) {
+                m0[c] = 0.5f * (v0[c] + v1[c]);
+                m1[c] = 0.5f * (v1[c] + v2[c]);
+                m2[c] = 0.5f * (v0[c] + v2[c]);
+            }
+            const float *vs[6] = {v0, v1, v2, m0, m1, m2};
+            for (const float *v : vs) p2.insert(p2.end(), v, v + 3);
+            const uint32_t b = (uint32_t)(6 * t);
+            i2.insert(i2.end(), {b, b + 3, b + 5, b + 3, b + 4, b + 5, b + 5, b + 4, b + 2, b + 3, b + 1, b + 4});
+        }
+        pos.swap(p2);
+        idx.swap(i2);
+    }
+    const size_t nv = pos.size() / 3;
+    nrm.resize(pos.size());
+    for (size_t v = 0; v < nv; ++v) {
+        float *p = &pos[3 * v];
+        const float inv = 1.0f / sqrtf((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
+        for (int c = 0; c < 3; ++c) {
+            nrm[3 * v + c] = p[c] * inv;
+            p[c] = radius * nrm[3 * v + c];
+        }
+    }
+}
+
 lt_status read_lmf(const std::string &path, uint8_t *vpp, std::vector<float> &pos, std::vector<uint32_t> &idx,
                    std::vector<float> &nrm, std::string *err) {
     std::vector<char> buf;
@@ -336,21 +413,45 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
         for (const Json &p : prims->arr) {
             const Json *type = p.get("type");
             const std::string pname = p.get("name") ? p.get("name")->str : "";
-            if (!type || type->str != "lmf") {
-                *err = "primitive " + pname + ": only lmf primitives are supported";
-                return LT_ERR_UNSUPPORTED;
-            }
-            const Json *fp = p.get("file_path");
-            if (!fp) { *err = "lmf primitive needs file_path"; return LT_ERR_PARSE; }
-            std::string file = fp->str;
-            if (file.empty() || file[0] != '/') file = dir + "/" + file;
-            uint8_t vpp = 0;
             std::vector<float> pos, nrm;
             std::vector<uint32_t> idx;
-            lt_status rs = read_lmf(file, &vpp, pos, idx, nrm, err);
-            if (rs != LT_OK) return rs;
-            if (vpp != 3) {
-                *err = file + ": only triangle LMF files are supported";
+            if (type && type->str == "lmf") {
+                const Json *fp = p.get("file_path");
+                if (!fp) { *err = "lmf primitive needs file_path"; return LT_ERR_PARSE; }
+                std::string file = fp->str;
+                if (file.empty() || file[0] != '/') file = dir + "/" + file;
+                uint8_t vpp = 0;
+                lt_status rs = read_lmf(file, &vpp, pos, idx, nrm, err);
+                if (rs != LT_OK) return rs;
+                if (vpp != 3) {
+                    *err = file + ": only triangle LMF files are supported";
+                    return LT_ERR_UNSUPPORTED;
+                }
+            } else if (type && type->str == "grid") {
+                float width = 0.0f, depth = 0.0f, n = 0.0f, m = 0.0f;
+                if (!num(p.get("width"), &width) || !num(p.get("depth"), &depth) || !num(p.get("n"), &n) ||
+                    !num(p.get("m"), &m)) {
+                    *err = "grid primitive " + pname + " needs width, depth, n, m";
+                    return LT_ERR_PARSE;
+                }
+                if (n < 2.0f || m < 2.0f || n > 65536.0f || m > 65536.0f) {
+                    *err = "grid primitive " + pname + ": n and m must be 2..65536";
+                    return LT_ERR_INVALID;
+                }
+                make_grid(width, depth, (uint32_t)m, (uint32_t)n, pos, nrm, idx);
+            } else if (type && type->str == "geosphere") {
+                float radius = 0.0f, n = 0.0f;
+                if (!num(p.get("radius"), &radius) || !num(p.get("n"), &n)) {
+                    *err = "geosphere primitive " + pname + " needs radius and n";
+                    return LT_ERR_PARSE;
+                }
+                if (n < 0.0f || n > 10.0f) {
+                    *err = "geosphere primitive " + pname + ": n (subdivisions) must be 0..10";
+                    return LT_ERR_INVALID;
+                }
+                make_geosphere(radius, (uint32_t)n, pos, nrm, idx);
+            } else {
+                *err = "primitive " + pname + ": unknown type (lmf, grid and geosphere are supported)";
                 return LT_ERR_UNSUPPORTED;
             }
             const size_t nv = pos.size() / 3;

@@ -644,10 +644,10 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
 }
 
 // One iteration of the bounce loop of Integrator::RenderPixel (integrator.cpp:115-243).
-// Occupancy hint: at most 64 registers (1024 threads per SM), so that more
-// warps hide the latency of the scattered normal / material loads.
+// Register budget: 768 threads per SM (at most 85 registers), measured faster
+// than 1024 threads with spills and than 512 threads.
 template <class Src>
-__global__ void __launch_bounds__(256, 4) k_shade(Src src, Wavefront W, int cur) {
+__global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur) {
     const uint32_t n = W.counters->count[cur];
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;

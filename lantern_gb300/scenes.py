@@ -211,6 +211,7 @@ class Scene:
     background: tuple = (0.0, 0.0, 0.0)
     render: dict = field(default_factory=dict)
     name: str = "scene"
+    procedural: List[dict] = field(default_factory=list)  # "grid" / "geosphere" primitive entries
 
     @property
     def num_triangles(self) -> int:
@@ -227,6 +228,7 @@ class Scene:
             if m.emission is not None:
                 p["emission"] = m.emission
             prims.append(p)
+        prims += [dict(p) for p in self.procedural]
         d = {"background_color": list(self.background), "camera": cam,
              "bsdfs": self.bsdfs, "materials": self.materials, "primitives": prims}
         if self.media:
@@ -484,6 +486,36 @@ def batch_scenes(count: int = 64, seed: int = 5, max_depth: int = 10, rr_depth: 
         _ground_and_light(sc)
         scenes.append(sc)
     return scenes
+
+
+def _translate(x, y, z):
+    return [1.0, 0.0, 0.0, x, 0.0, 1.0, 0.0, y, 0.0, 0.0, 1.0, z, 0.0, 0.0, 0.0, 1.0]
+
+
+def procedural_scene(width=64, height=64, spp=4, max_depth=8, rr_depth=3, name="procedural") -> Scene:
+    """The reference's generated primitives (scene.cpp:408-426): a ``grid``
+    floor (20 x 20, 11 x 11 vertices), a Lambert ``geosphere`` (radius 0.8,
+    3 subdivisions) and a glass one (radius 0.6, 2 subdivisions) placed by
+    transforms, under the LMF area light of the other scenes."""
+    sc = Scene(width, height,
+               camera={"phi": 1.1, "theta": 0.3, "radius": 6.0, "fov": 0.785398, "target": [0.0, 0.5, 0.0]},
+               render={"spp": spp, "max_depth": max_depth, "rr_depth": rr_depth}, name=name)
+    sc.bsdfs += [_lambert("floor", (0.6, 0.6, 0.55)), _lambert("red", (0.8, 0.25, 0.2)),
+                 {"name": "glass", "type": "ideal_specular_dielectric",
+                  "albedo": {"type": "constant", "value": [1.0, 1.0, 1.0]}, "ior": 1.5},
+                 _lambert("light", (0.0, 0.0, 0.0))]
+    for m in ("floor", "red", "glass", "light"):
+        sc.materials.append({"name": m, "bsdf": m})
+    sc.procedural += [
+        {"name": "floor", "type": "grid", "width": 20.0, "depth": 20.0, "n": 11, "m": 11, "material": "floor"},
+        {"name": "ball", "type": "geosphere", "radius": 0.8, "n": 3, "material": "red",
+         "transform": _translate(-1.0, 0.8, 0.0)},
+        {"name": "gem", "type": "geosphere", "radius": 0.6, "n": 2, "material": "glass",
+         "transform": _translate(1.2, 0.6, 0.5)}]
+    p, n, i = quad((0.0, 5.0, 0.0), 1.0, 1.0, -1.0)
+    sc.meshes.append(Mesh("light", p, n, i, "light",
+                          emission={"color": [1.0, 1.0, 1.0], "radiant_power": float(15.0 * np.pi * 4.0)}))
+    return sc
 
 
 def tiny_scene(width=32, height=32, spp=4, max_depth=8, rr_depth=3, name="tiny") -> Scene:

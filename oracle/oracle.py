@@ -192,6 +192,50 @@ def apply_transform(pos: np.ndarray, t: list) -> np.ndarray:
     return out
 
 
+def grid_mesh(width: float, depth: float, m: int, n: int):
+    """CreateGrid (geometry_generator.cpp:515-566) in float32: m rows of n
+    vertices, row i at z = -(depth/2 - i*dz), normals +y, two triangles per cell."""
+    f32 = np.float32
+    half_w, half_d = f32(0.5) * f32(width), f32(0.5) * f32(depth)
+    dx, dz = f32(width) / f32(n - 1), f32(depth) / f32(m - 1)
+    z = half_d - np.arange(m, dtype=f32) * dz
+    x = -half_w + np.arange(n, dtype=f32) * dx
+    pos = np.zeros((m, n, 3), f32)
+    pos[:, :, 0] = x[None, :]
+    pos[:, :, 2] = -z[:, None]
+    nrm = np.zeros((m * n, 3), f32)
+    nrm[:, 1] = 1.0
+    i, j = np.meshgrid(np.arange(m - 1, dtype=np.uint32), np.arange(n - 1, dtype=np.uint32), indexing="ij")
+    a = (i * n + j).reshape(-1)
+    b = ((i + 1) * n + j).reshape(-1)
+    idx = np.stack([a, a + 1, b, b, a + 1, b + 1], axis=1).reshape(-1).astype(np.uint32)
+    return pos.reshape(-1, 3), nrm, idx
+
+
+def geosphere_mesh(radius: float, subdivisions: int):
+    """CreateGeosphere with Subdivide (geometry_generator.cpp:214-356) in
+    float32: icosahedron, each subdivision four triangles per triangle with six
+    fresh vertices, then n = v * (1 / sqrt(dot(v, v))), position = radius * n."""
+    f32 = np.float32
+    X, Z = f32(0.525731), f32(0.850651)
+    pos = np.array([[-X, 0, -Z], [X, 0, -Z], [-X, 0, Z], [X, 0, Z], [0, Z, -X], [0, Z, X], [0, -Z, -X],
+                    [0, -Z, X], [Z, X, 0], [-Z, X, 0], [Z, -X, 0], [-Z, -X, 0]], dtype=f32)
+    tri = np.array([1, 4, 0, 4, 9, 0, 4, 5, 9, 8, 5, 4, 1, 8, 4, 1, 10, 8, 10, 3, 8, 8, 3, 5, 3, 2, 5, 3, 7, 2,
+                    3, 10, 7, 10, 6, 7, 6, 11, 7, 6, 0, 11, 6, 1, 0, 10, 1, 6, 11, 0, 9, 2, 11, 9, 5, 2, 9, 11,
+                    2, 7], dtype=np.uint32).reshape(-1, 3)
+    half = f32(0.5)
+    for _ in range(subdivisions):
+        v0, v1, v2 = pos[tri[:, 0]], pos[tri[:, 1]], pos[tri[:, 2]]
+        m0, m1, m2 = half * (v0 + v1), half * (v1 + v2), half * (v0 + v2)
+        pos = np.stack([v0, v1, v2, m0, m1, m2], axis=1).reshape(-1, 3)
+        b = (6 * np.arange(tri.shape[0], dtype=np.uint32))[:, None]
+        tri = (b + np.array([0, 3, 5, 3, 4, 5, 5, 4, 2, 3, 1, 4], dtype=np.uint32)[None, :]).reshape(-1, 3)
+    d = (pos[:, 0] * pos[:, 0] + pos[:, 1] * pos[:, 1]) + pos[:, 2] * pos[:, 2]
+    inv = f32(1) / np.sqrt(d)
+    nrm = (pos * inv[:, None]).astype(f32)
+    return (f32(radius) * nrm).astype(f32), nrm, tri.reshape(-1).astype(np.uint32)
+
+
 class OracleScene:
     """A scene loaded into the oracle."""
 
@@ -235,16 +279,22 @@ class OracleScene:
         self._keep = []
         base = os.path.dirname(self.path)
         for p in j.get("primitives", []):
-            if p["type"] != "lmf":
-                raise NotImplementedError("oracle scenes use LMF primitives")
-            lmf = read_lmf(os.path.join(base, p["file_path"]))
-            if lmf["vpp"] != 3:
-                raise NotImplementedError("triangle LMF only")
-            pos = np.ascontiguousarray(lmf["positions"], dtype=f32)
+            if p["type"] == "lmf":
+                lmf = read_lmf(os.path.join(base, p["file_path"]))
+                if lmf["vpp"] != 3:
+                    raise NotImplementedError("triangle LMF only")
+                pos, nrm, idx = lmf["positions"], lmf["normals"], lmf["indices"]
+            elif p["type"] == "grid":
+                pos, nrm, idx = grid_mesh(p["width"], p["depth"], int(p["m"]), int(p["n"]))
+            elif p["type"] == "geosphere":
+                pos, nrm, idx = geosphere_mesh(p["radius"], int(p["n"]))
+            else:
+                raise NotImplementedError(f"primitive type {p['type']}")
+            pos = np.ascontiguousarray(pos, dtype=f32)
             if "transform" in p:
-                pos = apply_transform(pos, p["transform"])
-            nrm = None if lmf["normals"] is None else np.ascontiguousarray(lmf["normals"], dtype=f32)
-            idx = np.ascontiguousarray(lmf["indices"], dtype=np.uint32)
+                pos = apply_transform(pos, p["transform"])  # normals stay as generated (scene.cpp:481-482)
+            nrm = None if nrm is None else np.ascontiguousarray(nrm, dtype=f32)
+            idx = np.ascontiguousarray(idx, dtype=np.uint32)
             em = None
             power = f32(0)
             if "emission" in p:

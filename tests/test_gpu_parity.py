@@ -7,6 +7,8 @@
   colours agree pixel by pixel except where a transcendental function's last
   bit (CUDA vs glibc sinf/cosf/logf/expf) sends a path elsewhere.
 """
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -26,12 +28,20 @@ def ctx():
     c.close()
 
 
+def _positions(path, p):
+    """World-space vertices of one scene-JSON primitive (as the oracle builds them)."""
+    if p["type"] == "lmf":
+        pos = O.read_lmf(os.path.join(os.path.dirname(path), p["file_path"]))["positions"]
+    elif p["type"] == "grid":
+        pos = O.grid_mesh(p["width"], p["depth"], int(p["m"]), int(p["n"]))[0]
+    else:
+        pos = O.geosphere_mesh(p["radius"], int(p["n"]))[0]
+    return O.apply_transform(pos, p["transform"]) if "transform" in p else pos
+
+
 def _scene_rays(path, n, seed):
     orc = O.OracleScene(path)
-    pos = []
-    for p in orc.json["primitives"]:
-        pos.append(O.read_lmf(__import__("os").path.join(__import__("os").path.dirname(path), p["file_path"]))["positions"])
-    allp = np.concatenate(pos)
+    allp = np.concatenate([_positions(path, p) for p in orc.json["primitives"]])
     lo, hi = allp.min(0), allp.max(0)
     c, e = (lo + hi) / 2, (hi - lo) / 2
     rays = S.random_rays(n, c - 0.6 * e, c + 0.6 * e, seed=seed)
@@ -66,6 +76,7 @@ def width(request, ctx):
     lambda: S.nine_spheres(width=64, height=64, name="isect_nine"),
     lambda: S.displaced_icosphere_scene(width=64, height=64, levels=5, name="isect_ico5"),
     lambda: S.tiny_scene(name="isect_tiny"),
+    lambda: S.procedural_scene(name="isect_procedural"),
 ])
 def test_intersect_matches_oracle(ctx, width, scene_dir, make):
     path = make().write(scene_dir)
@@ -108,6 +119,7 @@ def test_intersect_tnear_tfar_rule(ctx, width, scene_dir):
     (lambda: S.nine_spheres(width=64, height=64, name="paths_nine"), 4, 8),
     (lambda: S.medium_sphere_scene(width=40, height=40, reference_expressible=True, name="paths_med_ref"), 4, 32),
     (lambda: S.medium_sphere_scene(width=40, height=40, name="paths_med_hg"), 4, 32),
+    (lambda: S.procedural_scene(width=48, height=40, name="paths_procedural"), 4, 8),
 ])
 @pytest.mark.parametrize("bvh_width", [2, 8])
 def test_render_matches_oracle_path_by_path(scene_dir, make, spp, depth, bvh_width):

@@ -24,6 +24,7 @@ def _bits(a):
     (lambda: S.medium_sphere_scene(width=32, height=32, reference_expressible=True,
                                    name="medium_ref_32"), 2, 32, 3),
     (lambda: S.tiny_scene(width=24, height=16, name="tiny_24x16"), 2, 1500, 3),
+    (lambda: S.procedural_scene(width=40, height=32, name="procedural_40"), 3, 8, 3),
 ])
 def test_tile_keyed_oracle_matches_reference(reference_available, scene_dir, make, frames, depth, rr):
     if not reference_available:
