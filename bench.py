@@ -36,6 +36,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Msamples/s & Mrays/s on 1 GB300 vs host CPU at matched RMSE; adjoint grads/s"
 SCENES = os.path.join(ROOT, "_scenes")
+# DRAM bytes (read + write) per ray traced by k_trace on the icosphere workload, measured
+# with ncu dram__bytes_{read,write}.sum over every k_trace launch of a 4-spp render
+# (profiles/k_trace_k_shade_icosphere-1.3M.md)
+TRACE_DRAM_BYTES_PER_RAY = 129.1
 
 
 def _peaks():
@@ -255,7 +259,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     total_ms, trace_ms, shade_ms, rays, launches = 0.0, 0.0, 0.0, 0, 0
-    main_rays, conn_traced = 0, 0
+    main_rays, conn_traced, trace_launches = 0, 0, 0
     for _ in range(args.steps):
         flush.fill_(1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -271,6 +275,7 @@ def main():
         main_rays += st.main_rays
         conn_traced += st.light_traversals
         launches += st.kernel_launches
+        trace_launches += st.iterations
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -315,8 +320,13 @@ def main():
             # k_trace traces the path rays and the connection rays that needed a
             # query; both are charged the closest-hit bytes of one ray
             achieved = (main_rays + conn_traced) * bpr / (trace_ms / 1e3) / 1e9
+            traced_per_launch = (main_rays + conn_traced) / max(trace_launches, 1)
             roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_trace",
+                    "frac": round(achieved / peak, 4), "kernel": "k_trace",
+                    # DRAM bytes per launch: ncu-measured bytes per traced ray x rays per launch
+                    "traffic": (round(TRACE_DRAM_BYTES_PER_RAY * traced_per_launch)
+                                if args.workload == "icosphere-1.3M" else None),
+                    "algorithmic_bytes_per_launch": round(bpr * traced_per_launch),
                     "bytes_per_ray": round(bpr, 1), "node_tests_per_ray": round(n_node, 2),
                     "tri_tests_per_ray": round(n_tri, 2), "peak_kind": peak_kind,
                     "rays_traced_per_step": (main_rays + conn_traced) // args.steps,

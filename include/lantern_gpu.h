@@ -66,12 +66,26 @@ enum { LT_BSDF_LAMBERT = 0, LT_BSDF_MIRROR = 1, LT_BSDF_DIELECTRIC = 2 };
  * plus LT_MEDIUM_HG: RGB sigma_s and a Henyey-Greenstein phase (extension). */
 enum { LT_MEDIUM_NON_SCATTERING = 1, LT_MEDIUM_ISOTROPIC = 2, LT_MEDIUM_HG = 3 };
 
+/* Albedo textures (materials/textures): ConstantTexture, UVTexture (albedo =
+ * (u, v, 0) of the hit's texture coordinate) and ImageTexture (nearest texel
+ * at (round(u * width), round((1 - v) * height)), 8-bit value / 256). */
+enum { LT_ALBEDO_CONSTANT = 0, LT_ALBEDO_UV = 1, LT_ALBEDO_IMAGE = 2 };
+
 typedef struct lt_material_desc {
     int32_t bsdf;      /* LT_BSDF_* */
-    float albedo[3];
+    float albedo[3];   /* LT_ALBEDO_CONSTANT */
     float ior;         /* dielectric only */
     int32_t medium;    /* index into lt_scene_desc.media, or -1 */
+    int32_t albedo_kind;  /* LT_ALBEDO_*; 0 = constant */
+    uint32_t image;       /* LT_ALBEDO_IMAGE: index into lt_scene_desc.images */
 } lt_material_desc;
+
+/* An image texture: 8-bit samples, rows from the top, `channels` (1-4) per
+ * texel -- what stbi_load(path, &w, &h, &n, 0) returns (image_cache.cpp:23-31). */
+typedef struct lt_image_desc {
+    const uint8_t *texels;
+    uint32_t width, height, channels;
+} lt_image_desc;
 
 typedef struct lt_medium_desc {
     int32_t type;      /* LT_MEDIUM_* */
@@ -90,6 +104,7 @@ typedef struct lt_mesh_desc {
     int32_t emissive;         /* nonzero: the mesh is an area light */
     float emission_color[3];  /* AreaLight: radiance = color * power / (pi * area) */
     float radiant_power;
+    const float *texcoords;   /* num_vertices * 2, or NULL (the hit's texture coordinate is then (0, 0)) */
 } lt_mesh_desc;
 
 typedef struct lt_camera_desc {
@@ -108,6 +123,8 @@ typedef struct lt_scene_desc {
     uint32_t num_media;
     const lt_mesh_desc *meshes; /* geomID = position in this array */
     uint32_t num_meshes;
+    const lt_image_desc *images;
+    uint32_t num_images;
 } lt_scene_desc;
 
 /* Uploads the scene and builds its BVH; replaces any previous scene.
@@ -124,11 +141,22 @@ enum { LT_BVH_GPU = 0, LT_BVH_HOST = 1 };
 lt_status lt_set_bvh_builder(lt_ctx *ctx, int32_t builder);
 
 /* Scene::LoadSceneFromJSON (scene.h:71): reads a Lantern scene JSON and the
- * LMF files it names (triangle LMF, transform, constant albedo, media,
- * emission), generates its "grid" and "geosphere" primitives as CreateGrid /
- * CreateGeosphere do (geometry_generator.cpp:214-356,515-566; scene.cpp:408-426),
- * then lt_scene_create. */
+ * LMF files it names (triangle LMF with normals and texture coordinates,
+ * transform, constant / uv / image albedo, media, emission), generates its
+ * "grid" and "geosphere" primitives as CreateGrid / CreateGeosphere do
+ * (geometry_generator.cpp:214-356,515-566; scene.cpp:408-426), decodes PNG
+ * image textures (lt_image_load), then lt_scene_create. */
 lt_status lt_scene_load_json(lt_ctx *ctx, const char *path);
+
+/* Decodes a PNG file as the scene loader reads image textures, matching
+ * stbi_load(path, &w, &h, &n, 0): 8-bit samples; grey 1, grey+alpha 2, RGB 3,
+ * RGBA 4 channels (palette -> RGB or RGBA, a tRNS key adds alpha, 16-bit keeps
+ * the high byte); not interlaced. Fills width/height/channels; copies the
+ * texels (width*height*channels bytes) when `texels` is not NULL and
+ * `capacity` is large enough. No context and no GPU: errors are read with
+ * lt_last_error(NULL). */
+lt_status lt_image_load(const char *path, uint8_t *texels, size_t capacity, uint32_t *width, uint32_t *height,
+                        uint32_t *channels);
 
 typedef struct lt_scene_info {
     uint32_t width, height;

@@ -29,7 +29,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-u
              "-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
 
 CU_SOURCES = ["lt_kernels.cu", "lt_bvh_gpu.cu", "lt_noalloc.cu", "lt_resolve.cu"]
-CPP_SOURCES = ["lt_api.cpp", "lt_scene.cpp", "lt_json.cpp", "lt_bvh8.cpp"]
+CPP_SOURCES = ["lt_api.cpp", "lt_scene.cpp", "lt_json.cpp", "lt_bvh8.cpp", "lt_image.cpp"]
 
 
 def _sources():

@@ -309,6 +309,9 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     if ((st = upload(c, h.tri_geom, &d.tri_geom)) != LT_OK) return st;
     if ((st = upload(c, h.tri_vidx, &d.tri_vidx)) != LT_OK) return st;
     if ((st = upload(c, h.vnormal, &d.vnormal)) != LT_OK) return st;
+    if ((st = upload(c, h.vtex, &d.vtex)) != LT_OK) return st;
+    if ((st = upload(c, h.texels, &d.texels)) != LT_OK) return st;
+    if ((st = upload(c, h.images, &d.images)) != LT_OK) return st;
     if ((st = upload(c, h.geoms, &d.geoms)) != LT_OK) return st;
     if ((st = upload(c, h.materials, &d.mats)) != LT_OK) return st;
     if ((st = upload(c, h.media, &d.meds)) != LT_OK) return st;
@@ -1141,4 +1144,20 @@ extern "C" lt_status lt_render_diff_batch(lt_ctx *c, const lt_diff_job *jobs, ui
 
 extern "C" lt_status lt_render_adjoint_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n) {
     return diff_batch(c, jobs, n, true);
+}
+
+// ------------------------------------------------------------------ lt_image_load
+extern "C" lt_status lt_image_load(const char *path, uint8_t *texels, size_t capacity, uint32_t *width,
+                                   uint32_t *height, uint32_t *channels) {
+    if (!path || !width || !height || !channels) return fail(nullptr, LT_ERR_INVALID, "NULL argument");
+    std::vector<uint8_t> data;
+    std::string err;
+    lt_status st = load_png(path, &data, width, height, channels, &err);
+    if (st != LT_OK) return fail(nullptr, st, "%s", err.c_str());
+    if (texels) {
+        if (capacity < data.size())
+            return fail(nullptr, LT_ERR_INVALID, "%s: needs %zu bytes, buffer holds %zu", path, data.size(), capacity);
+        memcpy(texels, data.data(), data.size());
+    }
+    return LT_OK;
 }

@@ -17,6 +17,9 @@ struct DevScene {
     const uint32_t *tri_geom;   // per global triangle
     const uint32_t *tri_vidx;   // 3 per global triangle
     const float *vnormal;       // 3 per vertex
+    const float *vtex;          // 2 per vertex
+    const uint8_t *texels;      // image textures
+    const ImageInfo *images;
     const GeomInfo *geoms;
     const MaterialInfo *mats;
     const MediumInfo *meds;

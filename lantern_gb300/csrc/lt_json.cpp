@@ -171,11 +171,13 @@ bool float3(const Json *j, float out[3]) {
 // CreateGrid (geometry_generator.cpp:515-566): m rows of n vertices in the xz
 // plane, row i at z = -(depth/2 - i * dz), normals +y, two triangles per cell.
 void make_grid(float width, float depth, uint32_t m, uint32_t n, std::vector<float> &pos, std::vector<float> &nrm,
-               std::vector<uint32_t> &idx) {
+               std::vector<float> &tex, std::vector<uint32_t> &idx) {
     const float half_w = 0.5f * width, half_d = 0.5f * depth;
     const float dx = width / (float)(n - 1), dz = depth / (float)(m - 1);
+    const float du = 1.0f / (float)(n - 1), dv = 1.0f / (float)(m - 1);
     pos.resize(3 * (size_t)m * n);
     nrm.resize(3 * (size_t)m * n);
+    tex.resize(2 * (size_t)m * n);
     for (uint32_t i = 0; i < m; ++i) {
         const float z = half_d - (float)i * dz;
         for (uint32_t j = 0; j < n; ++j) {
@@ -183,6 +185,8 @@ void make_grid(float width, float depth, uint32_t m, uint32_t n, std::vector<flo
             float *p = &pos[3 * ((size_t)i * n + j)], *q = &nrm[3 * ((size_t)i * n + j)];
             p[0] = x; p[1] = 0.0f; p[2] = -z;
             q[0] = 0.0f; q[1] = 1.0f; q[2] = 0.0f;
+            tex[2 * ((size_t)i * n + j)] = (float)j * du;  // stretched over the grid
+            tex[2 * ((size_t)i * n + j) + 1] = (float)i * dv;
         }
     }
     idx.clear();
@@ -245,7 +249,7 @@ void make_geosphere(float radius, uint32_t subdivisions, std::vector<float> &pos
 }
 
 lt_status read_lmf(const std::string &path, uint8_t *vpp, std::vector<float> &pos, std::vector<uint32_t> &idx,
-                   std::vector<float> &nrm, std::string *err) {
+                   std::vector<float> &nrm, std::vector<float> &tex, std::string *err) {
     std::vector<char> buf;
     if (!read_file(path, buf)) {
         *err = "cannot read LMF file " + path;
@@ -281,7 +285,21 @@ lt_status read_lmf(const std::string &path, uint8_t *vpp, std::vector<float> &po
         nrm.resize(nn);
         if (!take(nrm.data(), nn * 4)) { *err = path + ": truncated normals"; return LT_ERR_PARSE; }
     }
+    tex.clear();
+    if (flags & 2u) {
+        uint64_t nt = 0;
+        if (!take(&nt, 8) || nt > buf.size() / 4) { *err = path + ": truncated texcoord count"; return LT_ERR_PARSE; }
+        tex.resize(nt);
+        if (!take(tex.data(), nt * 4)) { *err = path + ": truncated texcoords"; return LT_ERR_PARSE; }
+    }
     return LT_OK;
+}
+
+bool file_exists(const std::string &path) {
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    fclose(f);
+    return true;
 }
 
 }  // namespace
@@ -330,6 +348,7 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
     if (const Json *t = cam->get("target")) float3(t, c.target);
 
     std::map<std::string, int> medium_ix, material_ix;
+    std::map<std::string, uint32_t> image_ix;
     if (const Json *media = root.get("media")) {
         for (const Json &m : media->arr) {
             const Json *name = m.get("name"), *type = m.get("type");
@@ -393,13 +412,39 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
                 *err = "unknown bsdf type " + type;
                 return LT_ERR_PARSE;
             }
+            // albedo texture (scene.cpp:266-318): constant, uv or image
             const Json *alb = b.get("albedo");
             const Json *at = alb ? alb->get("type") : nullptr;
-            if (!at || at->str != "constant") {
-                *err = "bsdf " + bn->str + ": only constant albedo textures are supported";
+            const std::string akind = at ? at->str : "";
+            if (akind == "constant") {
+                md.albedo_kind = LT_ALBEDO_CONSTANT;
+                if (!float3(alb->get("value"), md.albedo)) { *err = "constant albedo needs value"; return LT_ERR_PARSE; }
+            } else if (akind == "uv") {
+                md.albedo_kind = LT_ALBEDO_UV;
+            } else if (akind == "image") {
+                const Json *ip = alb->get("file_path");
+                if (!ip || ip->str.empty()) { *err = "image albedo needs file_path"; return LT_ERR_PARSE; }
+                // as given (the reference's image cache opens it from the working
+                // directory), else next to the scene file
+                std::string ipath = ip->str;
+                if (ipath[0] != '/' && !file_exists(ipath)) ipath = dir + "/" + ipath;
+                auto found = image_ix.find(ipath);
+                if (found == image_ix.end()) {
+                    lt_image_desc id;
+                    std::vector<uint8_t> texels;
+                    lt_status rs = load_png(ipath, &texels, &id.width, &id.height, &id.channels, err);
+                    if (rs != LT_OK) return rs;
+                    st->bytes.push_back(std::move(texels));
+                    id.texels = st->bytes.back().data();
+                    found = image_ix.emplace(ipath, (uint32_t)st->images.size()).first;
+                    st->images.push_back(id);
+                }
+                md.albedo_kind = LT_ALBEDO_IMAGE;
+                md.image = found->second;
+            } else {
+                *err = "bsdf " + bn->str + ": unknown albedo type " + akind;
                 return LT_ERR_UNSUPPORTED;
             }
-            if (!float3(alb->get("value"), md.albedo)) { *err = "constant albedo needs value"; return LT_ERR_PARSE; }
             if (const Json *mn = m.get("medium")) {
                 auto mi = medium_ix.find(mn->str);
                 if (mi == medium_ix.end()) continue;  // scene.cpp:354-357 skips it
@@ -413,7 +458,7 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
         for (const Json &p : prims->arr) {
             const Json *type = p.get("type");
             const std::string pname = p.get("name") ? p.get("name")->str : "";
-            std::vector<float> pos, nrm;
+            std::vector<float> pos, nrm, tex;
             std::vector<uint32_t> idx;
             if (type && type->str == "lmf") {
                 const Json *fp = p.get("file_path");
@@ -421,7 +466,7 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
                 std::string file = fp->str;
                 if (file.empty() || file[0] != '/') file = dir + "/" + file;
                 uint8_t vpp = 0;
-                lt_status rs = read_lmf(file, &vpp, pos, idx, nrm, err);
+                lt_status rs = read_lmf(file, &vpp, pos, idx, nrm, tex, err);
                 if (rs != LT_OK) return rs;
                 if (vpp != 3) {
                     *err = file + ": only triangle LMF files are supported";
@@ -438,7 +483,7 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
                     *err = "grid primitive " + pname + ": n and m must be 2..65536";
                     return LT_ERR_INVALID;
                 }
-                make_grid(width, depth, (uint32_t)m, (uint32_t)n, pos, nrm, idx);
+                make_grid(width, depth, (uint32_t)m, (uint32_t)n, pos, nrm, tex, idx);
             } else if (type && type->str == "geosphere") {
                 float radius = 0.0f, n = 0.0f;
                 if (!num(p.get("radius"), &radius) || !num(p.get("n"), &n)) {
@@ -491,6 +536,10 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
                 st->floats.push_back(std::move(nrm));
                 md.normals = st->floats.back().data();
             }
+            if (tex.size() == nv * 2 && nv) {
+                st->floats.push_back(std::move(tex));
+                md.texcoords = st->floats.back().data();
+            }
             st->uints.push_back(std::move(idx));
             md.indices = st->uints.back().data();
             st->meshes.push_back(md);
@@ -502,6 +551,8 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
     desc->num_media = (uint32_t)st->media.size();
     desc->meshes = st->meshes.data();
     desc->num_meshes = (uint32_t)st->meshes.size();
+    desc->images = st->images.data();
+    desc->num_images = (uint32_t)st->images.size();
     return LT_OK;
 }
 

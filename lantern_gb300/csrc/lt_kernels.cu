@@ -383,6 +383,41 @@ __device__ __forceinline__ v3 interp_normal(const DevScene &S, uint32_t prim, fl
     return (n0 * w + n1 * u) + n2 * v;
 }
 
+// Albedo texture at a hit (BSDF::Eval's m_albedoTexture->Sample): constant;
+// UVTexture (uv_texture.h:16-18): (u, v, 0) of the interpolated texture
+// coordinate; ImageTexture (image_texture.h:32-39, image_cache.cpp:33-62): v
+// flipped, nearest texel at (round(u * W), round(v * H)), 8-bit value / 256,
+// grey -> (g, g, g), two channels -> (r, g, 0). The texel index is
+// (y * W + x) * channels as the reference computes it (x == W reads the next
+// row's first texel), kept inside the image. A mesh without texture
+// coordinates samples (0, 0) (integrator.cpp:184-188).
+__device__ __forceinline__ v3 material_albedo(const DevScene &S, const MaterialInfo &m, const GeomInfo &G,
+                                              uint32_t prim, float u, float v) {
+    if (m.tex == kAlbedoConstant) return mk(m.albedo[0], m.albedo[1], m.albedo[2]);
+    float tu = 0.0f, tv = 0.0f;
+    if (G.has_texcoords) {
+        const uint32_t i0 = __ldg(S.tri_vidx + 3 * prim), i1 = __ldg(S.tri_vidx + 3 * prim + 1),
+                       i2 = __ldg(S.tri_vidx + 3 * prim + 2);
+        const float w = 1.0f - u - v;
+        tu = (__ldg(S.vtex + 2 * i0) * w + __ldg(S.vtex + 2 * i1) * u) + __ldg(S.vtex + 2 * i2) * v;
+        tv = (__ldg(S.vtex + 2 * i0 + 1) * w + __ldg(S.vtex + 2 * i1 + 1) * u) + __ldg(S.vtex + 2 * i2 + 1) * v;
+    }
+    if (m.tex == kAlbedoUV) return mk(tu, tv, 0.0f);
+    const ImageInfo I = S.images[m.tex];
+    tv = 1.0f - tv;
+    const float fx = fminf(fmaxf(roundf(tu * (float)I.width), 0.0f), 65536.0f);
+    const float fy = fminf(fmaxf(roundf(tv * (float)I.height), 0.0f), 65536.0f);
+    uint64_t texel = (uint64_t)fy * I.width + (uint64_t)fx;
+    const uint64_t last = (uint64_t)I.width * I.height - 1;
+    if (texel > last) texel = last;
+    const uint8_t *t = S.texels + I.offset + texel * I.channels;
+    const float r = (float)__ldg(t) / 256.0f;
+    if (I.channels == 1) return mk(r, r, r);
+    const float g = (float)__ldg(t + 1) / 256.0f;
+    if (I.channels == 2) return mk(r, g, 0.0f);
+    return mk(r, g, (float)__ldg(t + 2) / 256.0f);
+}
+
 // Distance to the closest of the light's own triangles along (org, dir), t in
 // (0.001, inf): 0 when the ray misses the light, -1 when the light has more
 // than kLightBrute triangles and was not tested. `out` (optional) gets the hit.
@@ -537,8 +572,7 @@ __device__ __forceinline__ void bsdf_sample(const MaterialInfo &m, Inter &it, Pc
     }
 }
 
-__device__ __forceinline__ v3 bsdf_eval(const MaterialInfo &m, const Inter &it) {
-    v3 alb = mk(m.albedo[0], m.albedo[1], m.albedo[2]);
+__device__ __forceinline__ v3 bsdf_eval(const MaterialInfo &m, v3 alb, const Inter &it) {
     if (m.bsdf == LT_BSDF_LAMBERT) return (alb * kInvPi) * dot(it.wi, it.N);
     return alb;
 }
@@ -725,6 +759,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                     Inter it;
                     it.P = origin + direction * t;
                     it.N = G.has_normals ? normalize(interp_normal(S, prim, hv.y, hv.z)) : normalize(mk(0, 0, 0));
+                    const v3 alb = material_albedo(S, m, G, prim, hv.y, hv.z);
                     it.wo = -direction;
                     it.ioro = 0.0f;
                     it.iori = p.iori;
@@ -757,7 +792,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                             c.wi = ldir;
                             if (dot(ldir, c.N) > 0.0f) {
                                 n_ref_rays++;  // the reference traces this ray (area_light.cpp:58)
-                                v3 f = bsdf_eval(m, c);
+                                v3 f = bsdf_eval(m, alb, c);
                                 float spdf = bsdf_pdf(m, c);
                                 if (!is_black(Le) && spdf != 0.0f && !is_black(f)) {
                                     // a ray that misses the light's own triangles cannot contribute
@@ -773,7 +808,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                             }
                         }
                         bsdf_sample(m, c, p.rng);
-                        v3 f = bsdf_eval(m, c);
+                        v3 f = bsdf_eval(m, alb, c);
                         float spdf = bsdf_pdf(m, c);
                         // AreaLight::PdfLi horizon test (area_light.cpp:76-78)
                         if (spdf != 0.0f && !is_black(f) && dot(c.wi, c.N) > 0.0f) {
@@ -791,7 +826,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                     // main path BSDF sample (integrator.cpp:199-209)
                     bsdf_sample(m, it, p.rng);
                     float pdf = bsdf_pdf(m, it);
-                    p.T = (p.T * bsdf_eval(m, it)) / pdf;
+                    p.T = (p.T * bsdf_eval(m, alb, it)) / pdf;
                     if (it.lobe == kLobeSTrans) {
                         it.iori = it.ioro;
                         p.medium = m.medium;

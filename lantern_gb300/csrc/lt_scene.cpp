@@ -80,7 +80,39 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
         mi.medium = m.medium;
         mi.ior = m.ior;
         for (int c = 0; c < 3; ++c) mi.albedo[c] = m.albedo[c];
+        if (m.albedo_kind == LT_ALBEDO_CONSTANT) {
+            mi.tex = kAlbedoConstant;
+        } else if (m.albedo_kind == LT_ALBEDO_UV) {
+            mi.tex = kAlbedoUV;
+        } else if (m.albedo_kind == LT_ALBEDO_IMAGE) {
+            if (m.image >= d->num_images) {
+                *err = "material image index out of range";
+                return LT_ERR_INVALID;
+            }
+            mi.tex = (int32_t)m.image;
+        } else {
+            *err = "unknown albedo kind";
+            return LT_ERR_INVALID;
+        }
         s->materials.push_back(mi);
+    }
+    s->images.clear();
+    s->texels.clear();
+    for (uint32_t i = 0; i < d->num_images; ++i) {
+        const lt_image_desc &im = d->images[i];
+        if (!im.texels || im.width == 0 || im.height == 0 || im.channels < 1 || im.channels > 4 ||
+            im.width > 65536 || im.height > 65536) {
+            *err = "image " + std::to_string(i) + ": texels, size or channel count invalid";
+            return LT_ERR_INVALID;
+        }
+        ImageInfo ii;
+        memset(&ii, 0, sizeof ii);
+        ii.offset = s->texels.size();
+        ii.width = im.width;
+        ii.height = im.height;
+        ii.channels = im.channels;
+        s->texels.insert(s->texels.end(), im.texels, im.texels + (size_t)im.width * im.height * im.channels);
+        s->images.push_back(ii);
     }
 
     size_t ntri = 0, nvert = 0;
@@ -99,6 +131,7 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
     s->tri_geom.assign(ntri, 0);
     s->tri_vidx.assign(ntri * 3, 0);
     s->vnormal.assign(nvert * 3, 0.0f);
+    s->vtex.assign(nvert * 2, 0.0f);
     size_t t0 = 0, vbase = 0;
     for (uint32_t g = 0; g < d->num_meshes; ++g) {
         const lt_mesh_desc &m = d->meshes[g];
@@ -114,6 +147,7 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
         gi.material = m.material;
         gi.light = -1;
         gi.has_normals = m.normals != nullptr;
+        gi.has_texcoords = m.texcoords != nullptr;
         gi.first_tri = (uint32_t)t0;
         float area = 0.0f;
         for (uint32_t t = 0; t < m.num_triangles; ++t) {
@@ -138,6 +172,8 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
         }
         if (m.normals)
             memcpy(&s->vnormal[3 * vbase], m.normals, (size_t)m.num_vertices * 3 * sizeof(float));
+        if (m.texcoords)
+            memcpy(&s->vtex[2 * vbase], m.texcoords, (size_t)m.num_vertices * 2 * sizeof(float));
         if (m.emissive) {
             LightInfo li;
             memset(&li, 0, sizeof li);

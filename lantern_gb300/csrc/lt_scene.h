@@ -16,16 +16,24 @@ namespace lt {
 struct alignas(16) GeomInfo {
     int32_t material;
     int32_t light;        // index into lights, or -1
-    int32_t has_normals;
+    int16_t has_normals;
+    int16_t has_texcoords;
     uint32_t first_tri;   // global index of the mesh's first triangle
 };
+
+constexpr int32_t kAlbedoConstant = -1, kAlbedoUV = -2;  // MaterialInfo::tex; >= 0: image index
 
 struct alignas(16) MaterialInfo {
     int32_t bsdf;
     int32_t medium;
     float ior;
-    float pad;
+    int32_t tex;          // kAlbedoConstant, kAlbedoUV or an index into the scene's images
     float albedo[4];
+};
+
+struct alignas(16) ImageInfo {
+    uint64_t offset;      // first byte in the scene's texel array
+    uint32_t width, height, channels, pad;
 };
 
 struct alignas(16) MediumInfo {
@@ -96,6 +104,9 @@ struct HostScene {
     std::vector<uint32_t> tri_geom;
     std::vector<uint32_t> tri_vidx;  // 3 global vertex indices per triangle
     std::vector<float> vnormal;      // 3 floats per global vertex
+    std::vector<float> vtex;         // 2 floats per global vertex (0 where a mesh has none)
+    std::vector<uint8_t> texels;     // all image textures, 8-bit samples
+    std::vector<ImageInfo> images;
     // BVH
     std::vector<BvhNode> nodes;
     std::vector<float> leaf_tris;    // 12 floats per triangle in leaf order: v0,prim | e1,0 | e2,0
@@ -120,10 +131,18 @@ void build_bvh(HostScene *s);
 uint32_t build_bvh8(const std::vector<BvhNode> &nodes, const std::vector<float> &leaf_tris,
                     std::vector<Bvh8Node> *out, std::vector<float> *tris8);
 
+// PNG decoding as stbi_load(path, &w, &h, &n, 0) returns it (lt_image.cpp).
+lt_status decode_png(const uint8_t *file, size_t size, std::vector<uint8_t> *data, uint32_t *w, uint32_t *h,
+                     uint32_t *n, std::string *err);
+lt_status load_png(const std::string &path, std::vector<uint8_t> *data, uint32_t *w, uint32_t *h, uint32_t *n,
+                   std::string *err);
+
 // Scene::ParseJSON subset (scene.cpp:154-446) into a description whose
 // arrays live in `storage`.
 struct JsonSceneStorage {
     std::vector<lt_material_desc> materials;
+    std::vector<lt_image_desc> images;
+    std::vector<std::vector<uint8_t>> bytes;
     std::vector<lt_medium_desc> media;
     std::vector<lt_mesh_desc> meshes;
     std::vector<std::vector<float>> floats;

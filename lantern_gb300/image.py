@@ -40,23 +40,25 @@ def _chunk(tag: bytes, data: bytes) -> bytes:
     return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
 
 
-def write_png(path: str, rgba8) -> None:
-    """8-bit RGBA (H, W, 4) array or tensor to a PNG file (colour type 6)."""
-    a = rgba8.cpu().numpy() if isinstance(rgba8, torch.Tensor) else np.asarray(rgba8)
+def write_png(path: str, img8) -> None:
+    """8-bit (H, W, C) array or tensor, C = 1 (grey), 2 (grey + alpha), 3 (RGB)
+    or 4 (RGBA), to a PNG file."""
+    a = img8.cpu().numpy() if isinstance(img8, torch.Tensor) else np.asarray(img8)
     a = np.ascontiguousarray(a, dtype=np.uint8)
     h, w, c = a.shape
-    if c != 4:
-        raise ValueError("write_png wants 4 channels")
-    raw = np.concatenate([np.zeros((h, 1), np.uint8), a.reshape(h, w * 4)], axis=1).tobytes()
+    if c not in (1, 2, 3, 4):
+        raise ValueError("write_png wants 1 to 4 channels")
+    ctype = {1: 0, 2: 4, 3: 2, 4: 6}[c]
+    raw = np.concatenate([np.zeros((h, 1), np.uint8), a.reshape(h, w * c)], axis=1).tobytes()
     with open(path, "wb") as fh:
         fh.write(b"\x89PNG\r\n\x1a\n")
-        fh.write(_chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        fh.write(_chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, ctype, 0, 0, 0)))
         fh.write(_chunk(b"IDAT", zlib.compress(raw, 6)))
         fh.write(_chunk(b"IEND", b""))
 
 
 def read_png(path: str) -> np.ndarray:
-    """Reader for the files write_png makes (8-bit RGBA, filter 0 rows)."""
+    """Reader for the RGBA files write_png makes (8-bit, filter 0 rows)."""
     data = open(path, "rb").read()
     if data[:8] != b"\x89PNG\r\n\x1a\n":
         raise ValueError("not a PNG file")

@@ -25,7 +25,7 @@ SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error",
            "lt_scene_create", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
-           "lt_render_diff_batch", "lt_render_adjoint_batch"]
+           "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load"]
 BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 MAX_BATCH = 2048  # LT_MAX_BATCH
@@ -38,8 +38,16 @@ class LanternError(RuntimeError):
         self.status = status
 
 
+ALBEDO_CONSTANT, ALBEDO_UV, ALBEDO_IMAGE = 0, 1, 2
+
+
 class MaterialDesc(C.Structure):
-    _fields_ = [("bsdf", C.c_int32), ("albedo", C.c_float * 3), ("ior", C.c_float), ("medium", C.c_int32)]
+    _fields_ = [("bsdf", C.c_int32), ("albedo", C.c_float * 3), ("ior", C.c_float), ("medium", C.c_int32),
+                ("albedo_kind", C.c_int32), ("image", C.c_uint32)]
+
+
+class ImageDesc(C.Structure):
+    _fields_ = [("texels", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("channels", C.c_uint32)]
 
 
 class MediumDesc(C.Structure):
@@ -50,7 +58,8 @@ class MeshDesc(C.Structure):
     _fields_ = [("positions", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
                 ("indices", C.POINTER(C.c_uint32)), ("num_vertices", C.c_uint32),
                 ("num_triangles", C.c_uint32), ("material", C.c_int32), ("emissive", C.c_int32),
-                ("emission_color", C.c_float * 3), ("radiant_power", C.c_float)]
+                ("emission_color", C.c_float * 3), ("radiant_power", C.c_float),
+                ("texcoords", C.POINTER(C.c_float))]
 
 
 class CameraDesc(C.Structure):
@@ -62,7 +71,8 @@ class SceneDesc(C.Structure):
     _fields_ = [("camera", CameraDesc), ("background", C.c_float * 3),
                 ("materials", C.POINTER(MaterialDesc)), ("num_materials", C.c_uint32),
                 ("media", C.POINTER(MediumDesc)), ("num_media", C.c_uint32),
-                ("meshes", C.POINTER(MeshDesc)), ("num_meshes", C.c_uint32)]
+                ("meshes", C.POINTER(MeshDesc)), ("num_meshes", C.c_uint32),
+                ("images", C.POINTER(ImageDesc)), ("num_images", C.c_uint32)]
 
 
 class SceneInfo(C.Structure):
@@ -142,6 +152,8 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_autotune_batch.argtypes = [p, C.POINTER(p), C.POINTER(RenderParams), C.c_uint32, C.c_uint32,
                                         C.POINTER(Tuning)]
         L.lt_resolve.argtypes = [p, C.POINTER(Film), C.c_int32, C.c_float, p, p, C.POINTER(SppRange)]
+        L.lt_image_load.argtypes = [C.c_char_p, p, C.c_size_t, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                    C.POINTER(C.c_uint32)]
         _lib = L
         return L
 
@@ -149,6 +161,23 @@ def load(build_if_needed: bool = True) -> C.CDLL:
 def check(L, ctx, status: int) -> None:
     if status != LT_OK:
         raise LanternError(status, L.lt_last_error(ctx).decode(errors="replace"))
+
+
+def load_image(path: str):
+    """lt_image_load: a PNG file as the scene loader decodes image textures,
+    (height, width, channels) uint8 (stbi_load with 0 requested channels)."""
+    import numpy as np
+    L = load()
+    w, h, n = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    b = os.path.abspath(path).encode()
+    st = L.lt_image_load(b, None, 0, C.byref(w), C.byref(h), C.byref(n))
+    if st != LT_OK:
+        raise LanternError(st, L.lt_last_error(None).decode(errors="replace"))
+    out = np.empty((h.value, w.value, n.value), np.uint8)
+    st = L.lt_image_load(b, out.ctypes.data, out.nbytes, C.byref(w), C.byref(h), C.byref(n))
+    if st != LT_OK:
+        raise LanternError(st, L.lt_last_error(None).decode(errors="replace"))
+    return out
 
 
 class Context:

@@ -44,6 +44,7 @@ class Mesh:
     indices: np.ndarray    # (T, 3) uint32
     material: str
     emission: Optional[dict] = None  # {"color": [r,g,b], "radiant_power": p}
+    texcoords: Optional[np.ndarray] = None  # (V, 2) float32
 
     @property
     def num_triangles(self) -> int:
@@ -244,7 +245,7 @@ class Scene:
         names = {}
         for m in self.meshes:
             fn = f"{self.name}_{m.name}.lmf"
-            write_lmf(os.path.join(directory, fn), m.positions, m.indices, m.normals)
+            write_lmf(os.path.join(directory, fn), m.positions, m.indices, m.normals, m.texcoords)
             names[m.name] = fn
         path = os.path.join(directory, f"{self.name}.json")
         with open(path, "w") as fh:
@@ -512,6 +513,55 @@ def procedural_scene(width=64, height=64, spp=4, max_depth=8, rr_depth=3, name="
          "transform": _translate(-1.0, 0.8, 0.0)},
         {"name": "gem", "type": "geosphere", "radius": 0.6, "n": 2, "material": "glass",
          "transform": _translate(1.2, 0.6, 0.5)}]
+    p, n, i = quad((0.0, 5.0, 0.0), 1.0, 1.0, -1.0)
+    sc.meshes.append(Mesh("light", p, n, i, "light",
+                          emission={"color": [1.0, 1.0, 1.0], "radiant_power": float(15.0 * np.pi * 4.0)}))
+    return sc
+
+
+def texture_images(directory: str):
+    """Two seeded test images written as PNG into `directory`: a 37x23 RGB
+    pattern and a 16x9 grey ramp. Returns their absolute paths."""
+    from .image import write_png
+    os.makedirs(directory, exist_ok=True)
+    rng = np.random.default_rng(11)
+    y, x = np.mgrid[0:23, 0:37]
+    rgb = np.stack([(x * 7) % 256, (y * 11) % 256, rng.integers(0, 256, (23, 37))], axis=-1).astype(np.uint8)
+    grey = np.tile((np.arange(16) * 16)[None, :], (9, 1)).astype(np.uint8)[:, :, None]
+    paths = [os.path.abspath(os.path.join(directory, "tex_rgb.png")),
+             os.path.abspath(os.path.join(directory, "tex_grey.png"))]
+    write_png(paths[0], rgb)
+    write_png(paths[1], grey)
+    return paths
+
+
+def textured_scene(image_dir: str, width=64, height=48, spp=4, max_depth=8, rr_depth=3,
+                   name="textured") -> Scene:
+    """Albedo textures (scene.cpp:266-318): a grid floor with the ``uv``
+    texture (albedo = (u, v, 0)), two upright LMF quads with ``image``
+    textures (an RGB and a grey PNG; texture coordinates inside [0.1, 0.9], the
+    range where the reference's nearest lookup stays inside the image), and a
+    constant-albedo geosphere, under the LMF area light."""
+    rgb_png, grey_png = texture_images(image_dir)
+    sc = Scene(width, height,
+               camera={"phi": 1.2, "theta": 0.2, "radius": 6.5, "fov": 0.785398, "target": [0.0, 0.8, 0.0]},
+               render={"spp": spp, "max_depth": max_depth, "rr_depth": rr_depth}, name=name)
+    sc.bsdfs += [{"name": "uvfloor", "type": "lambert", "albedo": {"type": "uv"}},
+                 {"name": "picture", "type": "lambert", "albedo": {"type": "image", "file_path": rgb_png}},
+                 {"name": "ramp", "type": "mirror", "albedo": {"type": "image", "file_path": grey_png}},
+                 _lambert("ball", (0.7, 0.7, 0.7)), _lambert("light", (0.0, 0.0, 0.0))]
+    for m in ("uvfloor", "picture", "ramp", "ball", "light"):
+        sc.materials.append({"name": m, "bsdf": m})
+    sc.procedural += [
+        {"name": "floor", "type": "grid", "width": 12.0, "depth": 12.0, "n": 5, "m": 4, "material": "uvfloor"},
+        {"name": "ball", "type": "geosphere", "radius": 0.5, "n": 2, "material": "ball",
+         "transform": _translate(0.0, 0.5, 1.0)}]
+    for nm, mat, x0 in (("picture", "picture", -2.2), ("ramp", "ramp", 0.3)):
+        p = np.array([[x0, 0.0, -1.0], [x0 + 1.9, 0.0, -1.0], [x0 + 1.9, 2.2, -1.0], [x0, 2.2, -1.0]], F32)
+        n = np.tile(np.array([[0.0, 0.0, 1.0]], F32), (4, 1))
+        t = np.array([[0.1, 0.1], [0.9, 0.1], [0.9, 0.9], [0.1, 0.9]], F32)
+        i = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+        sc.meshes.append(Mesh(nm, p, n, i, mat, texcoords=t))
     p, n, i = quad((0.0, 5.0, 0.0), 1.0, 1.0, -1.0)
     sc.meshes.append(Mesh("light", p, n, i, "light",
                           emission={"color": [1.0, 1.0, 1.0], "radiant_power": float(15.0 * np.pi * 4.0)}))

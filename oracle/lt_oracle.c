@@ -135,10 +135,11 @@ float orc_filter_sample(float x) {
 }
 
 /* ------------------------------------------------------------------ scene */
-typedef struct { int bsdf; v3 albedo; float ior; int medium; } material;
+typedef struct { int bsdf; v3 albedo; float ior; int medium; int tex; } material; /* tex: -1 constant, -2 uv, >= 0 image */
+typedef struct { uint8_t *texels; uint32_t w, h, ch; } image;
 typedef struct { int type; v3 sigma_a; v3 sigma_s; float g; } medium;
 typedef struct { int geom; v3 radiance; float area; float sphere[4]; } light;
-typedef struct { uint32_t tri_begin, tri_count; int material, light, has_normals; } geom;
+typedef struct { uint32_t tri_begin, tri_count; int material, light, has_normals, has_texcoords; uint32_t vbase, nverts; } geom;
 
 typedef struct { float lo[3], hi[3]; int32_t left, right; uint32_t first, count; } bnode;
 
@@ -160,6 +161,8 @@ struct orc_scene {
     uint32_t *tri_geom;
     uint32_t *tri_vidx;
     float *vnormal; uint32_t nverts, cverts;
+    float *vtex;       /* 2 per vertex, 0 where a mesh has none */
+    image *images; int nimages, cimages;
 
     bnode *nodes; uint32_t nnodes;
     uint32_t *order; /* BVH leaf order -> triangle index */
@@ -184,7 +187,9 @@ orc_scene *orc_scene_new(void) {
 void orc_scene_free(orc_scene *s) {
     if (!s) return;
     free(s->mats); free(s->meds); free(s->lights); free(s->geoms);
-    free(s->tri); free(s->tri_geom); free(s->tri_vidx); free(s->vnormal);
+    free(s->tri); free(s->tri_geom); free(s->tri_vidx); free(s->vnormal); free(s->vtex);
+    for (int i = 0; i < s->nimages; ++i) free(s->images[i].texels);
+    free(s->images);
     free(s->nodes); free(s->order);
     free(s);
 }
@@ -236,7 +241,7 @@ int orc_add_medium_ref(orc_scene *s, int type, const float color[3], float at_di
 
 int orc_add_material(orc_scene *s, int bsdf, const float albedo[3], float ior, int med) {
     GROW(s->mats, s->nmats, s->cmats, 1, material);
-    material m = {bsdf, ld3(albedo), ior, med};
+    material m = {bsdf, ld3(albedo), ior, med, -1};
     s->mats[s->nmats] = m;
     return s->nmats++;
 }
@@ -280,11 +285,17 @@ int orc_add_mesh(orc_scene *s, const float *pos, uint32_t nv, const float *nrm,
     g->material = mat;
     g->light = -1;
     g->has_normals = nrm != NULL;
+    g->has_texcoords = 0;
 
     uint32_t vbase = s->nverts;
+    g->vbase = vbase;
+    g->nverts = nv;
     s->vnormal = (float *)realloc(s->vnormal, (size_t)(s->nverts + nv) * 3 * sizeof(float));
-    for (uint32_t i = 0; i < nv; ++i)
+    s->vtex = (float *)realloc(s->vtex, (size_t)(s->nverts + nv) * 2 * sizeof(float));
+    for (uint32_t i = 0; i < nv; ++i) {
         for (int c = 0; c < 3; ++c) s->vnormal[3 * (vbase + i) + c] = nrm ? nrm[3 * i + c] : 0.0f;
+        s->vtex[2 * (vbase + i)] = s->vtex[2 * (vbase + i) + 1] = 0.0f;
+    }
     s->nverts += nv;
 
     size_t T = (size_t)s->ntris + nt;
@@ -739,7 +750,7 @@ static inline float power_heuristic(float f, float g) {
 enum { LOBE_NULL = 0, LOBE_SREFL = 1, LOBE_STRANS = 2, LOBE_DIFFUSE = 4, LOBE_SPECULAR = 3 };
 
 /* SurfaceInteraction, integrator/surface_interaction.h:14-30 */
-typedef struct { v3 P, N, wi, wo; int lobe; float iori, ioro; } inter;
+typedef struct { v3 P, N, wi, wo; int lobe; float iori, ioro; v3 albedo; } inter;
 
 /* BSDF Sample / Eval / Pdf, materials/bsdfs/{lambert_bsdf.h:26-38, mirror_bsdf.h:27-38,
  * ideal_specular_dielectric.h:31-68} */
@@ -783,8 +794,8 @@ static inline void bsdf_sample(const material *m, inter *it, pcg *g) {
 }
 
 static inline v3 bsdf_eval(const material *m, const inter *it) {
-    if (m->bsdf == ORC_BSDF_LAMBERT) return muls(muls(m->albedo, INV_PI_F), dot(it->wi, it->N));
-    return m->albedo;
+    if (m->bsdf == ORC_BSDF_LAMBERT) return muls(muls(it->albedo, INV_PI_F), dot(it->wi, it->N));
+    return it->albedo;
 }
 static inline float bsdf_pdf(const material *m, const inter *it) {
     if (m->bsdf == ORC_BSDF_LAMBERT) return dot(it->wi, it->N) * INV_PI_F;
@@ -800,6 +811,57 @@ static inline v3 interp_normal(const orc_scene *s, uint32_t prim, float u, float
     v3 n2 = ld3(s->vnormal + 3 * (size_t)vi[2]);
     float w = 1.0f - u - v;
     return add(add(muls(n0, w), muls(n1, u)), muls(n2, v));
+}
+
+/* The albedo texture at a hit. ConstantTexture; UVTexture (uv_texture.h:16-18):
+ * (u, v, 0) of the texture coordinate rtcInterpolate1 gives on slot 1
+ * (scene.cpp:134-143; (0, 0) without texture coordinates, integrator.cpp:184-188);
+ * ImageTexture (image_texture.h:32-39) flips v and ImageCache::SampleImage
+ * (image_cache.cpp:33-62) takes texel (round(u*W), round(v*H)), index
+ * (y*W + x)*channels, value/256. The index is kept inside the image. */
+static inline v3 material_albedo(const orc_scene *s, const material *m, const geom *G, uint32_t prim, float u,
+                                 float v) {
+    if (m->tex == -1) return m->albedo;
+    float tu = 0.0f, tv = 0.0f;
+    if (G->has_texcoords) {
+        const uint32_t *vi = s->tri_vidx + 3 * (size_t)prim;
+        float w = 1.0f - u - v;
+        tu = s->vtex[2 * (size_t)vi[0]] * w + s->vtex[2 * (size_t)vi[1]] * u + s->vtex[2 * (size_t)vi[2]] * v;
+        tv = s->vtex[2 * (size_t)vi[0] + 1] * w + s->vtex[2 * (size_t)vi[1] + 1] * u +
+             s->vtex[2 * (size_t)vi[2] + 1] * v;
+    }
+    if (m->tex == -2) return mk(tu, tv, 0.0f);
+    const image *I = &s->images[m->tex];
+    tv = 1.0f - tv;
+    float fx = fminf(fmaxf(roundf(tu * (float)I->w), 0.0f), 65536.0f);
+    float fy = fminf(fmaxf(roundf(tv * (float)I->h), 0.0f), 65536.0f);
+    uint64_t texel = (uint64_t)fy * I->w + (uint64_t)fx, last = (uint64_t)I->w * I->h - 1;
+    if (texel > last) texel = last;
+    const uint8_t *t = I->texels + texel * I->ch;
+    float r = (float)t[0] / 256.0f;
+    if (I->ch == 1) return mk(r, r, r);
+    float gg = (float)t[1] / 256.0f;
+    if (I->ch == 2) return mk(r, gg, 0.0f);
+    return mk(r, gg, (float)t[2] / 256.0f);
+}
+
+int orc_add_image(orc_scene *s, const uint8_t *texels, uint32_t w, uint32_t h, uint32_t ch) {
+    GROW(s->images, s->nimages, s->cimages, 1, image);
+    image *I = &s->images[s->nimages];
+    I->w = w;
+    I->h = h;
+    I->ch = ch;
+    I->texels = (uint8_t *)malloc((size_t)w * h * ch);
+    memcpy(I->texels, texels, (size_t)w * h * ch);
+    return s->nimages++;
+}
+
+void orc_set_material_texture(orc_scene *s, int mat, int tex) { s->mats[mat].tex = tex; }
+
+void orc_set_mesh_texcoords(orc_scene *s, int geom_id, const float *tc) {
+    geom *g = &s->geoms[geom_id];
+    memcpy(s->vtex + 2 * (size_t)g->vbase, tc, (size_t)g->nverts * 2 * sizeof(float));
+    g->has_texcoords = 1;
 }
 
 typedef struct { uint64_t main, light, mis; } raystat;
@@ -964,6 +1026,7 @@ static void render_pixel(const orc_scene *s, const orc_render_opts *o, uint32_t 
             it.P = add(origin, muls(direction, h.t));
             if (G->has_normals) it.N = normalize(interp_normal(s, h.prim, h.u, h.v));
             else it.N = normalize(mk(0, 0, 0));
+            it.albedo = material_albedo(s, m, G, h.prim, h.u, h.v);
             it.wo = neg(direction);
             it.ioro = 0.0f;
             color = add(color, mul(T, sample_one_light(s, g, it, m, G->light, rs)));

@@ -62,6 +62,14 @@ int orc_add_mesh(orc_scene *s, const float *positions, uint32_t num_verts, const
 /* Build the BVH2 over all meshes. Returns 0 on success. */
 int orc_scene_commit(orc_scene *s);
 
+/* Albedo textures (before commit): an 8-bit image (rows from the top,
+ * channels 1-4) -> its index; a material's texture: -1 constant albedo,
+ * -2 uv, >= 0 image index; a mesh's per-vertex texture coordinates (2 floats
+ * per vertex of that mesh). */
+int orc_add_image(orc_scene *s, const uint8_t *texels, uint32_t w, uint32_t h, uint32_t ch);
+void orc_set_material_texture(orc_scene *s, int mat, int tex);
+void orc_set_mesh_texcoords(orc_scene *s, int geom_id, const float *tc);
+
 /* Light data derived at load (scene.cpp:49-80,463-473; area_light.h:16-21). */
 void orc_light_info(const orc_scene *s, int light, float *area, float sphere[4], float radiance[3]);
 uint32_t orc_num_triangles(const orc_scene *s);

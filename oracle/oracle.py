@@ -114,6 +114,10 @@ def lib():
                                           C.c_int]
             L.orc_resolve.argtypes = [fp, up, u64, C.c_int, f32, fp, C.POINTER(C.c_uint8), up,
                                       C.POINTER(C.c_uint64)]
+            L.orc_add_image.argtypes = [p, C.POINTER(C.c_uint8), u32, u32, u32]
+            L.orc_add_image.restype = i32
+            L.orc_set_material_texture.argtypes = [p, i32, i32]
+            L.orc_set_mesh_texcoords.argtypes = [p, i32, fp]
             _lib = L
     return _lib
 
@@ -137,6 +141,8 @@ def ref_lib():
             L.lref_pcg_stream.argtypes = [C.c_ulonglong, C.c_ulonglong, u32, up, fp]
             L.lref_filter_sample.argtypes = [fp, u32, fp]
             L.lref_camera_ray.argtypes = [p, u32, u32, C.c_ulonglong, C.c_ulonglong, fp]
+            L.lref_image_load.argtypes = [C.c_char_p, C.POINTER(C.c_uint8), C.c_size_t, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int), C.POINTER(C.c_int)]
             _ref = L
     return _ref
 
@@ -209,7 +215,11 @@ def grid_mesh(width: float, depth: float, m: int, n: int):
     a = (i * n + j).reshape(-1)
     b = ((i + 1) * n + j).reshape(-1)
     idx = np.stack([a, a + 1, b, b, a + 1, b + 1], axis=1).reshape(-1).astype(np.uint32)
-    return pos.reshape(-1, 3), nrm, idx
+    du, dv = f32(1) / f32(n - 1), f32(1) / f32(m - 1)
+    tex = np.zeros((m, n, 2), f32)
+    tex[:, :, 0] = (np.arange(n, dtype=f32) * du)[None, :]
+    tex[:, :, 1] = (np.arange(m, dtype=f32) * dv)[:, None]
+    return pos.reshape(-1, 3), nrm, idx, tex.reshape(-1, 2)
 
 
 def geosphere_mesh(radius: float, subdivisions: int):
@@ -233,7 +243,7 @@ def geosphere_mesh(radius: float, subdivisions: int):
     d = (pos[:, 0] * pos[:, 0] + pos[:, 1] * pos[:, 1]) + pos[:, 2] * pos[:, 2]
     inv = f32(1) / np.sqrt(d)
     nrm = (pos * inv[:, None]).astype(f32)
-    return (f32(radius) * nrm).astype(f32), nrm, tri.reshape(-1).astype(np.uint32)
+    return (f32(radius) * nrm).astype(f32), nrm, tri.reshape(-1).astype(np.uint32), None
 
 
 class OracleScene:
@@ -270,24 +280,37 @@ class OracleScene:
                     self.h, typ, fptr(col), f32(m["absorption_at_distance"]),
                     f32(m.get("scattering_distance", 1.0)))
         bsdfs = {b["name"]: b for b in j.get("bsdfs", [])}
-        mats = {}
+        mats, images = {}, {}
+        base = os.path.dirname(self.path)
         for m in j.get("materials", []):
             b = bsdfs[m["bsdf"]]
             alb = np.array(b["albedo"].get("value", [0, 0, 0]), dtype=f32)
-            mats[m["name"]] = L.orc_add_material(self.h, BSDF[b["type"]], fptr(alb),
-                                                 f32(b.get("ior", 1.0)), media.get(m.get("medium"), -1))
+            mi = L.orc_add_material(self.h, BSDF[b["type"]], fptr(alb), f32(b.get("ior", 1.0)),
+                                    media.get(m.get("medium"), -1))
+            kind = b["albedo"]["type"]
+            if kind == "uv":
+                L.orc_set_material_texture(self.h, mi, -2)
+            elif kind == "image":
+                ip = b["albedo"]["file_path"]
+                if not os.path.isabs(ip) and not os.path.exists(ip):
+                    ip = os.path.join(base, ip)
+                if ip not in images:
+                    tex = read_png(ip)
+                    images[ip] = L.orc_add_image(self.h, tex.ctypes.data_as(C.POINTER(C.c_uint8)), tex.shape[1],
+                                                 tex.shape[0], tex.shape[2])
+                L.orc_set_material_texture(self.h, mi, images[ip])
+            mats[m["name"]] = mi
         self._keep = []
-        base = os.path.dirname(self.path)
         for p in j.get("primitives", []):
             if p["type"] == "lmf":
                 lmf = read_lmf(os.path.join(base, p["file_path"]))
                 if lmf["vpp"] != 3:
                     raise NotImplementedError("triangle LMF only")
-                pos, nrm, idx = lmf["positions"], lmf["normals"], lmf["indices"]
+                pos, nrm, idx, tc = lmf["positions"], lmf["normals"], lmf["indices"], lmf["texcoords"]
             elif p["type"] == "grid":
-                pos, nrm, idx = grid_mesh(p["width"], p["depth"], int(p["m"]), int(p["n"]))
+                pos, nrm, idx, tc = grid_mesh(p["width"], p["depth"], int(p["m"]), int(p["n"]))
             elif p["type"] == "geosphere":
-                pos, nrm, idx = geosphere_mesh(p["radius"], int(p["n"]))
+                pos, nrm, idx, tc = geosphere_mesh(p["radius"], int(p["n"]))
             else:
                 raise NotImplementedError(f"primitive type {p['type']}")
             pos = np.ascontiguousarray(pos, dtype=f32)
@@ -301,8 +324,11 @@ class OracleScene:
                 em = np.array(p["emission"]["color"], dtype=f32)
                 power = f32(p["emission"]["radiant_power"])
             self._keep += [pos, nrm, idx, em]
-            L.orc_add_mesh(self.h, fptr(pos), pos.shape[0], fptr(nrm), uptr(idx), idx.size // 3,
-                           mats[p["material"]], fptr(em), power)
+            gid = L.orc_add_mesh(self.h, fptr(pos), pos.shape[0], fptr(nrm), uptr(idx), idx.size // 3,
+                                 mats[p["material"]], fptr(em), power)
+            if tc is not None and np.asarray(tc).size == 2 * pos.shape[0]:
+                tc = np.ascontiguousarray(tc, dtype=f32).reshape(-1)
+                L.orc_set_mesh_texcoords(self.h, gid, fptr(tc))
         L.orc_scene_commit(self.h)
         self._keep = []
 
@@ -469,3 +495,110 @@ def resolve(rgb, counts, tonemap: int, exposure_stops: float):
     L.orc_resolve(fptr(rgb), uptr(counts), h * w, tonemap, C.c_float(exposure_stops), fptr(out),
                   out8.ctypes.data_as(C.POINTER(C.c_uint8)), uptr(mm), C.byref(sm))
     return out, out8, (int(mm[0]), int(mm[1]), int(sm.value))
+
+
+def read_png(path: str) -> np.ndarray:
+    """A PNG file as stbi_load(path, &w, &h, &n, 0) returns it (the reference's
+    image cache, image_cache.cpp:23-31): (h, w, n) uint8; grey 1, grey+alpha 2,
+    RGB 3, RGBA 4 channels; palette -> RGB (RGBA with tRNS); a tRNS key on
+    grey/RGB adds alpha; 1/2/4-bit grey scaled to 0..255; 16-bit keeps the high
+    byte. Not interlaced."""
+    import zlib
+    data = open(path, "rb").read()
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError(f"{path}: not a PNG file")
+    pos, idat, plte, trns = 8, b"", b"", b""
+    w = h = depth = ctype = interlace = 0
+    while pos + 12 <= len(data):
+        n, tag = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        if tag == b"IHDR":
+            w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", body[:13])
+        elif tag == b"PLTE":
+            plte = body
+        elif tag == b"tRNS":
+            trns = body
+        elif tag == b"IDAT":
+            idat += body
+        elif tag == b"IEND":
+            break
+        pos += 12 + n
+    if interlace:
+        raise ValueError("interlaced PNG files are not supported")
+    chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    stride = (w * chans * depth + 7) // 8
+    bpp = max(1, (chans * depth + 7) // 8)
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8)[:h * (stride + 1)].reshape(h, stride + 1)
+    img = np.zeros((h, stride), np.int32)
+    prev = np.zeros(stride, np.int32)
+    for y in range(h):
+        f, src = raw[y, 0], raw[y, 1:].astype(np.int32)
+        row = np.zeros(stride, np.int32)
+        for i in range(stride):
+            a = row[i - bpp] if i >= bpp else 0
+            b = prev[i]
+            c = prev[i - bpp] if i >= bpp else 0
+            if f == 0:
+                pr = 0
+            elif f == 1:
+                pr = a
+            elif f == 2:
+                pr = b
+            elif f == 3:
+                pr = (a + b) >> 1
+            else:
+                p_ = a + b - c
+                pa, pb, pc = abs(p_ - a), abs(p_ - b), abs(p_ - c)
+                pr = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+            row[i] = (src[i] + pr) & 255
+        img[y] = row
+        prev = row
+    img = img.astype(np.uint32)
+    if depth == 16:
+        samples = (img[:, 0::2] << 8) | img[:, 1::2]
+    elif depth == 8:
+        samples = img
+    else:
+        per = 8 // depth
+        bits = np.zeros((h, stride * per), np.uint32)
+        for k in range(per):
+            bits[:, k::per] = (img >> (8 - depth * (k + 1))) & ((1 << depth) - 1)
+        samples = bits
+    samples = samples[:, :w * chans].reshape(h, w, chans)
+    if ctype == 3:
+        pal = np.frombuffer(plte, np.uint8).reshape(-1, 3)
+        idx = samples[:, :, 0]
+        out = pal[np.minimum(idx, len(pal) - 1)]
+        if trns:
+            t = np.frombuffer(trns, np.uint8)
+            alpha = np.where(idx < len(t), t[np.minimum(idx, len(t) - 1)], 255).astype(np.uint8)
+            out = np.concatenate([out, alpha[:, :, None]], axis=2)
+        return np.ascontiguousarray(out)
+    if depth == 16:
+        out = (samples >> 8).astype(np.uint8)
+    elif depth == 8:
+        out = samples.astype(np.uint8)
+    else:
+        out = (samples * (255 // ((1 << depth) - 1))).astype(np.uint8)
+    if trns and ctype in (0, 2):
+        key = [(trns[2 * c] << 8) | trns[2 * c + 1] for c in range(chans)]
+        if depth <= 8:
+            key = [k & 255 for k in key]
+        keyed = np.all(samples == np.array(key, np.uint32)[None, None, :], axis=2)
+        out = np.concatenate([out, np.where(keyed, 0, 255).astype(np.uint8)[:, :, None]], axis=2)
+    return np.ascontiguousarray(out)
+
+
+def reference_image_load(path: str):
+    """The reference's stb_image decode of `path` ((h, w, n) uint8), or None
+    when the reference build is absent."""
+    L = ref_lib()
+    if L is None:
+        return None
+    w, h, n = C.c_int(), C.c_int(), C.c_int()
+    if L.lref_image_load(path.encode(), None, 0, C.byref(w), C.byref(h), C.byref(n)) != 0:
+        raise ValueError(f"stb_image could not load {path}")
+    out = np.empty((h.value, w.value, n.value), np.uint8)
+    L.lref_image_load(path.encode(), out.ctypes.data_as(C.POINTER(C.c_uint8)), out.nbytes, C.byref(w), C.byref(h),
+                      C.byref(n))
+    return out

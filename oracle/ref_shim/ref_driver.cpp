@@ -33,6 +33,7 @@
 #include "camera/pinhole_camera.h"
 #include "scene/light.h"
 #include "scene/image_cache.h"
+#include "stb_image.h"
 #define private public
 #include "integrator/integrator.h"
 #include "scene/scene.h"
@@ -134,6 +135,18 @@ void lref_camera_ray(void *s, unsigned x, unsigned y, unsigned long long seed, u
     RTCRay r = sc->Camera->CalculateRayFromPixel(x, y, &smp);
     out[0] = r.org_x; out[1] = r.org_y; out[2] = r.org_z;
     out[3] = r.dir_x; out[4] = r.dir_y; out[5] = r.dir_z;
+}
+
+// stbi_load(path, &w, &h, &n, 0) of the reference's vendored stb_image (its
+// image cache, image_cache.cpp:23-31): the texels are copied into `out` when it
+// holds w*h*n bytes. Returns 0, or -1 when stb_image fails.
+int lref_image_load(const char *path, unsigned char *out, size_t cap, int *w, int *h, int *n) {
+    unsigned char *d = stbi_load(path, w, h, n, 0);
+    if (!d) return -1;
+    const size_t size = (size_t)*w * (size_t)*h * (size_t)*n;
+    if (out && cap >= size) memcpy(out, d, size);
+    stbi_image_free(d);
+    return 0;
 }
 
 }  // extern "C"
