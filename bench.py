@@ -60,6 +60,10 @@ def make_scene(name: str):
     if name == "nine-spheres":
         sc = S.nine_spheres(width=256, height=256, spp=16, max_depth=8, rr_depth=3, name="bench_nine")
         return sc, {"spp": 16, "max_depth": 8, "rr_depth": 3}
+    if name == "medium-c2r":  # the reference-expressible medium scene (isotropic, scalar sigma_s)
+        sc = S.medium_sphere_scene(width=512, height=512, spp=256, max_depth=32, rr_depth=3,
+                                   reference_expressible=True, name="bench_c2r")
+        return sc, {"spp": 256, "max_depth": 32, "rr_depth": 3}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -166,9 +170,11 @@ def run_reference(args, workload):
     sc, rp = make_scene(workload)
     path = __import__("lantern_gb300.scenes", fromlist=["x"]).ensure_written(sc, SCENES)
     ref = O.ReferenceScene(path)
-    frames_per_step = 1
+    t1 = 1.0
     for _ in range(args.warmup):
-        ref.render(frames_per_step, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
+        t1 = ref.render(1, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])["seconds"]
+    # each step: a bounded sample of about 2 s of CPU work (whole frames)
+    frames_per_step = int(max(1, min(64, round(2.0 / max(t1, 1e-6)))))
     secs, rays = 0.0, 0
     for k in range(args.steps):
         r = ref.render(frames_per_step, first_frame=1000 + k, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
@@ -557,11 +563,14 @@ def cpu_baseline(path, rp):
         if not os.path.exists(O.REF_SO):
             return None
         ref = O.ReferenceScene(path)
-        r = ref.render(1, first_frame=99, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
-        n = ref.width * ref.height
+        t1 = ref.render(1, first_frame=98, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])["seconds"]
+        frames = int(max(1, min(256, round(10.0 / max(t1, 1e-6)))))  # about 10 s of CPU work
+        r = ref.render(frames, first_frame=99, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
+        n = ref.width * ref.height * frames
         return {"value": round(n / r["seconds"] / 1e6, 4), "unit": "Msamples/s",
                 "cores": int(os.environ.get("LT_REF_THREADS", os.cpu_count())), "kind": "reference",
-                "sample": f"1 frame (1 spp) of {ref.width}x{ref.height}", "mrays": round(r["rays"] / r["seconds"] / 1e6, 3)}
+                "sample": f"{frames} frame(s) (1 spp each) of {ref.width}x{ref.height}, {r['seconds']:.1f} s",
+                "mrays": round(r["rays"] / r["seconds"] / 1e6, 3)}
     except Exception as e:
         return {"error": str(e)[:200]}
 

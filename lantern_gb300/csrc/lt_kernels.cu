@@ -339,6 +339,7 @@ struct Bvh2 {
     using State = Trav;
     using Entry = int;
     static constexpr int kDepth = kStack;
+    static constexpr int kMinBlocks256 = 0;  // k_trace register budget: 0 = no minimum (compiler's choice)
     __device__ static Geo geo(const DevScene &S) { return geo_of(S); }
     __device__ static void start(State &r, Entry *st, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip) {
         trav_start(r, st, O, D, tnear, tfar, any, skip);
@@ -352,6 +353,7 @@ struct Bvh8 {
     using State = Trav8;
     using Entry = uint2;
     static constexpr int kDepth = kStack8;
+    static constexpr int kMinBlocks256 = 0;  // k_trace register budget: 0 = no minimum (compiler's choice)
     __device__ static Geo geo(const DevScene &S) {
         return Geo{S.nodes8, S.tris8, S.tri_geom, S.num_nodes8, S.num_tris};
     }
@@ -954,7 +956,7 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // counters->trace_fetch (zeroed by the launch before). Path rays come first so
 // that the short connection queries fill the tail.
 template <class Src, class B>
-__global__ void __launch_bounds__(256) k_trace(Src src, Wavefront W, int cur) {
+__global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefront W, int cur) {
     const uint32_t n = W.counters->count[cur];
     const uint32_t nc = W.counters->ccount[cur ^ 1];
     const uint32_t total = n + nc;
