@@ -233,6 +233,8 @@ typedef struct lt_render_stats {
     float trace_ms;          /* device time in the trace kernel (path rays + connection rays) */
     float shade_ms;          /* ... in the shade kernel (incl. camera-ray generation) */
     uint64_t light_traversals; /* connection rays traced (the rest were resolved against the light alone) */
+    uint64_t nonfinite_samples; /* film contributions with a NaN or infinite channel (e.g. a mesh
+                                 * without normals shades with normalize(0), integrator.cpp:182) */
 } lt_render_stats;
 lt_status lt_render_stats_get(lt_ctx *ctx, lt_render_stats *out);
 
@@ -375,6 +377,13 @@ typedef struct lt_hit { float t, u, v; uint32_t prim; } lt_hit; /* 16 B; prim = 
  * Embree's Moeller-Trumbore acceptance rule (tnear exclusive, tfar inclusive).
  * rays/hits are device pointers when on_device, else host memory. */
 lt_status lt_intersect(lt_ctx *ctx, const lt_ray *rays, lt_hit *hits, uint64_t n, int32_t on_device);
+
+/* ---------------------------------------------------------------- fault injection */
+/* For failure-handling tests: after `after` more successful device or pinned
+ * host allocations by the library, the next one fails as out-of-memory
+ * (LT_ERR_OOM) without reaching the CUDA runtime. UINT32_MAX (the initial
+ * state) turns injection off. Process-wide. No counterpart in the reference. */
+void lt_debug_fail_allocations(uint32_t after);
 
 #ifdef __cplusplus
 }

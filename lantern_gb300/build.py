@@ -75,7 +75,7 @@ def build(force: bool = False, verbose: bool = False, extra_nvcc=()) -> str:
         msg = "\n".join(" ".join(j) + "\n" + out for j, out in failed)
         raise RuntimeError("liblantern_gpu build failed:\n" + msg)
     tmp = LIB + f".{os.getpid()}.tmp"
-    link = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+    link = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

@@ -1,13 +1,17 @@
 // lt_api.cpp -- the C ABI declared in include/lantern_gpu.h.
 //
-// A context owns a CUDA stream, the device copy of one scene (triangles, BVH,
-// shading tables) and the wavefront buffers, which are sized once and reused.
-// lt_render queues the wavefront: an initial camera-ray launch, then batches of
-// (trace, shade, connect) iterations, reading the queue length back once per
-// batch until no path is left.
+// A context owns a CUDA stream, the device copy of one scene (triangles, BVH2
+// and on demand the 8-wide BVH, shading tables, textures) and the wavefront
+// buffers, which are sized once and reused. lt_render queues the wavefront: an
+// initial camera-ray launch, then batches of (trace, shade) iterations, reading
+// the queue lengths back once per batch until no path or connection record is
+// left. lt_render_batch runs the same loop over many contexts' scenes as one
+// captured CUDA graph.
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <atomic>
+#include <climits>
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
@@ -15,6 +19,8 @@
 #include <new>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "lantern_gpu.h"
 #include "lt_device.h"
@@ -70,6 +76,37 @@ struct lt_ctx {
 };
 
 static thread_local std::string g_create_error;
+
+// NVTX range over one API call (visible in Nsight Systems / ncu timelines;
+// no cost without a tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
+// Allocation fault injection (lt_debug_fail_allocations): after `left` more
+// successful device or pinned-host allocations, the next one fails with
+// cudaErrorMemoryAllocation without reaching the CUDA runtime.
+static std::atomic<uint32_t> g_alloc_left{UINT32_MAX};
+
+static bool injected_alloc_failure() {
+    uint32_t left = g_alloc_left.load();
+    while (left != UINT32_MAX) {
+        if (left == 0) return true;
+        if (g_alloc_left.compare_exchange_weak(left, left - 1)) return false;
+    }
+    return false;
+}
+
+static cudaError_t dev_malloc(void **p, size_t bytes) {
+    if (injected_alloc_failure()) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
+static cudaError_t host_malloc(void **p, size_t bytes) {
+    if (injected_alloc_failure()) return cudaErrorMemoryAllocation;
+    return cudaMallocHost(p, bytes);
+}
 
 static lt_status fail(lt_ctx *c, lt_status st, const char *fmt, ...) {
     char buf[1024];
@@ -148,8 +185,8 @@ lt_status lt_ctx_create(int device, lt_ctx **out) {
     c->device = device;
     e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->counters_host, sizeof(WaveCounters));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&c->isect_fetch, 256);
+    if (e == cudaSuccess) e = host_malloc((void **)&c->counters_host, sizeof(WaveCounters));
+    if (e == cudaSuccess) e = dev_malloc((void **)&c->isect_fetch, 256);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e != cudaSuccess) {
@@ -210,7 +247,7 @@ template <typename T>
 static lt_status upload(lt_ctx *c, const std::vector<T> &v, const T **dst) {
     size_t bytes = v.size() * sizeof(T);
     void *p = nullptr;
-    CUDA_TRY(c, cudaMalloc(&p, bytes ? bytes : 16));
+    CUDA_TRY(c, dev_malloc(&p, bytes ? bytes : 16));
     c->scene_allocs.push_back(p);
     c->scene_bytes += bytes;
     if (bytes) CUDA_TRY(c, cudaMemcpyAsync(p, v.data(), bytes, cudaMemcpyHostToDevice, c->stream));
@@ -258,6 +295,7 @@ static lt_status ensure_bvh8(lt_ctx *c) {
 extern "C" {
 
 lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
+    NvtxRange nvtx_("lt_scene_create");
     if (!c || !desc) return fail(c, LT_ERR_INVALID, "NULL argument");
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -360,7 +398,7 @@ static lt_status ensure_scratch(lt_ctx *c, size_t bytes) {
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     c->scratch_bytes = 0;
-    CUDA_TRY(c, cudaMalloc(&c->scratch, bytes));
+    CUDA_TRY(c, dev_malloc(&c->scratch, bytes));
     c->scratch_bytes = bytes;
     return LT_OK;
 }
@@ -398,7 +436,7 @@ static lt_status ensure_wave(lt_ctx *c, uint32_t cap) {
     Wavefront sizing;
     size_t bytes = carve_wave(nullptr, cap, &sizing);
     char *a = nullptr;
-    CUDA_TRY(c, cudaMalloc((void **)&a, bytes));
+    CUDA_TRY(c, dev_malloc((void **)&a, bytes));
     carve_wave(a, cap, &c->wave);
     c->wave.arena = a;
     c->wave.arena_bytes = bytes;
@@ -423,6 +461,7 @@ static Wavefront wave_view(const lt_ctx *c, uint32_t cap) {
 extern "C" {
 
 lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
+    NvtxRange nvtx_("lt_render");
     if (!c || !p || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "lt_render without a scene");
     const uint32_t W = c->host.camera.width, H = c->host.camera.height;
@@ -498,6 +537,7 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
         c->stats.main_rays = c->counters_host->main_rays;
         c->stats.light_rays = c->counters_host->light_rays;
         c->stats.bsdf_rays = c->counters_host->bsdf_rays;
+        c->stats.nonfinite_samples = c->counters_host->nonfinite;
         c->stats.iterations = iters;
         c->stats.kernel_launches = launches;
         if (nev == c->stage_events.size()) {
@@ -538,6 +578,7 @@ lt_status lt_render_stats_get(lt_ctx *c, lt_render_stats *out) {
 }
 
 lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, int32_t on_device) {
+    NvtxRange nvtx_("lt_intersect");
     if (!c || (n && (!rays || !hits))) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "lt_intersect without a scene");
     if (n == 0) return LT_OK;
@@ -604,6 +645,7 @@ static lt_status diff_setup(lt_ctx *c, const lt_render_params *p, const lt_diff_
 
 lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, lt_film *film,
                          float *sample_radiance) {
+    NvtxRange nvtx_("lt_render_diff");
     if (!c || !p || !dp || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     DiffParams P;
     RenderArgs a;
@@ -624,6 +666,7 @@ lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_par
 lt_status lt_render_adjoint(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, const float *dI,
                             float *g_albedo, float *g_emission, float *g_sigma_a, float *g_sigma_s,
                             const uint32_t *crop, const float *sample_radiance) {
+    NvtxRange nvtx_("lt_render_adjoint");
     if (!c || !p || !dp || !dI || !g_albedo || !g_emission) return fail(c, LT_ERR_INVALID, "NULL argument");
     DiffParams P;
     RenderArgs a;
@@ -783,7 +826,7 @@ extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) {
 
 // ------------------------------------------------------------------ lt_render_batch
 // Captures the batched loop for wavefront `w`: memset(counters), camera rays,
-// then a while node whose body runs loop_iterations (trace, shade, connect)
+// then a while node whose body runs loop_iterations (trace, shade)
 // iterations and the condition kernel. Captured on the context's own stream in
 // thread-local mode, so other threads' CUDA calls are not affected.
 static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
@@ -845,8 +888,8 @@ static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
 // batch's table upload (from the pinned host copy) has completed.
 static lt_status ensure_table(lt_ctx *c) {
     if (!c->table_host) {
-        CUDA_TRY(c, cudaMallocHost((void **)&c->table_host, sizeof(SceneTable)));
-        CUDA_TRY(c, cudaMalloc((void **)&c->table_dev, sizeof(SceneTable)));
+        CUDA_TRY(c, host_malloc((void **)&c->table_host, sizeof(SceneTable)));
+        CUDA_TRY(c, dev_malloc((void **)&c->table_dev, sizeof(SceneTable)));
     }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return LT_OK;
@@ -854,6 +897,7 @@ static lt_status ensure_table(lt_ctx *c) {
 
 extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_render_params *params,
                                      lt_film *films, uint32_t n) {
+    NvtxRange nvtx_("lt_render_batch");
     if (!c || (n && (!scenes || !params || !films))) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u scenes; a batch holds at most %u", n, LT_MAX_BATCH);
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -922,6 +966,7 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
         c->stats.iterations = (uint32_t)k.iterations;
         launches += 1 + kStages * (uint32_t)k.iterations + (uint32_t)(k.iterations / c->tuning.loop_iterations);
         c->stats.light_traversals = k.light_traversals;
+        c->stats.nonfinite_samples = k.nonfinite;
     } else {
         CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -1010,6 +1055,7 @@ extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const l
 // ------------------------------------------------------------------ lt_resolve
 extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap, float exposure_stops, float *rgba,
                                 uint8_t *rgba8, lt_spp_range *spp) {
+    NvtxRange nvtx_("lt_resolve");
     if (!c || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (tonemap != LT_TONEMAP_CLAMP && tonemap != LT_TONEMAP_FILMIC)
         return fail(c, LT_ERR_INVALID, "unknown tone mapper %d", tonemap);
@@ -1068,6 +1114,7 @@ extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap,
 
 // ------------------------------------------------------------------ batched differentiable rendering
 static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool adjoint) {
+    NvtxRange nvtx_("diff_batch");
     if (!c || (n && !jobs)) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u jobs; a batch holds at most %u", n, LT_MAX_BATCH);
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -1161,3 +1208,5 @@ extern "C" lt_status lt_image_load(const char *path, uint8_t *texels, size_t cap
     }
     return LT_OK;
 }
+
+extern "C" void lt_debug_fail_allocations(uint32_t after) { g_alloc_left.store(after); }

@@ -59,6 +59,7 @@ struct WaveCounters {
     uint32_t error;               // nonzero: a device-side bound was exceeded
     unsigned long long light_traversals;  // connection rays that needed an occlusion query
     unsigned long long iterations;        // wavefront iterations of a captured loop
+    unsigned long long nonfinite;         // film contributions with a NaN or infinite channel
 };
 
 struct Wavefront {

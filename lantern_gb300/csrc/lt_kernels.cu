@@ -102,7 +102,35 @@ struct Trav {
     uint32_t skip_geom;
 };
 
-__device__ __forceinline__ void trav_start(Trav &r, int *stack, v3 O, v3 D, float tnear, float tfar, bool any,
+// Traversal stacks. LocalStack: a per-thread array (local memory). SharedStack:
+// the first kSharedStack entries of every thread in the block's dynamic shared
+// memory (column-interleaved, entry i of thread t at [i * blockDim + t], so a
+// warp's accesses to one depth fall in distinct banks), deeper entries local.
+#ifndef LT_SHARED_STACK
+#define LT_SHARED_STACK 0
+#endif
+constexpr int kSharedStack = LT_SHARED_STACK;
+extern __shared__ int lt_dyn_smem[];
+
+struct LocalStack {
+    int *a;
+    __device__ __forceinline__ int get(int i) const { return a[i]; }
+    __device__ __forceinline__ void set(int i, int v) { a[i] = v; }
+};
+
+struct SharedStack {
+    int *loc;  // entries kSharedStack.. (local memory)
+    __device__ __forceinline__ int get(int i) const {
+        return i < kSharedStack ? lt_dyn_smem[i * blockDim.x + threadIdx.x] : loc[i - kSharedStack];
+    }
+    __device__ __forceinline__ void set(int i, int v) {
+        if (i < kSharedStack) lt_dyn_smem[i * blockDim.x + threadIdx.x] = v;
+        else loc[i - kSharedStack] = v;
+    }
+};
+
+template <class St>
+__device__ __forceinline__ void trav_start(Trav &r, St stack, v3 O, v3 D, float tnear, float tfar, bool any,
                                            uint32_t skip_geom) {
     r.O = O;
     r.D = D;
@@ -114,7 +142,7 @@ __device__ __forceinline__ void trav_start(Trav &r, int *stack, v3 O, v3 D, floa
     r.node = 0;
     r.leaf = 0;
     r.sp = 0;
-    stack[0] = kSentinel;
+    stack.set(0, kSentinel);
     r.any = any;
     r.skip_geom = skip_geom;
 }
@@ -130,7 +158,8 @@ __device__ __forceinline__ Geo geo_of(const DevScene &S) { return Geo{S.nodes, S
 
 // Advances the ray until it is finished (r.node == kSentinel) or the warp
 // should refill idle lanes.
-__device__ __forceinline__ void traverse(const Geo &S, Trav &r, int *stack) {
+template <class St>
+__device__ __forceinline__ void traverse(const Geo &S, Trav &r, St stack) {
     while (r.node != kSentinel) {
         while ((unsigned)r.node < (unsigned)kSentinel) {
             const float4 *n = S.nodes + 4 * r.node;
@@ -140,18 +169,18 @@ __device__ __forceinline__ void traverse(const Geo &S, Trav &r, int *stack) {
             bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r.O, r.inv, r.tnear, r.h.t, t1);
             int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
             if (!h0 && !h1) {
-                r.node = stack[r.sp--];
+                r.node = stack.get(r.sp--);
             } else {
                 r.node = h0 ? c0 : c1;
                 if (h0 && h1) {
                     int far = c1;
                     if (t1 < t0) { far = c0; r.node = c1; }
-                    stack[++r.sp] = far;
+                    stack.set(++r.sp, far);
                 }
             }
             if (r.node < 0 && r.leaf >= 0) {  // postpone the first leaf, keep descending
                 r.leaf = r.node;
-                r.node = stack[r.sp--];
+                r.node = stack.get(r.sp--);
             }
             if (!__any_sync(__activemask(), r.leaf >= 0)) break;
         }
@@ -174,7 +203,7 @@ __device__ __forceinline__ void traverse(const Geo &S, Trav &r, int *stack) {
                 }
             }
             r.leaf = r.node;
-            if (r.node < 0) r.node = stack[r.sp--];
+            if (r.node < 0) r.node = stack.get(r.sp--);
         }
         if (__popc(__activemask()) < kFetchThreshold) return;
     }
@@ -338,13 +367,18 @@ __device__ __forceinline__ void traverse8(const Geo &g, Trav8 &r, uint2 *stack) 
 struct Bvh2 {
     using State = Trav;
     using Entry = int;
-    static constexpr int kDepth = kStack;
+    static constexpr int kDepth = kStack - kSharedStack;  // local entries
+    static constexpr int kSharedBytesPerThread = 4 * kSharedStack;
     static constexpr int kMinBlocks256 = 0;  // k_trace register budget: 0 = no minimum (compiler's choice)
     __device__ static Geo geo(const DevScene &S) { return geo_of(S); }
     __device__ static void start(State &r, Entry *st, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip) {
-        trav_start(r, st, O, D, tnear, tfar, any, skip);
+        if (kSharedStack) trav_start(r, SharedStack{st}, O, D, tnear, tfar, any, skip);
+        else trav_start(r, LocalStack{st}, O, D, tnear, tfar, any, skip);
     }
-    __device__ static void run(const Geo &g, State &r, Entry *st) { traverse(g, r, st); }
+    __device__ static void run(const Geo &g, State &r, Entry *st) {
+        if (kSharedStack) traverse(g, r, SharedStack{st});
+        else traverse(g, r, LocalStack{st});
+    }
     __device__ static bool done(const State &r) { return r.node == kSentinel; }
     __device__ static void idle(State &r) { r.node = kSentinel; }
 };
@@ -353,6 +387,7 @@ struct Bvh8 {
     using State = Trav8;
     using Entry = uint2;
     static constexpr int kDepth = kStack8;
+    static constexpr int kSharedBytesPerThread = 0;
     static constexpr int kMinBlocks256 = 0;  // k_trace register budget: 0 = no minimum (compiler's choice)
     __device__ static Geo geo(const DevScene &S) {
         return Geo{S.nodes8, S.tris8, S.tri_geom, S.num_nodes8, S.num_tris};
@@ -876,6 +911,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
         bool regen = false;
         if (done) {
             const FilmPtrs &F = src.film(p.scene);
+            if (!(isfinite(p.color.x) && isfinite(p.color.y) && isfinite(p.color.z)))
+                atomicAdd(&W.counters->nonfinite, 1ull);
             film_add(F, p.pixel, p.color);
             atomicAdd(F.bounces + p.pixel, p.bounces);
             atomicAdd(F.counts + p.pixel, 1u);
@@ -945,7 +982,9 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     if (!is_bsdf) c = ((f * Le) * power_heuristic(lpdf, spdf)) / lpdf;
     else c = ((f * Le) * power_heuristic(spdf, lpdf)) / spdf;
     v3 T = mk(r1.x, r1.y, r1.z);
-    film_add(F, pixel, T * (c * (float)S.num_lights));
+    const v3 add = T * (c * (float)S.num_lights);
+    if (!(isfinite(add.x) && isfinite(add.y) && isfinite(add.z))) atomicAdd(&W.counters->nonfinite, 1ull);
+    film_add(F, pixel, add);
 }
 
 // Path rays of iteration `cur` (closest hit into W.hits) and, in the same
@@ -1054,9 +1093,9 @@ __device__ __forceinline__ Hit trace_all(const DevScene &S, v3 O, v3 D, float tn
     const Geo g = geo_of(S);
     Trav r;
     int stack[kStack];
-    trav_start(r, stack, O, D, tnear, tfar, any, skip_geom);
+    trav_start(r, LocalStack{stack}, O, D, tnear, tfar, any, skip_geom);
     do {
-        traverse(g, r, stack);
+        traverse(g, r, LocalStack{stack});
     } while (r.node != kSentinel);
     return r.h;
 }
@@ -1462,10 +1501,16 @@ __global__ void __launch_bounds__(128) k_diff_adjoint_batch(SceneTable *t) {
 }  // namespace
 
 template <class F>
-static int blocks_for(F kernel, int threads, int sms) {
+static int blocks_for(F kernel, int threads, int sms, size_t smem = 0) {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem);
     return sms * (b > 0 ? b : 1);
+}
+
+// dynamic shared memory of a traversal kernel with `threads` threads per block
+template <class B>
+static size_t trav_smem(int threads) {
+    return (size_t)B::kSharedBytesPerThread * (size_t)threads;
 }
 
 void query_launch_shape(int device, bool batch, LaunchShape *out) {
@@ -1474,16 +1519,18 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
     const int sms = prop.multiProcessorCount;
     out->sms = sms;
     const bool w8 = out->bvh_width == 8;
+    const int tt = out->trace_threads;
     if (batch) {
-        out->trace_blocks = w8 ? blocks_for(k_trace<ManyScenes, Bvh8>, out->trace_threads, sms)
-                               : blocks_for(k_trace<ManyScenes, Bvh2>, out->trace_threads, sms);
+        out->trace_blocks = w8 ? blocks_for(k_trace<ManyScenes, Bvh8>, tt, sms, trav_smem<Bvh8>(tt))
+                               : blocks_for(k_trace<ManyScenes, Bvh2>, tt, sms, trav_smem<Bvh2>(tt));
         out->shade_blocks = blocks_for(k_shade<ManyScenes>, out->shade_threads, sms);
     } else {
-        out->trace_blocks = w8 ? blocks_for(k_trace<OneScene, Bvh8>, out->trace_threads, sms)
-                               : blocks_for(k_trace<OneScene, Bvh2>, out->trace_threads, sms);
+        out->trace_blocks = w8 ? blocks_for(k_trace<OneScene, Bvh8>, tt, sms, trav_smem<Bvh8>(tt))
+                               : blocks_for(k_trace<OneScene, Bvh2>, tt, sms, trav_smem<Bvh2>(tt));
         out->shade_blocks = blocks_for(k_shade<OneScene>, out->shade_threads, sms);
     }
-    out->isect_blocks = w8 ? blocks_for(k_intersect<Bvh8>, 128, sms) : blocks_for(k_intersect<Bvh2>, 128, sms);
+    out->isect_blocks = w8 ? blocks_for(k_intersect<Bvh8>, 128, sms, trav_smem<Bvh8>(128))
+                           : blocks_for(k_intersect<Bvh2>, 128, sms, trav_smem<Bvh2>(128));
     out->diff_blocks = blocks_for(k_diff_adjoint, 128, sms);
     out->diff_fwd_batch_blocks = blocks_for(k_diff_forward_batch, 128, sms);
     out->diff_adj_batch_blocks = blocks_for(k_diff_adjoint_batch, 128, sms);
@@ -1518,8 +1565,10 @@ cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits
         if (e != cudaSuccess) return e;
         unsigned long long need = (m + 127) / 128;
         int blocks = (int)(need < (unsigned long long)ls.isect_blocks ? need : ls.isect_blocks);
-        if (ls.bvh_width == 8) k_intersect<Bvh8><<<blocks, 128, 0, st>>>(s, rays + 2 * off, hits + off, m, fetch);
-        else k_intersect<Bvh2><<<blocks, 128, 0, st>>>(s, rays + 2 * off, hits + off, m, fetch);
+        if (ls.bvh_width == 8)
+            k_intersect<Bvh8><<<blocks, 128, trav_smem<Bvh8>(128), st>>>(s, rays + 2 * off, hits + off, m, fetch);
+        else
+            k_intersect<Bvh2><<<blocks, 128, trav_smem<Bvh2>(128), st>>>(s, rays + 2 * off, hits + off, m, fetch);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -1536,8 +1585,9 @@ static cudaError_t stage(int stage, const Src &src, const Wavefront &w, int cur,
                          cudaStream_t st) {
     const bool w8 = ls.bvh_width == 8;
     if (stage == kStageTrace) {
-        if (w8) k_trace<Src, Bvh8><<<ls.trace_blocks, ls.trace_threads, 0, st>>>(src, w, cur);
-        else k_trace<Src, Bvh2><<<ls.trace_blocks, ls.trace_threads, 0, st>>>(src, w, cur);
+        const int tt = ls.trace_threads;
+        if (w8) k_trace<Src, Bvh8><<<ls.trace_blocks, tt, trav_smem<Bvh8>(tt), st>>>(src, w, cur);
+        else k_trace<Src, Bvh2><<<ls.trace_blocks, tt, trav_smem<Bvh2>(tt), st>>>(src, w, cur);
     } else {
         k_shade<Src><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(src, w, cur);
     }

@@ -47,6 +47,24 @@ class FrameBuffer:
         (visualizer.cpp:361-364)."""
         return self.ColorData / self.ColorSampleCount.clamp(min=1).unsqueeze(-1).to(torch.float32)
 
+    def save(self, path: str, frame_number: int) -> None:
+        """Checkpoint: colour sums, bounce sums, sample counts and the next frame
+        number (an .npz file). The reference keeps exactly this state between
+        RenderFrame calls (integrator.h:38-41)."""
+        np.savez(path, rgb=self.ColorData.cpu().numpy(), bounces=self.Bounces.cpu().numpy(),
+                 counts=self.ColorSampleCount.cpu().numpy(), frame_number=np.int64(frame_number))
+
+    @staticmethod
+    def load(path: str, device: int | str | torch.device = "cuda"):
+        """(FrameBuffer, next frame number) from a checkpoint written by save()."""
+        z = np.load(path)
+        h, w = z["counts"].shape
+        fb = FrameBuffer(w, h, device)
+        fb.ColorData.copy_(torch.from_numpy(z["rgb"]))
+        fb.Bounces.copy_(torch.from_numpy(z["bounces"]))
+        fb.ColorSampleCount.copy_(torch.from_numpy(z["counts"]))
+        return fb, int(z["frame_number"])
+
 
 class Scene:
     """Scene (source/core/scene/scene.h:33-98) for the GPU integrator."""
@@ -89,6 +107,17 @@ class Integrator:
 
     def stats(self):
         return self.scene.ctx.stats()
+
+    def checkpoint(self, path: str) -> None:
+        """Saves the film and the frame number. Because every sample's sampler is
+        keyed by (pixel, frame), resume() + RenderFrame(n) continues with exactly
+        the samples an uninterrupted render would have taken."""
+        self.frame_buffer.save(path, self.frame_number)
+
+    @staticmethod
+    def resume(scene: "Scene", path: str, max_depth: int = 1500, rr_depth: int = 3) -> "Integrator":
+        fb, frame = FrameBuffer.load(path, torch.device(f"cuda:{scene.device}"))
+        return Integrator(scene, fb, max_depth=max_depth, rr_depth=rr_depth, first_frame=frame)
 
 
 def render_host(ctx: Context, width: int, height: int, spp: int, first_frame: int = 0, max_depth: int = 1500,

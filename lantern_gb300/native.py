@@ -25,7 +25,8 @@ SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error",
            "lt_scene_create", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
-           "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load"]
+           "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load",
+           "lt_debug_fail_allocations"]
 BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 MAX_BATCH = 2048  # LT_MAX_BATCH
@@ -95,7 +96,7 @@ class RenderStats(C.Structure):
     _fields_ = [("main_rays", C.c_uint64), ("light_rays", C.c_uint64), ("bsdf_rays", C.c_uint64),
                 ("samples", C.c_uint64), ("iterations", C.c_uint32), ("kernel_launches", C.c_uint32),
                 ("gpu_ms", C.c_float), ("trace_ms", C.c_float), ("shade_ms", C.c_float),
-                ("light_traversals", C.c_uint64)]
+                ("light_traversals", C.c_uint64), ("nonfinite_samples", C.c_uint64)]
 
 
 class Tuning(C.Structure):
@@ -154,6 +155,8 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_resolve.argtypes = [p, C.POINTER(Film), C.c_int32, C.c_float, p, p, C.POINTER(SppRange)]
         L.lt_image_load.argtypes = [C.c_char_p, p, C.c_size_t, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                     C.POINTER(C.c_uint32)]
+        L.lt_debug_fail_allocations.argtypes = [C.c_uint32]
+        L.lt_debug_fail_allocations.restype = None
         _lib = L
         return L
 

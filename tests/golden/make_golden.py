@@ -10,6 +10,8 @@ comes out of the reference's own code (liblantern_ref.so):
   nine-sphere scene;
 * reference_film_tiny.npz -- both swap films of 3 RenderFrame calls of the
   three-material scene at 24x16, max depth 8 (integrator.cpp);
+* reference_ico_images.npz, reference_textured_images.npz -- the same pairs for the
+  1.3M-triangle icosphere scene and the textured / procedural scene;
 * reference_c0_images.npz -- the nine-sphere scene (config 0: 256x256, 16 spp,
   max depth 8, roulette after bounce 3) rendered twice with independent
   streams (frames 0-15 and 1000000-1000015), stored as float16 images
@@ -97,10 +99,25 @@ def c0_images():
                512, 32, "reference_c2r_images.npz")
 
 
+def more_images():
+    # config 1's scene (1,310,724 triangles; Lambert, mirror, dielectric meshes) at
+    # 160x160, 64 spp, max depth 10
+    image_pair(S.displaced_icosphere_scene(width=160, height=160, name="golden_ico"), 64, 10,
+               "reference_ico_images.npz")
+    # uv and image albedo textures, grid and geosphere primitives: 96x96, 64 spp, depth 8
+    image_pair(S.textured_scene(os.path.join(SCENES, "golden_textures"), width=96, height=96,
+                                name="golden_textured"), 64, 8, "reference_textured_images.npz")
+
+
 if __name__ == "__main__":
+    import sys
     O.build_reference()
+    if "--more" in sys.argv:  # only the fixtures added last
+        more_images()
+        sys.exit(0)
     blocks()
     film_tiny()
     c0_images()
+    more_images()
     for f in sorted(os.listdir(OUT)):
         print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -41,11 +41,19 @@ def _rmse(x, y):
     (lambda: S.tiny_scene(width=96, height=96, name="golden_tiny96"), 64, 12, "reference_tiny_images.npz"),
     (lambda: S.medium_sphere_scene(width=128, height=128, reference_expressible=True, name="golden_c2r"),
      512, 32, "reference_c2r_images.npz"),
+    (lambda: S.displaced_icosphere_scene(width=160, height=160, name="golden_ico"), 64, 10,
+     "reference_ico_images.npz"),
+    ("textured", 64, 8, "reference_textured_images.npz"),
 ])
 def test_image_matches_reference_statistically(scene_dir, make, spp, depth, fixture):
     g = np.load(os.path.join(GOLDEN, fixture))
     a, b = g["a"].astype(np.float64), g["b"].astype(np.float64)
-    img = _render(make().write(scene_dir), spp, depth)
+    if make == "textured":
+        scene = S.textured_scene(os.path.join(scene_dir, "golden_textures"), width=96, height=96,
+                                 name="golden_textured")
+    else:
+        scene = make()
+    img = _render(scene.write(scene_dir), spp, depth)
     assert np.all(np.isfinite(img))
     ma = 0.5 * (a.mean((0, 1)) + b.mean((0, 1)))
     assert np.all(np.abs(img.mean((0, 1)) - ma) <= 0.01 * ma), (img.mean((0, 1)), ma)
