@@ -105,6 +105,9 @@ typedef struct lt_mesh_desc {
     float emission_color[3];  /* AreaLight: radiance = color * power / (pi * area) */
     float radiant_power;
     const float *texcoords;   /* num_vertices * 2, or NULL (the hit's texture coordinate is then (0, 0)) */
+    const float *transform;   /* 16 floats, row-major: positions become transform * (p, 1) as the
+                               * reference's AddLMF / AddMesh compute it (scene.cpp:456-461,517-522);
+                               * normals are used as given (scene.cpp:481-482,560). NULL = identity */
 } lt_mesh_desc;
 
 typedef struct lt_camera_desc {

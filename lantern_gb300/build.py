@@ -28,7 +28,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompile
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
              "-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["lt_kernels.cu", "lt_bvh_gpu.cu", "lt_noalloc.cu", "lt_resolve.cu"]
+CU_SOURCES = ["lt_kernels.cu", "lt_bvh_gpu.cu", "lt_noalloc.cu", "lt_resolve.cu", "lt_setup.cu"]
 CPP_SOURCES = ["lt_api.cpp", "lt_scene.cpp", "lt_json.cpp", "lt_bvh8.cpp", "lt_image.cpp"]
 
 

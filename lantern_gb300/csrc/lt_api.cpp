@@ -26,6 +26,7 @@
 #include "lt_device.h"
 #include "lt_bvh_gpu.h"
 #include "lt_scene.h"
+#include "lt_setup.h"
 
 using namespace lt;
 
@@ -243,6 +244,30 @@ lt_status lt_sync(lt_ctx *c) {
 
 }  // extern "C"
 
+// Temporary device buffers of one call, freed when it returns (after the
+// call's work on `stream`, which may still read them, has finished).
+struct Temp {
+    cudaStream_t stream;
+    std::vector<void *> ptrs;
+    cudaError_t alloc(void **p, size_t bytes) {
+        cudaError_t e = dev_malloc(p, bytes);
+        if (e == cudaSuccess) ptrs.push_back(*p);
+        return e;
+    }
+    ~Temp() {
+        if (!ptrs.empty()) cudaStreamSynchronize(stream);
+        for (void *p : ptrs) cudaFree(p);
+    }
+};
+
+// A device buffer owned by the context's scene.
+static lt_status scene_alloc(lt_ctx *c, size_t bytes, void **p) {
+    CUDA_TRY(c, dev_malloc(p, bytes));
+    c->scene_allocs.push_back(*p);
+    c->scene_bytes += bytes;
+    return LT_OK;
+}
+
 template <typename T>
 static lt_status upload(lt_ctx *c, const std::vector<T> &v, const T **dst) {
     size_t bytes = v.size() * sizeof(T);
@@ -300,21 +325,72 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     free_scene(c);
+    size_t ntri = 0, nvert = 0;
+    for (uint32_t g = 0; g < desc->num_meshes; ++g) {
+        ntri += desc->meshes[g].num_triangles;
+        nvert += desc->meshes[g].num_vertices;
+    }
+    // GPU builder: transform and triangle setup on the device as well
+    const bool gpu_setup = c->bvh_builder == LT_BVH_GPU && ntri > 4;
     std::string err;
-    lt_status st = build_host_scene(desc, &c->host, &err);
+    lt_status st = build_host_scene(desc, &c->host, &err, !gpu_setup);
     if (st != LT_OK) return fail(c, st, "%s", err.c_str());
     HostScene &h = c->host;
     DevScene &d = c->dev;
-    const size_t ntri = h.tri_geom.size();
-    if (c->bvh_builder == LT_BVH_GPU && ntri > 4) {
+    if (gpu_setup) {
+        // raw mesh arrays -> device, then transform + triangle setup (lt_setup.cu)
+        Temp tmp{c->stream, {}};
+        float *d_pos = nullptr, *d_tri = nullptr, *d_nrm = nullptr, *d_tex = nullptr;
+        uint32_t *d_idx = nullptr, *d_vidx = nullptr;
+        MeshSetup *d_meshes = nullptr;
+        CUDA_TRY(c, tmp.alloc((void **)&d_pos, nvert * 12 + 16));
+        CUDA_TRY(c, tmp.alloc((void **)&d_idx, ntri * 12));
+        CUDA_TRY(c, tmp.alloc((void **)&d_tri, ntri * 36));
+        CUDA_TRY(c, tmp.alloc((void **)&d_meshes, desc->num_meshes * sizeof(MeshSetup) + 16));
+        if ((st = scene_alloc(c, nvert * 12 + 16, (void **)&d_nrm)) != LT_OK) return st;
+        if ((st = scene_alloc(c, nvert * 8 + 16, (void **)&d_tex)) != LT_OK) return st;
+        if ((st = scene_alloc(c, ntri * 12, (void **)&d_vidx)) != LT_OK) return st;
+        std::vector<MeshSetup> ms(desc->num_meshes);
+        size_t vb = 0, tb = 0;
+        for (uint32_t g = 0; g < desc->num_meshes; ++g) {
+            const lt_mesh_desc &m = desc->meshes[g];
+            MeshSetup &M = ms[g];
+            memset(&M, 0, sizeof M);
+            M.vbase = (uint32_t)vb;
+            M.tbase = (uint32_t)tb;
+            M.nverts = m.num_vertices;
+            M.ntris = m.num_triangles;
+            if (m.transform) {
+                M.has_transform = 1;
+                memcpy(M.m, m.transform, 12 * sizeof(float));
+            }
+            const size_t nv = m.num_vertices, nt = m.num_triangles;
+            if (nv) {
+                CUDA_TRY(c, cudaMemcpyAsync(d_pos + 3 * vb, m.positions, nv * 12, cudaMemcpyHostToDevice, c->stream));
+                if (m.normals)
+                    CUDA_TRY(c, cudaMemcpyAsync(d_nrm + 3 * vb, m.normals, nv * 12, cudaMemcpyHostToDevice, c->stream));
+                else
+                    CUDA_TRY(c, cudaMemsetAsync(d_nrm + 3 * vb, 0, nv * 12, c->stream));
+                if (m.texcoords)
+                    CUDA_TRY(c, cudaMemcpyAsync(d_tex + 2 * vb, m.texcoords, nv * 8, cudaMemcpyHostToDevice, c->stream));
+                else
+                    CUDA_TRY(c, cudaMemsetAsync(d_tex + 2 * vb, 0, nv * 8, c->stream));
+            }
+            if (nt) CUDA_TRY(c, cudaMemcpyAsync(d_idx + 3 * tb, m.indices, nt * 12, cudaMemcpyHostToDevice, c->stream));
+            vb += nv;
+            tb += nt;
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(d_meshes, ms.data(), ms.size() * sizeof(MeshSetup), cudaMemcpyHostToDevice,
+                                    c->stream));
+        CUDA_TRY(c, setup_triangles_gpu(d_pos, d_idx, d_meshes, desc->num_meshes, (uint32_t)nvert, (uint32_t)ntri,
+                                        d_tri, d_vidx, c->stream));
+        d.vnormal = d_nrm;
+        d.vtex = d_tex;
+        d.tri_vidx = d_vidx;
         // binned-SAH build on the device from the triangles in global order
-        const float *tri = nullptr;
-        if ((st = upload(c, h.tri_v0e1e2, &tri)) != LT_OK) return st;
         GpuBvh gb;
-        cudaError_t e = build_bvh_gpu(tri, (uint32_t)ntri, &gb, c->stream);
-        cudaFree((void *)tri);
-        c->scene_allocs.pop_back();
-        c->scene_bytes -= h.tri_v0e1e2.size() * sizeof(float);
+        cudaError_t e = build_bvh_gpu(d_tri, (uint32_t)ntri, &gb, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess)
             return fail(c, e == cudaErrorMemoryAllocation ? LT_ERR_OOM : LT_ERR_CUDA, "GPU BVH build: %s",
                         cudaGetErrorString(e));
@@ -345,9 +421,11 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
         return fail(c, LT_ERR_UNSUPPORTED, "%zu lights / %zu media: at most %u and %u", h.lights.size(),
                     h.media.size(), kMaxLights, kMaxMedia);
     if ((st = upload(c, h.tri_geom, &d.tri_geom)) != LT_OK) return st;
-    if ((st = upload(c, h.tri_vidx, &d.tri_vidx)) != LT_OK) return st;
-    if ((st = upload(c, h.vnormal, &d.vnormal)) != LT_OK) return st;
-    if ((st = upload(c, h.vtex, &d.vtex)) != LT_OK) return st;
+    if (!gpu_setup) {
+        if ((st = upload(c, h.tri_vidx, &d.tri_vidx)) != LT_OK) return st;
+        if ((st = upload(c, h.vnormal, &d.vnormal)) != LT_OK) return st;
+        if ((st = upload(c, h.vtex, &d.vtex)) != LT_OK) return st;
+    }
     if ((st = upload(c, h.texels, &d.texels)) != LT_OK) return st;
     if ((st = upload(c, h.images, &d.images)) != LT_OK) return st;
     if ((st = upload(c, h.geoms, &d.geoms)) != LT_OK) return st;

@@ -500,17 +500,12 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
                 return LT_ERR_UNSUPPORTED;
             }
             const size_t nv = pos.size() / 3;
-            if (const Json *t = p.get("transform")) {
+            std::vector<float> xform;
+            if (const Json *t = p.get("transform")) {  // applied by lt_scene_create (transform_points)
                 if (t->type != Json::Array || t->arr.size() != 16) { *err = "transform needs 16 numbers"; return LT_ERR_PARSE; }
-                float m[16];
+                xform.resize(16);
                 for (int k = 0; k < 16; ++k)
-                    if (!num(&t->arr[k], &m[k])) { *err = "transform needs 16 numbers"; return LT_ERR_PARSE; }
-                // transform * float3a(p, 1) (scene.cpp:517-522; linearspace4.h:43-47,165)
-                for (size_t v = 0; v < nv; ++v) {
-                    float x = pos[3 * v], y = pos[3 * v + 1], z = pos[3 * v + 2];
-                    for (int r = 0; r < 3; ++r)
-                        pos[3 * v + r] = ((x * m[4 * r] + y * m[4 * r + 1]) + z * m[4 * r + 2]) + 1.0f * m[4 * r + 3];
-                }
+                    if (!num(&t->arr[k], &xform[k])) { *err = "transform needs 16 numbers"; return LT_ERR_PARSE; }
             }
             const Json *mn = p.get("material");
             auto mi = mn ? material_ix.find(mn->str) : material_ix.end();
@@ -539,6 +534,10 @@ lt_status load_scene_json(const char *path, lt_scene_desc *desc, JsonSceneStorag
             if (tex.size() == nv * 2 && nv) {
                 st->floats.push_back(std::move(tex));
                 md.texcoords = st->floats.back().data();
+            }
+            if (!xform.empty()) {
+                st->floats.push_back(std::move(xform));
+                md.transform = st->floats.back().data();
             }
             st->uints.push_back(std::move(idx));
             md.indices = st->uints.back().data();

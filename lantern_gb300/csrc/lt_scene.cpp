@@ -38,7 +38,17 @@ static void bounding_sphere(const float *p, uint32_t n, float out[4]) {
     out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = r;
 }
 
-lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *err) {
+// transform * float3a(p, 1) (scene.cpp:456-461, 517-522; linearspace4.h:43-47,165):
+// row r = ((x*m[4r] + y*m[4r+1]) + z*m[4r+2]) + 1*m[4r+3].
+void transform_points(const float *m, const float *in, uint32_t n, float *out) {
+    for (uint32_t v = 0; v < n; ++v) {
+        const float x = in[3 * (size_t)v], y = in[3 * (size_t)v + 1], z = in[3 * (size_t)v + 2];
+        for (int r = 0; r < 3; ++r)
+            out[3 * (size_t)v + r] = ((x * m[4 * r] + y * m[4 * r + 1]) + z * m[4 * r + 2]) + 1.0f * m[4 * r + 3];
+    }
+}
+
+lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *err, bool host_setup) {
     const lt_camera_desc &cd = d->camera;
     if (cd.width == 0 || cd.height == 0) {
         *err = "camera width and height must be positive";
@@ -127,12 +137,20 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
     s->geoms.clear();
     s->lights.clear();
     s->light_tris.clear();
-    s->tri_v0e1e2.assign(ntri * 9, 0.0f);
     s->tri_geom.assign(ntri, 0);
-    s->tri_vidx.assign(ntri * 3, 0);
-    s->vnormal.assign(nvert * 3, 0.0f);
-    s->vtex.assign(nvert * 2, 0.0f);
+    if (host_setup) {
+        s->tri_v0e1e2.assign(ntri * 9, 0.0f);
+        s->tri_vidx.assign(ntri * 3, 0);
+        s->vnormal.assign(nvert * 3, 0.0f);
+        s->vtex.assign(nvert * 2, 0.0f);
+    } else {  // the device builds these (lt_setup.cu)
+        s->tri_v0e1e2.clear();
+        s->tri_vidx.clear();
+        s->vnormal.clear();
+        s->vtex.clear();
+    }
     size_t t0 = 0, vbase = 0;
+    std::vector<float> moved;
     for (uint32_t g = 0; g < d->num_meshes; ++g) {
         const lt_mesh_desc &m = d->meshes[g];
         if (m.material < 0 || m.material >= (int32_t)d->num_materials) {
@@ -143,54 +161,65 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
             *err = "mesh arrays missing";
             return LT_ERR_INVALID;
         }
+        for (size_t k = 0; k < 3 * (size_t)m.num_triangles; ++k)
+            if (m.indices[k] >= m.num_vertices) {
+                *err = "triangle index out of range in mesh " + std::to_string(g);
+                return LT_ERR_INVALID;
+            }
         GeomInfo gi;
         gi.material = m.material;
         gi.light = -1;
         gi.has_normals = m.normals != nullptr;
         gi.has_texcoords = m.texcoords != nullptr;
         gi.first_tri = (uint32_t)t0;
-        float area = 0.0f;
-        for (uint32_t t = 0; t < m.num_triangles; ++t) {
-            uint32_t i0 = m.indices[3 * t], i1 = m.indices[3 * t + 1], i2 = m.indices[3 * t + 2];
-            if (i0 >= m.num_vertices || i1 >= m.num_vertices || i2 >= m.num_vertices) {
-                *err = "triangle index out of range in mesh " + std::to_string(g);
-                return LT_ERR_INVALID;
-            }
-            v3 a = ld3(m.positions + 3 * (size_t)i0);
-            v3 b = ld3(m.positions + 3 * (size_t)i1);
-            v3 c = ld3(m.positions + 3 * (size_t)i2);
-            float *dst = &s->tri_v0e1e2[9 * (t0 + t)];
-            v3 e1 = a - b, e2 = c - a;
-            dst[0] = a.x; dst[1] = a.y; dst[2] = a.z;
-            dst[3] = e1.x; dst[4] = e1.y; dst[5] = e1.z;
-            dst[6] = e2.x; dst[7] = e2.y; dst[8] = e2.z;
-            s->tri_geom[t0 + t] = g;
-            s->tri_vidx[3 * (t0 + t)] = (uint32_t)(vbase + i0);
-            s->tri_vidx[3 * (t0 + t) + 1] = (uint32_t)(vbase + i1);
-            s->tri_vidx[3 * (t0 + t) + 2] = (uint32_t)(vbase + i2);
-            area += 0.5f * length(cross(a - b, a - c));  // scene.cpp:527-534
+        for (uint32_t t = 0; t < m.num_triangles; ++t) s->tri_geom[t0 + t] = g;
+        // world-space positions on the host: every mesh for a host setup, else
+        // only the lights' (area, bounding sphere, light triangles)
+        const float *pos = m.positions;
+        if (m.transform && (host_setup || m.emissive)) {
+            moved.resize(3 * (size_t)m.num_vertices);
+            transform_points(m.transform, m.positions, m.num_vertices, moved.data());
+            pos = moved.data();
         }
-        if (m.normals)
-            memcpy(&s->vnormal[3 * vbase], m.normals, (size_t)m.num_vertices * 3 * sizeof(float));
-        if (m.texcoords)
-            memcpy(&s->vtex[2 * vbase], m.texcoords, (size_t)m.num_vertices * 2 * sizeof(float));
+        if (host_setup) {
+            for (uint32_t t = 0; t < m.num_triangles; ++t) {
+                uint32_t i0 = m.indices[3 * t], i1 = m.indices[3 * t + 1], i2 = m.indices[3 * t + 2];
+                v3 a = ld3(pos + 3 * (size_t)i0), b = ld3(pos + 3 * (size_t)i1), c = ld3(pos + 3 * (size_t)i2);
+                float *dst = &s->tri_v0e1e2[9 * (t0 + t)];
+                v3 e1 = a - b, e2 = c - a;
+                dst[0] = a.x; dst[1] = a.y; dst[2] = a.z;
+                dst[3] = e1.x; dst[4] = e1.y; dst[5] = e1.z;
+                dst[6] = e2.x; dst[7] = e2.y; dst[8] = e2.z;
+                s->tri_vidx[3 * (t0 + t)] = (uint32_t)(vbase + i0);
+                s->tri_vidx[3 * (t0 + t) + 1] = (uint32_t)(vbase + i1);
+                s->tri_vidx[3 * (t0 + t) + 2] = (uint32_t)(vbase + i2);
+            }
+            if (m.normals)
+                memcpy(&s->vnormal[3 * vbase], m.normals, (size_t)m.num_vertices * 3 * sizeof(float));
+            if (m.texcoords)
+                memcpy(&s->vtex[2 * vbase], m.texcoords, (size_t)m.num_vertices * 2 * sizeof(float));
+        }
         if (m.emissive) {
             LightInfo li;
             memset(&li, 0, sizeof li);
             li.geom = (int32_t)g;
-            li.area = area;
-            if (m.num_vertices) bounding_sphere(m.positions, m.num_vertices, li.sphere);
-            // AreaLight ctor (area_light.h:16-21): color * radiantPower * (float)M_1_PI / area
-            v3 rad = ((ld3(m.emission_color) * m.radiant_power) * kInvPi) / area;
-            li.radiance[0] = rad.x; li.radiance[1] = rad.y; li.radiance[2] = rad.z;
+            float area = 0.0f;
             li.tri_first = (uint32_t)(s->light_tris.size() / 12);
             li.tri_count = m.num_triangles;
             for (uint32_t t = 0; t < m.num_triangles; ++t) {
-                const float *d = &s->tri_v0e1e2[9 * (t0 + t)];
-                const float row[12] = {d[0], d[1], d[2], bits_to_float((uint32_t)(t0 + t)),
-                                       d[3], d[4], d[5], 0.0f, d[6], d[7], d[8], 0.0f};
+                uint32_t i0 = m.indices[3 * t], i1 = m.indices[3 * t + 1], i2 = m.indices[3 * t + 2];
+                v3 a = ld3(pos + 3 * (size_t)i0), b = ld3(pos + 3 * (size_t)i1), c = ld3(pos + 3 * (size_t)i2);
+                area += 0.5f * length(cross(a - b, a - c));  // scene.cpp:527-534
+                v3 e1 = a - b, e2 = c - a;
+                const float row[12] = {a.x, a.y, a.z, bits_to_float((uint32_t)(t0 + t)),
+                                       e1.x, e1.y, e1.z, 0.0f, e2.x, e2.y, e2.z, 0.0f};
                 s->light_tris.insert(s->light_tris.end(), row, row + 12);
             }
+            li.area = area;
+            if (m.num_vertices) bounding_sphere(pos, m.num_vertices, li.sphere);
+            // AreaLight ctor (area_light.h:16-21): color * radiantPower * (float)M_1_PI / area
+            v3 rad = ((ld3(m.emission_color) * m.radiant_power) * kInvPi) / area;
+            li.radiance[0] = rad.x; li.radiance[1] = rad.y; li.radiance[2] = rad.z;
             gi.light = (int32_t)s->lights.size();
             s->lights.push_back(li);
         }

@@ -116,7 +116,14 @@ struct HostScene {
 };
 
 // Fills `out` from a scene description. Returns LT_OK or an error with `err`.
-lt_status build_host_scene(const lt_scene_desc *desc, HostScene *out, std::string *err);
+// With host_setup false the per-triangle arrays (tri_v0e1e2, tri_vidx) and the
+// vertex arrays (vnormal, vtex) stay empty: the device builds them
+// (setup_triangles_gpu); lights, tables and tri_geom are always filled.
+lt_status build_host_scene(const lt_scene_desc *desc, HostScene *out, std::string *err, bool host_setup = true);
+
+// transform * (p, 1) for n points (a row-major 4x4 matrix, float arithmetic of
+// the reference's transform).
+void transform_points(const float *m, const float *in, uint32_t n, float *out);
 
 // Binned-SAH BVH2 (32 bins, at most 4 triangles per leaf) over the scene's
 // triangles; fills nodes and leaf_tris.

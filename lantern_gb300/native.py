@@ -60,7 +60,7 @@ class MeshDesc(C.Structure):
                 ("indices", C.POINTER(C.c_uint32)), ("num_vertices", C.c_uint32),
                 ("num_triangles", C.c_uint32), ("material", C.c_int32), ("emissive", C.c_int32),
                 ("emission_color", C.c_float * 3), ("radiant_power", C.c_float),
-                ("texcoords", C.POINTER(C.c_float))]
+                ("texcoords", C.POINTER(C.c_float)), ("transform", C.POINTER(C.c_float))]
 
 
 class CameraDesc(C.Structure):

@@ -192,9 +192,11 @@ def test_errors_are_reported(ctx, scene_dir, tmp_path):
 @pytest.mark.parametrize("make", [
     lambda: S.nine_spheres(width=64, height=64, name="isect_nine"),
     lambda: S.displaced_icosphere_scene(width=64, height=64, levels=6, name="isect_ico6"),
+    lambda: S.procedural_scene(name="isect_procedural_build"),
 ])
 def test_gpu_bvh_build_matches_host_build(scene_dir, make):
-    """The device builder makes the host builder's splits: same node count and
+    """The device path (triangle setup and mesh transforms in lt_setup.cu, then
+    the device builder) makes the host path's splits: same node count and
     depth, and closest hits identical to the oracle's."""
     from lantern_gb300.native import BVH_GPU, BVH_HOST
     path = make().write(scene_dir)
