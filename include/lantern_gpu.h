@@ -289,7 +289,9 @@ lt_status lt_set_tuning(lt_ctx *ctx, const lt_tuning *t);
  * - films must be on the device (on_device = 1), of each camera's size, and
  *   must not overlap;
  * - n <= LT_MAX_BATCH; each scene may have at most 1,048,576 lights and 8,190 media;
- * - returns after the batch has finished (the film writes are complete). */
+ * - returns after the batch has finished (the film writes are complete);
+ * - the scene contexts must not be in use by other threads during the call
+ *   (with bvh_width 8 the call builds their 8-wide BVHs on first use). */
 #define LT_MAX_BATCH 2048
 lt_status lt_render_batch(lt_ctx *ctx, lt_ctx *const *scenes, const lt_render_params *params, lt_film *films,
                           uint32_t n);
