@@ -212,6 +212,8 @@ static int run_case(const char *name, std::vector<float> P, std::vector<uint32_t
         lo[k % 3] = fminf(lo[k % 3], P[k]);
         hi[k % 3] = fmaxf(hi[k % 3], P[k]);
     }
+    if (P.empty())  // rays through the unit box around the origin
+        for (int c = 0; c < 3; ++c) { lo[c] = -1.0f; hi[c] = 1.0f; }
     std::mt19937 rng(2);
     std::uniform_real_distribution<float> u01(0.0f, 1.0f);
     std::normal_distribution<float> nd(0.0f, 1.0f);
@@ -267,6 +269,9 @@ int main() {
         run_case("one", P, I, 500);
         I = {0, 1, 2, 1, 2, 3, 2, 3, 4, 3, 4, 5, 0, 4, 5};
         run_case("five", P, I, 500);
+    }
+    {  // empty: no triangles at all (every ray misses)
+        run_case("empty", {}, {}, 200);
     }
     {  // flat: all triangles in one plane (zero extent on an axis)
         std::vector<float> P;
