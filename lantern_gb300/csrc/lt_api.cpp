@@ -493,7 +493,6 @@ static size_t carve_wave(char *base, uint32_t cap, Wavefront *w) {
         s.pixel = (uint32_t *)take(4 * P);
         s.frame = (uint32_t *)take(4 * P);
         s.T = (float *)take(12 * P);
-        s.color = (float *)take(12 * P);
         s.bounces = (uint32_t *)take(4 * P);
         s.flags = (uint32_t *)take(4 * P);
         s.iori = (float *)take(4 * P);
@@ -522,7 +521,7 @@ static lt_status ensure_wave(lt_ctx *c, uint32_t cap) {
 }
 
 // Paths in flight for `total` work items: the tuning's count, else 2M path
-// slots (~650 MB), and never more than the work.
+// slots (~600 MB), and never more than the work.
 static uint32_t capacity_for(const lt_ctx *c, unsigned long long total) {
     const unsigned long long cap = c->tuning.paths_in_flight ? c->tuning.paths_in_flight : 1ull << 21;
     return (uint32_t)(total < cap ? total : cap);

@@ -44,7 +44,6 @@ struct PathState {
     uint32_t *pixel;
     uint32_t *frame;
     float *T;          // throughput, 3 planes of capacity
-    float *color;      // accumulated radiance, 3 planes
     uint32_t *bounces;
     uint32_t *flags;   // bits 0-7 sampled lobe, bits 8-23 medium index + 1
     float *iori;

@@ -493,7 +493,7 @@ __device__ __forceinline__ unsigned long long warp_reserve64(unsigned long long 
 struct Path {
     Pcg rng;
     uint32_t pixel, frame;
-    v3 T, color;
+    v3 T;
     uint32_t bounces, lobe;
     int medium;
     float iori;
@@ -523,7 +523,6 @@ __device__ __forceinline__ void start_path(const DevScene &S, const RenderArgs &
     org = S.cam.origin;
     tnear = 0.0f;
     p.T = mk(1.0f, 1.0f, 1.0f);
-    p.color = mk(0.0f, 0.0f, 0.0f);
     p.bounces = 0;
     p.lobe = kLobeNull;
     p.medium = -1;
@@ -536,7 +535,6 @@ __device__ __forceinline__ void store_path(const PathState &ps, uint32_t cap, ui
     ps.pixel[slot] = p.pixel;
     ps.frame[slot] = p.frame;
     ps.T[slot] = p.T.x; ps.T[cap + slot] = p.T.y; ps.T[2 * cap + slot] = p.T.z;
-    ps.color[slot] = p.color.x; ps.color[cap + slot] = p.color.y; ps.color[2 * cap + slot] = p.color.z;
     ps.bounces[slot] = p.bounces;
     ps.flags[slot] = p.lobe | ((uint32_t)(p.medium + 1) << kFlagMediumShift) | (p.scene << kFlagSceneShift);
     ps.iori[slot] = p.iori;
@@ -548,7 +546,6 @@ __device__ __forceinline__ void load_path(const PathState &ps, uint32_t cap, uin
     p.frame = ps.frame[slot];
     p.rng.inc = (uint64_t)p.frame | 1u;
     p.T = mk(ps.T[slot], ps.T[cap + slot], ps.T[2 * cap + slot]);
-    p.color = mk(ps.color[slot], ps.color[cap + slot], ps.color[2 * cap + slot]);
     p.bounces = ps.bounces[slot];
     uint32_t fl = ps.flags[slot];
     p.lobe = fl & 0xFFu;
@@ -623,6 +620,13 @@ __device__ __forceinline__ void film_add(const FilmPtrs &f, uint32_t pixel, v3 c
     if (c.x != 0.0f) atomicAdd(f.rgb + 3 * (size_t)pixel, c.x);
     if (c.y != 0.0f) atomicAdd(f.rgb + 3 * (size_t)pixel + 1, c.y);
     if (c.z != 0.0f) atomicAdd(f.rgb + 3 * (size_t)pixel + 2, c.z);
+}
+
+// One radiance contribution of a path to its pixel, counted when a channel is
+// not finite.
+__device__ __forceinline__ void film_contribute(WaveCounters *counters, const FilmPtrs &f, uint32_t pixel, v3 c) {
+    if (!(isfinite(c.x) && isfinite(c.y) && isfinite(c.z))) atomicAdd(&counters->nonfinite, 1ull);
+    film_add(f, pixel, c);
 }
 
 // ------------------------------------------------------------------ scene sources
@@ -746,7 +750,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
             uint32_t prim = __float_as_uint(hv.w);
             float t = hv.x;
             if (prim == kMiss) {
-                p.color = p.color + p.T * S.background;
+                film_contribute(W.counters, src.film(p.scene), p.pixel, p.T * S.background);
                 done = true;
             } else {
                 v3 origin = mk(r0.x, r0.y, r0.z);
@@ -791,7 +795,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                     const MaterialInfo m = S.mats[G.material];
                     if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0) {
                         const LightInfo &L = S.lights[G.light];
-                        p.color = p.color + p.T * mk(L.radiance[0], L.radiance[1], L.radiance[2]);
+                        film_contribute(W.counters, src.film(p.scene), p.pixel,
+                                        p.T * mk(L.radiance[0], L.radiance[1], L.radiance[2]));
                     }
                     Inter it;
                     it.P = origin + direction * t;
@@ -906,14 +911,12 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                 W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, b_tl);
             }
         }
-        // finished paths: film write (integrator.cpp:245-249); the thread then
-        // starts the next work item in their place
+        // finished paths: film write (integrator.cpp:245-249; the radiance went to
+        // the film as it was found); the thread then starts the next work item
+        // in their place
         bool regen = false;
         if (done) {
             const FilmPtrs &F = src.film(p.scene);
-            if (!(isfinite(p.color.x) && isfinite(p.color.y) && isfinite(p.color.z)))
-                atomicAdd(&W.counters->nonfinite, 1ull);
-            film_add(F, p.pixel, p.color);
             atomicAdd(F.bounces + p.pixel, p.bounces);
             atomicAdd(F.counts + p.pixel, 1u);
         }
@@ -982,9 +985,7 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     if (!is_bsdf) c = ((f * Le) * power_heuristic(lpdf, spdf)) / lpdf;
     else c = ((f * Le) * power_heuristic(spdf, lpdf)) / spdf;
     v3 T = mk(r1.x, r1.y, r1.z);
-    const v3 add = T * (c * (float)S.num_lights);
-    if (!(isfinite(add.x) && isfinite(add.y) && isfinite(add.z))) atomicAdd(&W.counters->nonfinite, 1ull);
-    film_add(F, pixel, add);
+    film_contribute(W.counters, F, pixel, T * (c * (float)S.num_lights));
 }
 
 // Path rays of iteration `cur` (closest hit into W.hits) and, in the same
