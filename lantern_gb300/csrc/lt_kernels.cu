@@ -30,6 +30,16 @@ constexpr uint32_t kLightBrute = 16;
 
 __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
 
+// The wavefront queues (path state, rays, hits, connection records) are read
+// once by the next kernel and stream through L2 in far larger volume than it
+// holds. Their loads and stores carry the streaming hint (evict first) so that
+// the scene the traversal gathers from (nodes, triangles, normals) keeps its
+// place in L2 from one kernel to the next.
+template <class T>
+__device__ __forceinline__ T ld_s(const T *p) { return __ldcs(p); }
+template <class T>
+__device__ __forceinline__ void st_s(T *p, T v) { __stcs(p, v); }
+
 __device__ __forceinline__ float safe_inv(float d) {
     return 1.0f / (fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
 }
@@ -531,32 +541,34 @@ __device__ __forceinline__ void start_path(const DevScene &S, const RenderArgs &
 }
 
 __device__ __forceinline__ void store_path(const PathState &ps, uint32_t cap, uint32_t slot, const Path &p) {
-    ps.rng[slot] = p.rng.state;
-    ps.pixel[slot] = p.pixel;
-    ps.frame[slot] = p.frame;
-    ps.T[slot] = p.T.x; ps.T[cap + slot] = p.T.y; ps.T[2 * cap + slot] = p.T.z;
-    ps.bounces[slot] = p.bounces;
-    ps.flags[slot] = p.lobe | ((uint32_t)(p.medium + 1) << kFlagMediumShift) | (p.scene << kFlagSceneShift);
-    ps.iori[slot] = p.iori;
+    st_s(ps.rng + slot, (uint64_t)p.rng.state);
+    st_s(ps.pixel + slot, p.pixel);
+    st_s(ps.frame + slot, p.frame);
+    st_s(ps.T + slot, p.T.x);
+    st_s(ps.T + cap + slot, p.T.y);
+    st_s(ps.T + 2 * cap + slot, p.T.z);
+    st_s(ps.bounces + slot, p.bounces);
+    st_s(ps.flags + slot, p.lobe | ((uint32_t)(p.medium + 1) << kFlagMediumShift) | (p.scene << kFlagSceneShift));
+    st_s(ps.iori + slot, p.iori);
 }
 
 __device__ __forceinline__ void load_path(const PathState &ps, uint32_t cap, uint32_t slot, Path &p) {
-    p.rng.state = ps.rng[slot];
-    p.pixel = ps.pixel[slot];
-    p.frame = ps.frame[slot];
+    p.rng.state = ld_s(ps.rng + slot);
+    p.pixel = ld_s(ps.pixel + slot);
+    p.frame = ld_s(ps.frame + slot);
     p.rng.inc = (uint64_t)p.frame | 1u;
-    p.T = mk(ps.T[slot], ps.T[cap + slot], ps.T[2 * cap + slot]);
-    p.bounces = ps.bounces[slot];
-    uint32_t fl = ps.flags[slot];
+    p.T = mk(ld_s(ps.T + slot), ld_s(ps.T + cap + slot), ld_s(ps.T + 2 * cap + slot));
+    p.bounces = ld_s(ps.bounces + slot);
+    uint32_t fl = ld_s(ps.flags + slot);
     p.lobe = fl & 0xFFu;
     p.medium = (int)((fl >> kFlagMediumShift) & kFlagMediumMask) - 1;
     p.scene = fl >> kFlagSceneShift;
-    p.iori = ps.iori[slot];
+    p.iori = ld_s(ps.iori + slot);
 }
 
 __device__ __forceinline__ void write_ray(float4 *rays, uint32_t i, v3 o, float tnear, v3 d) {
-    rays[2 * i] = make_float4(o.x, o.y, o.z, tnear);
-    rays[2 * i + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+    st_s(rays + 2 * i, make_float4(o.x, o.y, o.z, tnear));
+    st_s(rays + 2 * i + 1, make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000)));
 }
 
 // SurfaceInteraction (integrator/surface_interaction.h:14-30)
@@ -685,11 +697,11 @@ __global__ void __launch_bounds__(128) k_intersect(DevScene S, const float4 *__r
         if (B::done(r)) {
             idx = fetch_next(fetch);
             if (idx >= n) break;
-            float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
+            float4 a = ld_s(rays + 2 * idx), b = ld_s(rays + 2 * idx + 1);
             B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
         }
         B::run(g, r, stack);
-        if (B::done(r)) hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
+        if (B::done(r)) st_s(hits + idx, make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
     }
 }
 
@@ -745,8 +757,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
             load_path(W.p[cur], cap, q, p);
             const DevScene &S = src.scene(p.scene);
             const RenderArgs &A = src.args(p.scene);
-            float4 hv = W.hits[q];
-            float4 r0 = W.ray[cur][2 * q], r1 = W.ray[cur][2 * q + 1];
+            float4 hv = ld_s(W.hits + q);
+            float4 r0 = ld_s(W.ray[cur] + 2 * q), r1 = ld_s(W.ray[cur] + 2 * q + 1);
             uint32_t prim = __float_as_uint(hv.w);
             float t = hv.x;
             if (prim == kMiss) {
@@ -897,18 +909,18 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
             conn_light |= p.scene << kConnSceneShift;
             uint32_t idx = warp_reserve(&W.counters->ccount[cur], emit_l);
             if (emit_l) {
-                W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light));
-                W.cray[2 * idx + 1] = make_float4(l_dir.x, l_dir.y, l_dir.z, __uint_as_float(p.pixel));
-                W.crec[2 * idx] = make_float4(l_f.x, l_f.y, l_f.z, l_pdf);
-                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, l_tl);
+                st_s(W.cray + 2 * idx, make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light)));
+                st_s(W.cray + 2 * idx + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, __uint_as_float(p.pixel)));
+                st_s(W.crec + 2 * idx, make_float4(l_f.x, l_f.y, l_f.z, l_pdf));
+                st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, l_tl));
             }
             idx = warp_reserve(&W.counters->ccount[cur], emit_b);
             if (emit_b) {
-                W.cray[2 * idx] = make_float4(conn_org.x, conn_org.y, conn_org.z,
-                                              __uint_as_float(conn_light | kConnectBsdf));
-                W.cray[2 * idx + 1] = make_float4(b_dir.x, b_dir.y, b_dir.z, __uint_as_float(p.pixel));
-                W.crec[2 * idx] = make_float4(b_f.x, b_f.y, b_f.z, b_pdf);
-                W.crec[2 * idx + 1] = make_float4(conn_T.x, conn_T.y, conn_T.z, b_tl);
+                st_s(W.cray + 2 * idx,
+                     make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light | kConnectBsdf)));
+                st_s(W.cray + 2 * idx + 1, make_float4(b_dir.x, b_dir.y, b_dir.z, __uint_as_float(p.pixel)));
+                st_s(W.crec + 2 * idx, make_float4(b_f.x, b_f.y, b_f.z, b_pdf));
+                st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, b_tl));
             }
         }
         // finished paths: film write (integrator.cpp:245-249; the radiance went to
@@ -977,7 +989,7 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     float cosl = is_bsdf ? dot(nrm, dir) : dot(nrm, -dir);
     float lpdf = d2 / (fabsf(cosl) * L.area);
     if (lpdf == 0.0f) return;
-    float4 r0 = ldg4(W.crec + 2 * idx), r1 = ldg4(W.crec + 2 * idx + 1);
+    float4 r0 = ld_s(W.crec + 2 * idx), r1 = ld_s(W.crec + 2 * idx + 1);
     v3 f = mk(r0.x, r0.y, r0.z);
     float spdf = r0.w;
     v3 Le = mk(L.radiance[0], L.radiance[1], L.radiance[2]);
@@ -1016,13 +1028,13 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
             idx = fetch_next(&W.counters->trace_fetch);
             if (idx >= total) break;
             if (idx < n) {
-                if (Src::kMany) g = B::geo(src.scene(W.p[cur].flags[idx] >> kFlagSceneShift));
-                float4 a = ldg4(rays + 2 * idx), b = ldg4(rays + 2 * idx + 1);
+                if (Src::kMany) g = B::geo(src.scene(ld_s(W.p[cur].flags + idx) >> kFlagSceneShift));
+                float4 a = ld_s(rays + 2 * idx), b = ld_s(rays + 2 * idx + 1);
                 B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
             } else {
                 const uint32_t c = idx - n;
-                float4 a = ldg4(W.cray + 2 * c), b = ldg4(W.cray + 2 * c + 1);
-                float tl = ldg4(W.crec + 2 * c + 1).w;
+                float4 a = ld_s(W.cray + 2 * c), b = ld_s(W.cray + 2 * c + 1);
+                float tl = ld_s(W.crec + 2 * c + 1).w;
                 kl = __float_as_uint(a.w);
                 pixel = __float_as_uint(b.w);
                 const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
@@ -1039,7 +1051,7 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
         B::run(g, r, stack);
         if (B::done(r)) {
             if (idx < n) {
-                W.hits[idx] = make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim));
+                st_s(W.hits + idx, make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
                 resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, pixel, r);
