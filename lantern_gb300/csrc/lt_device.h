@@ -66,8 +66,8 @@ struct Wavefront {
     PathState p[2] = {};                    // ping-pong, in queue order
     float4 *ray[2] = {nullptr, nullptr};    // 2 float4 per entry: (org, tnear) (dir, tfar)
     float4 *hits = nullptr;                 // (t, u, v, prim bits)
-    float4 *cray = nullptr;                 // 2 float4 per record: (org, kind|light) (dir, pixel)
-    float4 *crec = nullptr;                 // 2 float4 per record: (f, bsdf pdf) (throughput, -)
+    float4 *cray = nullptr;                 // 2 float4 per record: (org, kind|light) (dir, light distance)
+    float4 *crec = nullptr;                 // 2 float4 per record: (f, bsdf pdf) (throughput, pixel)
     WaveCounters *counters = nullptr;
     void *arena = nullptr;
     size_t arena_bytes = 0;

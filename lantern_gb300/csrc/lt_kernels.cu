@@ -910,17 +910,17 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
             uint32_t idx = warp_reserve(&W.counters->ccount[cur], emit_l);
             if (emit_l) {
                 st_s(W.cray + 2 * idx, make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light)));
-                st_s(W.cray + 2 * idx + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, __uint_as_float(p.pixel)));
+                st_s(W.cray + 2 * idx + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, l_tl));
                 st_s(W.crec + 2 * idx, make_float4(l_f.x, l_f.y, l_f.z, l_pdf));
-                st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, l_tl));
+                st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
             }
             idx = warp_reserve(&W.counters->ccount[cur], emit_b);
             if (emit_b) {
                 st_s(W.cray + 2 * idx,
                      make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light | kConnectBsdf)));
-                st_s(W.cray + 2 * idx + 1, make_float4(b_dir.x, b_dir.y, b_dir.z, __uint_as_float(p.pixel)));
+                st_s(W.cray + 2 * idx + 1, make_float4(b_dir.x, b_dir.y, b_dir.z, b_tl));
                 st_s(W.crec + 2 * idx, make_float4(b_f.x, b_f.y, b_f.z, b_pdf));
-                st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, b_tl));
+                st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
             }
         }
         // finished paths: film write (integrator.cpp:245-249; the radiance went to
@@ -970,7 +970,7 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
 // kLightBrute triangles (distance -1 in the record) use a full closest-hit query.
 template <class State>
 __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wavefront &W, const FilmPtrs &F,
-                                                   uint32_t idx, uint32_t kl, uint32_t pixel, const State &r) {
+                                                   uint32_t idx, uint32_t kl, const State &r) {
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
     const LightInfo &L = S.lights[kl & kConnLightMask];
     Hit h;
@@ -990,6 +990,7 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     float lpdf = d2 / (fabsf(cosl) * L.area);
     if (lpdf == 0.0f) return;
     float4 r0 = ld_s(W.crec + 2 * idx), r1 = ld_s(W.crec + 2 * idx + 1);
+    const uint32_t pixel = __float_as_uint(r1.w);
     v3 f = mk(r0.x, r0.y, r0.z);
     float spdf = r0.w;
     v3 Le = mk(L.radiance[0], L.radiance[1], L.radiance[2]);
@@ -1022,7 +1023,7 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
     typename B::State r;
     typename B::Entry stack[B::kDepth];
     B::idle(r);
-    uint32_t idx = 0, kl = 0, pixel = 0, n_trav = 0;
+    uint32_t idx = 0, kl = 0, n_trav = 0;
     for (;;) {
         if (B::done(r)) {
             idx = fetch_next(&W.counters->trace_fetch);
@@ -1034,9 +1035,8 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
             } else {
                 const uint32_t c = idx - n;
                 float4 a = ld_s(W.cray + 2 * c), b = ld_s(W.cray + 2 * c + 1);
-                float tl = ld_s(W.crec + 2 * c + 1).w;
+                const float tl = b.w;
                 kl = __float_as_uint(a.w);
-                pixel = __float_as_uint(b.w);
                 const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
                 if (Src::kMany) g = B::geo(S);
                 const LightInfo &L = S.lights[kl & kConnLightMask];
@@ -1054,7 +1054,7 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
                 st_s(W.hits + idx, make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
-                resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, pixel, r);
+                resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
             }
         }
     }
