@@ -586,9 +586,12 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
         size_t nev = 0;
         c->stage_of_event.clear();
         int cur = 0;
-        const int kBatch = 4;
+        // Iterations launched between two reads of the queue lengths. While
+        // work items remain, at most `cap` of them start per iteration, so the
+        // loop cannot end within remaining / cap iterations.
+        uint32_t batch = 4;
         for (;;) {
-            for (int k = 0; k < kBatch; ++k) {
+            for (uint32_t k = 0; k < batch; ++k) {
                 for (int stage = 0; stage < kStages; ++stage) {
                     if (nev == c->stage_events.size()) {
                         cudaEvent_t e;
@@ -610,6 +613,9 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
             if (c->counters_host->count[cur] == 0 && c->counters_host->ccount[cur ^ 1] == 0) break;
             if (iters > 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u)
                 return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
+            const unsigned long long next = c->counters_host->work_next;
+            const unsigned long long left_iters = next < a.total ? (a.total - next) / cap : 0;
+            batch = left_iters > 4 ? (left_iters < 64 ? (uint32_t)left_iters : 64u) : 4u;
         }
         c->stats.main_rays = c->counters_host->main_rays;
         c->stats.light_rays = c->counters_host->light_rays;
@@ -837,10 +843,10 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
         CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
         uint32_t launches = 1, iters = 0;
         int cur = 0;
-        const int kBatch = 4;
+        uint32_t batch = 4;  // iterations between reads of the queue lengths, as in lt_render
         const uint32_t limit = 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u;
         for (;;) {
-            for (int k = 0; k < kBatch; ++k) {
+            for (uint32_t k = 0; k < batch; ++k) {
                 for (int stage = 0; stage < kStages; ++stage)
                     CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
                 launches += kStages;
@@ -852,6 +858,9 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
             if (c->counters_host->count[cur] == 0 && c->counters_host->ccount[cur ^ 1] == 0) break;
             if (iters > limit) return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
+            const unsigned long long next = c->counters_host->work_next;
+            const unsigned long long left_iters = next < a.total ? (a.total - next) / cap : 0;
+            batch = left_iters > 4 ? (left_iters < 64 ? (uint32_t)left_iters : 64u) : 4u;
         }
         c->stats.main_rays = c->counters_host->main_rays;
         c->stats.light_rays = c->counters_host->light_rays;
