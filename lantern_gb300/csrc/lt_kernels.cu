@@ -479,27 +479,6 @@ __device__ __forceinline__ float light_distance(const DevScene &S, const LightIn
     return lh.prim == kMiss ? 0.0f : lh.t;
 }
 
-// warp-aggregated slot reservation: returns this lane's index (valid if pred)
-__device__ __forceinline__ uint32_t warp_reserve(uint32_t *counter, bool pred) {
-    unsigned mask = __ballot_sync(0xFFFFFFFFu, pred);
-    uint32_t lane = threadIdx.x & 31u;
-    uint32_t base = 0;
-    int leader = mask ? __ffs(mask) - 1 : 0;
-    if (mask && lane == (uint32_t)leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
-}
-
-__device__ __forceinline__ unsigned long long warp_reserve64(unsigned long long *counter, bool pred) {
-    unsigned mask = __ballot_sync(0xFFFFFFFFu, pred);
-    uint32_t lane = threadIdx.x & 31u;
-    unsigned long long base = 0;
-    int leader = mask ? __ffs(mask) - 1 : 0;
-    if (mask && lane == (uint32_t)leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
-}
-
 struct Path {
     Pcg rng;
     uint32_t pixel, frame;
@@ -904,17 +883,43 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                 else push = true;
             }
         }
-        // connection records
+        // Slots of this warp, reserved by one lane: the connection records and the
+        // finished paths' next work items together, then the queue entries (their
+        // number depends on how many work items were left), so a warp waits for
+        // two atomic round trips rather than four.
+        const uint32_t lane = threadIdx.x & 31u;
+        const unsigned below = (1u << lane) - 1u;
+        const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
+        const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
+        uint32_t c_base = 0, q_base = 0, n_regen = 0;
+        unsigned long long w_base = 0;
+        if (lane == 0) {
+            const uint32_t nc = __popc(m_l) + __popc(m_b);
+            if (nc) c_base = atomicAdd(&W.counters->ccount[cur], nc);
+            if (m_d) {
+                w_base = atomicAdd(&W.counters->work_next, (unsigned long long)__popc(m_d));
+                const unsigned long long tot = src.total();
+                const unsigned long long left = w_base < tot ? tot - w_base : 0ull;
+                n_regen = left < (unsigned long long)__popc(m_d) ? (uint32_t)left : (uint32_t)__popc(m_d);
+            }
+            const uint32_t ne = (uint32_t)__popc(m_p) + n_regen;
+            if (ne) q_base = atomicAdd(&W.counters->count[nxt], ne);
+        }
+        c_base = __shfl_sync(0xFFFFFFFFu, c_base, 0);
+        w_base = __shfl_sync(0xFFFFFFFFu, w_base, 0);
+        n_regen = __shfl_sync(0xFFFFFFFFu, n_regen, 0);
+        q_base = __shfl_sync(0xFFFFFFFFu, q_base, 0);
+        // connection records: the warp's light samples, then its BSDF samples
         {
             conn_light |= p.scene << kConnSceneShift;
-            uint32_t idx = warp_reserve(&W.counters->ccount[cur], emit_l);
+            uint32_t idx = c_base + __popc(m_l & below);
             if (emit_l) {
                 st_s(W.cray + 2 * idx, make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light)));
                 st_s(W.cray + 2 * idx + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, l_tl));
                 st_s(W.crec + 2 * idx, make_float4(l_f.x, l_f.y, l_f.z, l_pdf));
                 st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
             }
-            idx = warp_reserve(&W.counters->ccount[cur], emit_b);
+            idx = c_base + __popc(m_l) + __popc(m_b & below);
             if (emit_b) {
                 st_s(W.cray + 2 * idx,
                      make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light | kConnectBsdf)));
@@ -932,17 +937,19 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
             atomicAdd(F.bounces + p.pixel, p.bounces);
             atomicAdd(F.counts + p.pixel, 1u);
         }
-        unsigned long long item = warp_reserve64(&W.counters->work_next, done);
-        if (done && item < src.total()) {
+        // work items go to the finished lanes in lane order
+        const uint32_t rank_d = __popc(m_d & below);
+        if (done && rank_d < n_regen) {
             unsigned long long local;
-            const uint32_t sid = src.locate(item, local);
+            const uint32_t sid = src.locate(w_base + rank_d, local);
             start_path(src.scene(sid), src.args(sid), local, p, norg, ndir, ntnear);
             p.scene = sid;
             regen = true;
         }
-        bool enqueue = push || regen;
-        uint32_t qi = warp_reserve(&W.counters->count[nxt], enqueue);
+        const bool enqueue = push || regen;
+        const unsigned m_e = __ballot_sync(0xFFFFFFFFu, enqueue);
         if (enqueue) {
+            const uint32_t qi = q_base + __popc(m_e & below);
             write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
             store_path(W.p[nxt], cap, qi, p);
         }
