@@ -610,7 +610,9 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
                                         cudaMemcpyDeviceToHost, c->stream));
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
             // done when no path ray is queued and the last shade emitted no connection
-            if (c->counters_host->count[cur] == 0 && c->counters_host->ccount[cur ^ 1] == 0) break;
+            if (c->counters_host->count[cur] == 0 && c->counters_host->rcount[cur] == 0 &&
+                c->counters_host->ccount[cur ^ 1] == 0)
+                break;
             if (iters > 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u)
                 return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
             const unsigned long long next = c->counters_host->work_next;
@@ -856,7 +858,9 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
             CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
                                         c->stream));
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-            if (c->counters_host->count[cur] == 0 && c->counters_host->ccount[cur ^ 1] == 0) break;
+            if (c->counters_host->count[cur] == 0 && c->counters_host->rcount[cur] == 0 &&
+                c->counters_host->ccount[cur ^ 1] == 0)
+                break;
             if (iters > limit) return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
             const unsigned long long next = c->counters_host->work_next;
             const unsigned long long left_iters = next < a.total ? (a.total - next) / cap : 0;

@@ -50,7 +50,8 @@ struct PathState {
 };
 
 struct WaveCounters {
-    uint32_t count[2];           // path-ray queue lengths (ping-pong by iteration parity)
+    uint32_t count[2];           // path-ray queue lengths (ping-pong by iteration parity): continuing paths
+    uint32_t rcount[2];          // and regenerated paths (camera rays), kept apart at the top of the queue
     uint32_t ccount[2];          // connection records written by k_shade(parity)
     unsigned long long work_next; // next (pixel, frame) work item
     unsigned long long main_rays, light_rays, bsdf_rays;

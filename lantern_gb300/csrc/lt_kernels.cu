@@ -479,6 +479,15 @@ __device__ __forceinline__ float light_distance(const DevScene &S, const LightIn
     return lh.prim == kMiss ? 0.0f : lh.t;
 }
 
+// A path queue holds the paths that continue (entries 0 .. n_push - 1, in the
+// order their warps enqueued them) and, apart from them at the top of the
+// arrays, the paths that start with a camera ray (slots cap - n_cam .. cap - 1),
+// so that camera rays of neighbouring pixels fill warps of their own. Entry q of
+// the queue lives in slot:
+__device__ __forceinline__ uint32_t queue_slot(uint32_t q, uint32_t n_push, uint32_t n_cam, uint32_t cap) {
+    return q < n_push ? q : cap - n_cam + (q - n_push);
+}
+
 struct Path {
     Pcg rng;
     uint32_t pixel, frame;
@@ -703,6 +712,7 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters->count[0] = (uint32_t)first;
         W.counters->count[1] = 0;
+        W.counters->rcount[0] = W.counters->rcount[1] = 0;
         W.counters->ccount[0] = W.counters->ccount[1] = 0;
         W.counters->work_next = first;
         W.counters->trace_fetch = 0;
@@ -714,14 +724,16 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
 // than 1024 threads with spills and than 512 threads.
 template <class Src>
 __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur) {
-    const uint32_t n = W.counters->count[cur];
+    const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
+    const uint32_t n = n_push + n_cam;
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
     uint32_t n_ref_rays = 0, n_ref_rays_b = 0;  // connection rays the reference would trace
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        uint32_t q = base + threadIdx.x;
-        bool active = q < n;
+        const uint32_t q = base + threadIdx.x;
+        const bool active = q < n;
+        const uint32_t slot = active ? queue_slot(q, n_push, n_cam, cap) : 0u;
         Path p;
         bool done = false, push = false;
         v3 norg = mk(0, 0, 0), ndir = mk(0, 0, 0);
@@ -733,11 +745,11 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
         uint32_t conn_light = 0;
         v3 conn_T = mk(0, 0, 0);
         if (active) {
-            load_path(W.p[cur], cap, q, p);
+            load_path(W.p[cur], cap, slot, p);
             const DevScene &S = src.scene(p.scene);
             const RenderArgs &A = src.args(p.scene);
-            float4 hv = ld_s(W.hits + q);
-            float4 r0 = ld_s(W.ray[cur] + 2 * q), r1 = ld_s(W.ray[cur] + 2 * q + 1);
+            float4 hv = ld_s(W.hits + slot);
+            float4 r0 = ld_s(W.ray[cur] + 2 * slot), r1 = ld_s(W.ray[cur] + 2 * slot + 1);
             uint32_t prim = __float_as_uint(hv.w);
             float t = hv.x;
             if (prim == kMiss) {
@@ -883,32 +895,33 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
                 else push = true;
             }
         }
-        // Slots of this warp, reserved by one lane: the connection records and the
-        // finished paths' next work items together, then the queue entries (their
-        // number depends on how many work items were left), so a warp waits for
-        // two atomic round trips rather than four.
+        // Slots of this warp, reserved by one lane: the connection records, the
+        // continuing paths' queue entries and the finished paths' next work items
+        // together, then the camera-ray entries (their number depends on how many
+        // work items were left), so a warp waits for two atomic round trips.
         const uint32_t lane = threadIdx.x & 31u;
         const unsigned below = (1u << lane) - 1u;
         const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
         const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
-        uint32_t c_base = 0, q_base = 0, n_regen = 0;
+        uint32_t c_base = 0, q_base = 0, r_base = 0, n_regen = 0;
         unsigned long long w_base = 0;
         if (lane == 0) {
             const uint32_t nc = __popc(m_l) + __popc(m_b);
             if (nc) c_base = atomicAdd(&W.counters->ccount[cur], nc);
+            if (m_p) q_base = atomicAdd(&W.counters->count[nxt], (uint32_t)__popc(m_p));
             if (m_d) {
                 w_base = atomicAdd(&W.counters->work_next, (unsigned long long)__popc(m_d));
                 const unsigned long long tot = src.total();
                 const unsigned long long left = w_base < tot ? tot - w_base : 0ull;
                 n_regen = left < (unsigned long long)__popc(m_d) ? (uint32_t)left : (uint32_t)__popc(m_d);
+                if (n_regen) r_base = atomicAdd(&W.counters->rcount[nxt], n_regen);
             }
-            const uint32_t ne = (uint32_t)__popc(m_p) + n_regen;
-            if (ne) q_base = atomicAdd(&W.counters->count[nxt], ne);
         }
         c_base = __shfl_sync(0xFFFFFFFFu, c_base, 0);
+        q_base = __shfl_sync(0xFFFFFFFFu, q_base, 0);
+        r_base = __shfl_sync(0xFFFFFFFFu, r_base, 0);
         w_base = __shfl_sync(0xFFFFFFFFu, w_base, 0);
         n_regen = __shfl_sync(0xFFFFFFFFu, n_regen, 0);
-        q_base = __shfl_sync(0xFFFFFFFFu, q_base, 0);
         // connection records: the warp's light samples, then its BSDF samples
         {
             conn_light |= p.scene << kConnSceneShift;
@@ -946,10 +959,8 @@ __global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur)
             p.scene = sid;
             regen = true;
         }
-        const bool enqueue = push || regen;
-        const unsigned m_e = __ballot_sync(0xFFFFFFFFu, enqueue);
-        if (enqueue) {
-            const uint32_t qi = q_base + __popc(m_e & below);
+        if (push || regen) {
+            const uint32_t qi = push ? q_base + __popc(m_p & below) : cap - 1u - (r_base + rank_d);
             write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
             store_path(W.p[nxt], cap, qi, p);
         }
@@ -1012,16 +1023,20 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // persistent launch, the connection records that the previous k_shade wrote
 // (parity cur ^ 1; occlusion query or closest hit, then resolve_connection).
 // Both come from one launch of k_shade, so one traversal kernel serves them:
-// items [0, n) are path rays, [n, n + nc) connection records, fetched from
+// items [0, n) are path rays (queue entries, placed by queue_slot), [n, n + nc)
+// connection records, fetched from
 // counters->trace_fetch (zeroed by the launch before). Path rays come first so
 // that the short connection queries fill the tail.
 template <class Src, class B>
 __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefront W, int cur) {
-    const uint32_t n = W.counters->count[cur];
+    const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
+    const uint32_t n = n_push + n_cam;
     const uint32_t nc = W.counters->ccount[cur ^ 1];
     const uint32_t total = n + nc;
+    const uint32_t cap = W.capacity;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters->count[cur ^ 1] = 0;  // filled by the next k_shade
+        W.counters->rcount[cur ^ 1] = 0;
         W.counters->ccount[cur] = 0;
         W.counters->main_rays += n;
     }
@@ -1036,8 +1051,9 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
             idx = fetch_next(&W.counters->trace_fetch);
             if (idx >= total) break;
             if (idx < n) {
-                if (Src::kMany) g = B::geo(src.scene(ld_s(W.p[cur].flags + idx) >> kFlagSceneShift));
-                float4 a = ld_s(rays + 2 * idx), b = ld_s(rays + 2 * idx + 1);
+                const uint32_t s = queue_slot(idx, n_push, n_cam, cap);
+                if (Src::kMany) g = B::geo(src.scene(ld_s(W.p[cur].flags + s) >> kFlagSceneShift));
+                float4 a = ld_s(rays + 2 * s), b = ld_s(rays + 2 * s + 1);
                 B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
             } else {
                 const uint32_t c = idx - n;
@@ -1058,7 +1074,8 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
         B::run(g, r, stack);
         if (B::done(r)) {
             if (idx < n) {
-                st_s(W.hits + idx, make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
+                st_s(W.hits + queue_slot(idx, n_push, n_cam, cap),
+                     make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
                 resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
@@ -1073,7 +1090,7 @@ __global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefr
 __global__ void k_loop_condition(WaveCounters *c, const SceneTable *t, cudaGraphConditionalHandle h, int cur,
                                  uint32_t iters) {
     c->iterations += iters;
-    unsigned int more = c->count[cur] != 0u || c->ccount[cur ^ 1] != 0u;
+    unsigned int more = c->count[cur] != 0u || c->rcount[cur] != 0u || c->ccount[cur ^ 1] != 0u;
     if (more && c->iterations >= t->iteration_limit) {
         c->error = 2;
         more = 0;
