@@ -211,6 +211,9 @@ def main():
                     help="also time the path-replay adjoint on the differentiable workload")
     ap.add_argument("--spp", type=int, default=None,
                     help="override the workload's samples per pixel (small cases for profiling)")
+    ap.add_argument("--paths-in-flight", type=int, default=None,
+                    help="wavefront path slots (lt_tuning.paths_in_flight); default: the whole render, "
+                         "up to 67,108,864")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8],
                     help="BVH width of the traversal (lt_tuning.bvh_width)")
     ap.add_argument("--batch", action=argparse.BooleanOptionalAction, default=True,
@@ -247,7 +250,8 @@ def main():
         path = os.path.join(SCENES, f"{sc.name}.json")
     scene = Scene(local)
     scene.LoadSceneFromJSON(path)
-    scene.ctx.set_tuning(bvh_width=args.bvh_width)
+    paths_in_flight = args.paths_in_flight or min(scene.width * scene.height * rp["spp"], 1 << 26)
+    scene.ctx.set_tuning(bvh_width=args.bvh_width, paths_in_flight=paths_in_flight)
     info = scene.info()
     fb = FrameBuffer(scene.width, scene.height, f"cuda:{local}")
     integ = Integrator(scene, fb, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
@@ -350,7 +354,7 @@ def main():
                 "config": {"workload": args.workload, "width": scene.width, "height": scene.height, "spp": spp,
                            "max_depth": rp["max_depth"], "rr_depth": rp["rr_depth"],
                            "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
-                           "bvh_width": args.bvh_width,
+                           "bvh_width": args.bvh_width, "paths_in_flight": paths_in_flight,
                            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1
                            else "single GPU"},
                 "mrays": round(mrays, 2), "gpu_launches": launches,

@@ -206,7 +206,7 @@ lt_status lt_render(lt_ctx *ctx, const lt_render_params *params, lt_film *film);
  * forbids allocations afterwards, or an interactive loop in which cudaMalloc /
  * cudaFree (which can synchronise the whole device) would stall other work.
  * The wavefront state lives in a fixed array inside liblantern_gpu.so of
- * LT_NOALLOC_MAX_PATHS path slots (about 20.5 MB), reserved on every GPU that
+ * LT_NOALLOC_MAX_PATHS path slots (about 18.9 MB), reserved on every GPU that
  * loads the library until the process exits. Same sampling, same film
  * semantics and same result as lt_render; only the number of paths in flight
  * is bounded.
@@ -263,7 +263,9 @@ lt_status lt_resolve(lt_ctx *ctx, const lt_film *film, int32_t tonemap, float ex
  * scene per Integrator (integrator.cpp:28-43): the wavefront's launch
  * configuration, and many scenes rendered together in one captured loop. */
 typedef struct lt_tuning {
-    uint32_t paths_in_flight;  /* wavefront path slots; 0 = min(samples, 2,097,152) */
+    uint32_t paths_in_flight;  /* wavefront path slots of this context, 1024..67,108,864 (288 B
+                                  each); 0 = min(samples, 16,777,216), halved while the
+                                  allocation fails (down to 1,048,576) */
     uint32_t trace_threads;    /* threads per block of the trace kernel: 64, 128 or 256 */
     uint32_t shade_threads;    /* ... of the shade kernel (and camera-ray generation) */
     uint32_t loop_iterations;  /* wavefront iterations per body of lt_render_batch's loop: 2, 4 or 8 */

@@ -506,25 +506,46 @@ static size_t carve_wave(char *base, uint32_t cap, Wavefront *w) {
     return off;
 }
 
-// Sizes the context's wavefront arena for `cap` entries (one allocation, reused).
-static lt_status ensure_wave(lt_ctx *c, uint32_t cap) {
-    if (c->wave.capacity >= cap && c->wave.arena) return LT_OK;
+// Wavefront sizes. Without a paths_in_flight tuning a context's arena holds up
+// to kDefaultPaths slots (16M, 4.6 GB); fewer, longer iterations amortise each
+// launch's tail: on the 1.3M-triangle workload (67M samples) 2M slots give
+// 941 Msamples/s, 8M 1268, 16M 1341, the whole render (64M) 1498.
+constexpr unsigned long long kDefaultPaths = 1ull << 24, kMinDefaultPaths = 1ull << 20, kMaxPaths = 1ull << 26;
+
+// Sizes the context's wavefront arena for *cap entries (one allocation,
+// reused). With `shrink` (the default size), an allocation that fails is
+// retried at half the size down to kMinDefaultPaths; *cap is the size obtained.
+static lt_status ensure_wave(lt_ctx *c, uint32_t *cap, bool shrink) {
+    if (c->wave.capacity >= *cap && c->wave.arena) return LT_OK;
     free_wave(c);
-    Wavefront sizing;
-    size_t bytes = carve_wave(nullptr, cap, &sizing);
-    char *a = nullptr;
-    CUDA_TRY(c, dev_malloc((void **)&a, bytes));
-    carve_wave(a, cap, &c->wave);
-    c->wave.arena = a;
-    c->wave.arena_bytes = bytes;
-    return LT_OK;
+    for (;;) {
+        Wavefront sizing;
+        const size_t bytes = carve_wave(nullptr, *cap, &sizing);
+        char *a = nullptr;
+        const cudaError_t e = dev_malloc((void **)&a, bytes);
+        if (e == cudaSuccess) {
+            carve_wave(a, *cap, &c->wave);
+            c->wave.arena = a;
+            c->wave.arena_bytes = bytes;
+            return LT_OK;
+        }
+        cudaGetLastError();
+        if (!shrink || e != cudaErrorMemoryAllocation || *cap / 2 < kMinDefaultPaths)
+            return fail(c, e == cudaErrorMemoryAllocation ? LT_ERR_OOM : LT_ERR_CUDA,
+                        "wavefront arena of %zu bytes: %s", bytes, cudaGetErrorString(e));
+        *cap /= 2;
+    }
 }
 
-// Paths in flight for `total` work items: the tuning's count, else 2M path
-// slots (~600 MB), and never more than the work.
-static uint32_t capacity_for(const lt_ctx *c, unsigned long long total) {
-    const unsigned long long cap = c->tuning.paths_in_flight ? c->tuning.paths_in_flight : 1ull << 21;
-    return (uint32_t)(total < cap ? total : cap);
+// Paths in flight for `total` work items (never more than the work): the
+// tuning's count, else kDefaultPaths. Allocates the arena.
+static lt_status prepare_wave(lt_ctx *c, unsigned long long total, uint32_t *cap_out) {
+    const bool fixed = c->tuning.paths_in_flight != 0;
+    const unsigned long long cap = fixed ? c->tuning.paths_in_flight : kDefaultPaths;
+    uint32_t n = (uint32_t)(total < cap ? total : cap);
+    const lt_status st = ensure_wave(c, &n, !fixed);
+    *cap_out = n;
+    return st;
 }
 
 // The context's arena laid out for `cap` entries (cap <= the arena's capacity).
@@ -576,8 +597,8 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
         CUDA_TRY(c, launch_add_counts(f, (uint32_t)npix, p->spp, c->stream));
         c->stats.kernel_launches = 1;
     } else if (a.total > 0) {
-        const uint32_t cap = capacity_for(c, a.total);
-        lt_status st = ensure_wave(c, cap);
+        uint32_t cap = 0;
+        lt_status st = prepare_wave(c, a.total, &cap);
         if (st != LT_OK) return st;
         const Wavefront w = wave_view(c, cap);
         CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
@@ -902,8 +923,8 @@ extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) {
         return fail(c, LT_ERR_INVALID, "loop_iterations must be 2, 4 or 8");
     if (n.bvh_width != 2 && n.bvh_width != 8)
         return fail(c, LT_ERR_UNSUPPORTED, "BVH width %u: the widths built are 2 and 8", n.bvh_width);
-    if (n.paths_in_flight && (n.paths_in_flight < 1024 || n.paths_in_flight > (1u << 24)))
-        return fail(c, LT_ERR_INVALID, "paths_in_flight %u outside 1024..16777216", n.paths_in_flight);
+    if (n.paths_in_flight && (n.paths_in_flight < 1024 || n.paths_in_flight > kMaxPaths))
+        return fail(c, LT_ERR_INVALID, "paths_in_flight %u outside 1024..67108864", n.paths_in_flight);
     CUDA_TRY(c, cudaSetDevice(c->device));
     if (n.bvh_width == 8 && c->has_scene) {
         lt_status st = ensure_bvh8(c);
@@ -1030,8 +1051,8 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
     }
     c->stats.samples = total;
     if (count) {
-        const uint32_t cap = capacity_for(c, total);
-        lt_status st = ensure_wave(c, cap);
+        uint32_t cap = 0;
+        lt_status st = prepare_wave(c, total, &cap);
         if (st != LT_OK) return st;
         const Wavefront w = wave_view(c, cap);
         T.count = count;
@@ -1113,7 +1134,7 @@ extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const l
     float cur_ms = 0.0f;
     if ((st = measure(cur, &cur_ms)) != LT_OK) return st;
     const uint32_t widths[] = {2, 8};
-    const uint32_t paths[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
+    const uint32_t paths[] = {1u << 20, 1u << 22, 1u << 24, 1u << 26};
     const uint32_t threads[] = {64, 128, 256};
     const uint32_t iters[] = {2, 4, 8};
     for (int coord = 0; coord < 5; ++coord) {
