@@ -379,7 +379,10 @@ struct Bvh2 {
     using Entry = int;
     static constexpr int kDepth = kStack - kSharedStack;  // local entries
     static constexpr int kSharedBytesPerThread = 4 * kSharedStack;
-    static constexpr int kMinBlocks256 = 0;  // k_trace register budget: 0 = no minimum (compiler's choice)
+    // k_trace<OneScene> register budget: 5 x 256 threads per SM (at most 51
+    // registers), measured 1.3% faster than the compiler's own choice of 51
+    // (the batched instantiation keeps the compiler's choice: it spilled)
+    static constexpr int kMinBlocks256 = 5;
     __device__ static Geo geo(const DevScene &S) { return geo_of(S); }
     __device__ static void start(State &r, Entry *st, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip) {
         if (kSharedStack) trav_start(r, SharedStack{st}, O, D, tnear, tfar, any, skip);
@@ -1028,7 +1031,7 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // counters->trace_fetch (zeroed by the launch before). Path rays come first so
 // that the short connection queries fill the tail.
 template <class Src, class B>
-__global__ void __launch_bounds__(256, B::kMinBlocks256) k_trace(Src src, Wavefront W, int cur) {
+__global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trace(Src src, Wavefront W, int cur) {
     const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
     const uint32_t n = n_push + n_cam;
     const uint32_t nc = W.counters->ccount[cur ^ 1];
