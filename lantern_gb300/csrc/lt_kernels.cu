@@ -723,10 +723,11 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
 }
 
 // One iteration of the bounce loop of Integrator::RenderPixel (integrator.cpp:115-243).
-// Register budget: 768 threads per SM (at most 85 registers), measured faster
-// than 1024 threads with spills and than 512 threads.
+// Register budget: 1024 threads per SM (64 registers, a few spilled) for the
+// single-scene instantiation, measured 1.1% faster than 768 threads (76
+// registers) with the whole render in flight; the batched one keeps 768.
 template <class Src>
-__global__ void __launch_bounds__(256, 3) k_shade(Src src, Wavefront W, int cur) {
+__global__ void __launch_bounds__(256, Src::kMany ? 3 : 4) k_shade(Src src, Wavefront W, int cur) {
     const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
     const uint32_t n = n_push + n_cam;
     const uint32_t cap = W.capacity;
