@@ -39,7 +39,7 @@ SCENES = os.path.join(ROOT, "_scenes")
 # DRAM bytes (read + write) per ray traced by k_trace on the icosphere workload, measured
 # with ncu dram__bytes_{read,write}.sum over every k_trace launch of a 4-spp render
 # (profiles/k_trace_k_shade_icosphere-1.3M.md)
-TRACE_DRAM_BYTES_PER_RAY = 94.5
+TRACE_DRAM_BYTES_PER_RAY = 97.1
 
 
 def _peaks():
