@@ -214,7 +214,7 @@ def main():
     ap.add_argument("--paths-in-flight", type=int, default=None,
                     help="wavefront path slots (lt_tuning.paths_in_flight); default: the whole render, "
                          "up to 67,108,864")
-    ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8],
+    ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 4, 8],
                     help="BVH width of the traversal (lt_tuning.bvh_width)")
     ap.add_argument("--batch", action=argparse.BooleanOptionalAction, default=True,
                     help="also time the 64-scene batch: one lt_render_batch vs one lt_render per scene")

@@ -269,7 +269,8 @@ typedef struct lt_tuning {
     uint32_t trace_threads;    /* threads per block of the trace kernel: 64, 128 or 256 */
     uint32_t shade_threads;    /* ... of the shade kernel (and camera-ray generation) */
     uint32_t loop_iterations;  /* wavefront iterations per body of lt_render_batch's loop: 2, 4 or 8 */
-    uint32_t bvh_width;        /* children per BVH node: 2 (BVH2) or 8 (compressed 8-wide, built on demand) */
+    uint32_t bvh_width;        /* children per BVH node: 2 (BVH2), 4 (4-wide) or 8 (compressed 8-wide);
+                                  the wide trees are built from the BVH2 on first use */
     float ms;                  /* lt_autotune_batch: device time of the chosen tuning on its sample */
 } lt_tuning;
 /* The context's tuning; it applies to lt_render, lt_render_batch and the
@@ -293,7 +294,7 @@ lt_status lt_set_tuning(lt_ctx *ctx, const lt_tuning *t);
  * - n <= LT_MAX_BATCH; each scene may have at most 1,048,576 lights and 8,190 media;
  * - returns after the batch has finished (the film writes are complete);
  * - the scene contexts must not be in use by other threads during the call
- *   (with bvh_width 8 the call builds their 8-wide BVHs on first use). */
+ *   (with bvh_width 4 or 8 the call builds their wide BVHs on first use). */
 #define LT_MAX_BATCH 2048
 lt_status lt_render_batch(lt_ctx *ctx, lt_ctx *const *scenes, const lt_render_params *params, lt_film *films,
                           uint32_t n);

@@ -39,7 +39,7 @@ struct lt_ctx {
 
     // scene
     bool has_scene = false;
-    bool has_bvh8 = false;
+    bool has_bvh8 = false, has_bvh4 = false;
     uint32_t bvh8_depth = 0;
     HostScene host;
     DevScene dev{};
@@ -134,6 +134,7 @@ static void free_scene(lt_ctx *c) {
     c->scene_bytes = 0;
     c->has_scene = false;
     c->has_bvh8 = false;
+    c->has_bvh4 = false;
     c->dev = DevScene{};
 }
 
@@ -317,6 +318,9 @@ static lt_status ensure_bvh8(lt_ctx *c) {
     return LT_OK;
 }
 
+// The wide BVH a tuning's width needs (4 or 8: built once per scene).
+static lt_status ensure_width(lt_ctx *c, uint32_t width);
+
 extern "C" {
 
 lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
@@ -442,8 +446,7 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     d.filter = h.filter;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->has_scene = true;
-    if (c->tuning.bvh_width == 8) return ensure_bvh8(c);
-    return LT_OK;
+    return ensure_width(c, c->tuning.bvh_width);
 }
 
 lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) {
@@ -554,6 +557,41 @@ static Wavefront wave_view(const lt_ctx *c, uint32_t cap) {
     w.arena_bytes = carve_wave((char *)c->wave.arena, cap, &w);
     w.arena = c->wave.arena;
     return w;
+}
+
+// Builds the 4-wide BVH of the context's scene from its BVH2 (read back from
+// the device when the GPU built it) and uploads it; its leaves index the
+// BVH2's triangles.
+static lt_status ensure_bvh4(lt_ctx *c) {
+    if (c->has_bvh4) return LT_OK;
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
+    std::vector<BvhNode> nodes = c->host.nodes;
+    if (nodes.empty()) {
+        nodes.resize(c->num_nodes);
+        CUDA_TRY(c, cudaMemcpyAsync(nodes.data(), c->dev.nodes, nodes.size() * sizeof(BvhNode),
+                                    cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    std::vector<Bvh4Node> n4;
+    const uint32_t depth = build_bvh4(nodes, &n4);
+    if (3 * depth + 1 > 64)
+        return fail(c, LT_ERR_UNSUPPORTED, "4-wide BVH depth %u exceeds the traversal stack", depth);
+    std::vector<float> nf(n4.size() * 32);
+    memcpy(nf.data(), n4.data(), nf.size() * sizeof(float));
+    const float *d_nodes = nullptr;
+    lt_status st = upload(c, nf, &d_nodes);
+    if (st != LT_OK) return st;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->dev.nodes4 = (const float4 *)d_nodes;
+    c->dev.num_nodes4 = (uint32_t)n4.size();
+    c->has_bvh4 = true;
+    return LT_OK;
+}
+
+static lt_status ensure_width(lt_ctx *c, uint32_t width) {
+    if (width == 8) return ensure_bvh8(c);
+    if (width == 4) return ensure_bvh4(c);
+    return LT_OK;
 }
 
 extern "C" {
@@ -921,13 +959,13 @@ extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) {
         return fail(c, LT_ERR_INVALID, "threads per block must be 64, 128 or 256");
     if (n.loop_iterations != 2 && n.loop_iterations != 4 && n.loop_iterations != 8)
         return fail(c, LT_ERR_INVALID, "loop_iterations must be 2, 4 or 8");
-    if (n.bvh_width != 2 && n.bvh_width != 8)
-        return fail(c, LT_ERR_UNSUPPORTED, "BVH width %u: the widths built are 2 and 8", n.bvh_width);
+    if (n.bvh_width != 2 && n.bvh_width != 4 && n.bvh_width != 8)
+        return fail(c, LT_ERR_UNSUPPORTED, "BVH width %u: the widths built are 2, 4 and 8", n.bvh_width);
     if (n.paths_in_flight && (n.paths_in_flight < 1024 || n.paths_in_flight > kMaxPaths))
         return fail(c, LT_ERR_INVALID, "paths_in_flight %u outside 1024..67108864", n.paths_in_flight);
     CUDA_TRY(c, cudaSetDevice(c->device));
-    if (n.bvh_width == 8 && c->has_scene) {
-        lt_status st = ensure_bvh8(c);
+    if (c->has_scene) {
+        lt_status st = ensure_width(c, n.bvh_width);
         if (st != LT_OK) return st;
     }
     c->tuning = n;
@@ -1025,8 +1063,8 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
         const lt_film &f = films[i];
         if (!s || !s->has_scene) return fail(c, LT_ERR_STATE, "batch scene %u: no scene", i);
         if (s->device != c->device) return fail(c, LT_ERR_INVALID, "batch scene %u is on another device", i);
-        if (c->tuning.bvh_width == 8 && !s->has_bvh8) {
-            lt_status sb = ensure_bvh8(const_cast<lt_ctx *>(s));
+        if ((c->tuning.bvh_width == 8 && !s->has_bvh8) || (c->tuning.bvh_width == 4 && !s->has_bvh4)) {
+            lt_status sb = ensure_width(const_cast<lt_ctx *>(s), c->tuning.bvh_width);
             if (sb != LT_OK) return fail(c, sb, "batch scene %u: %s", i, s->error.c_str());
         }
         const uint32_t W = s->host.camera.width, H = s->host.camera.height;
@@ -1133,13 +1171,13 @@ extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const l
     lt_tuning cur = c->tuning;
     float cur_ms = 0.0f;
     if ((st = measure(cur, &cur_ms)) != LT_OK) return st;
-    const uint32_t widths[] = {2, 8};
+    const uint32_t widths[] = {2, 4, 8};
     const uint32_t paths[] = {1u << 20, 1u << 22, 1u << 24, 1u << 26};
     const uint32_t threads[] = {64, 128, 256};
     const uint32_t iters[] = {2, 4, 8};
     for (int coord = 0; coord < 5; ++coord) {
         const uint32_t *vals = coord == 0 ? widths : coord == 1 ? paths : coord == 4 ? iters : threads;
-        const int nv = coord == 0 ? 2 : coord == 1 ? 4 : 3;
+        const int nv = coord == 1 ? 4 : 3;
         for (int v = 0; v < nv; ++v) {
             lt_tuning t = cur;
             uint32_t *field = coord == 0   ? &t.bvh_width

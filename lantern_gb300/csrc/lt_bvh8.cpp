@@ -198,4 +198,72 @@ uint32_t build_bvh8(const std::vector<BvhNode> &nodes, const std::vector<float> 
     return max_depth;
 }
 
+
+uint32_t build_bvh4(const std::vector<BvhNode> &nodes, std::vector<Bvh4Node> *out) {
+    out->clear();
+    if (nodes.empty()) return 0;
+    struct Child {
+        float lo[3], hi[3];
+        int32_t ref;
+    };
+    auto child_of = [&](const BvhNode &n, int k) {
+        Child c;
+        const float *xy = k == 0 ? n.a : n.b;
+        c.lo[0] = xy[0]; c.hi[0] = xy[1]; c.lo[1] = xy[2]; c.hi[1] = xy[3];
+        c.lo[2] = n.c[2 * k]; c.hi[2] = n.c[2 * k + 1];
+        c.ref = n.ref[k];
+        return c;
+    };
+    struct Task {
+        int32_t bvh2;   // BVH2 node whose children form the 4-wide node
+        uint32_t slot;  // its index in *out
+        uint32_t depth;
+    };
+    std::vector<Task> stack;
+    out->push_back(Bvh4Node());
+    stack.push_back({0, 0, 1});
+    uint32_t depth = 0;
+    while (!stack.empty()) {
+        const Task t = stack.back();
+        stack.pop_back();
+        if (t.depth > depth) depth = t.depth;
+        Child ch[4];
+        int n = 0;
+        const BvhNode &b = nodes[(size_t)t.bvh2];
+        for (int k = 0; k < 2; ++k) {
+            const Child c = child_of(b, k);
+            if (c.ref >= 0) {  // open an inner child into its two children
+                const BvhNode &g = nodes[(size_t)c.ref];
+                ch[n++] = child_of(g, 0);
+                ch[n++] = child_of(g, 1);
+            } else {
+                ch[n++] = c;
+            }
+        }
+        Bvh4Node w;
+        memset(&w, 0, sizeof w);
+        w.count = (uint32_t)n;
+        for (int s = 0; s < 4; ++s) {
+            if (s >= n) {
+                w.lo_x[s] = w.lo_y[s] = w.lo_z[s] = 0.0f;
+                w.hi_x[s] = w.hi_y[s] = w.hi_z[s] = 0.0f;
+                w.ref[s] = kEmptyRef4;
+                continue;
+            }
+            w.lo_x[s] = ch[s].lo[0]; w.hi_x[s] = ch[s].hi[0];
+            w.lo_y[s] = ch[s].lo[1]; w.hi_y[s] = ch[s].hi[1];
+            w.lo_z[s] = ch[s].lo[2]; w.hi_z[s] = ch[s].hi[2];
+            if (ch[s].ref >= 0) {
+                const uint32_t slot = (uint32_t)out->size();
+                out->push_back(Bvh4Node());
+                w.ref[s] = (int32_t)slot;
+                stack.push_back({ch[s].ref, slot, t.depth + 1});
+            } else {
+                w.ref[s] = ch[s].ref;
+            }
+        }
+        (*out)[t.slot] = w;
+    }
+    return depth;
+}
 }  // namespace lt

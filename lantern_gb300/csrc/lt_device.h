@@ -27,6 +27,8 @@ struct DevScene {
     const float4 *light_tris;   // emissive meshes' triangles, 3 float4 each
     const float4 *nodes8;       // compressed 8-wide BVH (Bvh8Node, 5 float4 each), or null
     const float4 *tris8;        // triangles in 8-wide leaf order, 3 float4 each
+    const float4 *nodes4;       // 4-wide BVH (Bvh4Node, 8 float4 each; leaves index `tris`), or null
+    uint32_t num_nodes4;
     uint32_t num_lights;
     uint32_t num_tris;
     uint32_t num_nodes8;

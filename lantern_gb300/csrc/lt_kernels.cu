@@ -219,6 +219,86 @@ __device__ __forceinline__ void traverse(const Geo &S, Trav &r, St stack) {
     }
 }
 
+// ------------------------------------------------------------------ 4-wide traversal
+// 4-wide BVH (Bvh4Node, lt_scene.h: the children of a BVH2 node with its inner
+// children opened), traversed by the while-while loop above: a node's child
+// boxes are tested together, the children hit are taken nearest first (the
+// others stacked, farthest deepest), leaves are the BVH2's.
+__device__ __forceinline__ void cswap(float &ta, int &ca, float &tb, int &cb) {
+    if (tb < ta) {
+        const float t = ta;
+        ta = tb;
+        tb = t;
+        const int c = ca;
+        ca = cb;
+        cb = c;
+    }
+}
+
+template <class St>
+__device__ __forceinline__ void traverse4(const Geo &S, Trav &r, St stack) {
+    const float kInf = __int_as_float(0x7f800000);
+    while (r.node != kSentinel) {
+        while ((unsigned)r.node < (unsigned)kSentinel) {
+            const float4 *n = S.nodes + 8 * (size_t)r.node;
+            const float4 lx = ldg4(n), hx = ldg4(n + 1), ly = ldg4(n + 2), hy = ldg4(n + 3), lz = ldg4(n + 4),
+                         hz = ldg4(n + 5), rf = ldg4(n + 6);
+            int c0 = __float_as_int(rf.x), c1 = __float_as_int(rf.y), c2 = __float_as_int(rf.z),
+                c3 = __float_as_int(rf.w);
+            float t0, t1, t2, t3;
+            const bool b0 = slab(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, r.O, r.inv, r.tnear, r.h.t, t0) && c0 != kEmptyRef4;
+            const bool b1 = slab(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, r.O, r.inv, r.tnear, r.h.t, t1) && c1 != kEmptyRef4;
+            const bool b2 = slab(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, r.O, r.inv, r.tnear, r.h.t, t2) && c2 != kEmptyRef4;
+            const bool b3 = slab(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, r.O, r.inv, r.tnear, r.h.t, t3) && c3 != kEmptyRef4;
+            const int nh = (int)b0 + (int)b1 + (int)b2 + (int)b3;
+            if (nh == 0) {
+                r.node = stack.get(r.sp--);
+            } else {
+                if (!b0) t0 = kInf;
+                if (!b1) t1 = kInf;
+                if (!b2) t2 = kInf;
+                if (!b3) t3 = kInf;
+                cswap(t0, c0, t1, c1);  // sorting network, nearest first
+                cswap(t2, c2, t3, c3);
+                cswap(t0, c0, t2, c2);
+                cswap(t1, c1, t3, c3);
+                cswap(t1, c1, t2, c2);
+                if (nh > 3) stack.set(++r.sp, c3);
+                if (nh > 2) stack.set(++r.sp, c2);
+                if (nh > 1) stack.set(++r.sp, c1);
+                r.node = c0;
+            }
+            if (r.node < 0 && r.leaf >= 0) {  // postpone the first leaf, keep descending
+                r.leaf = r.node;
+                r.node = stack.get(r.sp--);
+            }
+            if (!__any_sync(__activemask(), r.leaf >= 0)) break;
+        }
+        while (r.leaf < 0) {
+            const uint32_t code = ~(uint32_t)r.leaf;
+            const uint32_t first = code >> kLeafBits, count = code & ((1u << kLeafBits) - 1u);
+            for (uint32_t k = 0; k < count; ++k) {
+                const float4 *tri = S.tris + 3 * (first + k);
+                if (!r.any) {
+                    tri_test(tri, r.O, r.D, r.tnear, r.h);
+                } else {
+                    Hit c = r.h;
+                    tri_test(tri, r.O, r.D, r.tnear, c);
+                    if (c.prim != kMiss && __ldg(S.tri_geom + c.prim) != r.skip_geom) {
+                        r.h.prim = c.prim;  // occluded
+                        r.node = kSentinel;
+                        r.leaf = 0;
+                        return;
+                    }
+                }
+            }
+            r.leaf = r.node;
+            if (r.node < 0) r.node = stack.get(r.sp--);
+        }
+        if (__popc(__activemask()) < kFetchThreshold) return;
+    }
+}
+
 // ------------------------------------------------------------------ 8-wide traversal
 // Compressed 8-wide BVH (Bvh8Node, lt_scene.h), traversed as in Ylitie,
 // Karras and Laine (HPG 2017): the ray keeps a node group -- the children of
@@ -392,6 +472,21 @@ struct Bvh2 {
         if (kSharedStack) traverse(g, r, SharedStack{st});
         else traverse(g, r, LocalStack{st});
     }
+    __device__ static bool done(const State &r) { return r.node == kSentinel; }
+    __device__ static void idle(State &r) { r.node = kSentinel; }
+};
+
+struct Bvh4 {
+    using State = Trav;
+    using Entry = int;
+    static constexpr int kDepth = kStack;
+    static constexpr int kSharedBytesPerThread = 0;
+    static constexpr int kMinBlocks256 = 0;  // k_trace register budget: compiler's choice
+    __device__ static Geo geo(const DevScene &S) { return Geo{S.nodes4, S.tris, S.tri_geom, S.num_nodes4, S.num_tris}; }
+    __device__ static void start(State &r, Entry *st, v3 O, v3 D, float tnear, float tfar, bool any, uint32_t skip) {
+        trav_start(r, LocalStack{st}, O, D, tnear, tfar, any, skip);
+    }
+    __device__ static void run(const Geo &g, State &r, Entry *st) { traverse4(g, r, LocalStack{st}); }
     __device__ static bool done(const State &r) { return r.node == kSentinel; }
     __device__ static void idle(State &r) { r.node = kSentinel; }
 };
@@ -1559,19 +1654,22 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
     cudaGetDeviceProperties(&prop, device);
     const int sms = prop.multiProcessorCount;
     out->sms = sms;
-    const bool w8 = out->bvh_width == 8;
+    const bool w8 = out->bvh_width == 8, w4 = out->bvh_width == 4;
     const int tt = out->trace_threads;
     if (batch) {
-        out->trace_blocks = w8 ? blocks_for(k_trace<ManyScenes, Bvh8>, tt, sms, trav_smem<Bvh8>(tt))
-                               : blocks_for(k_trace<ManyScenes, Bvh2>, tt, sms, trav_smem<Bvh2>(tt));
+        out->trace_blocks = w8   ? blocks_for(k_trace<ManyScenes, Bvh8>, tt, sms, trav_smem<Bvh8>(tt))
+                            : w4 ? blocks_for(k_trace<ManyScenes, Bvh4>, tt, sms, trav_smem<Bvh4>(tt))
+                                 : blocks_for(k_trace<ManyScenes, Bvh2>, tt, sms, trav_smem<Bvh2>(tt));
         out->shade_blocks = blocks_for(k_shade<ManyScenes>, out->shade_threads, sms);
     } else {
-        out->trace_blocks = w8 ? blocks_for(k_trace<OneScene, Bvh8>, tt, sms, trav_smem<Bvh8>(tt))
-                               : blocks_for(k_trace<OneScene, Bvh2>, tt, sms, trav_smem<Bvh2>(tt));
+        out->trace_blocks = w8   ? blocks_for(k_trace<OneScene, Bvh8>, tt, sms, trav_smem<Bvh8>(tt))
+                            : w4 ? blocks_for(k_trace<OneScene, Bvh4>, tt, sms, trav_smem<Bvh4>(tt))
+                                 : blocks_for(k_trace<OneScene, Bvh2>, tt, sms, trav_smem<Bvh2>(tt));
         out->shade_blocks = blocks_for(k_shade<OneScene>, out->shade_threads, sms);
     }
-    out->isect_blocks = w8 ? blocks_for(k_intersect<Bvh8>, 128, sms, trav_smem<Bvh8>(128))
-                           : blocks_for(k_intersect<Bvh2>, 128, sms, trav_smem<Bvh2>(128));
+    out->isect_blocks = w8   ? blocks_for(k_intersect<Bvh8>, 128, sms, trav_smem<Bvh8>(128))
+                        : w4 ? blocks_for(k_intersect<Bvh4>, 128, sms, trav_smem<Bvh4>(128))
+                             : blocks_for(k_intersect<Bvh2>, 128, sms, trav_smem<Bvh2>(128));
     out->diff_blocks = blocks_for(k_diff_adjoint, 128, sms);
     out->diff_fwd_batch_blocks = blocks_for(k_diff_forward_batch, 128, sms);
     out->diff_adj_batch_blocks = blocks_for(k_diff_adjoint_batch, 128, sms);
@@ -1608,6 +1706,8 @@ cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits
         int blocks = (int)(need < (unsigned long long)ls.isect_blocks ? need : ls.isect_blocks);
         if (ls.bvh_width == 8)
             k_intersect<Bvh8><<<blocks, 128, trav_smem<Bvh8>(128), st>>>(s, rays + 2 * off, hits + off, m, fetch);
+        else if (ls.bvh_width == 4)
+            k_intersect<Bvh4><<<blocks, 128, trav_smem<Bvh4>(128), st>>>(s, rays + 2 * off, hits + off, m, fetch);
         else
             k_intersect<Bvh2><<<blocks, 128, trav_smem<Bvh2>(128), st>>>(s, rays + 2 * off, hits + off, m, fetch);
         e = cudaGetLastError();
@@ -1628,6 +1728,7 @@ static cudaError_t stage(int stage, const Src &src, const Wavefront &w, int cur,
     if (stage == kStageTrace) {
         const int tt = ls.trace_threads;
         if (w8) k_trace<Src, Bvh8><<<ls.trace_blocks, tt, trav_smem<Bvh8>(tt), st>>>(src, w, cur);
+        else if (ls.bvh_width == 4) k_trace<Src, Bvh4><<<ls.trace_blocks, tt, trav_smem<Bvh4>(tt), st>>>(src, w, cur);
         else k_trace<Src, Bvh2><<<ls.trace_blocks, tt, trav_smem<Bvh2>(tt), st>>>(src, w, cur);
     } else {
         k_shade<Src><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(src, w, cur);

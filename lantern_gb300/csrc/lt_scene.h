@@ -138,6 +138,23 @@ void build_bvh(HostScene *s);
 uint32_t build_bvh8(const std::vector<BvhNode> &nodes, const std::vector<float> &leaf_tris,
                     std::vector<Bvh8Node> *out, std::vector<float> *tris8);
 
+// 4-wide BVH node, 128 bytes (eight 16-byte words), the four child boxes as
+// structure of arrays: [0] lo.x [1] hi.x [2] lo.y [3] hi.y [4] lo.z [5] hi.z of
+// children 0-3, [6] child refs (BVH2 encoding: inner >= 0, leaf < 0; an unused
+// slot holds kEmptyRef4), [7] number of children, 0, 0, 0.
+constexpr int32_t kEmptyRef4 = 0x7FFFFFFF;
+struct alignas(16) Bvh4Node {
+    float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4];
+    int32_t ref[4];
+    uint32_t count, pad[3];
+};
+
+// Collapses a BVH2 into 4-wide nodes: each 4-wide node takes the children of
+// one BVH2 node, opening every inner child into its two children (2-4 slots).
+// Leaf references are the BVH2's, so the BVH2's leaf-ordered triangles serve
+// both trees. Returns the depth of the 4-wide tree.
+uint32_t build_bvh4(const std::vector<BvhNode> &nodes, std::vector<Bvh4Node> *out);
+
 // PNG decoding as stbi_load(path, &w, &h, &n, 0) returns it (lt_image.cpp).
 lt_status decode_png(const uint8_t *file, size_t size, std::vector<uint8_t> *data, uint32_t *w, uint32_t *h,
                      uint32_t *n, std::string *err);

@@ -130,6 +130,63 @@ static Hit traverse8(const std::vector<Bvh8Node> &N, const std::vector<float> &T
     return h;
 }
 
+// Host emulation of the device's 4-wide traversal (traverse4): slab tests of
+// the node's child slots, hit children taken nearest first (the rest stacked),
+// leaf references into the BVH2's leaf-ordered triangles.
+static Hit traverse4(const std::vector<Bvh4Node> &N, const std::vector<float> &T, const float O[3], const float D[3],
+                     float tnear, uint32_t *visits) {
+    Hit h{INFINITY, 0, 0, 0xFFFFFFFFu};
+    float inv[3];
+    for (int c = 0; c < 3; ++c) inv[c] = 1.0f / (fabsf(D[c]) > 1e-30f ? D[c] : copysignf(1e-30f, D[c]));
+    std::vector<int32_t> st;
+    st.push_back(0);
+    int guard = 0;
+    while (!st.empty() && ++guard < 10000000) {
+        const int32_t ref = st.back();
+        st.pop_back();
+        if (ref < 0) {
+            const uint32_t code = ~(uint32_t)ref, first = code >> kLeafBits, cnt = code & ((1u << kLeafBits) - 1u);
+            for (uint32_t k = 0; k < cnt; ++k) {
+                CHECK(12 * (size_t)(first + k) < T.size(), "4-wide leaf triangle %u", first + k);
+                if (12 * (size_t)(first + k) >= T.size()) return h;
+                tri_test(&T[12 * (size_t)(first + k)], O, D, tnear, h);
+            }
+            continue;
+        }
+        CHECK((size_t)ref < N.size(), "4-wide node %d", ref);
+        if ((size_t)ref >= N.size()) return h;
+        const Bvh4Node &n = N[(size_t)ref];
+        ++*visits;
+        float tk[4];
+        int32_t ck[4];
+        int nh = 0;
+        for (int s = 0; s < 4; ++s) {
+            if (n.ref[s] == kEmptyRef4) continue;
+            CHECK((uint32_t)s < n.count, "4-wide node %d slot %d beyond its count", ref, s);
+            const float lo[3] = {n.lo_x[s], n.lo_y[s], n.lo_z[s]}, hi[3] = {n.hi_x[s], n.hi_y[s], n.hi_z[s]};
+            float tmin = tnear, tmax = h.t;
+            for (int c = 0; c < 3; ++c) {
+                const float a = (lo[c] - O[c]) * inv[c], b = (hi[c] - O[c]) * inv[c];
+                tmin = fmaxf(tmin, fminf(a, b));
+                tmax = fminf(tmax, fmaxf(a, b));
+            }
+            if (tmin <= tmax * 1.0000004f) {
+                tk[nh] = tmin;
+                ck[nh] = n.ref[s];
+                ++nh;
+            }
+        }
+        for (int i = 1; i < nh; ++i)  // nearest first
+            for (int j = i; j > 0 && tk[j] < tk[j - 1]; --j) {
+                std::swap(tk[j], tk[j - 1]);
+                std::swap(ck[j], ck[j - 1]);
+            }
+        for (int i = nh - 1; i >= 0; --i) st.push_back(ck[i]);
+        CHECK(st.size() <= 64, "4-wide stack depth %zu", st.size());
+    }
+    return h;
+}
+
 static void add_sphere(std::vector<float> &P, std::vector<uint32_t> &I, float cx, float cy, float cz, float r,
                        int sl, int stc) {
     uint32_t base = (uint32_t)(P.size() / 3);
@@ -236,6 +293,54 @@ static int run_case(const char *name, std::vector<float> P, std::vector<uint32_t
     CHECK(mism == 0, "%s: %d of %d rays differ from brute force", name, mism, nrays);
     printf("%s: %zu wide nodes, depth %u, %.2f node visits per ray\n", name, N.size(), depth,
            (double)visits / nrays);
+    // 4-wide tree: every BVH2 node's children, inner ones opened; BVH2 leaves
+    std::vector<Bvh4Node> N4;
+    const uint32_t depth4 = build_bvh4(hs.nodes, &N4);
+    CHECK(3 * depth4 + 1 <= 64, "%s: 4-wide depth %u", name, depth4);
+    std::vector<int> seen4(ntri, 0);
+    for (size_t i = 0; i < N4.size(); ++i) {
+        const Bvh4Node &n = N4[i];
+        CHECK(n.count >= 2 && n.count <= 4, "%s: 4-wide node %zu has %u children", name, i, n.count);
+        for (uint32_t s = 0; s < 4; ++s) {
+            if (s >= n.count) {
+                CHECK(n.ref[s] == kEmptyRef4, "%s: 4-wide node %zu slot %u not empty", name, i, s);
+                continue;
+            }
+            if (n.ref[s] >= 0) {
+                CHECK((size_t)n.ref[s] < N4.size() && (size_t)n.ref[s] > i, "%s: 4-wide node %zu child %d", name, i,
+                      n.ref[s]);
+            } else {
+                const uint32_t code = ~(uint32_t)n.ref[s], first = code >> kLeafBits,
+                               cnt = code & ((1u << kLeafBits) - 1u);
+                for (uint32_t k = 0; k < cnt; ++k) {
+                    CHECK(12 * (size_t)(first + k) < hs.leaf_tris.size(), "%s: 4-wide leaf range", name);
+                    const uint32_t prim = f_bits(hs.leaf_tris[12 * (size_t)(first + k) + 3]);
+                    if (prim < ntri) seen4[prim]++;
+                }
+            }
+        }
+    }
+    for (size_t t = 0; t < ntri; ++t) CHECK(seen4[t] == 1, "%s: triangle %zu in %d 4-wide leaves", name, t, seen4[t]);
+    std::mt19937 rng4(3);
+    uint64_t visits4 = 0;
+    int mism4 = 0;
+    for (int r = 0; r < nrays; ++r) {
+        float O[3], D[3];
+        for (int c = 0; c < 3; ++c) O[c] = lo[c] - 0.2f * (hi[c] - lo[c]) + 1.4f * (hi[c] - lo[c]) * u01(rng4);
+        float l = 0.0f;
+        for (int c = 0; c < 3; ++c) { D[c] = nd(rng4); l += D[c] * D[c]; }
+        for (int c = 0; c < 3; ++c) D[c] /= sqrtf(l);
+        uint32_t v = 0;
+        Hit a = traverse4(N4, hs.leaf_tris, O, D, 0.0f, &v);
+        visits4 += v;
+        Hit b{INFINITY, 0, 0, 0xFFFFFFFFu};
+        for (size_t k = 0; k < ntri; ++k) tri_test(&hs.leaf_tris[12 * k], O, D, 0.0f, b);
+        bool same = (a.prim == 0xFFFFFFFFu) == (b.prim == 0xFFFFFFFFu) && (a.prim == 0xFFFFFFFFu || a.t == b.t);
+        if (!same) ++mism4;
+    }
+    CHECK(mism4 == 0, "%s: %d of %d rays differ from brute force (4-wide)", name, mism4, nrays);
+    printf("%s: %zu 4-wide nodes, depth %u, %.2f node visits per ray\n", name, N4.size(), depth4,
+           (double)visits4 / nrays);
     return 0;
 }
 

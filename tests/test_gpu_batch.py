@@ -95,7 +95,7 @@ def test_batch_rejects_bad_arguments(scene_dir):
     with pytest.raises(LanternError, match="LT_ERR_INVALID"):
         s.ctx.set_tuning(trace_threads=96)
     with pytest.raises(LanternError, match="LT_ERR_UNSUPPORTED"):
-        s.ctx.set_tuning(bvh_width=4)
+        s.ctx.set_tuning(bvh_width=3)
 
 
 def test_generated_batch_with_tuning(scene_dir):

@@ -62,7 +62,7 @@ def _render_both(path, spp, depth, bvh_width):
     return got, ref
 
 
-@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("bvh_width", [2, 4, 8])
 def test_empty_scene_renders_the_background(scene_dir, bvh_width):
     path = _empty().write(scene_dir)
     got, ref = _render_both(path, 3, 8, bvh_width)
@@ -77,7 +77,7 @@ def test_empty_scene_renders_the_background(scene_dir, bvh_width):
     (_two_lights, 4, 8),
     (lambda: S.tiny_scene(width=37, height=23, name="edge_ragged"), 3, 10),
 ], ids=["no_lights", "two_lights", "ragged_37x23"])
-@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("bvh_width", [2, 4, 8])
 def test_edge_scene_matches_oracle_path_by_path(scene_dir, make, spp, depth, bvh_width):
     path = make().write(scene_dir)
     got, ref = _render_both(path, spp, depth, bvh_width)
@@ -89,7 +89,7 @@ def test_edge_scene_matches_oracle_path_by_path(scene_dir, make, spp, depth, bvh
     assert abs(m_g - m_o) <= 0.01 * abs(m_o) + 1e-6
 
 
-@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("bvh_width", [2, 4, 8])
 def test_single_pixel_film(scene_dir, bvh_width):
     """One pixel, direct light only (depth 1: no roulette, no bounce sampled
     from a transcendental), so every path takes the oracle's decisions."""
@@ -100,7 +100,7 @@ def test_single_pixel_film(scene_dir, bvh_width):
     assert np.allclose(got["rgb"], ref["rgb"], rtol=2e-4, atol=1e-5)
 
 
-@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("bvh_width", [2, 4, 8])
 def test_intersect_degenerate_rays(scene_dir, bvh_width):
     path = S.nine_spheres(width=16, height=16, slices=16, stacks=8, name="edge_isect").write(scene_dir)
     sc = Scene(0)

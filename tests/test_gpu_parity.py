@@ -63,7 +63,7 @@ def _compare_hits(gh, oh):
     return int(hit.sum()), int(diff.sum())
 
 
-@pytest.fixture(params=[2, 8], ids=["bvh2", "bvh8"])
+@pytest.fixture(params=[2, 4, 8], ids=["bvh2", "bvh4", "bvh8"])
 def width(request, ctx):
     """BVH width of the traversal (lt_tuning.bvh_width); the shared context is
     set back to 2 afterwards."""
@@ -121,7 +121,7 @@ def test_intersect_tnear_tfar_rule(ctx, width, scene_dir):
     (lambda: S.medium_sphere_scene(width=40, height=40, name="paths_med_hg"), 4, 32),
     (lambda: S.procedural_scene(width=48, height=40, name="paths_procedural"), 4, 8),
 ])
-@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("bvh_width", [2, 4, 8])
 def test_render_matches_oracle_path_by_path(scene_dir, make, spp, depth, bvh_width):
     path = make().write(scene_dir)
     sc = Scene(0)

@@ -145,7 +145,7 @@ def test_textured_oracle_matches_reference(reference_available, scene_dir):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bvh_width", [2, 8])
+@pytest.mark.parametrize("bvh_width", [2, 4, 8])
 def test_gpu_textured_render_matches_oracle(scene_dir, bvh_width):
     import torch
     from lantern_gb300.integrator import FrameBuffer, Integrator, Scene
