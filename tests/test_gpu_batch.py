@@ -151,6 +151,8 @@ def test_batch_of_the_maximum_size(scene_dir):
     s = _load(scene_dir, S.tiny_scene(width=4, height=3, name="bt_max"))
     ctx = s.ctx
     fbs = [FrameBuffer(s.width, s.height, "cuda:0") for _ in range(MAX_BATCH + 1)]
+    # the films are torch tensors made on torch's stream: the batch runs there too
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
     params = [(1 + (i % 3), i, 6, 3) for i in range(MAX_BATCH + 1)]
     with pytest.raises(LanternError, match="LT_ERR_INVALID"):
         ctx.render_batch([ctx] * (MAX_BATCH + 1), params, [f.film() for f in fbs])
