@@ -1171,13 +1171,13 @@ extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const l
     lt_tuning cur = c->tuning;
     float cur_ms = 0.0f;
     if ((st = measure(cur, &cur_ms)) != LT_OK) return st;
-    const uint32_t widths[] = {2, 4, 8};
+    const uint32_t widths[] = {2, 8};
     const uint32_t paths[] = {1u << 20, 1u << 22, 1u << 24, 1u << 26};
     const uint32_t threads[] = {64, 128, 256};
     const uint32_t iters[] = {2, 4, 8};
     for (int coord = 0; coord < 5; ++coord) {
         const uint32_t *vals = coord == 0 ? widths : coord == 1 ? paths : coord == 4 ? iters : threads;
-        const int nv = coord == 1 ? 4 : 3;
+        const int nv = coord == 0 ? 2 : coord == 1 ? 4 : 3;
         for (int v = 0; v < nv; ++v) {
             lt_tuning t = cur;
             uint32_t *field = coord == 0   ? &t.bvh_width
