@@ -42,6 +42,23 @@ SCENES = os.path.join(ROOT, "_scenes")
 TRACE_DRAM_BYTES_PER_RAY = 97.1
 
 
+def max_over_ranks(value: float, dist=None, device="cpu") -> float:
+    """The largest of every rank's `value` (a time): the whole job is as slow as
+    its slowest replica. Without a process group, `value` itself."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units all replicas processed per second, in millions (weak scaling: each
+    of the `world` ranks renders the same workload)."""
+    return units_per_rank * world / seconds / 1e6
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -291,13 +308,9 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     samples = scene.width * scene.height * spp * args.steps
-    t_ms = total_ms
-    if dist:
-        tt = torch.tensor([t_ms], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    value = samples * world / (t_ms / 1e3) / 1e6
-    mrays = rays * world / (t_ms / 1e3) / 1e6
+    t_ms = max_over_ranks(total_ms, dist, f"cuda:{local}")
+    value = whole_job_rate(samples, world, t_ms / 1e3)
+    mrays = whole_job_rate(rays, world, t_ms / 1e3)
 
     e2e = None
     if not args.no_e2e:
@@ -311,8 +324,8 @@ def main():
         t0 = time.perf_counter()
         for k in range(args.steps):
             render_host(scene.ctx, scene.width, scene.height, spp, 7 + k, rp["max_depth"], rp["rr_depth"], host)
-        e2e_s = time.perf_counter() - t0
-        e2e = {"value": round(samples * world / e2e_s / 1e6, 3), "unit": "Msamples/s",
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{local}")
+        e2e = {"value": round(whole_job_rate(samples, world, e2e_s), 3), "unit": "Msamples/s",
                "h2d_bytes_per_step": npix * 20, "d2h_bytes_per_step": npix * 20}
 
     micro = None
