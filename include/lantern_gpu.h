@@ -277,7 +277,8 @@ typedef struct lt_tuning {
  * tuner's starting point. Zero fields of lt_set_tuning keep their defaults
  * (0 paths = automatic, 128 threads, 2 iterations, width 2). Width 8 builds
  * the scene's compressed 8-wide BVH from its BVH2 (Ylitie, Karras, Laine, HPG
- * 2017 node layout); lt_scene_create then builds it for every new scene. */
+ * 2017 node layout), width 4 an uncompressed 4-wide one sharing the BVH2's
+ * triangles; lt_scene_create then builds it for every new scene. */
 lt_status lt_get_tuning(const lt_ctx *ctx, lt_tuning *out);
 lt_status lt_set_tuning(lt_ctx *ctx, const lt_tuning *t);
 
