@@ -3,6 +3,7 @@ scene: the same samples are traced either way, so per pixel the sample counts
 and summed path lengths are equal and the colour sums agree up to the order of
 the float additions into the film."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -166,3 +167,13 @@ def test_batch_of_the_maximum_size(scene_dir):
         Integrator(s, one, max_depth=6, rr_depth=3, first_frame=i).RenderFrame(params[i][0])
         torch.cuda.synchronize()
         _same(one, fbs[i])
+
+
+def test_batch_with_textures_and_procedural_primitives(scene_dir):
+    """Image and uv albedo textures and grid / geosphere primitives in a batch,
+    next to a plain scene, equal to one render per scene."""
+    scenes = [_load(scene_dir, S.textured_scene(os.path.join(scene_dir, "textures"), width=40, height=32,
+                                                name="bt_tex")),
+              _load(scene_dir, S.procedural_scene(width=32, height=24, name="bt_proc")),
+              _load(scene_dir, S.tiny_scene(width=24, height=20, name="bt_tiny2"))]
+    _check_batch(scenes, [3, 4, 2], [8, 8, 6], [2, 9, 0])

@@ -25,10 +25,12 @@ DEPTH, RR = 12, 3
 CALLS = [(0, 6, 4096), (100, 3, NOALLOC_MAX_PATHS)]  # (first frame, spp, paths in flight)
 
 
-def test_noalloc_render_matches_render(scene_dir):
+@pytest.mark.parametrize("bvh_width", [2, 8])
+def test_noalloc_render_matches_render(scene_dir, bvh_width):
     path = S.tiny_scene(width=48, height=40, name="noalloc_tiny").write(scene_dir)
     ctx = Context(0)
     ctx.load_scene_json(path)
+    ctx.set_tuning(bvh_width=bvh_width)
     info = ctx.scene_info()
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
     expected = []
