@@ -136,6 +136,12 @@ typedef struct lt_scene_desc {
  * sphere and radiance the way AddLMF and AreaLight's constructor do. */
 lt_status lt_scene_create(lt_ctx *ctx, const lt_scene_desc *desc);
 
+/* Frees the context's scene (its device arrays, BVHs and captured batch loop)
+ * and keeps the context; renders then fail with LT_ERR_STATE until a new
+ * scene is created. Replaces the Scene destructor's frees (scene.cpp:584-606).
+ * Waits for the context's stream first. */
+lt_status lt_scene_destroy(lt_ctx *ctx);
+
 /* Which builder lt_scene_create uses for the BVH (rtcCommitScene's job):
  * LT_BVH_GPU (default) -- binned SAH (32 bins, <= 4 triangles per leaf) built
  * level by level on the device; LT_BVH_HOST -- the same algorithm on the host

@@ -449,6 +449,16 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     return ensure_width(c, c->tuning.bvh_width);
 }
 
+lt_status lt_scene_destroy(lt_ctx *c) {
+    if (!c) return LT_ERR_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    free_graph(c);  // its scene table entries point into the scene
+    free_scene(c);
+    c->host = HostScene{};
+    return LT_OK;
+}
+
 lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) {
     if (!c || !out) return LT_ERR_INVALID;
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");

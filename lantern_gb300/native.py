@@ -22,7 +22,7 @@ MISS = 0xFFFFFFFF
 # exported symbols (include/lantern_gpu.h)
 SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error", "lt_set_stream", "lt_get_stream",
            "lt_sync",
-           "lt_scene_create", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
+           "lt_scene_create", "lt_scene_destroy", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
            "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load",
@@ -140,6 +140,7 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_sync.argtypes = [p]
         L.lt_scene_create.argtypes = [p, C.POINTER(SceneDesc)]
         L.lt_scene_load_json.argtypes = [p, C.c_char_p]
+        L.lt_scene_destroy.argtypes = [p]
         L.lt_scene_info_get.argtypes = [p, C.POINTER(SceneInfo)]
         L.lt_scene_mesh_offsets.argtypes = [p, C.POINTER(C.c_uint32), C.c_uint32]
         L.lt_render.argtypes = [p, C.POINTER(RenderParams), C.POINTER(Film)]
@@ -228,6 +229,10 @@ class Context:
 
     def create_scene(self, desc: SceneDesc):
         self._check(self.L.lt_scene_create(self.h, C.byref(desc)))
+
+    def destroy_scene(self):
+        """lt_scene_destroy: frees the scene, keeps the context."""
+        self._check(self.L.lt_scene_destroy(self.h))
 
     def scene_info(self) -> SceneInfo:
         info = SceneInfo()

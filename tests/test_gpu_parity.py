@@ -212,3 +212,21 @@ def test_gpu_bvh_build_matches_host_build(scene_dir, make):
         c.close()
     assert infos[BVH_GPU].num_bvh_nodes == infos[BVH_HOST].num_bvh_nodes
     assert infos[BVH_GPU].num_triangles == infos[BVH_HOST].num_triangles
+
+
+def test_scene_destroy_keeps_the_context(scene_dir):
+    """lt_scene_destroy frees the scene; rendering then reports LT_ERR_STATE,
+    and the same context loads and renders a scene again."""
+    path = S.tiny_scene(width=8, height=8, name="scene_destroy").write(scene_dir)
+    c = Context(0)
+    c.load_scene_json(path)
+    first = render_host(c, 8, 8, 2)
+    c.destroy_scene()
+    with pytest.raises(LanternError) as e:
+        render_host(c, 8, 8, 1)
+    assert e.value.status == 8  # LT_ERR_STATE
+    c.load_scene_json(path)
+    again = render_host(c, 8, 8, 2)
+    assert np.array_equal(first["counts"], again["counts"]) and np.array_equal(first["bounces"], again["bounces"])
+    assert np.allclose(first["rgb"], again["rgb"], rtol=1e-5, atol=1e-6)
+    c.close()
