@@ -1,4 +1,4 @@
-"""Benchmark: Lantern's path-tracing loop on one GB300 (configs: BASELINE workload names).
+"""Benchmark: Lantern's path-tracing loop on one GB300 (workloads named by scene and size).
 
 Default workload ("icosphere-1.3M"): the displaced icosphere scene --
 1,310,720 + 4 triangles, Lambert / mirror / dielectric meshes, 1024x1024,
