@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -115,10 +116,32 @@ static lt_status fail(lt_ctx *c, lt_status st, const char *fmt, ...) {
     va_start(ap, fmt);
     vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
-    if (c) c->error = buf;
-    else g_create_error = buf;
+    try {
+        if (c) c->error = buf;
+        else g_create_error = buf;
+    } catch (...) {  // no memory for the message: the status still goes back
+    }
     return st;
 }
+
+// No C++ exception crosses the C ABI: every entry point's body is a function
+// try block ending in LT_CATCH. Host allocation failures (std::bad_alloc, or
+// std::length_error for an impossible container size) become LT_ERR_OOM; any
+// other exception LT_ERR_INVALID. `c` is the context whose lt_last_error
+// carries the message (NULL: the thread's creation error).
+#define LT_CATCH(c)                                                                         \
+    catch (const std::bad_alloc &) {                                                        \
+        return fail(c, LT_ERR_OOM, "host memory allocation failed");                        \
+    }                                                                                       \
+    catch (const std::length_error &) {                                                     \
+        return fail(c, LT_ERR_OOM, "host container size out of range");                     \
+    }                                                                                       \
+    catch (const std::exception &e_) {                                                      \
+        return fail(c, LT_ERR_INVALID, "unexpected host error: %s", e_.what());             \
+    }                                                                                       \
+    catch (...) {                                                                           \
+        return fail(c, LT_ERR_INVALID, "unexpected host error");                            \
+    }
 
 #define CUDA_TRY(c, expr)                                                                           \
     do {                                                                                            \
@@ -174,7 +197,7 @@ extern "C" {
 
 int lt_abi_version(void) { return LT_ABI_VERSION; }
 
-lt_status lt_ctx_create(int device, lt_ctx **out) {
+lt_status lt_ctx_create(int device, lt_ctx **out) try {
     if (!out) return fail(nullptr, LT_ERR_INVALID, "out is NULL");
     *out = nullptr;
     int n = 0;
@@ -200,7 +223,7 @@ lt_status lt_ctx_create(int device, lt_ctx **out) {
     apply_tuning(c);
     *out = c;
     return LT_OK;
-}
+} LT_CATCH(nullptr)
 
 void lt_ctx_destroy(lt_ctx *c) {
     if (!c) return;
@@ -222,26 +245,26 @@ void lt_ctx_destroy(lt_ctx *c) {
 
 const char *lt_last_error(const lt_ctx *c) { return c ? c->error.c_str() : g_create_error.c_str(); }
 
-lt_status lt_set_stream(lt_ctx *c, void *stream) {
+lt_status lt_set_stream(lt_ctx *c, void *stream) try {
     if (!c) return LT_ERR_INVALID;
     c->stream = (cudaStream_t)stream;
     return LT_OK;
-}
+} LT_CATCH(c)
 
 void *lt_get_stream(const lt_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
-lt_status lt_set_bvh_builder(lt_ctx *c, int32_t builder) {
+lt_status lt_set_bvh_builder(lt_ctx *c, int32_t builder) try {
     if (!c) return LT_ERR_INVALID;
     if (builder != LT_BVH_GPU && builder != LT_BVH_HOST) return fail(c, LT_ERR_INVALID, "unknown BVH builder %d", builder);
     c->bvh_builder = builder;
     return LT_OK;
-}
+} LT_CATCH(c)
 
-lt_status lt_sync(lt_ctx *c) {
+lt_status lt_sync(lt_ctx *c) try {
     if (!c) return LT_ERR_INVALID;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return LT_OK;
-}
+} LT_CATCH(c)
 
 }  // extern "C"
 
@@ -323,7 +346,7 @@ static lt_status ensure_width(lt_ctx *c, uint32_t width);
 
 extern "C" {
 
-lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
+lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) try {
     NvtxRange nvtx_("lt_scene_create");
     if (!c || !desc) return fail(c, LT_ERR_INVALID, "NULL argument");
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -447,9 +470,9 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) {
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->has_scene = true;
     return ensure_width(c, c->tuning.bvh_width);
-}
+} LT_CATCH(c)
 
-lt_status lt_scene_destroy(lt_ctx *c) {
+lt_status lt_scene_destroy(lt_ctx *c) try {
     if (!c) return LT_ERR_INVALID;
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -457,9 +480,9 @@ lt_status lt_scene_destroy(lt_ctx *c) {
     free_scene(c);
     c->host = HostScene{};
     return LT_OK;
-}
+} LT_CATCH(c)
 
-lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) {
+lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) try {
     if (!c || !out) return LT_ERR_INVALID;
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
     out->width = c->host.camera.width;
@@ -472,15 +495,15 @@ lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) {
     out->device_bytes = c->scene_bytes;
     out->build_ms = c->host.build_ms;
     return LT_OK;
-}
+} LT_CATCH(c)
 
-lt_status lt_scene_mesh_offsets(lt_ctx *c, uint32_t *first, uint32_t capacity) {
+lt_status lt_scene_mesh_offsets(lt_ctx *c, uint32_t *first, uint32_t capacity) try {
     if (!c || !first) return LT_ERR_INVALID;
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
     if (capacity < c->host.geoms.size()) return fail(c, LT_ERR_INVALID, "capacity below mesh count");
     for (size_t g = 0; g < c->host.geoms.size(); ++g) first[g] = c->host.geoms[g].first_tri;
     return LT_OK;
-}
+} LT_CATCH(c)
 
 }  // extern "C"
 
@@ -606,7 +629,7 @@ static lt_status ensure_width(lt_ctx *c, uint32_t width) {
 
 extern "C" {
 
-lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
+lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) try {
     NvtxRange nvtx_("lt_render");
     if (!c || !p || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "lt_render without a scene");
@@ -720,18 +743,18 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) {
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     }
     return LT_OK;
-}
+} LT_CATCH(c)
 
-lt_status lt_render_stats_get(lt_ctx *c, lt_render_stats *out) {
+lt_status lt_render_stats_get(lt_ctx *c, lt_render_stats *out) try {
     if (!c || !out) return LT_ERR_INVALID;
     *out = c->stats;
     float ms = 0.0f;
     if (cudaEventSynchronize(c->ev1) == cudaSuccess && cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess)
         out->gpu_ms = ms;
     return LT_OK;
-}
+} LT_CATCH(c)
 
-lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, int32_t on_device) {
+lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, int32_t on_device) try {
     NvtxRange nvtx_("lt_intersect");
     if (!c || (n && (!rays || !hits))) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "lt_intersect without a scene");
@@ -753,9 +776,9 @@ lt_status lt_intersect(lt_ctx *c, const lt_ray *rays, lt_hit *hits, uint64_t n, 
     CUDA_TRY(c, cudaMemcpyAsync(hits, dh, n * 16, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return LT_OK;
-}
+} LT_CATCH(c)
 
-lt_status lt_diff_defaults(lt_ctx *c, float *albedo, float *emission, float *sigma_a, float *sigma_s) {
+lt_status lt_diff_defaults(lt_ctx *c, float *albedo, float *emission, float *sigma_a, float *sigma_s) try {
     if (!c) return LT_ERR_INVALID;
     if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
     const HostScene &h = c->host;
@@ -773,7 +796,7 @@ lt_status lt_diff_defaults(lt_ctx *c, float *albedo, float *emission, float *sig
             if (sigma_s) sigma_s[3 * i + k] = h.media[i].sigma_s[k];
         }
     return LT_OK;
-}
+} LT_CATCH(c)
 
 static lt_status diff_setup(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, DiffParams *P,
                             RenderArgs *a) {
@@ -798,7 +821,7 @@ static lt_status diff_setup(lt_ctx *c, const lt_render_params *p, const lt_diff_
 }
 
 lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, lt_film *film,
-                         float *sample_radiance) {
+                         float *sample_radiance) try {
     NvtxRange nvtx_("lt_render_diff");
     if (!c || !p || !dp || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     DiffParams P;
@@ -815,11 +838,11 @@ lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_par
     c->stats.samples = a.total;
     c->stats.kernel_launches = 1;
     return LT_OK;
-}
+} LT_CATCH(c)
 
 lt_status lt_render_adjoint(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, const float *dI,
                             float *g_albedo, float *g_emission, float *g_sigma_a, float *g_sigma_s,
-                            const uint32_t *crop, const float *sample_radiance) {
+                            const uint32_t *crop, const float *sample_radiance) try {
     NvtxRange nvtx_("lt_render_adjoint");
     if (!c || !p || !dp || !dI || !g_albedo || !g_emission) return fail(c, LT_ERR_INVALID, "NULL argument");
     DiffParams P;
@@ -843,9 +866,9 @@ lt_status lt_render_adjoint(lt_ctx *c, const lt_render_params *p, const lt_diff_
     c->stats.samples = a.total;
     c->stats.kernel_launches = 1;
     return LT_OK;
-}
+} LT_CATCH(c)
 
-lt_status lt_scene_load_json(lt_ctx *c, const char *path) {
+lt_status lt_scene_load_json(lt_ctx *c, const char *path) try {
     if (!c || !path) return fail(c, LT_ERR_INVALID, "NULL argument");
     lt_scene_desc desc;
     JsonSceneStorage storage;
@@ -853,7 +876,7 @@ lt_status lt_scene_load_json(lt_ctx *c, const char *path) {
     lt_status st = load_scene_json(path, &desc, &storage, &err);
     if (st != LT_OK) return fail(c, st, "%s", err.c_str());
     return lt_scene_create(c, &desc);
-}
+} LT_CATCH(c)
 
 }  // extern "C"
 
@@ -872,7 +895,7 @@ static Wavefront carve_noalloc(char *a, uint32_t cap) {
 }
 
 extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_film *film,
-                                       uint32_t paths_in_flight) {
+                                       uint32_t paths_in_flight) try {
     if (!c || !p || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (paths_in_flight == 0 || paths_in_flight > LT_NOALLOC_MAX_PATHS)
         return fail(c, LT_ERR_INVALID, "paths_in_flight = %u; lt_render_noalloc holds 1..%u paths", paths_in_flight,
@@ -944,7 +967,7 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
     c->stats.samples = a.total;
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     return LT_OK;
-}
+} LT_CATCH(c)
 
 // ------------------------------------------------------------------ tuning
 extern "C" lt_status lt_get_tuning(const lt_ctx *c, lt_tuning *out) {
@@ -955,7 +978,7 @@ extern "C" lt_status lt_get_tuning(const lt_ctx *c, lt_tuning *out) {
 
 static bool valid_threads(uint32_t t) { return t == 64 || t == 128 || t == 256; }
 
-extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) {
+extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) try {
     if (!c || !t) return fail(c, LT_ERR_INVALID, "NULL argument");
     lt_tuning n;
     default_tuning(&n);
@@ -981,7 +1004,7 @@ extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) {
     c->tuning = n;
     apply_tuning(c);
     return LT_OK;
-}
+} LT_CATCH(c)
 
 // ------------------------------------------------------------------ lt_render_batch
 // Captures the batched loop for wavefront `w`: memset(counters), camera rays,
@@ -1055,7 +1078,7 @@ static lt_status ensure_table(lt_ctx *c) {
 }
 
 extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_render_params *params,
-                                     lt_film *films, uint32_t n) {
+                                     lt_film *films, uint32_t n) try {
     NvtxRange nvtx_("lt_render_batch");
     if (!c || (n && (!scenes || !params || !films))) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u scenes; a batch holds at most %u", n, LT_MAX_BATCH);
@@ -1132,11 +1155,11 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
     }
     c->stats.kernel_launches = launches;
     return LT_OK;
-}
+} LT_CATCH(c)
 
 // ------------------------------------------------------------------ lt_autotune_batch
 extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_render_params *params, uint32_t n,
-                                       uint32_t spp_cap, lt_tuning *best) {
+                                       uint32_t spp_cap, lt_tuning *best) try {
     if (!c || !n || !scenes || !params) return fail(c, LT_ERR_INVALID, "NULL argument or empty batch");
     if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u scenes; a batch holds at most %u", n, LT_MAX_BATCH);
     if (spp_cap == 0) spp_cap = 1;
@@ -1209,11 +1232,11 @@ extern "C" lt_status lt_autotune_batch(lt_ctx *c, lt_ctx *const *scenes, const l
     if ((st = lt_set_tuning(c, &cur)) != LT_OK) return st;
     if (best) *best = c->tuning;
     return LT_OK;
-}
+} LT_CATCH(c)
 
 // ------------------------------------------------------------------ lt_resolve
 extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap, float exposure_stops, float *rgba,
-                                uint8_t *rgba8, lt_spp_range *spp) {
+                                uint8_t *rgba8, lt_spp_range *spp) try {
     NvtxRange nvtx_("lt_resolve");
     if (!c || !film) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (tonemap != LT_TONEMAP_CLAMP && tonemap != LT_TONEMAP_FILMIC)
@@ -1269,7 +1292,7 @@ extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap,
         }
     }
     return LT_OK;
-}
+} LT_CATCH(c)
 
 // ------------------------------------------------------------------ batched differentiable rendering
 static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool adjoint) {
@@ -1344,17 +1367,17 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
     return LT_OK;
 }
 
-extern "C" lt_status lt_render_diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n) {
+extern "C" lt_status lt_render_diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n) try {
     return diff_batch(c, jobs, n, false);
-}
+} LT_CATCH(c)
 
-extern "C" lt_status lt_render_adjoint_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n) {
+extern "C" lt_status lt_render_adjoint_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n) try {
     return diff_batch(c, jobs, n, true);
-}
+} LT_CATCH(c)
 
 // ------------------------------------------------------------------ lt_image_load
 extern "C" lt_status lt_image_load(const char *path, uint8_t *texels, size_t capacity, uint32_t *width,
-                                   uint32_t *height, uint32_t *channels) {
+                                   uint32_t *height, uint32_t *channels) try {
     if (!path || !width || !height || !channels) return fail(nullptr, LT_ERR_INVALID, "NULL argument");
     std::vector<uint8_t> data;
     std::string err;
@@ -1366,6 +1389,6 @@ extern "C" lt_status lt_image_load(const char *path, uint8_t *texels, size_t cap
         memcpy(texels, data.data(), data.size());
     }
     return LT_OK;
-}
+} LT_CATCH(nullptr)
 
 extern "C" void lt_debug_fail_allocations(uint32_t after) { g_alloc_left.store(after); }

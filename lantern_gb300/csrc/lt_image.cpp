@@ -238,8 +238,13 @@ lt_status decode_png(const uint8_t *file, size_t size, std::vector<uint8_t> *dat
     const bool depth_ok = depth == 8 || depth == 16 || ((ctype == 0 || ctype == 3) && (depth == 1 || depth == 2 || depth == 4));
     if (!depth_ok || (ctype == 3 && depth == 16)) { *err = "bad PNG bit depth"; return LT_ERR_PARSE; }
     if (ctype == 3 && (plte.empty() || plte.size() % 3)) { *err = "PNG palette missing"; return LT_ERR_PARSE; }
+    // deflate expands at most 1032:1 (258-byte matches in 2-bit codes), so a
+    // header whose filtered image cannot come out of this much data is
+    // rejected before anything of its size is allocated
+    const size_t raw_bytes = (size_t)H * (((size_t)W * chans * depth + 7) / 8 + 1);
+    if (raw_bytes / 1032 > idat.size() + 1) { *err = "PNG image data too short"; return LT_ERR_PARSE; }
     std::vector<uint8_t> raw;
-    raw.reserve((size_t)H * (((size_t)W * chans * depth + 7) / 8 + 1));
+    raw.reserve(raw_bytes);
     if (!inflate_zlib(idat.data(), idat.size(), raw)) { *err = "corrupt PNG image data"; return LT_ERR_PARSE; }
     const size_t stride = ((size_t)W * chans * depth + 7) / 8;
     const size_t bpp = ((size_t)chans * depth + 7) / 8;  // filter unit, bytes

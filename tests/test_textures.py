@@ -125,6 +125,13 @@ def test_image_load_errors(tmp_path):
         native.load_image(str(bad))
     with pytest.raises(native.LanternError, match="LT_ERR_IO"):
         native.load_image(str(tmp_path / "missing.png"))
+    # a 65536 x 65536 16-bit RGBA header over a few bytes of image data: rejected
+    # as malformed before a 34 GB buffer is reserved for it
+    huge = tmp_path / "huge.png"
+    huge.write_bytes(b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", 65536, 65536, 16, 6, 0, 0, 0))
+                     + _chunk(b"IDAT", zlib.compress(b"\x00" * 64)) + _chunk(b"IEND", b""))
+    with pytest.raises(native.LanternError, match="LT_ERR_PARSE"):
+        native.load_image(str(huge))
 
 
 def test_textured_oracle_matches_reference(reference_available, scene_dir):
