@@ -17,9 +17,13 @@ Reported (one JSON line on rank 0):
                child-box test + 40 B per triangle test, node/triangle counts
                from the oracle's BVH2 on a pixel-subsampled render of the same
                frame) / trace-kernel device time, against measured HBM GB/s
-  cpu_baseline the reference integrator (oracle/_ref) on the host cores, one
-               frame of the same scene
---impl reference runs only the reference CPU path (its own arm).
+  cpu_baseline the reference integrator (oracle/_ref) on the host cores, whole
+               frames of the same scene for about 10 s (the oracle's
+               restatement for medium-c2, whose HG phase and RGB sigma_s the
+               reference's scene JSON cannot state)
+--impl reference runs only that CPU path (its own arm).
+Other workloads (--workload): nine-spheres (256x256, 16 spp, depth 8),
+medium-c2r and medium-c2 (the medium sphere, 512x512, 256 spp, depth 32).
 """
 from __future__ import annotations
 
@@ -81,7 +85,43 @@ def make_scene(name: str):
         sc = S.medium_sphere_scene(width=512, height=512, spp=256, max_depth=32, rr_depth=3,
                                    reference_expressible=True, name="bench_c2r")
         return sc, {"spp": 256, "max_depth": 32, "rr_depth": 3}
+    if name == "medium-c2":  # the full medium scene: RGB sigma_s, Henyey-Greenstein g = 0.3
+        sc = S.medium_sphere_scene(width=512, height=512, spp=256, max_depth=32, rr_depth=3, name="bench_c2")
+        return sc, {"spp": 256, "max_depth": 32, "rr_depth": 3}
     raise SystemExit(f"unknown workload {name}")
+
+
+# Workloads whose scene the reference's JSON cannot state (its media have an
+# isotropic phase and a scalar sigma_s): their CPU baseline is the oracle's C
+# restatement of the same estimator, run on every host core.
+PORT_ONLY = {"medium-c2"}
+
+
+def cpu_renderer(path, workload):
+    """The CPU implementation a workload is timed with: the reference integrator
+    (oracle/_ref) or, for PORT_ONLY workloads, the oracle. Returns (render,
+    width, height, kind, cores) with render(frames, first_frame, max_depth,
+    rr_depth) -> (seconds, rays), or None when the reference is not built."""
+    from oracle import oracle as O
+    cores = int(os.environ.get("LT_REF_THREADS", os.cpu_count()))
+    if workload in PORT_ONLY:
+        sc = O.OracleScene(path)
+
+        def render(frames, first, max_depth, rr_depth):
+            t0 = time.perf_counter()
+            r = sc.render(frames, first_frame=first, max_depth=max_depth, rr_depth=rr_depth, threads=cores)
+            return time.perf_counter() - t0, sum(r["rays"])
+        return render, sc.width, sc.height, "port", cores
+    if not os.path.exists(O.REF_SO):
+        O.build_reference()
+    if not os.path.exists(O.REF_SO):
+        return None
+    ref = O.ReferenceScene(path)
+
+    def render(frames, first, max_depth, rr_depth):
+        r = ref.render(frames, first_frame=first, max_depth=max_depth, rr_depth=rr_depth)
+        return r["seconds"], r["rays"]
+    return render, ref.width, ref.height, "reference", cores
 
 
 class ClockSampler:
@@ -171,45 +211,43 @@ def bytes_per_ray(scene_path: str, width: int, height: int, max_depth: int, rr_d
 
 
 def run_reference(args, workload):
-    """The reference CPU integrator (oracle/_ref) on this host's cores."""
-    from oracle import oracle as O
+    """The reference CPU integrator (oracle/_ref) on this host's cores (the
+    oracle's restatement for PORT_ONLY workloads)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    sc, rp = make_scene(workload)
+    path = __import__("lantern_gb300.scenes", fromlist=["x"]).ensure_written(sc, SCENES)
     try:
-        if not os.path.exists(O.REF_SO):
-            O.build_reference()
+        cr = cpu_renderer(path, workload)
     except RuntimeError as e:
         print(json.dumps({"impl": "reference", "unavailable": f"reference build failed: {str(e)[:200]}"}))
         return
-    if not os.path.exists(O.REF_SO):
+    if cr is None:
         print(json.dumps({"impl": "reference", "unavailable": "reference sources not staged (oracle/_ref/src)"}))
         return
-    sc, rp = make_scene(workload)
-    path = __import__("lantern_gb300.scenes", fromlist=["x"]).ensure_written(sc, SCENES)
-    ref = O.ReferenceScene(path)
+    render, width, height, kind, cores = cr
     t1 = 1.0
     for _ in range(args.warmup):
-        t1 = ref.render(1, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])["seconds"]
+        t1 = render(1, 0, rp["max_depth"], rp["rr_depth"])[0]
     # each step: a bounded sample of about 2 s of CPU work (whole frames)
     frames_per_step = int(max(1, min(64, round(2.0 / max(t1, 1e-6)))))
     secs, rays = 0.0, 0
     for k in range(args.steps):
-        r = ref.render(frames_per_step, first_frame=1000 + k, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
-        secs += r["seconds"]
-        rays += r["rays"]
-    samples = sc.width * sc.height * frames_per_step * args.steps
+        s, r = render(frames_per_step, 1000 + k, rp["max_depth"], rp["rr_depth"])
+        secs += s
+        rays += r
+    samples = width * height * frames_per_step * args.steps
     v = samples / secs / 1e6
-    cores = int(os.environ.get("LT_REF_THREADS", os.cpu_count()))
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Msamples/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": workload, "width": sc.width, "height": sc.height, "spp_per_step": frames_per_step,
+            "config": {"workload": workload, "width": width, "height": height, "spp_per_step": frames_per_step,
                        "max_depth": rp["max_depth"], "rr_depth": rp["rr_depth"], "triangles": sc.num_triangles},
             "mrays": round(rays / secs / 1e6, 4),
-            "cpu_baseline": {"value": round(v, 4), "unit": "Msamples/s", "cores": cores, "kind": "reference",
-                             "sample": f"{args.steps} x {frames_per_step} frame(s) of {sc.width}x{sc.height}"},
+            "cpu_baseline": {"value": round(v, 4), "unit": "Msamples/s", "cores": cores, "kind": kind,
+                             "sample": f"{args.steps} x {frames_per_step} frame(s) of {width}x{height}"},
             "e2e": {"value": round(v, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -360,7 +398,7 @@ def main():
             roof = {"error": str(e)[:200]}
         cpu = None
         if not args.no_cpu_baseline:
-            cpu = cpu_baseline(path, rp)
+            cpu = cpu_baseline(path, rp, args.workload)
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_ms / args.steps, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -572,23 +610,21 @@ def microbench(scene, path, local, n=1 << 24):
     return out
 
 
-def cpu_baseline(path, rp):
-    """Reference CPU integrator on this host, one frame of the same scene."""
-    from oracle import oracle as O
+def cpu_baseline(path, rp, workload):
+    """The workload's CPU implementation (cpu_renderer) on this host, whole
+    frames of the same scene for about 10 s."""
     try:
-        if not os.path.exists(O.REF_SO):
-            O.build_reference()
-        if not os.path.exists(O.REF_SO):
+        cr = cpu_renderer(path, workload)
+        if cr is None:
             return None
-        ref = O.ReferenceScene(path)
-        t1 = ref.render(1, first_frame=98, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])["seconds"]
+        render, width, height, kind, cores = cr
+        t1 = render(1, 98, rp["max_depth"], rp["rr_depth"])[0]
         frames = int(max(1, min(256, round(10.0 / max(t1, 1e-6)))))  # about 10 s of CPU work
-        r = ref.render(frames, first_frame=99, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
-        n = ref.width * ref.height * frames
-        return {"value": round(n / r["seconds"] / 1e6, 4), "unit": "Msamples/s",
-                "cores": int(os.environ.get("LT_REF_THREADS", os.cpu_count())), "kind": "reference",
-                "sample": f"{frames} frame(s) (1 spp each) of {ref.width}x{ref.height}, {r['seconds']:.1f} s",
-                "mrays": round(r["rays"] / r["seconds"] / 1e6, 3)}
+        secs, rays = render(frames, 99, rp["max_depth"], rp["rr_depth"])
+        n = width * height * frames
+        return {"value": round(n / secs / 1e6, 4), "unit": "Msamples/s", "cores": cores, "kind": kind,
+                "sample": f"{frames} frame(s) (1 spp each) of {width}x{height}, {secs:.1f} s",
+                "mrays": round(rays / secs / 1e6, 3)}
     except Exception as e:
         return {"error": str(e)[:200]}
 
