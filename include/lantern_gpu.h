@@ -307,7 +307,7 @@ lt_status lt_render_batch(lt_ctx *ctx, lt_ctx *const *scenes, const lt_render_pa
                           uint32_t n);
 
 /* Autotuner: renders the batch (into scratch films, spp capped at spp_cap) under
- * candidate tunings -- BVH width, paths in flight, threads per block of each
+ * candidate tunings -- BVH width 2 or 8, paths in flight, threads per block of each
  * stage, iterations per loop body -- by coordinate descent from ctx's tuning,
  * keeps the fastest in ctx and returns it in *best (may be NULL). Trying width
  * 8 builds the 8-wide BVH of every scene of the batch. */

@@ -1,7 +1,7 @@
 // lt_api.cpp -- the C ABI declared in include/lantern_gpu.h.
 //
 // A context owns a CUDA stream, the device copy of one scene (triangles, BVH2
-// and on demand the 8-wide BVH, shading tables, textures) and the wavefront
+// and on demand the 4- and 8-wide BVHs, shading tables, textures) and the wavefront
 // buffers, which are sized once and reused. lt_render queues the wavefront: an
 // initial camera-ray launch, then batches of (trace, shade) iterations, reading
 // the queue lengths back once per batch until no path or connection record is

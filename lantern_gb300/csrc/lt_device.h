@@ -94,7 +94,7 @@ struct RenderArgs {
 // the occupancy of the kernel at that size (persistent grids: one full wave).
 struct LaunchShape {
     int sms = 0;
-    int bvh_width = 2;  // 2: BVH2 traversal; 8: compressed 8-wide traversal
+    int bvh_width = 2;  // 2: BVH2 traversal; 4: 4-wide; 8: compressed 8-wide
     int trace_threads = 128, shade_threads = 128;
     int trace_blocks = 0, shade_blocks = 0, isect_blocks = 0;
     int diff_blocks = 0;
