@@ -175,6 +175,16 @@ static void free_wave(lt_ctx *c) {
     c->wave = Wavefront{};
 }
 
+// Wavefront iterations to queue before the first read of the queue lengths.
+// With every sample in flight nothing is regenerated, and every event of a path
+// (surface bounce or medium scatter) adds a bounce, so max_depth iterations end
+// every path and one more traces the last shade's connection records: a short
+// render then needs a single read. Otherwise 4; the loop checks the queues
+// after each batch either way, so the bound only saves synchronisations.
+static uint32_t first_batch(unsigned long long total, uint32_t cap, uint32_t max_depth) {
+    return total <= cap && max_depth < 64u ? max_depth + 1u : 4u;
+}
+
 static void default_tuning(lt_tuning *t) {
     *t = lt_tuning{};
     t->trace_threads = t->shade_threads = 128;
@@ -681,7 +691,7 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) try {
         // Iterations launched between two reads of the queue lengths. While
         // work items remain, at most `cap` of them start per iteration, so the
         // loop cannot end within remaining / cap iterations.
-        uint32_t batch = 4;
+        uint32_t batch = first_batch(a.total, cap, p->max_depth);
         for (;;) {
             for (uint32_t k = 0; k < batch; ++k) {
                 for (int stage = 0; stage < kStages; ++stage) {
@@ -937,7 +947,7 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
         CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
         uint32_t launches = 1, iters = 0;
         int cur = 0;
-        uint32_t batch = 4;  // iterations between reads of the queue lengths, as in lt_render
+        uint32_t batch = first_batch(a.total, cap, p->max_depth);  // as in lt_render
         const uint32_t limit = 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u;
         for (;;) {
             for (uint32_t k = 0; k < batch; ++k) {
