@@ -13,8 +13,10 @@
  * Plain pointers and sizes only; no exceptions cross this boundary. Every call
  * returns an lt_status; lt_last_error() gives the message of the last failure
  * on that context. One host thread drives one context; all GPU work is issued
- * on the context's stream and lt_render/lt_intersect return once it is queued
- * (device buffers) or finished (host buffers).
+ * on the context's stream. lt_render returns when the render has finished
+ * (it reads the wavefront's queue lengths to know when to stop, so its film
+ * writes are complete, device or host film); lt_intersect returns once its
+ * work is queued (device buffers) or finished (host buffers).
  */
 #ifndef LANTERN_GPU_H
 #define LANTERN_GPU_H
