@@ -362,20 +362,26 @@ def displaced_icosphere_scene(width=1024, height=1024, spp=64, max_depth=10, rr_
 
 
 def medium_sphere_scene(width=512, height=512, spp=256, max_depth=32, rr_depth=3,
-                        reference_expressible=False, name="medium_sphere") -> Scene:
+                        reference_expressible=False, name="medium_sphere", non_scattering=False) -> Scene:
     """Dielectric sphere (IOR 1.33, 128x64) holding a homogeneous medium, on the
     nine-sphere ground under the same light. The full form has RGB
     sigma_s=(2.0,1.5,1.0), sigma_a=(0.05,0.1,0.2) and Henyey-Greenstein g=0.3
     (an extension). ``reference_expressible`` gives the form the reference JSON
     can state: isotropic phase, scalar sigma_s=1.5 as ``scattering_distance``
-    1/1.5, and sigma_a as ``absorption_color`` exp(-sigma_a) at distance 1."""
+    1/1.5, and sigma_a as ``absorption_color`` exp(-sigma_a) at distance 1.
+    ``non_scattering`` gives the reference's absorbing-only medium
+    (non_scattering_medium.h) with the same sigma_a."""
     sc = Scene(width, height,
                camera={"phi": 1.1, "theta": 0.0, "radius": 6.0, "fov": 0.785398,
                        "target": [0.0, 0.8, 0.0]},
                render={"spp": spp, "max_depth": max_depth, "rr_depth": rr_depth},
                name=name)
     sigma_a = np.array([0.05, 0.1, 0.2])
-    if reference_expressible:
+    if non_scattering:
+        sc.media.append({"name": "fog", "type": "non_scattering",
+                         "absorption_color": [float(x) for x in np.exp(-sigma_a)],
+                         "absorption_at_distance": 1.0})
+    elif reference_expressible:
         sc.media.append({"name": "fog", "type": "isotropic_scattering",
                          "absorption_color": [float(x) for x in np.exp(-sigma_a)],
                          "absorption_at_distance": 1.0,

@@ -119,6 +119,7 @@ def test_intersect_tnear_tfar_rule(ctx, width, scene_dir):
     (lambda: S.nine_spheres(width=64, height=64, name="paths_nine"), 4, 8),
     (lambda: S.medium_sphere_scene(width=40, height=40, reference_expressible=True, name="paths_med_ref"), 4, 32),
     (lambda: S.medium_sphere_scene(width=40, height=40, name="paths_med_hg"), 4, 32),
+    (lambda: S.medium_sphere_scene(width=40, height=40, non_scattering=True, name="paths_med_absorb"), 4, 32),
     (lambda: S.procedural_scene(width=48, height=40, name="paths_procedural"), 4, 8),
 ])
 @pytest.mark.parametrize("bvh_width", [2, 4, 8])

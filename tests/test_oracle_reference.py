@@ -23,6 +23,7 @@ def _bits(a):
     (lambda: S.tiny_scene(width=40, height=40, name="tiny_40"), 4, 12, 3),
     (lambda: S.medium_sphere_scene(width=32, height=32, reference_expressible=True,
                                    name="medium_ref_32"), 2, 32, 3),
+    (lambda: S.medium_sphere_scene(width=32, height=32, non_scattering=True, name="medium_absorb_32"), 2, 32, 3),
     (lambda: S.tiny_scene(width=24, height=16, name="tiny_24x16"), 2, 1500, 3),
     (lambda: S.procedural_scene(width=40, height=32, name="procedural_40"), 3, 8, 3),
 ])
