@@ -608,10 +608,17 @@ static_assert(kMaxLights <= kConnLightMask + 1 && kMaxMedia < kFlagMediumMask, "
 // with the sampler of (pixel, frame).
 __device__ __forceinline__ void start_path(const DevScene &S, const RenderArgs &a, unsigned long long item, Path &p,
                                            v3 &org, v3 &dir, float &tnear) {
-    uint32_t npix = a.width * a.height;
-    p.frame = a.first_frame + (uint32_t)(item / npix);
-    p.pixel = (uint32_t)(item % npix);
-    uint32_t x = p.pixel % a.width, y = p.pixel / a.width;
+    const uint32_t npix = a.width * a.height;
+    uint32_t fo;
+    if (item >> 32 == 0) {  // 32-bit division when the item index fits (the same quotient)
+        fo = (uint32_t)item / npix;
+        p.pixel = (uint32_t)item - fo * npix;
+    } else {
+        fo = (uint32_t)(item / npix);
+        p.pixel = (uint32_t)(item - (unsigned long long)fo * npix);
+    }
+    p.frame = a.first_frame + fo;
+    const uint32_t y = p.pixel / a.width, x = p.pixel - y * a.width;
     p.rng = sampler_for(p.pixel, p.frame);
     float u = tent_sample(S.filter, p.rng.next_float());
     float v = tent_sample(S.filter, p.rng.next_float());
