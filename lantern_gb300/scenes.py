@@ -597,6 +597,30 @@ def tiny_scene(width=32, height=32, spp=4, max_depth=8, rr_depth=3, name="tiny")
     return sc
 
 
+def unlit_scene(width=13, height=7, name="unlit") -> Scene:
+    """tiny_scene without its emitter, under a (0.5, 0.6, 0.7) background:
+    SampleOneLight returns black (integrator.cpp:255-261), so only the
+    background reaches the film."""
+    sc = tiny_scene(width=width, height=height, name=name)
+    sc.meshes = [m for m in sc.meshes if m.emission is None]
+    sc.background = (0.5, 0.6, 0.7)
+    return sc
+
+
+def two_light_scene(width=24, height=20, name="two_lights") -> Scene:
+    """tiny_scene plus a second, smaller emitter (a 0.5 x 0.5 quad at
+    (2.5, 3, 0), colour (1, 0.5, 0.25), radiant power 8 pi): the light choice's
+    rejection loop and its x numLights weight (integrator.cpp:263-270) apply on
+    paths that hit either light."""
+    sc = tiny_scene(width=width, height=height, name=name)
+    p, n, i = quad((2.5, 3.0, 0.0), 0.5, 0.5, -1.0)
+    sc.bsdfs.append({"name": "light2", "type": "lambert", "albedo": {"type": "constant", "value": [0.0, 0.0, 0.0]}})
+    sc.materials.append({"name": "light2", "bsdf": "light2"})
+    sc.meshes.append(Mesh("light2", p, n, i, "light2",
+                          emission={"color": [1.0, 0.5, 0.25], "radiant_power": float(8.0 * np.pi)}))
+    return sc
+
+
 def random_rays(n: int, lo: np.ndarray, hi: np.ndarray, seed: int = 2) -> np.ndarray:
     """(n, 8) float32 ray records (org.xyz, tnear, dir.xyz, tfar): origins uniform
     in the box [lo, hi], directions uniform on the sphere, tnear 0, tfar inf."""

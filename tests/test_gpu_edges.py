@@ -32,20 +32,11 @@ def _empty(width=5, height=3, name="edge_empty"):
 
 
 def _no_lights(name="edge_nolight"):
-    sc = S.tiny_scene(width=13, height=7, name=name)
-    sc.meshes = [m for m in sc.meshes if m.emission is None]
-    sc.background = (0.5, 0.6, 0.7)
-    return sc
+    return S.unlit_scene(name=name)
 
 
 def _two_lights(name="edge_twolights"):
-    sc = S.tiny_scene(width=24, height=20, name=name)
-    p, n, i = S.quad((2.5, 3.0, 0.0), 0.5, 0.5, -1.0)
-    sc.bsdfs.append({"name": "light2", "type": "lambert", "albedo": {"type": "constant", "value": [0.0, 0.0, 0.0]}})
-    sc.materials.append({"name": "light2", "bsdf": "light2"})
-    sc.meshes.append(S.Mesh("light2", p, n, i, "light2",
-                            emission={"color": [1.0, 0.5, 0.25], "radiant_power": float(8.0 * np.pi)}))
-    return sc
+    return S.two_light_scene(name=name)
 
 
 def _render_both(path, spp, depth, bvh_width):

@@ -26,6 +26,8 @@ def _bits(a):
     (lambda: S.medium_sphere_scene(width=32, height=32, non_scattering=True, name="medium_absorb_32"), 2, 32, 3),
     (lambda: S.tiny_scene(width=24, height=16, name="tiny_24x16"), 2, 1500, 3),
     (lambda: S.procedural_scene(width=40, height=32, name="procedural_40"), 3, 8, 3),
+    (lambda: S.unlit_scene(name="unlit_13x7"), 4, 8, 3),
+    (lambda: S.two_light_scene(name="two_lights_24x20"), 4, 8, 3),
 ])
 def test_tile_keyed_oracle_matches_reference(reference_available, scene_dir, make, frames, depth, rr):
     if not reference_available:
