@@ -28,6 +28,7 @@ def _bits(a):
     (lambda: S.procedural_scene(width=40, height=32, name="procedural_40"), 3, 8, 3),
     (lambda: S.unlit_scene(name="unlit_13x7"), 4, 8, 3),
     (lambda: S.two_light_scene(name="two_lights_24x20"), 4, 8, 3),
+    (lambda: S.displaced_icosphere_scene(width=32, height=24, levels=3, name="ico3_32x24"), 2, 10, 3),
 ])
 def test_tile_keyed_oracle_matches_reference(reference_available, scene_dir, make, frames, depth, rr):
     if not reference_available:
