@@ -96,3 +96,24 @@ def test_malformed_inputs_are_statuses(checker, tmp_path):
     (a, b, *_), (a4, b4, *_) = _run(checker, [str(p3), str(p4)])
     assert a == 0 and b == 1                  # loads, then LT_ERR_INVALID: index out of range
     assert (a4, b4) == (6, -1)                # an unknown material: LT_ERR_PARSE
+
+
+def test_malformed_media_are_statuses(checker, tmp_path):
+    """A medium missing a field its type needs is LT_ERR_PARSE (the reference
+    reads absorption_color, absorption_at_distance and, for isotropic media,
+    scattering_distance: scene.cpp:322-334); each well-formed kind loads."""
+    paths, want = [], []
+    for kind, kw in (("iso", {"reference_expressible": True}), ("absorb", {"non_scattering": True}), ("hg", {})):
+        sc = S.medium_sphere_scene(width=8, height=8, name=f"med_{kind}", **kw)
+        path = sc.write(str(tmp_path))
+        paths.append(path)
+        want.append((0, 0))
+        doc = json.load(open(path))
+        drop = {"iso": "scattering_distance", "absorb": "absorption_at_distance", "hg": "sigma_s"}[kind]
+        del doc["media"][0][drop]
+        bad = tmp_path / f"med_{kind}_bad.json"
+        bad.write_text(json.dumps(doc))
+        paths.append(str(bad))
+        want.append((6, -1))
+    res = _run(checker, paths)
+    assert [r[:2] for r in res] == want, res
