@@ -5,8 +5,8 @@
 # reference CPU path used by tests/ (oracle pinning, golden vectors) and by
 # bench.py --impl reference. It is never part of the shipped library.
 #
-# Stage (only where the reference tree exists, LANTERN_REFERENCE or
-# /root/reference): copy the reference sources this build needs into
+# Stage (only where the reference tree exists: LANTERN_REFERENCE, else a
+# checkout named "reference" next to this repository): copy the reference sources this build needs into
 # oracle/_ref/src, unmodified except for integrator.cpp, where the two loop
 # constants of RenderPixel (maxBounces = 1500 at :114, the roulette threshold
 # "bounces > 3" at :235) become variables. oracle/_ref is git-ignored.
@@ -15,7 +15,7 @@
 # math, parallel_for, rtc* over the oracle intersector, headless driver).
 set -euo pipefail
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${LANTERN_REFERENCE:-/root/reference}
+REF=${LANTERN_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 OUT=$HERE/_ref
 SRC=$OUT/src
 OBJ=$OUT/obj

@@ -31,6 +31,9 @@ BUILD = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD, "liboracle.so")
 REF_SO = os.path.join(REF_DIR, "liblantern_ref.so")
+# The reference tree: LANTERN_REFERENCE, else a checkout named "reference" next
+# to this repository.
+REF_TREE = os.environ.get("LANTERN_REFERENCE") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 BSDF = {"lambert": 0, "mirror": 1, "ideal_specular_dielectric": 2}
 MED_NON_SCATTERING, MED_ISOTROPIC, MED_HG = 1, 2, 3
@@ -67,10 +70,10 @@ def build_oracle(force: bool = False) -> str:
 def build_reference() -> Optional[str]:
     """Run oracle/build_ref.sh (stages from the reference tree when present,
     else compiles already-staged sources). Returns the library path or None."""
-    if not (os.path.isdir("/root/reference/source") or os.path.isdir(os.path.join(REF_DIR, "src"))
-            or os.environ.get("LANTERN_REFERENCE")):
+    if not (os.path.isdir(os.path.join(REF_TREE, "source")) or os.path.isdir(os.path.join(REF_DIR, "src"))):
         return None
-    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], capture_output=True, text=True)
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], capture_output=True, text=True,
+                       env=dict(os.environ, LANTERN_REFERENCE=REF_TREE))
     if r.returncode != 0:
         raise RuntimeError("reference build failed:\n" + r.stdout[-2000:] + r.stderr[-4000:])
     return REF_SO

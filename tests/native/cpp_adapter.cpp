@@ -24,12 +24,21 @@
 
 #include "lantern_gpu.h"
 
+#ifdef LT_REFERENCE_FRAME_BUFFER
+// The reference's own FrameBuffer (camera/frame_buffer.{h,cpp}): raw arrays of
+// float3 colour sums, uint bounces and uint sample counts.
+#include "camera/frame_buffer.h"
+static_assert(sizeof(float3) == 12, "FrameBuffer::ColorData must be packed float3 for lt_film");
+static float *color_of(Lantern::FrameBuffer *f) { return &f->ColorData[0].x; }
+static uint32_t *bounces_of(Lantern::FrameBuffer *f) { return f->Bounces; }
+static uint32_t *counts_of(Lantern::FrameBuffer *f) { return f->ColorSampleCount; }
+#else
+// Without the reference tree: a stand-in with the film fields RenderFrame
+// touches, in the reference's layout (camera/frame_buffer.h:17-34).
 namespace Lantern {
 struct float3 {
     float x, y, z;
 };
-// The film fields RenderFrame touches, with the reference's types
-// (camera/frame_buffer.h).
 struct FrameBuffer {
     FrameBuffer(uint32_t w, uint32_t h) : Width(w), Height(h), ColorData(w * h), Bounces(w * h), ColorSampleCount(w * h) {}
     uint32_t Width, Height;
@@ -39,6 +48,10 @@ struct FrameBuffer {
     bool Empty = true;
 };
 }  // namespace Lantern
+static float *color_of(Lantern::FrameBuffer *f) { return &f->ColorData[0].x; }
+static uint32_t *bounces_of(Lantern::FrameBuffer *f) { return f->Bounces.data(); }
+static uint32_t *counts_of(Lantern::FrameBuffer *f) { return f->ColorSampleCount.data(); }
+#endif
 
 class GpuIntegrator {
 public:
@@ -53,8 +66,8 @@ public:
     void RenderFrame() {
         m_current = std::atomic_exchange(m_swap, m_current);
         m_current->Empty = false;
-        lt_film film = {&m_current->ColorData[0].x, m_current->Bounces.data(), m_current->ColorSampleCount.data(),
-                        m_current->Width, m_current->Height, /*on_device=*/0};
+        lt_film film = {color_of(m_current), bounces_of(m_current), counts_of(m_current), m_current->Width,
+                        m_current->Height, /*on_device=*/0};
         lt_render_params p = {/*spp=*/1, m_frame, m_maxDepth, m_rrDepth};
         if (lt_render(m_ctx, &p, &film) != LT_OK) throw std::runtime_error(lt_last_error(m_ctx));
         ++m_frame;

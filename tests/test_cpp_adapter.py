@@ -1,8 +1,10 @@
 """The C++ drop-in for the reference's Integrator (tests/native/cpp_adapter.cpp:
-GpuIntegrator over lt_render with FrameBuffer's own host layout, two films
+GpuIntegrator over lt_render with the reference's FrameBuffer, two films
 swapped per RenderFrame as the reference's render loop does). It compiles and
-links against include/lantern_gpu.h and liblantern_gpu.so on any machine; on a
-GPU its films, summed, equal the Python path's render of the same frames."""
+links against include/lantern_gpu.h and liblantern_gpu.so; where the reference
+sources are staged (oracle/_ref/src) it uses the reference's own
+camera/frame_buffer.{h,cpp}, else a stand-in of the same layout. On a GPU its
+films, summed, equal the Python path's render of the same frames."""
 import os
 import shutil
 import subprocess
@@ -12,6 +14,11 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_DIR = os.path.join(ROOT, "lantern_gb300", "_build")
+REF_SRC = os.path.join(ROOT, "oracle", "_ref", "src")
+
+
+def reference_frame_buffer() -> bool:
+    return os.path.exists(os.path.join(REF_SRC, "core", "camera", "frame_buffer.h"))
 
 
 def _build(tmp_path):
@@ -21,9 +28,16 @@ def _build(tmp_path):
     if not os.path.exists(os.path.join(LIB_DIR, "liblantern_gpu.so")):
         pytest.skip("liblantern_gpu.so not built")
     exe = str(tmp_path / "cpp_adapter")
-    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I" + os.path.join(ROOT, "include"),
-           os.path.join(ROOT, "tests", "native", "cpp_adapter.cpp"), "-L" + LIB_DIR, "-llantern_gpu",
-           "-Wl,-rpath," + LIB_DIR, "-o", exe]
+    srcs = [os.path.join(ROOT, "tests", "native", "cpp_adapter.cpp")]
+    flags = ["-std=c++17", "-O2", "-Wall", "-I" + os.path.join(ROOT, "include")]
+    if reference_frame_buffer():
+        # the reference's FrameBuffer with the scalar stand-ins of Embree's vector
+        # headers that oracle/build_ref.sh compiles the reference with
+        flags += ["-DLT_REFERENCE_FRAME_BUFFER", "-include", "cstring", "-DEMBREE_STATIC_LIB",
+                  "-I" + os.path.join(ROOT, "oracle", "ref_shim"), "-I" + os.path.join(REF_SRC, "core"),
+                  "-I" + os.path.join(REF_SRC, "embree", "include")]
+        srcs.append(os.path.join(REF_SRC, "core", "camera", "frame_buffer.cpp"))
+    cmd = [cxx] + flags + srcs + ["-L" + LIB_DIR, "-llantern_gpu", "-Wl,-rpath," + LIB_DIR, "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
     return exe
@@ -31,6 +45,14 @@ def _build(tmp_path):
 
 def test_cpp_adapter_builds_against_the_c_abi(tmp_path):
     assert os.path.exists(_build(tmp_path))
+
+
+def test_cpp_adapter_uses_the_reference_frame_buffer(tmp_path):
+    if not reference_frame_buffer():
+        pytest.skip("reference sources not staged (oracle/_ref/src)")
+    exe = _build(tmp_path)
+    r = subprocess.run(["nm", "-C", exe], capture_output=True, text=True)
+    assert "Lantern::FrameBuffer::FrameBuffer(unsigned int, unsigned int)" in r.stdout
 
 
 @pytest.mark.gpu
