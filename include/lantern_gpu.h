@@ -53,7 +53,9 @@ void lt_ctx_destroy(lt_ctx *ctx);
 const char *lt_last_error(const lt_ctx *ctx);
 /* Issue all further work on `stream` (a cudaStream_t; NULL is CUDA's legacy
  * default stream). A new context uses a non-blocking stream of its own, which
- * lt_get_stream returns before any lt_set_stream call. */
+ * lt_get_stream returns before any lt_set_stream call. Work the context queued
+ * on its previous stream comes first: the new stream waits for it on the
+ * device (an event), the host does not block. */
 lt_status lt_set_stream(lt_ctx *ctx, void *stream);
 void *lt_get_stream(const lt_ctx *ctx);
 /* Waits for all work queued on the context's stream. */
@@ -214,21 +216,24 @@ lt_status lt_render(lt_ctx *ctx, const lt_render_params *params, lt_film *film);
  * forbids allocations afterwards, or an interactive loop in which cudaMalloc /
  * cudaFree (which can synchronise the whole device) would stall other work.
  * The wavefront state lives in a fixed array inside liblantern_gpu.so of
- * LT_NOALLOC_MAX_PATHS path slots (about 18.9 MB), reserved on every GPU that
- * loads the library until the process exits. Same sampling, same film
+ * LT_NOALLOC_MAX_PATHS path slots (about 18.9 MB), reserved on every GPU on
+ * which a context is created, until the process exits. Same sampling, same film
  * semantics and same result as lt_render; only the number of paths in flight
  * is bounded.
  *
  * - film must be on the device (on_device = 1): host films need staging memory.
  * - paths_in_flight: path slots to use, 1..LT_NOALLOC_MAX_PATHS; anything else
  *   is rejected with LT_ERR_INVALID. More slots keep more of the GPU busy.
- * - The first call on a device looks up the array's device address; make that
- *   first call before any stream capture on that device.
+ * - Set-up happens in lt_ctx_create, with the device current: the array's
+ *   module and the wavefront kernels are loaded and the array's device address
+ *   is looked up (cudaGetSymbolAddress) and kept, so no call of
+ *   lt_render_noalloc allocates or loads anything on the device.
  * - All calls in the process share the one array per device: calls whose GPU
  *   work overlaps (other threads, other contexts, other streams) race and
  *   corrupt each other. Serialise them. The array keeps the last call's
  *   contents; each call clears what it needs before use.
- * - No per-stage timing is recorded (lt_render_stats: stage times are 0). */
+ * - No per-stage timing is recorded (lt_render_stats: trace_ms and shade_ms
+ *   are 0; the ray, iteration and non-finite counts are filled as lt_render's). */
 #define LT_NOALLOC_MAX_PATHS 65536
 lt_status lt_render_noalloc(lt_ctx *ctx, const lt_render_params *params, lt_film *film,
                             uint32_t paths_in_flight);
@@ -401,6 +406,16 @@ lt_status lt_intersect(lt_ctx *ctx, const lt_ray *rays, lt_hit *hits, uint64_t n
  * (LT_ERR_OOM) without reaching the CUDA runtime. UINT32_MAX (the initial
  * state) turns injection off. Process-wide. No counterpart in the reference. */
 void lt_debug_fail_allocations(uint32_t after);
+
+/* For failure-handling tests: caps the wavefront iterations of every render
+ * (lt_render, lt_render_noalloc, lt_render_batch) at `limit`. A render whose
+ * wavefront has not drained by then stops and returns LT_ERR_TIMEOUT, the
+ * status of the library's own bound (about 4 x (max_depth + 8) x the number of
+ * wavefront refills); the film then holds part of the samples. 0 (the initial
+ * state) = the library's own bound only. Process-wide. The reference has no
+ * such bound (its loop constant is 1500 bounces, integrator.cpp:114) and
+ * reports failures as bool + printf (scene.cpp:200-213). */
+void lt_debug_set_iteration_limit(uint64_t limit);
 
 #ifdef __cplusplus
 }

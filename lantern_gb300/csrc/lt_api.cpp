@@ -26,10 +26,21 @@
 #include "lantern_gpu.h"
 #include "lt_device.h"
 #include "lt_bvh_gpu.h"
+#include "lt_noalloc.h"
+#include "lt_order.h"
 #include "lt_scene.h"
 #include "lt_setup.h"
 
 using namespace lt;
+
+// The CUDA runtime behind WorkOrder (lt_order.h).
+struct CudaRt {
+    using Event = cudaEvent_t;
+    using Stream = cudaStream_t;
+    int record(Event e, Stream s) { return (int)cudaEventRecord(e, s); }
+    int wait(Stream s, Event e) { return (int)cudaStreamWaitEvent(s, e, 0); }
+    int sync(Event e) { return (int)cudaEventSynchronize(e); }
+};
 
 struct lt_ctx {
     int device = 0;
@@ -70,6 +81,10 @@ struct lt_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<uintptr_t> graph_key;
 
+    // ordering across stream switches and of host writes into the scene table
+    CudaRt rt;
+    WorkOrder<CudaRt> order;
+
     lt_render_stats stats{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // stage timing: one event before each stage launch and one after the last
@@ -98,6 +113,21 @@ static bool injected_alloc_failure() {
         if (g_alloc_left.compare_exchange_weak(left, left - 1)) return false;
     }
     return false;
+}
+
+// Wavefront iteration cap for failure-handling tests
+// (lt_debug_set_iteration_limit); 0 = the library's own bound.
+static std::atomic<unsigned long long> g_iteration_limit{0};
+
+// Iterations a render may take before it reports LT_ERR_TIMEOUT: every path
+// ends within max_depth iterations of its start and at most `cap` work items
+// start per iteration, so a render needs about max_depth * total / cap; the
+// bound leaves a factor of four and some slack. 64-bit: with few paths in
+// flight the product exceeds 32 bits.
+static unsigned long long drain_limit(unsigned long long total, uint32_t cap, uint32_t max_depth) {
+    const unsigned long long own = 4ull * ((unsigned long long)max_depth + 8ull) * ((total + cap - 1) / cap) + 64ull;
+    const unsigned long long dbg = g_iteration_limit.load();
+    return dbg && dbg < own ? dbg : own;
 }
 
 static cudaError_t dev_malloc(void **p, size_t bytes) {
@@ -151,7 +181,11 @@ static lt_status fail(lt_ctx *c, lt_status st, const char *fmt, ...) {
                         #expr, cudaGetErrorString(e_), __FILE__, __LINE__);                         \
     } while (0)
 
+// Frees the context's scene. Any context's queued batched work may read it
+// (lt_render_diff_batch and lt_render_adjoint_batch return once queued), so
+// the device is synchronised first.
 static void free_scene(lt_ctx *c) {
+    if (!c->scene_allocs.empty()) cudaDeviceSynchronize();
     for (void *p : c->scene_allocs) cudaFree(p);
     c->scene_allocs.clear();
     c->scene_bytes = 0;
@@ -170,6 +204,7 @@ static void free_graph(lt_ctx *c) {
 }
 
 static void free_wave(lt_ctx *c) {
+    if (c->wave.arena && c->stream) cudaStreamSynchronize(c->stream);  // the context's work is on its stream
     free_graph(c);  // its kernels point into the arena
     if (c->wave.arena) cudaFree(c->wave.arena);
     c->wave = Wavefront{};
@@ -224,6 +259,14 @@ lt_status lt_ctx_create(int device, lt_ctx **out) try {
     if (e == cudaSuccess) e = dev_malloc((void **)&c->isect_fetch, 256);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->order.switch_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->order.table_ev, cudaEventDisableTiming);
+    // lt_render_noalloc's set-up: load the module holding its fixed scratch
+    // array (reserving the array on this device) and the wavefront kernels now,
+    // so that no call of it loads code or data onto the device
+    void *noalloc_ptr = nullptr;
+    if (e == cudaSuccess) e = noalloc_scratch(device, &noalloc_ptr);
+    if (e == cudaSuccess) e = preload_wave_kernels();
     if (e != cudaSuccess) {
         lt_ctx_destroy(c);
         return fail(nullptr, LT_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
@@ -239,6 +282,7 @@ void lt_ctx_destroy(lt_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->own_stream && c->own_stream != c->stream) cudaStreamSynchronize(c->own_stream);
     free_scene(c);
     free_wave(c);
     if (c->table_dev) cudaFree(c->table_dev);
@@ -248,6 +292,8 @@ void lt_ctx_destroy(lt_ctx *c) {
     if (c->isect_fetch) cudaFree(c->isect_fetch);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->order.switch_ev) cudaEventDestroy(c->order.switch_ev);
+    if (c->order.table_ev) cudaEventDestroy(c->order.table_ev);
     for (cudaEvent_t e : c->stage_events) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
@@ -257,6 +303,9 @@ const char *lt_last_error(const lt_ctx *c) { return c ? c->error.c_str() : g_cre
 
 lt_status lt_set_stream(lt_ctx *c, void *stream) try {
     if (!c) return LT_ERR_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    // work queued on the old stream comes before anything queued on the new one
+    CUDA_TRY(c, (cudaError_t)c->order.switch_stream(c->rt, c->stream, (cudaStream_t)stream));
     c->stream = (cudaStream_t)stream;
     return LT_OK;
 } LT_CATCH(c)
@@ -637,6 +686,85 @@ static lt_status ensure_width(lt_ctx *c, uint32_t width) {
     return LT_OK;
 }
 
+// The wavefront loop of one render over `w`: camera rays, then batches of
+// (trace, shade) iterations, reading the queue lengths back after each batch
+// until no path ray, camera ray or connection record is left. With
+// stage_timing an event goes before each stage launch (lt_render_stats'
+// trace_ms / shade_ms); without it nothing is created or allocated. Fills
+// c->stats (except samples and gpu_ms).
+static lt_status run_wave(lt_ctx *c, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, bool stage_timing) {
+    const uint32_t cap = w.capacity;
+    CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
+    CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
+    uint32_t launches = 1;
+    unsigned long long iters = 0;
+    size_t nev = 0;
+    if (stage_timing) c->stage_of_event.clear();
+    int cur = 0;
+    const unsigned long long limit = drain_limit(a.total, cap, a.max_depth);
+    // Iterations launched between two reads of the queue lengths. While work
+    // items remain, at most `cap` of them start per iteration, so the loop
+    // cannot end within remaining / cap iterations.
+    unsigned long long batch = first_batch(a.total, cap, a.max_depth);
+    for (;;) {
+        if (batch > limit - iters) batch = limit - iters;  // iters < limit here
+        for (unsigned long long k = 0; k < batch; ++k) {
+            for (int stage = 0; stage < kStages; ++stage) {
+                if (stage_timing) {
+                    if (nev == c->stage_events.size()) {
+                        cudaEvent_t e;
+                        CUDA_TRY(c, cudaEventCreate(&e));
+                        c->stage_events.push_back(e);
+                    }
+                    CUDA_TRY(c, cudaEventRecord(c->stage_events[nev++], c->stream));
+                    c->stage_of_event.push_back(stage);
+                }
+                CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
+            }
+            launches += kStages;
+            cur ^= 1;
+            ++iters;
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        // done when no path ray is queued and the last shade emitted no connection
+        if (c->counters_host->count[cur] == 0 && c->counters_host->rcount[cur] == 0 &&
+            c->counters_host->ccount[cur ^ 1] == 0)
+            break;
+        if (iters >= limit) return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %llu iterations", iters);
+        const unsigned long long next = c->counters_host->work_next;
+        const unsigned long long left_iters = next < a.total ? (a.total - next) / cap : 0;
+        batch = left_iters > 4 ? (left_iters < 64 ? left_iters : 64ull) : 4ull;
+    }
+    const WaveCounters &k = *c->counters_host;
+    c->stats.main_rays = k.main_rays;
+    c->stats.light_rays = k.light_rays;
+    c->stats.bsdf_rays = k.bsdf_rays;
+    c->stats.nonfinite_samples = k.nonfinite;
+    c->stats.light_traversals = k.light_traversals;
+    c->stats.iterations = (uint32_t)iters;
+    c->stats.kernel_launches = launches;
+    if (stage_timing) {
+        if (nev == c->stage_events.size()) {
+            cudaEvent_t e;
+            CUDA_TRY(c, cudaEventCreate(&e));
+            c->stage_events.push_back(e);
+        }
+        CUDA_TRY(c, cudaEventRecord(c->stage_events[nev], c->stream));
+        CUDA_TRY(c, cudaEventSynchronize(c->stage_events[nev]));
+        float acc[kStages] = {0, 0};
+        for (size_t i = 0; i < nev; ++i) {
+            float ms = 0.0f;
+            CUDA_TRY(c, cudaEventElapsedTime(&ms, c->stage_events[i], c->stage_events[i + 1]));
+            acc[c->stage_of_event[i]] += ms;
+        }
+        c->stats.trace_ms = acc[kStageTrace];
+        c->stats.shade_ms = acc[kStageShade];
+    }
+    return LT_OK;
+}
+
 extern "C" {
 
 lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) try {
@@ -682,67 +810,7 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) try {
         lt_status st = prepare_wave(c, a.total, &cap);
         if (st != LT_OK) return st;
         const Wavefront w = wave_view(c, cap);
-        CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
-        CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
-        uint32_t launches = 1, iters = 0;
-        size_t nev = 0;
-        c->stage_of_event.clear();
-        int cur = 0;
-        // Iterations launched between two reads of the queue lengths. While
-        // work items remain, at most `cap` of them start per iteration, so the
-        // loop cannot end within remaining / cap iterations.
-        uint32_t batch = first_batch(a.total, cap, p->max_depth);
-        for (;;) {
-            for (uint32_t k = 0; k < batch; ++k) {
-                for (int stage = 0; stage < kStages; ++stage) {
-                    if (nev == c->stage_events.size()) {
-                        cudaEvent_t e;
-                        CUDA_TRY(c, cudaEventCreate(&e));
-                        c->stage_events.push_back(e);
-                    }
-                    CUDA_TRY(c, cudaEventRecord(c->stage_events[nev++], c->stream));
-                    c->stage_of_event.push_back(stage);
-                    CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
-                }
-                launches += kStages;
-                cur ^= 1;
-                ++iters;
-            }
-            CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters),
-                                        cudaMemcpyDeviceToHost, c->stream));
-            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-            // done when no path ray is queued and the last shade emitted no connection
-            if (c->counters_host->count[cur] == 0 && c->counters_host->rcount[cur] == 0 &&
-                c->counters_host->ccount[cur ^ 1] == 0)
-                break;
-            if (iters > 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u)
-                return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
-            const unsigned long long next = c->counters_host->work_next;
-            const unsigned long long left_iters = next < a.total ? (a.total - next) / cap : 0;
-            batch = left_iters > 4 ? (left_iters < 64 ? (uint32_t)left_iters : 64u) : 4u;
-        }
-        c->stats.main_rays = c->counters_host->main_rays;
-        c->stats.light_rays = c->counters_host->light_rays;
-        c->stats.bsdf_rays = c->counters_host->bsdf_rays;
-        c->stats.nonfinite_samples = c->counters_host->nonfinite;
-        c->stats.iterations = iters;
-        c->stats.kernel_launches = launches;
-        if (nev == c->stage_events.size()) {
-            cudaEvent_t e;
-            CUDA_TRY(c, cudaEventCreate(&e));
-            c->stage_events.push_back(e);
-        }
-        CUDA_TRY(c, cudaEventRecord(c->stage_events[nev], c->stream));
-        CUDA_TRY(c, cudaEventSynchronize(c->stage_events[nev]));
-        float acc[kStages] = {0, 0};
-        for (size_t i = 0; i < nev; ++i) {
-            float ms = 0.0f;
-            CUDA_TRY(c, cudaEventElapsedTime(&ms, c->stage_events[i], c->stage_events[i + 1]));
-            acc[c->stage_of_event[i]] += ms;
-        }
-        c->stats.trace_ms = acc[kStageTrace];
-        c->stats.shade_ms = acc[kStageShade];
-        c->stats.light_traversals = c->counters_host->light_traversals;
+        if ((st = run_wave(c, w, a, f, true)) != LT_OK) return st;
     }
     c->stats.samples = a.total;
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -895,8 +963,6 @@ lt_status lt_scene_load_json(lt_ctx *c, const char *path) try {
 // array of lt_noalloc.cu instead of a cudaMalloc'd arena. Nothing here
 // allocates: no cudaMalloc / cudaFree / cudaMallocHost, no new CUDA events, no
 // staging buffers (the film must already be on the device).
-#include "lt_noalloc.h"
-
 static Wavefront carve_noalloc(char *a, uint32_t cap) {
     Wavefront w;
     w.arena_bytes = carve_wave(a, cap, &w);
@@ -942,37 +1008,10 @@ extern "C" lt_status lt_render_noalloc(lt_ctx *c, const lt_render_params *p, lt_
         if (w.arena_bytes > kNoAllocScratchBytes)
             return fail(c, LT_ERR_INVALID, "internal: wavefront needs %zu bytes, fixed scratch holds %zu", w.arena_bytes,
                         kNoAllocScratchBytes);
-        // the array keeps the previous call's contents: the counters must start at zero
-        CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
-        CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
-        uint32_t launches = 1, iters = 0;
-        int cur = 0;
-        uint32_t batch = first_batch(a.total, cap, p->max_depth);  // as in lt_render
-        const uint32_t limit = 4u * (p->max_depth + 8u) * (uint32_t)((a.total + cap - 1) / cap) + 64u;
-        for (;;) {
-            for (uint32_t k = 0; k < batch; ++k) {
-                for (int stage = 0; stage < kStages; ++stage)
-                    CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
-                launches += kStages;
-                cur ^= 1;
-                ++iters;
-            }
-            CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
-                                        c->stream));
-            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-            if (c->counters_host->count[cur] == 0 && c->counters_host->rcount[cur] == 0 &&
-                c->counters_host->ccount[cur ^ 1] == 0)
-                break;
-            if (iters > limit) return fail(c, LT_ERR_TIMEOUT, "wavefront did not drain after %u iterations", iters);
-            const unsigned long long next = c->counters_host->work_next;
-            const unsigned long long left_iters = next < a.total ? (a.total - next) / cap : 0;
-            batch = left_iters > 4 ? (left_iters < 64 ? (uint32_t)left_iters : 64u) : 4u;
-        }
-        c->stats.main_rays = c->counters_host->main_rays;
-        c->stats.light_rays = c->counters_host->light_rays;
-        c->stats.bsdf_rays = c->counters_host->bsdf_rays;
-        c->stats.iterations = iters;
-        c->stats.kernel_launches = launches;
+        // the array keeps the previous call's contents: run_wave zeroes the
+        // counters before anything reads them
+        lt_status st = run_wave(c, w, a, f, false);
+        if (st != LT_OK) return st;
     }
     c->stats.samples = a.total;
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -1076,14 +1115,15 @@ static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
     return LT_OK;
 }
 
-// The scene table's host and device copies; waits until the previous
-// batch's table upload (from the pinned host copy) has completed.
+// The scene table's host and device copies; waits until the last queued
+// reader of the table (and with it the upload from the pinned host copy) has
+// completed, so that the host may rewrite the pinned copy.
 static lt_status ensure_table(lt_ctx *c) {
     if (!c->table_host) {
         CUDA_TRY(c, host_malloc((void **)&c->table_host, sizeof(SceneTable)));
         CUDA_TRY(c, dev_malloc((void **)&c->table_dev, sizeof(SceneTable)));
     }
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    CUDA_TRY(c, (cudaError_t)c->order.before_table_write(c->rt));
     return LT_OK;
 }
 
@@ -1139,13 +1179,14 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
         T.count = count;
         T.pad = 0;
         T.total = total;
-        T.iteration_limit = 4ull * (max_depth + 8ull) * ((total + cap - 1) / cap) + 64ull;
+        T.iteration_limit = drain_limit(total, cap, max_depth);
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev, c->table_host, offsetof(SceneTable, slots), cudaMemcpyHostToDevice,
                                     c->stream));
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->slots, T.slots, count * sizeof(SceneSlot), cudaMemcpyHostToDevice,
                                     c->stream));
         if ((st = build_batch_graph(c, w)) != LT_OK) return st;
         CUDA_TRY(c, cudaGraphLaunch(c->graph_exec, c->stream));
+        CUDA_TRY(c, (cudaError_t)c->order.table_read_queued(c->rt, c->stream));
         CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
                                     c->stream));
         CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -1371,6 +1412,7 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->diff, T.diff, count * sizeof(DiffSlot), cudaMemcpyHostToDevice,
                                     c->stream));
         CUDA_TRY(c, launch_diff_batch(adjoint, c->table_dev, c->shape, c->stream));
+        CUDA_TRY(c, (cudaError_t)c->order.table_read_queued(c->rt, c->stream));
         c->stats.kernel_launches = 1;
     }
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -1402,3 +1444,5 @@ extern "C" lt_status lt_image_load(const char *path, uint8_t *texels, size_t cap
 } LT_CATCH(nullptr)
 
 extern "C" void lt_debug_fail_allocations(uint32_t after) { g_alloc_left.store(after); }
+
+extern "C" void lt_debug_set_iteration_limit(uint64_t limit) { g_iteration_limit.store(limit); }

@@ -167,6 +167,9 @@ cudaError_t launch_resolve(const float *rgb, const uint32_t *counts, uint32_t np
                            float4 *out, uchar4 *out8, SppStats *stats, int sms, cudaStream_t st);
 
 // launchers (lt_kernels.cu)
+// Loads the single-scene wavefront kernels (camera rays, trace, shade, counts)
+// onto the current device, so that their first launch loads no code.
+cudaError_t preload_wave_kernels();
 // Fills the block counts of *out for its thread counts; `batch` selects the
 // ManyScenes instantiations of the stage kernels.
 void query_launch_shape(int device, bool batch, LaunchShape *out);

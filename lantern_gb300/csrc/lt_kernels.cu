@@ -1682,6 +1682,17 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
     out->diff_adj_batch_blocks = blocks_for(k_diff_adjoint_batch, 128, sms);
 }
 
+cudaError_t preload_wave_kernels() {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_raygen<OneScene>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_trace<OneScene, Bvh2>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_trace<OneScene, Bvh4>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_trace<OneScene, Bvh8>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<OneScene>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_add_counts);
+    return e;
+}
+
 cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
                                 float *sample_I, const LaunchShape &ls, cudaStream_t st) {
     if (a.total == 0) return cudaSuccess;

@@ -26,7 +26,7 @@ SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
            "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load",
-           "lt_debug_fail_allocations"]
+           "lt_debug_fail_allocations", "lt_debug_set_iteration_limit"]
 BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 MAX_BATCH = 2048  # LT_MAX_BATCH
@@ -158,6 +158,8 @@ def load(build_if_needed: bool = True) -> C.CDLL:
                                     C.POINTER(C.c_uint32)]
         L.lt_debug_fail_allocations.argtypes = [C.c_uint32]
         L.lt_debug_fail_allocations.restype = None
+        L.lt_debug_set_iteration_limit.argtypes = [C.c_uint64]
+        L.lt_debug_set_iteration_limit.restype = None
         _lib = L
         return L
 

@@ -7,6 +7,10 @@ adjoint, through the C ABI.
   estimator (sampling copies held at the base values, h = 1e-3, loss in
   float64): within 2% per parameter for every parameter whose gradient is
   not negligible, on 64 randomly chosen parameters including the medium's.
+* The GPU adjoint of a 32x32 crop agrees with the host restatement's gradient
+  in double precision (oracle/lt_diff_ref.cpp).
+Both checks run on a small scene and on the differentiable workload itself
+(nine spheres of 64x32 segments plus the fog sphere, 512x512, 32 spp, depth 8).
 """
 import numpy as np
 import pytest
@@ -38,13 +42,16 @@ def test_diff_forward_matches_render(scene_dir):
     assert torch.allclose(rgb, fb.ColorData, rtol=1e-4, atol=1e-6)
 
 
-def test_adjoint_matches_finite_differences(scene_dir):
-    path = _small(scene_dir)
+def _fd_check(path, spp, depth, min_checked):
+    """Adjoint of L = sum((image - target)^2) (image = film / spp, target
+    rendered with the true parameters) against central differences (h = 1e-3)
+    on 64 parameters drawn with seed 4: the three sigma_a and three sigma_s
+    channels, 48 albedo and 10 emission entries with a nonzero gradient.
+    Returns the largest relative difference over the parameters checked."""
     ds = DiffScene(path)
     a0, e0, sa0, ss0 = ds.defaults()
     true, init = S.differentiable_targets(ds.num_triangles)
     dev = ds.device
-    spp, depth = 8, 6
     # target image with the true parameters
     with torch.no_grad():
         target = render_image(ds, torch.from_numpy(true["albedo"]).to(dev), e0,
@@ -75,30 +82,44 @@ def test_adjoint_matches_finite_differences(scene_dir):
     cands = cands[:64]
     h = 1e-3
     gmax = max(np.abs(g).max() for g in grads)
-    bad = []
+    bad, worst, checked = [], 0.0, 0
     for k, i in cands:
         fd = (loss_at(k, i, h) - loss_at(k, i, -h)) / (2 * h)
         ad = float(grads[k].reshape(-1)[i])
         if max(abs(fd), abs(ad)) < 1e-4 * gmax:
             continue
-        if abs(ad - fd) > 0.02 * max(abs(fd), abs(ad)):
+        checked += 1
+        rel = abs(ad - fd) / max(abs(fd), abs(ad))
+        worst = max(worst, rel)
+        if rel > 0.02:
             bad.append((k, i, ad, fd))
     assert not bad, bad[:10]
+    assert checked >= min_checked, checked
+    return worst
 
 
-def test_adjoint_crop_matches_fp64_host_reference(scene_dir):
-    """GPU adjoint of the samples of a 32x32 crop against the same gradient from
-    the host restatement in double precision (oracle/lt_diff_ref.cpp)."""
+def test_adjoint_matches_finite_differences(scene_dir):
+    _fd_check(_small(scene_dir), spp=8, depth=6, min_checked=40)
+
+
+def test_adjoint_matches_finite_differences_on_the_differentiable_workload(scene_dir):
+    """The acceptance check at the workload's own size: 512x512, 32 spp, depth 8."""
+    path = S.ensure_written(S.differentiable_scene(name="diff_c3"), scene_dir)
+    _fd_check(path, spp=32, depth=8, min_checked=40)
+
+
+def _crop_check(path, spp, depth, crop):
+    """GPU adjoint of the samples of `crop` against the same gradient from the
+    host restatement in double precision (oracle/lt_diff_ref.cpp): relative
+    L2 error of each gradient array below 2e-3."""
     from oracle import oracle as O
-    path = _small(scene_dir)
     ds = DiffScene(path)
     orc = O.OracleScene(path)
     a0, e0, sa0, ss0 = ds.defaults()
     true, init = S.differentiable_targets(ds.num_triangles)
-    spp, depth, crop = 8, 6, (16, 8, 48, 40)
     e_np = e0.cpu().numpy()
-    tgt, _ = orc.diff_render(true["albedo"], e_np, true["sigma_a"], true["sigma_s"], spp, max_depth=depth)
-    cur, _ = orc.diff_render(init["albedo"], e_np, init["sigma_a"], init["sigma_s"], spp, max_depth=depth)
+    tgt, _ = orc.diff_render(true["albedo"], e_np, true["sigma_a"], true["sigma_s"], spp, max_depth=depth, crop=crop)
+    cur, _ = orc.diff_render(init["albedo"], e_np, init["sigma_a"], init["sigma_s"], spp, max_depth=depth, crop=crop)
     dI = (2.0 * (cur - tgt) / spp / spp).astype(np.float32)  # d/d(film sum) of sum((img - target)^2)
     _, g64 = orc.diff_render(init["albedo"], e_np, init["sigma_a"], init["sigma_s"], spp, max_depth=depth,
                              crop=crop, dI=dI, fp64=True)
@@ -107,9 +128,24 @@ def test_adjoint_crop_matches_fp64_host_reference(scene_dir):
                    torch.from_numpy(init["sigma_s"]).to(dev), torch.from_numpy(dI).to(dev), spp, 0, depth, 3,
                    crop=crop)
     torch.cuda.synchronize()
+    worst = 0.0
     for name, gg in zip(("albedo", "emission", "sigma_a", "sigma_s"), g):
         ref = g64[name].reshape(-1)
         got = gg.detach().cpu().numpy().astype(np.float64).reshape(-1)
         assert np.linalg.norm(ref) > 0, name
         rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
         assert rel < 2e-3, (name, rel)
+        worst = max(worst, rel)
+    return worst
+
+
+def test_adjoint_crop_matches_fp64_host_reference(scene_dir):
+    _crop_check(_small(scene_dir), spp=8, depth=6, crop=(16, 8, 48, 40))
+
+
+def test_adjoint_crop_matches_fp64_host_reference_on_the_differentiable_workload(scene_dir):
+    """A 32x32 crop of the 512x512, 32-spp, depth-8 workload (pixels 440-471 x
+    250-281): part of the fog sphere, a Lambert sphere and the ground, so every
+    gradient array (albedo, emission, sigma_a, sigma_s) is nonzero."""
+    path = S.ensure_written(S.differentiable_scene(name="diff_c3"), scene_dir)
+    _crop_check(path, spp=32, depth=8, crop=(440, 250, 472, 282))

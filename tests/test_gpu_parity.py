@@ -91,6 +91,34 @@ def test_intersect_matches_oracle(ctx, width, scene_dir, make):
     assert np.array_equal(gh.view(np.uint32), gh2.view(np.uint32))
 
 
+@pytest.fixture(scope="module")
+def icosphere_workload(scene_dir):
+    """The 1.3M-triangle workload's scene (8-level displaced icosphere on the
+    ground, under the light), its oracle and 1,048,576 rays of the intersection
+    micro-bench's distribution: origins uniform in the icosphere's bounding box,
+    directions uniform on the sphere, seed 2, tnear 0, tfar inf."""
+    import json
+    path = S.ensure_written(S.displaced_icosphere_scene(name="icosphere"), scene_dir)
+    with open(path) as fh:
+        prims = json.load(fh)["primitives"]
+    pos = np.concatenate([_positions(path, p) for p in prims if p["name"].startswith("ico_")])
+    rays = S.random_rays(1 << 20, pos.min(0), pos.max(0), seed=2)
+    orc = O.OracleScene(path)
+    return path, orc, rays, orc.intersect(rays)
+
+
+def test_intersect_matches_oracle_on_the_icosphere_workload(ctx, width, icosphere_workload):
+    """lt_intersect on the 1,310,720-triangle mesh the micro-bench times, all
+    three BVH widths, against the oracle's BVH2: primitive bit-exact except
+    exact ties, t within 1e-5 relative."""
+    path, orc, rays, oh = icosphere_workload
+    ctx.load_scene_json(path)
+    assert ctx.scene_info().num_triangles == 1310724
+    gh = intersect(ctx, torch.from_numpy(rays).cuda()).cpu().numpy()
+    nhit, nties = _compare_hits(gh, oh)
+    assert nhit > (1 << 19)
+
+
 def test_intersect_tnear_tfar_rule(ctx, width, scene_dir):
     """Rays clipped exactly at, and one float short of, each hit distance (and
     starting there) are accepted or rejected as the oracle's Embree rule says:

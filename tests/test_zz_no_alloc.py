@@ -9,7 +9,9 @@ slots). Called through the C ABI, two calls in a row must give what lt_render
 gives for the same samples: identical sample counts and path lengths, and
 colour sums equal up to float atomic-add order (rtol 1e-5). The array keeps
 the previous call's contents, so the second call also checks that a call
-starts from a clean state. This file is named to be collected last.
+starts from a clean state. A fresh context's first call leaves the device's
+free memory unchanged, and its statistics count what lt_render's count. This
+file is named to be collected last.
 """
 import numpy as np
 import pytest
@@ -67,4 +69,46 @@ def test_noalloc_rejects_sizes_beyond_its_limit(scene_dir):
     with pytest.raises(LanternError) as e:
         ctx.render_noalloc(Film(host[0].ctypes.data, host[1].ctypes.data, host[2].ctypes.data, 8, 8, 0), 1, 64)
     assert e.value.status == 1
+    ctx.close()
+
+
+def test_noalloc_first_call_on_a_fresh_context_allocates_nothing(scene_dir):
+    """lt_ctx_create did the set-up (loaded the module holding the fixed array
+    and the wavefront kernels, looked up the array's address): the first
+    lt_render_noalloc of a new context changes nothing in device memory."""
+    path = S.tiny_scene(width=32, height=24, name="noalloc_fresh").write(scene_dir)
+    ctx = Context(0)
+    ctx.load_scene_json(path)
+    info = ctx.scene_info()
+    fb = FrameBuffer(info.width, info.height, "cuda:0")
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    ctx.render_noalloc(fb.film(), 4, 8192, 0, DEPTH, RR)
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+    assert int(fb.ColorSampleCount.min()) == 4
+    ctx.close()
+
+
+def test_noalloc_stats_count_as_render(scene_dir):
+    """Ray, connection and non-finite counts of lt_render_noalloc equal
+    lt_render's for the same samples (a sphere without normals shades with
+    NaN, as the reference's integrator.cpp:179-183 does)."""
+    sc = S.tiny_scene(width=32, height=32, name="noalloc_nan")
+    sc.meshes[0].normals = np.zeros((0, 3), np.float32)
+    ctx = Context(0)
+    ctx.load_scene_json(sc.write(scene_dir))
+    info = ctx.scene_info()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    fa = FrameBuffer(info.width, info.height, "cuda:0")
+    ctx.render(fa.film(), 3, 0, 8, RR)
+    ra = ctx.stats()
+    fb = FrameBuffer(info.width, info.height, "cuda:0")
+    ctx.render_noalloc(fb.film(), 3, 2048, 0, 8, RR)
+    rb = ctx.stats()
+    assert ra.nonfinite_samples > 0 and rb.nonfinite_samples == ra.nonfinite_samples
+    for k in ("main_rays", "light_rays", "bsdf_rays", "light_traversals", "samples"):
+        assert getattr(rb, k) == getattr(ra, k), k
     ctx.close()
