@@ -462,9 +462,21 @@ def adjoint_bench(local):
     dI = (2.0 * (rgb / 32 - target) / 32).contiguous()
     adj = timed(lambda: ds.adjoint(*th, dI, 32, 0, 8, 3, samples=samples))
     nparams = 6 * ds.num_triangles + 6 * ds.num_media
+    # acceptance check of the gradients (outside the timings): 64 parameters
+    # (seed 4) against central differences, h = 1e-3
+    from lantern_gb300.diff import finite_difference_check
+    fdc = finite_difference_check(ds, th, target, 32, max_depth=8, count=64, seed=4, h=1e-3)
+    step = dfw + adj
     return {"config": "differentiable scene 512x512, 32 spp, depth 8", "parameters": nparams,
             "forward_ms": round(fwd, 3), "diff_forward_ms": round(dfw, 3), "adjoint_ms": round(adj, 3),
-            "adjoint_over_forward": round(adj / fwd, 3), "grads_per_s": round(1e3 / adj, 2)}
+            "adjoint_over_forward": round(adj / fwd, 3), "grads_per_s": round(1e3 / adj, 2),
+            "step_ms": round(step, 3), "step_over_forward": round(step / fwd, 3),
+            "grads_per_s_step": round(1e3 / step, 2),
+            "ratios": "adjoint_over_forward: adjoint pass / plain forward render; step_over_forward: "
+                      "(differentiable forward + adjoint) / plain forward render",
+            "fd_check": {"parameters": fdc["parameters"], "checked": fdc["checked"],
+                         "max_rel_err": round(fdc["max_rel_err"], 5), "h": 1e-3, "seed": 4,
+                         "within_2pct": not fdc["failures"]}}
 
 
 def batch_bench(local, count=64, reps=3):

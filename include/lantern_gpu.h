@@ -137,7 +137,9 @@ typedef struct lt_scene_desc {
 /* Uploads the scene and builds its BVH; replaces any previous scene.
  * Replaces Scene::ParseJSON's AddMesh/AddLMF + rtcCommitScene
  * (scene.cpp:451-582, :86): the library computes each light's area, bounding
- * sphere and radiance the way AddLMF and AreaLight's constructor do. */
+ * sphere and radiance the way AddLMF and AreaLight's constructor do (on the
+ * device with the GPU builder: the vertex transform, triangle setup, light
+ * setup and BVH build all run there). */
 lt_status lt_scene_create(lt_ctx *ctx, const lt_scene_desc *desc);
 
 /* Frees the context's scene (its device arrays, BVHs and captured batch loop)
@@ -180,6 +182,23 @@ typedef struct lt_scene_info {
     uint32_t num_media;
 } lt_scene_info;
 lt_status lt_scene_info_get(lt_ctx *ctx, lt_scene_info *out);
+
+/* The scene's area lights (Scene::GetLight / AreaLight, scene.h:74-79,
+ * area_light.h:16-21): per emissive mesh, in mesh order, its mesh index
+ * (geomID), triangle count, area (the sequential sum of scene.cpp:527-534),
+ * bounding sphere (CalculateBoundingSphere, scene.cpp:49-80) and radiance
+ * (color * radiant_power / (pi * area)). With the GPU builder the device
+ * computes them from the transformed vertices, with the host builder the host
+ * does; both give the same bits. `out` holds `capacity` entries (at least the
+ * scene's num_lights). */
+typedef struct lt_light_info {
+    uint32_t mesh;
+    uint32_t num_triangles;
+    float area;
+    float sphere[4];   /* centre x, y, z, radius */
+    float radiance[3];
+} lt_light_info;
+lt_status lt_scene_lights_get(lt_ctx *ctx, lt_light_info *out, uint32_t capacity);
 
 /* Per-mesh geometry offsets: first global triangle index of each mesh
  * (global triangle index = first[geomID] + primID). `first` holds num_meshes. */

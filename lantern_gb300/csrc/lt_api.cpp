@@ -470,6 +470,28 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) try {
                                     c->stream));
         CUDA_TRY(c, setup_triangles_gpu(d_pos, d_idx, d_meshes, desc->num_meshes, (uint32_t)nvert, (uint32_t)ntri,
                                         d_tri, d_vidx, c->stream));
+        // area lights from the transformed vertices: light triangles, area,
+        // bounding sphere, radiance (read back for the host's copy)
+        if (h.lights.size() > kMaxLights)
+            return fail(c, LT_ERR_UNSUPPORTED, "%zu lights: at most %u", h.lights.size(), kMaxLights);
+        const size_t nl = h.lights.size();
+        size_t nlt = 0;
+        for (const LightSource &ls : h.light_src) nlt += ls.ntris;
+        LightSource *d_src = nullptr;
+        LightInfo *d_lights = nullptr;
+        float4 *d_ltris = nullptr;
+        CUDA_TRY(c, tmp.alloc((void **)&d_src, nl * sizeof(LightSource) + 16));
+        if ((st = scene_alloc(c, nl * sizeof(LightInfo) + 16, (void **)&d_lights)) != LT_OK) return st;
+        if ((st = scene_alloc(c, nlt * 48 + 16, (void **)&d_ltris)) != LT_OK) return st;
+        if (nl) {
+            CUDA_TRY(c, cudaMemcpyAsync(d_src, h.light_src.data(), nl * sizeof(LightSource), cudaMemcpyHostToDevice,
+                                        c->stream));
+            CUDA_TRY(c, setup_lights_gpu(d_pos, d_idx, d_src, (uint32_t)nl, d_lights, d_ltris, c->stream));
+            CUDA_TRY(c, cudaMemcpyAsync(h.lights.data(), d_lights, nl * sizeof(LightInfo), cudaMemcpyDeviceToHost,
+                                        c->stream));
+        }
+        d.lights = d_lights;
+        d.light_tris = d_ltris;
         d.vnormal = d_nrm;
         d.vtex = d_tex;
         d.tri_vidx = d_vidx;
@@ -517,10 +539,12 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) try {
     if ((st = upload(c, h.geoms, &d.geoms)) != LT_OK) return st;
     if ((st = upload(c, h.materials, &d.mats)) != LT_OK) return st;
     if ((st = upload(c, h.media, &d.meds)) != LT_OK) return st;
-    if ((st = upload(c, h.lights, &d.lights)) != LT_OK) return st;
-    const float *ltris = nullptr;
-    if ((st = upload(c, h.light_tris, &ltris)) != LT_OK) return st;
-    d.light_tris = (const float4 *)ltris;
+    if (!gpu_setup) {  // the device set the lights up otherwise (above)
+        if ((st = upload(c, h.lights, &d.lights)) != LT_OK) return st;
+        const float *ltris = nullptr;
+        if ((st = upload(c, h.light_tris, &ltris)) != LT_OK) return st;
+        d.light_tris = (const float4 *)ltris;
+    }
     d.num_lights = (uint32_t)h.lights.size();
     d.num_tris = (uint32_t)h.tri_geom.size();
     d.background = h.background;
@@ -553,6 +577,22 @@ lt_status lt_scene_info_get(lt_ctx *c, lt_scene_info *out) try {
     out->num_media = (uint32_t)c->host.media.size();
     out->device_bytes = c->scene_bytes;
     out->build_ms = c->host.build_ms;
+    return LT_OK;
+} LT_CATCH(c)
+
+lt_status lt_scene_lights_get(lt_ctx *c, lt_light_info *out, uint32_t capacity) try {
+    if (!c || (capacity && !out)) return fail(c, LT_ERR_INVALID, "NULL argument");
+    if (!c->has_scene) return fail(c, LT_ERR_STATE, "no scene");
+    const std::vector<LightInfo> &L = c->host.lights;
+    if (capacity < L.size()) return fail(c, LT_ERR_INVALID, "capacity %u below the %zu lights", capacity, L.size());
+    for (size_t i = 0; i < L.size(); ++i) {
+        lt_light_info &o = out[i];
+        o.mesh = (uint32_t)L[i].geom;
+        o.num_triangles = L[i].tri_count;
+        o.area = L[i].area;
+        memcpy(o.sphere, L[i].sphere, sizeof o.sphere);
+        memcpy(o.radiance, L[i].radiance, sizeof o.radiance);
+    }
     return LT_OK;
 } LT_CATCH(c)
 

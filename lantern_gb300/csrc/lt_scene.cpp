@@ -9,35 +9,6 @@
 
 namespace lt {
 
-// CalculateBoundingSphere (scene.cpp:49-80): two Ritter passes and a
-// tightening pass over the transformed vertices.
-static void bounding_sphere(const float *p, uint32_t n, float out[4]) {
-    v3 c = ld3(p);
-    float r = 0.0001f;
-    for (int pass = 0; pass < 2; ++pass) {
-        for (uint32_t j = 0; j < n; ++j) {
-            v3 pos = ld3(p + 3 * (size_t)j);
-            float len = length(pos - c);
-            if (len > r) {
-                float a = len / r;
-                float a2 = a * a;
-                r = 0.5f * (a + 1 / a) * r;
-                c = (c * (1 + 1 / a2) + pos * (1 - 1 / a2)) * 0.5f;
-            }
-        }
-    }
-    for (uint32_t j = 0; j < n; ++j) {
-        v3 pos = ld3(p + 3 * (size_t)j);
-        v3 d = pos - c;
-        float len = length(d);
-        if (len > r) {
-            r = (r + len) / 2.0f;
-            c = c + d * ((len - r) / len);
-        }
-    }
-    out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = r;
-}
-
 // transform * float3a(p, 1) (scene.cpp:456-461, 517-522; linearspace4.h:43-47,165):
 // row r = ((x*m[4r] + y*m[4r+1]) + z*m[4r+2]) + 1*m[4r+3].
 void transform_points(const float *m, const float *in, uint32_t n, float *out) {
@@ -137,6 +108,7 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
     s->geoms.clear();
     s->lights.clear();
     s->light_tris.clear();
+    s->light_src.clear();
     s->tri_geom.assign(ntri, 0);
     if (host_setup) {
         s->tri_v0e1e2.assign(ntri * 9, 0.0f);
@@ -150,6 +122,7 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
         s->vtex.clear();
     }
     size_t t0 = 0, vbase = 0;
+    uint32_t light_tri_count = 0;
     std::vector<float> moved;
     for (uint32_t g = 0; g < d->num_meshes; ++g) {
         const lt_mesh_desc &m = d->meshes[g];
@@ -176,7 +149,7 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
         // world-space positions on the host: every mesh for a host setup, else
         // only the lights' (area, bounding sphere, light triangles)
         const float *pos = m.positions;
-        if (m.transform && (host_setup || m.emissive)) {
+        if (m.transform && host_setup) {
             moved.resize(3 * (size_t)m.num_vertices);
             transform_points(m.transform, m.positions, m.num_vertices, moved.data());
             pos = moved.data();
@@ -203,23 +176,35 @@ lt_status build_host_scene(const lt_scene_desc *d, HostScene *s, std::string *er
             LightInfo li;
             memset(&li, 0, sizeof li);
             li.geom = (int32_t)g;
-            float area = 0.0f;
-            li.tri_first = (uint32_t)(s->light_tris.size() / 12);
+            li.tri_first = light_tri_count;
             li.tri_count = m.num_triangles;
-            for (uint32_t t = 0; t < m.num_triangles; ++t) {
-                uint32_t i0 = m.indices[3 * t], i1 = m.indices[3 * t + 1], i2 = m.indices[3 * t + 2];
-                v3 a = ld3(pos + 3 * (size_t)i0), b = ld3(pos + 3 * (size_t)i1), c = ld3(pos + 3 * (size_t)i2);
-                area += 0.5f * length(cross(a - b, a - c));  // scene.cpp:527-534
-                v3 e1 = a - b, e2 = c - a;
-                const float row[12] = {a.x, a.y, a.z, bits_to_float((uint32_t)(t0 + t)),
-                                       e1.x, e1.y, e1.z, 0.0f, e2.x, e2.y, e2.z, 0.0f};
-                s->light_tris.insert(s->light_tris.end(), row, row + 12);
+            light_tri_count += m.num_triangles;
+            if (host_setup) {
+                for (uint32_t t = 0; t < m.num_triangles; ++t) {
+                    uint32_t i0 = m.indices[3 * t], i1 = m.indices[3 * t + 1], i2 = m.indices[3 * t + 2];
+                    v3 a = ld3(pos + 3 * (size_t)i0), b = ld3(pos + 3 * (size_t)i1), c = ld3(pos + 3 * (size_t)i2);
+                    v3 e1 = a - b, e2 = c - a;
+                    const float row[12] = {a.x, a.y, a.z, bits_to_float((uint32_t)(t0 + t)),
+                                           e1.x, e1.y, e1.z, 0.0f, e2.x, e2.y, e2.z, 0.0f};
+                    s->light_tris.insert(s->light_tris.end(), row, row + 12);
+                }
+                li.area = light_area(pos, m.indices, m.num_triangles);
+                if (m.num_vertices) light_bounding_sphere(pos, m.num_vertices, li.sphere);
+                const v3 rad = light_radiance(m.emission_color, m.radiant_power, li.area);
+                li.radiance[0] = rad.x; li.radiance[1] = rad.y; li.radiance[2] = rad.z;
+            } else {
+                LightSource src;
+                memset(&src, 0, sizeof src);
+                src.geom = g;
+                src.vbase = (uint32_t)vbase;
+                src.tbase = (uint32_t)t0;
+                src.nverts = m.num_vertices;
+                src.ntris = m.num_triangles;
+                src.tri_first = li.tri_first;
+                memcpy(src.color, m.emission_color, sizeof src.color);
+                src.power = m.radiant_power;
+                s->light_src.push_back(src);
             }
-            li.area = area;
-            if (m.num_vertices) bounding_sphere(pos, m.num_vertices, li.sphere);
-            // AreaLight ctor (area_light.h:16-21): color * radiantPower * (float)M_1_PI / area
-            v3 rad = ((ld3(m.emission_color) * m.radiant_power) * kInvPi) / area;
-            li.radiance[0] = rad.x; li.radiance[1] = rad.y; li.radiance[2] = rad.z;
             gi.light = (int32_t)s->lights.size();
             s->lights.push_back(li);
         }

@@ -54,6 +54,67 @@ struct alignas(16) LightInfo {
     float sphere[4];     // bounding sphere centre, radius
 };
 
+// An emissive mesh whose light data the device computes (device scene setup):
+// its vertices and triangles in the concatenated arrays, its first light
+// triangle, and AreaLight's constructor arguments.
+struct alignas(16) LightSource {
+    uint32_t geom, vbase, tbase, nverts, ntris, tri_first;
+    float color[3];
+    float power;
+    uint32_t pad[2];
+};
+
+// Light setup of one emissive mesh, shared by the host and device builds so
+// that both run the same float operations in the same order (no fused
+// multiply-add on either side). `pos` holds the mesh's world-space vertices,
+// `idx` its mesh-local triangle indices.
+//
+// Area: the sequential sum of 0.5 * |(a - b) x (a - c)| over the triangles
+// (scene.cpp:527-534).
+LT_HD float light_area(const float *pos, const uint32_t *idx, uint32_t ntris) {
+    float area = 0.0f;
+    for (uint32_t t = 0; t < ntris; ++t) {
+        const uint32_t i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
+        const v3 a = ld3(pos + 3 * (size_t)i0), b = ld3(pos + 3 * (size_t)i1), c = ld3(pos + 3 * (size_t)i2);
+        area += 0.5f * length(cross(a - b, a - c));
+    }
+    return area;
+}
+
+// CalculateBoundingSphere (scene.cpp:49-80): two Ritter passes and a
+// tightening pass over the vertices.
+LT_HD void light_bounding_sphere(const float *p, uint32_t n, float out[4]) {
+    v3 c = ld3(p);
+    float r = 0.0001f;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (uint32_t j = 0; j < n; ++j) {
+            v3 pos = ld3(p + 3 * (size_t)j);
+            float len = length(pos - c);
+            if (len > r) {
+                float a = len / r;
+                float a2 = a * a;
+                r = 0.5f * (a + 1 / a) * r;
+                c = (c * (1 + 1 / a2) + pos * (1 - 1 / a2)) * 0.5f;
+            }
+        }
+    }
+    for (uint32_t j = 0; j < n; ++j) {
+        v3 pos = ld3(p + 3 * (size_t)j);
+        v3 d = pos - c;
+        float len = length(d);
+        if (len > r) {
+            r = (r + len) / 2.0f;
+            c = c + d * ((len - r) / len);
+        }
+    }
+    out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = r;
+}
+
+// AreaLight's radiance (area_light.h:16-21): color * radiantPower * (float)M_1_PI / area.
+LT_HD v3 light_radiance(const float color[3], float power, float area) {
+    return ((ld3(color) * power) * kInvPi) / area;
+}
+
 // BVH2 node for the device, 64 bytes (four float4):
 //  [0] c0.lo.x c0.hi.x c0.lo.y c0.hi.y   [1] c1.lo.x c1.hi.x c1.lo.y c1.hi.y
 //  [2] c0.lo.z c0.hi.z c1.lo.z c1.hi.z   [3] c0 ref, c1 ref, c0 count, c1 count
@@ -111,14 +172,17 @@ struct HostScene {
     std::vector<BvhNode> nodes;
     std::vector<float> leaf_tris;    // 12 floats per triangle in leaf order: v0,prim | e1,0 | e2,0
     std::vector<float> light_tris;   // the emissive meshes' triangles, same 12-float layout
+    std::vector<LightSource> light_src;  // device setup: what the device computes the lights from
     uint32_t max_depth = 0;          // deepest leaf (the traversal stack holds 64)
     float build_ms = 0.0f;
 };
 
 // Fills `out` from a scene description. Returns LT_OK or an error with `err`.
-// With host_setup false the per-triangle arrays (tri_v0e1e2, tri_vidx) and the
-// vertex arrays (vnormal, vtex) stay empty: the device builds them
-// (setup_triangles_gpu); lights, tables and tri_geom are always filled.
+// With host_setup false the per-triangle arrays (tri_v0e1e2, tri_vidx), the
+// vertex arrays (vnormal, vtex) and the lights' geometry (area, bounding
+// sphere, radiance, light_tris) stay empty: the device computes them
+// (setup_triangles_gpu, setup_lights_gpu) from light_src; the lights' indices,
+// the tables and tri_geom are always filled.
 lt_status build_host_scene(const lt_scene_desc *desc, HostScene *out, std::string *err, bool host_setup = true);
 
 // transform * (p, 1) for n points (a row-major 4x4 matrix, float arithmetic of

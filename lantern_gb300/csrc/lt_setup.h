@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "lt_scene.h"
+
 namespace lt {
 
 // One mesh of the concatenated vertex / triangle arrays.
@@ -21,5 +23,13 @@ struct MeshSetup {
 // is a device array of nmesh entries in vbase / tbase order.
 cudaError_t setup_triangles_gpu(float *pos, const uint32_t *idx, const MeshSetup *meshes, uint32_t nmesh,
                                 uint32_t nvert, uint32_t ntri, float *tri9, uint32_t *vidx, cudaStream_t st);
+
+// Area lights from the transformed vertices (pos, after setup_triangles_gpu)
+// and the mesh-local indices (idx): lights[i] and the light triangles of
+// src[i] (light_tris, 3 float4 per triangle from src[i].tri_first), with the
+// host build's arithmetic (lt_scene.h: light_area, light_bounding_sphere,
+// light_radiance). src is a device array of nlights entries.
+cudaError_t setup_lights_gpu(const float *pos, const uint32_t *idx, const LightSource *src, uint32_t nlights,
+                             LightInfo *lights, float4 *light_tris, cudaStream_t st);
 
 }  // namespace lt

@@ -209,3 +209,61 @@ def adjoint_batch(scenes, params, d_loss_d_sum, spp, first_frame=0, max_depth: i
     torch.cuda.current_stream(scenes[0].device).synchronize()
     del keep
     return grads
+
+
+def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: int, first_frame: int = 0,
+                            max_depth: int = 8, rr_depth: int = 3, count: int = 64, seed: int = 4,
+                            h: float = 1e-3, rel_tol: float = 0.02):
+    """Adjoint gradient of L = sum((image - target)^2), image = film / spp,
+    against central finite differences of the same estimator.
+
+    theta = (albedo, emission, sigma_a, sigma_s) CUDA tensors; target is the
+    reference image (H, W, 3). The adjoint comes from RenderImage's backward;
+    each difference renders twice with one parameter moved by +-h and the
+    sampling copies (detached albedo, sigma_a, sigma_s) held at theta, so both
+    sides differentiate the same function of the parameters (the forward is
+    deterministic: one thread per pixel, samples summed in frame order).
+    Parameters, drawn with `seed`: every sigma_a and sigma_s entry, then up to
+    48 albedo and 10 emission entries whose adjoint gradient is nonzero, `count`
+    in all. A parameter is compared when either gradient exceeds 1e-4 of the
+    largest gradient of its array. Returns {"parameters", "checked",
+    "max_rel_err", "failures": [(array, index, adjoint, fd), ...]} with the
+    comparisons whose relative difference exceeds rel_tol."""
+    base = [t.detach().to(scene.device, torch.float32).contiguous() for t in theta]
+    tgt = target.detach().to(scene.device).double()
+    th = [t.clone().requires_grad_() for t in base]
+    img = render_image(scene, *th, spp, first_frame, max_depth, rr_depth)
+    loss = ((img.double() - tgt) ** 2).sum()
+    loss.backward()
+    grads = [t.grad.detach().cpu().numpy().reshape(-1) for t in th]
+    detached = (base[0], base[2], base[3])
+
+    def loss_at(k, idx, delta):
+        p = [t.clone() for t in base]
+        p[k].view(-1)[idx] += delta
+        rgb, _, _ = scene.render(*p, spp=spp, first_frame=first_frame, max_depth=max_depth, rr_depth=rr_depth,
+                                 detached=detached)
+        return float((((rgb / spp).double() - tgt) ** 2).sum())
+
+    rng = np.random.default_rng(seed)
+    cands = ([(2, i) for i in range(3 * scene.num_media)] + [(3, i) for i in range(3 * scene.num_media)])
+    nz = np.flatnonzero(np.abs(grads[0]) > 0)
+    cands += [(0, int(i)) for i in rng.choice(nz, size=min(48, nz.size), replace=False)]
+    nze = np.flatnonzero(np.abs(grads[1]) > 0)
+    cands += [(1, int(i)) for i in rng.choice(nze, size=min(10, nze.size), replace=False)]
+    cands = cands[:count]
+    gmax = [float(np.abs(g).max()) if g.size else 0.0 for g in grads]
+    names = ("albedo", "emission", "sigma_a", "sigma_s")
+    failures, worst, checked = [], 0.0, 0
+    for k, i in cands:
+        fd = (loss_at(k, i, h) - loss_at(k, i, -h)) / (2 * h)
+        ad = float(grads[k][i])
+        if max(abs(fd), abs(ad)) <= 1e-4 * gmax[k]:
+            continue
+        checked += 1
+        rel = abs(ad - fd) / max(abs(fd), abs(ad))
+        worst = max(worst, rel)
+        if rel > rel_tol:
+            failures.append((names[k], i, ad, fd))
+    return {"parameters": len(cands), "checked": checked, "max_rel_err": worst, "failures": failures}
+

@@ -22,7 +22,7 @@ MISS = 0xFFFFFFFF
 # exported symbols (include/lantern_gpu.h)
 SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error", "lt_set_stream", "lt_get_stream",
            "lt_sync",
-           "lt_scene_create", "lt_scene_destroy", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_render",
+           "lt_scene_create", "lt_scene_destroy", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_scene_lights_get", "lt_render",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
            "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load",
@@ -74,6 +74,11 @@ class SceneDesc(C.Structure):
                 ("media", C.POINTER(MediumDesc)), ("num_media", C.c_uint32),
                 ("meshes", C.POINTER(MeshDesc)), ("num_meshes", C.c_uint32),
                 ("images", C.POINTER(ImageDesc)), ("num_images", C.c_uint32)]
+
+
+class LightInfo(C.Structure):
+    _fields_ = [("mesh", C.c_uint32), ("num_triangles", C.c_uint32), ("area", C.c_float),
+                ("sphere", C.c_float * 4), ("radiance", C.c_float * 3)]
 
 
 class SceneInfo(C.Structure):
@@ -143,6 +148,7 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_scene_destroy.argtypes = [p]
         L.lt_scene_info_get.argtypes = [p, C.POINTER(SceneInfo)]
         L.lt_scene_mesh_offsets.argtypes = [p, C.POINTER(C.c_uint32), C.c_uint32]
+        L.lt_scene_lights_get.argtypes = [p, C.POINTER(LightInfo), C.c_uint32]
         L.lt_render.argtypes = [p, C.POINTER(RenderParams), C.POINTER(Film)]
         L.lt_render_stats_get.argtypes = [p, C.POINTER(RenderStats)]
         L.lt_intersect.argtypes = [p, p, p, C.c_uint64, C.c_int32]
@@ -240,6 +246,14 @@ class Context:
         info = SceneInfo()
         self._check(self.L.lt_scene_info_get(self.h, C.byref(info)))
         return info
+
+    def lights(self):
+        """lt_scene_lights_get: per area light (mesh, num_triangles, area,
+        sphere[4], radiance[3])."""
+        n = self.scene_info().num_lights
+        arr = (LightInfo * max(1, n))()
+        self._check(self.L.lt_scene_lights_get(self.h, arr, len(arr)))
+        return list(arr)[:n]
 
     def mesh_offsets(self):
         info = self.scene_info()

@@ -103,6 +103,8 @@ def lib():
             L.orc_light_info.argtypes = [p, i32, fp, fp, fp]
             L.orc_num_triangles.argtypes = [p]
             L.orc_num_triangles.restype = u32
+            L.orc_num_lights.argtypes = [p]
+            L.orc_num_lights.restype = i32
             L.orc_intersect.argtypes = [p, fp, up, u64, i32, up, i32]
             L.orc_render.argtypes = [p, p, u32, u32, fp, up, up, fp, up, up, C.POINTER(C.c_uint64)]
             L.orc_render_path.argtypes = [p, p, u32, u32, u32, fp, up]
@@ -393,6 +395,18 @@ class OracleScene:
             L.orc_medium_info(self.h, m, C.byref(ty), a3, s3, C.byref(g))
             sa[m], ss[m] = list(a3), list(s3)
         return albedo, emission, sa, ss
+
+    def lights(self):
+        """Per area light, in mesh order: (area, bounding sphere (4), radiance (3))
+        as float32 arrays, computed the way AddLMF and AreaLight's constructor
+        do (scene.cpp:49-80, 527-534; area_light.h:16-21)."""
+        L = lib()
+        out = []
+        for i in range(L.orc_num_lights(self.h)):
+            area, sph, r3 = C.c_float(), (C.c_float * 4)(), (C.c_float * 3)()
+            L.orc_light_info(self.h, i, C.byref(area), sph, r3)
+            out.append((np.float32(area.value), np.array(list(sph), np.float32), np.array(list(r3), np.float32)))
+        return out
 
     def diff_render(self, albedo, emission, sigma_a, sigma_s, spp: int, max_depth: int = 8, rr_depth: int = 3,
                     first_frame: int = 0, crop=None, dI=None, fp64: bool = True, threads: int = 0):
