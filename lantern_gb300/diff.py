@@ -223,9 +223,9 @@ def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: 
     sampling copies (detached albedo, sigma_a, sigma_s) held at theta, so both
     sides differentiate the same function of the parameters (the forward is
     deterministic: one thread per pixel, samples summed in frame order).
-    Parameters, drawn with `seed`: every sigma_a and sigma_s entry, then up to
-    48 albedo and 10 emission entries whose adjoint gradient is nonzero, `count`
-    in all. A parameter is compared when either gradient exceeds 1e-4 of the
+    Parameters, drawn with `seed`: every sigma_a and sigma_s entry, up to 10
+    emission entries whose adjoint gradient is nonzero, then albedo entries with
+    a nonzero gradient up to `count` in all. A parameter is compared when either gradient exceeds 1e-4 of the
     largest gradient of its array. Returns {"parameters", "checked",
     "max_rel_err", "failures": [(array, index, adjoint, fd), ...]} with the
     comparisons whose relative difference exceeds rel_tol."""
@@ -247,10 +247,10 @@ def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: 
 
     rng = np.random.default_rng(seed)
     cands = ([(2, i) for i in range(3 * scene.num_media)] + [(3, i) for i in range(3 * scene.num_media)])
-    nz = np.flatnonzero(np.abs(grads[0]) > 0)
-    cands += [(0, int(i)) for i in rng.choice(nz, size=min(48, nz.size), replace=False)]
     nze = np.flatnonzero(np.abs(grads[1]) > 0)
     cands += [(1, int(i)) for i in rng.choice(nze, size=min(10, nze.size), replace=False)]
+    nz = np.flatnonzero(np.abs(grads[0]) > 0)
+    cands += [(0, int(i)) for i in rng.choice(nz, size=min(max(count - len(cands), 0), nz.size), replace=False)]
     cands = cands[:count]
     gmax = [float(np.abs(g).max()) if g.size else 0.0 for g in grads]
     names = ("albedo", "emission", "sigma_a", "sigma_s")

@@ -45,7 +45,8 @@ def test_diff_forward_matches_render(scene_dir):
 def _fd_check(path, spp, depth, min_checked):
     """diff.finite_difference_check at the initial parameters (albedo 0.5,
     sigma_s = sigma_a = 1) against the image of the true ones (seed 3): 64
-    parameters (seed 4), h = 1e-3, every compared gradient within 2%."""
+    parameters (seed 4: the six medium coefficients, the light's emission
+    entries, albedo entries), h = 1e-3, every compared gradient within 2%."""
     ds = DiffScene(path)
     a0, e0, sa0, ss0 = ds.defaults()
     true, init = S.differentiable_targets(ds.num_triangles)
