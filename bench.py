@@ -324,7 +324,7 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    total_ms, trace_ms, shade_ms, rays, launches = 0.0, 0.0, 0.0, 0, 0
+    total_ms, trace_ms, shade_ms, init_ms, idle_ms, rays, launches = 0.0, 0.0, 0.0, 0.0, 0.0, 0, 0
     main_rays, conn_traced, trace_launches = 0, 0, 0
     for _ in range(args.steps):
         flush.fill_(1)
@@ -337,6 +337,8 @@ def main():
         st = integ.stats()
         trace_ms += st.trace_ms
         shade_ms += st.shade_ms
+        init_ms += st.init_ms
+        idle_ms += st.idle_ms
         rays += st.main_rays + st.light_rays + st.bsdf_rays
         main_rays += st.main_rays
         conn_traced += st.light_traversals
@@ -392,8 +394,12 @@ def main():
                     "bytes_per_ray": round(bpr, 1), "node_tests_per_ray": round(n_node, 2),
                     "tri_tests_per_ray": round(n_tri, 2), "peak_kind": peak_kind,
                     "rays_traced_per_step": (main_rays + conn_traced) // args.steps,
+                    # kernel time of each stage (events around every launch) and the
+                    # time between the render's kernels, as shares of the step
                     "trace_share": round(trace_ms / max(total_ms, 1e-9), 3),
-                    "shade_share": round(shade_ms / max(total_ms, 1e-9), 3)}
+                    "shade_share": round(shade_ms / max(total_ms, 1e-9), 3),
+                    "init_share": round(init_ms / max(total_ms, 1e-9), 3),
+                    "idle_share": round(idle_ms / max(total_ms, 1e-9), 3)}
         except Exception as e:  # the oracle is a checker; report its absence
             roof = {"error": str(e)[:200]}
         cpu = None
@@ -527,6 +533,22 @@ def batch_bench(local, count=64, reps=3):
         return best
 
     seq_default = timed(sequential)
+    # the ceiling of batching: in one more sequential pass, the kernel time of
+    # every render (events around each launch), the time each render's stream
+    # waited for the host between its batches of iterations, and the rest of the
+    # wall time (between renders)
+    busy = idle = inside = 0.0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for it, n in zip(integrators(), spps):
+        it.RenderFrame(n)
+        st_ = it.stats()
+        busy += st_.init_ms + st_.trace_ms + st_.shade_ms
+        idle += st_.idle_ms
+        inside += st_.gpu_ms
+    e1.record(stream)
+    e1.synchronize()
+    seq_wall = e0.elapsed_time(e1)
     owner = scenes[0].ctx
     owner.set_stream(stream.cuda_stream)
     t0 = time.perf_counter()
@@ -569,6 +591,12 @@ def batch_bench(local, count=64, reps=3):
             "sequential_ms": round(seq_default, 2), "sequential_tuned_ms": round(seq_tuned, 2),
             "batched_ms": round(bat, 2), "batched_msamples_per_s": round(samples / bat / 1e3, 2),
             "speedup_vs_sequential": round(seq / bat, 3), "tuning": tuned, "tune_s": round(tune_s, 2),
+            "sequential_ceiling": {"wall_ms": round(seq_wall, 2), "kernel_ms": round(busy, 2),
+                                   "idle_in_renders_ms": round(idle, 2),
+                                   "between_renders_ms": round(max(seq_wall - inside, 0.0), 2),
+                                   "max_speedup": round(seq_wall / max(busy, 1e-9), 3),
+                                   "note": "max_speedup = wall / kernel time: what batching reaches if it "
+                                           "removes every gap and runs the same kernels as fast"},
             "batched_iterations": st.iterations, "batched_kernel_launches": st.kernel_launches,
             "adjoint_scenes": len(marked), "adjoint_samples": adj_samples,
             "adjoint_sequential_ms": round(adj_seq, 2), "adjoint_batched_ms": round(adj_bat, 2),

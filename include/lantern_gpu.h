@@ -264,12 +264,16 @@ typedef struct lt_render_stats {
     uint64_t samples;
     uint32_t iterations;     /* wavefront iterations */
     uint32_t kernel_launches;
-    float gpu_ms;            /* device time of the last lt_render */
-    float trace_ms;          /* device time in the trace kernel (path rays + connection rays) */
-    float shade_ms;          /* ... in the shade kernel (incl. camera-ray generation) */
+    float gpu_ms;            /* device time of the last lt_render, first kernel to last */
+    float trace_ms;          /* kernel time of the trace stage (path rays + connection rays) */
+    float shade_ms;          /* ... of the shade stage (regenerated camera rays included) */
     uint64_t light_traversals; /* connection rays traced (the rest were resolved against the light alone) */
     uint64_t nonfinite_samples; /* film contributions with a NaN or infinite channel (e.g. a mesh
                                  * without normals shades with normalize(0), integrator.cpp:182) */
+    float init_ms;           /* kernel time of the first camera rays */
+    float idle_ms;           /* gpu_ms - init_ms - trace_ms - shade_ms: time between the render's
+                              * kernels (the stream waiting for the host between batches of
+                              * iterations, queue-length reads) */
 } lt_render_stats;
 lt_status lt_render_stats_get(lt_ctx *ctx, lt_render_stats *out);
 
@@ -368,9 +372,14 @@ typedef struct lt_diff_params {
 lt_status lt_diff_defaults(lt_ctx *ctx, float *albedo, float *emission, float *sigma_a, float *sigma_s);
 
 /* Forward render of the differentiable estimator into a device film
- * (additive, as lt_render). sample_radiance (device, optional): receives every
- * sample's radiance, 3 floats at ((frame - first_frame) * W * H + pixel); with
- * it the adjoint replays each path once instead of twice. */
+ * (additive, as lt_render), on the same wavefront as lt_render: every sample's
+ * radiance is gathered in the estimator's order and the colour sums are added
+ * per pixel in sample order, so the film is the same on every run (finite
+ * differences see no summation-order noise). Returns when the render has
+ * finished. sample_radiance (device, optional): receives every sample's
+ * radiance, 3 floats at ((frame - first_frame) * W * H + pixel); with it the
+ * adjoint replays each path once instead of twice (without it the library
+ * keeps such a buffer of its own). */
 lt_status lt_render_diff(lt_ctx *ctx, const lt_render_params *params, const lt_diff_params *dp, lt_film *film,
                          float *sample_radiance);
 

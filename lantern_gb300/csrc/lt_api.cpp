@@ -69,6 +69,14 @@ struct lt_ctx {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
 
+    // differentiable forward on the wavefront: the path extras (DiffWave) and,
+    // when the caller keeps no per-sample radiance, a buffer for it
+    void *diff_arena = nullptr;
+    size_t diff_arena_bytes = 0;
+    uint32_t diff_capacity = 0;
+    float *diff_samples = nullptr;
+    size_t diff_samples_bytes = 0;
+
     // launch configuration (lt_set_tuning / lt_autotune_batch); shape is the
     // single-scene instantiation's, batch_shape the batched one's
     lt_tuning tuning{};
@@ -288,6 +296,8 @@ void lt_ctx_destroy(lt_ctx *c) {
     if (c->table_dev) cudaFree(c->table_dev);
     if (c->table_host) cudaFreeHost(c->table_host);
     if (c->scratch) cudaFree(c->scratch);
+    if (c->diff_arena) cudaFree(c->diff_arena);
+    if (c->diff_samples) cudaFree(c->diff_samples);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->isect_fetch) cudaFree(c->isect_fetch);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -729,17 +739,36 @@ static lt_status ensure_width(lt_ctx *c, uint32_t width) {
 // The wavefront loop of one render over `w`: camera rays, then batches of
 // (trace, shade) iterations, reading the queue lengths back after each batch
 // until no path ray, camera ray or connection record is left. With
-// stage_timing an event goes before each stage launch (lt_render_stats'
-// trace_ms / shade_ms); without it nothing is created or allocated. Fills
-// c->stats (except samples and gpu_ms).
-static lt_status run_wave(lt_ctx *c, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, bool stage_timing) {
+// stage_timing a pair of events brackets every kernel launch, so that
+// lt_render_stats gets each stage's kernel time (init_ms, trace_ms, shade_ms)
+// apart from the time the stream waits for the host between batches; without
+// it nothing is created or allocated. Fills c->stats (except samples and gpu_ms).
+// `init` and `stage(stage, cur)` launch the kernels (plain or differentiable).
+template <class Init, class Stage>
+static lt_status run_loop(lt_ctx *c, const Wavefront &w, const RenderArgs &a, bool stage_timing, Init init,
+                          Stage launch_stage) {
     const uint32_t cap = w.capacity;
-    CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
-    CUDA_TRY(c, launch_wave_init(c->dev, w, a, f, c->shape, c->stream));
-    uint32_t launches = 1;
-    unsigned long long iters = 0;
     size_t nev = 0;
     if (stage_timing) c->stage_of_event.clear();
+    constexpr int kStageInit = kStages;  // the camera-ray kernel, after the two loop stages
+    // records the event before (after = false) or after a launch of `stage`
+    auto mark = [&](int stage, bool after) -> cudaError_t {
+        if (!stage_timing) return cudaSuccess;
+        if (nev == c->stage_events.size()) {
+            cudaEvent_t e;
+            const cudaError_t ce = cudaEventCreate(&e);
+            if (ce != cudaSuccess) return ce;
+            c->stage_events.push_back(e);
+        }
+        if (!after) c->stage_of_event.push_back(stage);
+        return cudaEventRecord(c->stage_events[nev++], c->stream);
+    };
+    CUDA_TRY(c, cudaMemsetAsync(w.counters, 0, sizeof(WaveCounters), c->stream));
+    CUDA_TRY(c, mark(kStageInit, false));
+    CUDA_TRY(c, init());
+    CUDA_TRY(c, mark(kStageInit, true));
+    uint32_t launches = 1;
+    unsigned long long iters = 0;
     int cur = 0;
     const unsigned long long limit = drain_limit(a.total, cap, a.max_depth);
     // Iterations launched between two reads of the queue lengths. While work
@@ -750,16 +779,9 @@ static lt_status run_wave(lt_ctx *c, const Wavefront &w, const RenderArgs &a, co
         if (batch > limit - iters) batch = limit - iters;  // iters < limit here
         for (unsigned long long k = 0; k < batch; ++k) {
             for (int stage = 0; stage < kStages; ++stage) {
-                if (stage_timing) {
-                    if (nev == c->stage_events.size()) {
-                        cudaEvent_t e;
-                        CUDA_TRY(c, cudaEventCreate(&e));
-                        c->stage_events.push_back(e);
-                    }
-                    CUDA_TRY(c, cudaEventRecord(c->stage_events[nev++], c->stream));
-                    c->stage_of_event.push_back(stage);
-                }
-                CUDA_TRY(c, launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream));
+                CUDA_TRY(c, mark(stage, false));
+                CUDA_TRY(c, launch_stage(stage, cur));
+                CUDA_TRY(c, mark(stage, true));
             }
             launches += kStages;
             cur ^= 1;
@@ -785,24 +807,24 @@ static lt_status run_wave(lt_ctx *c, const Wavefront &w, const RenderArgs &a, co
     c->stats.light_traversals = k.light_traversals;
     c->stats.iterations = (uint32_t)iters;
     c->stats.kernel_launches = launches;
-    if (stage_timing) {
-        if (nev == c->stage_events.size()) {
-            cudaEvent_t e;
-            CUDA_TRY(c, cudaEventCreate(&e));
-            c->stage_events.push_back(e);
-        }
-        CUDA_TRY(c, cudaEventRecord(c->stage_events[nev], c->stream));
-        CUDA_TRY(c, cudaEventSynchronize(c->stage_events[nev]));
-        float acc[kStages] = {0, 0};
-        for (size_t i = 0; i < nev; ++i) {
+    if (stage_timing) {  // the stream has been synchronised: every event has completed
+        float acc[kStages + 1] = {0, 0, 0};
+        for (size_t i = 0; i + 1 < nev; i += 2) {
             float ms = 0.0f;
             CUDA_TRY(c, cudaEventElapsedTime(&ms, c->stage_events[i], c->stage_events[i + 1]));
-            acc[c->stage_of_event[i]] += ms;
+            acc[c->stage_of_event[i / 2]] += ms;
         }
         c->stats.trace_ms = acc[kStageTrace];
         c->stats.shade_ms = acc[kStageShade];
+        c->stats.init_ms = acc[kStageInit];
     }
     return LT_OK;
+}
+
+static lt_status run_wave(lt_ctx *c, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, bool stage_timing) {
+    return run_loop(
+        c, w, a, stage_timing, [&]() { return launch_wave_init(c->dev, w, a, f, c->shape, c->stream); },
+        [&](int stage, int cur) { return launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream); });
 }
 
 extern "C" {
@@ -869,6 +891,10 @@ lt_status lt_render_stats_get(lt_ctx *c, lt_render_stats *out) try {
     float ms = 0.0f;
     if (cudaEventSynchronize(c->ev1) == cudaSuccess && cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess)
         out->gpu_ms = ms;
+    if (out->trace_ms + out->shade_ms + out->init_ms > 0.0f) {
+        const float busy = out->trace_ms + out->shade_ms + out->init_ms;
+        out->idle_ms = out->gpu_ms > busy ? out->gpu_ms - busy : 0.0f;
+    }
     return LT_OK;
 } LT_CATCH(c)
 
@@ -938,6 +964,58 @@ static lt_status diff_setup(lt_ctx *c, const lt_render_params *p, const lt_diff_
     return LT_OK;
 }
 
+// Lays the differentiable forward's path extras out from `base` for `cap`
+// paths (each array 256-byte aligned); returns the bytes used (base may be
+// nullptr to size).
+static size_t carve_dwave(char *base, uint32_t cap, DiffWave *d) {
+    const size_t P = cap;
+    size_t off = 0;
+    auto take = [&](size_t n) { char *p = base + off; off += (n + 255) & ~(size_t)255; return p; };
+    for (int k = 0; k < 2; ++k) {
+        d->C[k] = (float *)take(12 * P);
+        d->Ts[k] = (float *)take(12 * P);
+        d->rec[k] = (uint2 *)take(8 * P);
+        d->fin_id[k] = (uint2 *)take(8 * P);
+        d->fin_C[k] = (float4 *)take(16 * P);
+        d->fin_rec[k] = (uint2 *)take(8 * P);
+    }
+    d->res = (float4 *)take(32 * P);  // two connection records per path
+    d->sample_I = nullptr;
+    d->bytes = off;
+    return off;
+}
+
+static lt_status ensure_dwave(lt_ctx *c, uint32_t cap, DiffWave *d) {
+    if (c->diff_capacity < cap || !c->diff_arena) {
+        if (c->diff_arena) {
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            cudaFree(c->diff_arena);
+        }
+        c->diff_arena = nullptr;
+        c->diff_capacity = 0;
+        DiffWave sizing;
+        const size_t bytes = carve_dwave(nullptr, cap, &sizing);
+        CUDA_TRY(c, dev_malloc(&c->diff_arena, bytes));
+        c->diff_arena_bytes = bytes;
+        c->diff_capacity = cap;
+    }
+    carve_dwave((char *)c->diff_arena, cap, d);
+    return LT_OK;
+}
+
+static lt_status ensure_diff_samples(lt_ctx *c, size_t bytes) {
+    if (c->diff_samples_bytes >= bytes && c->diff_samples) return LT_OK;
+    if (c->diff_samples) {
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        cudaFree(c->diff_samples);
+    }
+    c->diff_samples = nullptr;
+    c->diff_samples_bytes = 0;
+    CUDA_TRY(c, dev_malloc((void **)&c->diff_samples, bytes));
+    c->diff_samples_bytes = bytes;
+    return LT_OK;
+}
+
 lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, lt_film *film,
                          float *sample_radiance) try {
     NvtxRange nvtx_("lt_render_diff");
@@ -948,13 +1026,38 @@ lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_par
     if (st != LT_OK) return st;
     if (!film->on_device || film->width != a.width || film->height != a.height)
         return fail(c, LT_ERR_INVALID, "lt_render_diff needs a device film of the camera's size");
+    if (!film->rgb || !film->bounces || !film->counts) return fail(c, LT_ERR_INVALID, "film buffers missing");
     FilmPtrs f{film->rgb, film->bounces, film->counts};
+    const uint32_t npix = a.width * a.height;
     c->stats = lt_render_stats{};
     CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-    CUDA_TRY(c, launch_diff_forward(c->dev, P, a, f, sample_radiance, c->shape, c->stream));
+    if (a.total > 0 && p->max_depth == 0) {  // the bounce loop never runs: every sample's radiance is 0
+        if (sample_radiance) CUDA_TRY(c, cudaMemsetAsync(sample_radiance, 0, a.total * 12, c->stream));
+        CUDA_TRY(c, launch_add_counts(f, npix, p->spp, c->stream));
+        c->stats.kernel_launches = 1;
+    } else if (a.total > 0) {
+        uint32_t cap = 0;
+        if ((st = prepare_wave(c, a.total, &cap)) != LT_OK) return st;
+        const Wavefront w = wave_view(c, cap);
+        DiffWave d;
+        if ((st = ensure_dwave(c, cap, &d)) != LT_OK) return st;
+        if (sample_radiance) {
+            d.sample_I = sample_radiance;
+        } else {
+            if ((st = ensure_diff_samples(c, a.total * 12)) != LT_OK) return st;
+            d.sample_I = c->diff_samples;
+        }
+        st = run_loop(
+            c, w, a, true, [&]() { return launch_dwave_init(c->dev, P, d, w, a, f, c->shape, c->stream); },
+            [&](int stage, int cur) {
+                return launch_dwave_stage(stage, c->dev, P, d, w, a, f, cur, c->shape, c->stream);
+            });
+        if (st != LT_OK) return st;
+        CUDA_TRY(c, launch_diff_film(d.sample_I, a, f, c->stream));
+        c->stats.kernel_launches += 1;
+    }
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     c->stats.samples = a.total;
-    c->stats.kernel_launches = 1;
     return LT_OK;
 } LT_CATCH(c)
 
@@ -979,7 +1082,9 @@ lt_status lt_render_adjoint(lt_ctx *c, const lt_render_params *p, const lt_diff_
     }
     c->stats = lt_render_stats{};
     CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-    CUDA_TRY(c, launch_diff_adjoint(c->dev, P, a, G, (uint32_t)c->host.media.size(), c->shape, c->stream));
+    // the adjoint's work counter: 8 bytes of the context's counter block, after lt_intersect's
+    CUDA_TRY(c, launch_diff_adjoint(c->dev, P, a, G, (uint32_t)c->host.media.size(),
+                                    (unsigned long long *)(c->isect_fetch + 16), c->shape, c->stream));
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     c->stats.samples = a.total;
     c->stats.kernel_launches = 1;

@@ -62,6 +62,7 @@ struct WaveCounters {
     unsigned long long light_traversals;  // connection rays that needed an occlusion query
     unsigned long long iterations;        // wavefront iterations of a captured loop
     unsigned long long nonfinite;         // film contributions with a NaN or infinite channel
+    uint32_t fcount[2];                   // differentiable forward: finishing entries by parity
 };
 
 struct Wavefront {
@@ -74,6 +75,23 @@ struct Wavefront {
     WaveCounters *counters = nullptr;
     void *arena = nullptr;
     size_t arena_bytes = 0;
+};
+
+// The differentiable forward on the wavefront (lt_render_diff): what a path
+// carries beyond PathState (ping-pong in queue order like it), the result of
+// every connection record, the paths that finished while their last records
+// were still to be traced, and the per-sample radiance.
+constexpr uint32_t kNoRecord = 0xFFFFFFFFu;
+struct DiffWave {
+    float *C[2];         // radiance gathered so far, 3 planes of capacity
+    float *Ts[2];        // throughput with the detached parameters (roulette), 3 planes
+    uint2 *rec[2];       // the path's light and BSDF records of the previous shade, or kNoRecord
+    float4 *res;         // per connection record: its contribution (rgb), w = 1 when it contributes
+    uint2 *fin_id[2];    // finishing paths (by parity): (pixel, frame)
+    float4 *fin_C[2];    //   radiance gathered before their last records
+    uint2 *fin_rec[2];   //   those records
+    float *sample_I;     // 3 floats per sample at ((frame - first_frame) * W * H + pixel)
+    size_t bytes = 0;
 };
 
 struct FilmPtrs {
@@ -98,6 +116,7 @@ struct LaunchShape {
     int trace_threads = 128, shade_threads = 128;
     int trace_blocks = 0, shade_blocks = 0, isect_blocks = 0;
     int diff_blocks = 0;
+    int dtrace_blocks = 0, dshade_blocks = 0;  // differentiable forward on the wavefront
     int diff_fwd_batch_blocks = 0, diff_adj_batch_blocks = 0;
 };
 
@@ -176,10 +195,19 @@ void query_launch_shape(int device, bool batch, LaunchShape *out);
 cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits, unsigned long long n,
                              uint32_t *fetch, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st);
-cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
-                                float *sample_I, const LaunchShape &ls, cudaStream_t st);
+// differentiable forward on the wavefront: camera rays (with the path extras
+// of d), then per iteration k_trace (connection records resolved into d.res)
+// and k_dshade; last, the film from the per-sample radiance (sample order, as
+// the one-thread-per-pixel form sums it)
+cudaError_t launch_dwave_init(const DevScene &s, const DiffParams &p, const DiffWave &d, const Wavefront &w,
+                              const RenderArgs &a, const FilmPtrs &f, const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_dwave_stage(int stage, const DevScene &s, const DiffParams &p, const DiffWave &d,
+                               const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, int cur,
+                               const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_diff_film(const float *sample_I, const RenderArgs &a, const FilmPtrs &f, cudaStream_t st);
 cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const RenderArgs &a, const DiffGrads &g,
-                                uint32_t num_media, const LaunchShape &ls, cudaStream_t st);
+                                uint32_t num_media, unsigned long long *fetch, const LaunchShape &ls,
+                                cudaStream_t st);
 cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
                              const LaunchShape &ls, cudaStream_t st);
 // Per wavefront iteration: k_trace (path rays of this iteration + connection

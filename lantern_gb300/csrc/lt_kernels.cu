@@ -742,7 +742,7 @@ __device__ __forceinline__ void film_contribute(WaveCounters *counters, const Fi
 // one sequence, slot i owning [begin[i], begin[i] + slots[i].a.total), and every
 // path carries its slot in its flags and connection records.
 struct OneScene {
-    static constexpr bool kMany = false;
+    static constexpr bool kMany = false, kDiff = false;
     DevScene s;
     RenderArgs a;
     FilmPtrs f;
@@ -757,7 +757,7 @@ struct OneScene {
 };
 
 struct ManyScenes {
-    static constexpr bool kMany = true;
+    static constexpr bool kMany = true, kDiff = false;
     const SceneTable *t;
     __device__ __forceinline__ const DevScene &scene(uint32_t i) const { return t->slots[i].s; }
     __device__ __forceinline__ const RenderArgs &args(uint32_t i) const { return t->slots[i].a; }
@@ -775,6 +775,36 @@ struct ManyScenes {
         return lo;
     }
 };
+
+// The differentiable forward (lt_render_diff) as a third source: one scene,
+// plus the estimator's parameters and the path extras of DiffWave. Its trace
+// stage writes each connection record's contribution into d.res instead of
+// the film.
+struct DiffOne {
+    static constexpr bool kMany = false, kDiff = true;
+    DevScene s;
+    RenderArgs a;
+    FilmPtrs f;
+    DiffParams p;
+    DiffWave d;
+    __device__ __forceinline__ const DevScene &scene(uint32_t) const { return s; }
+    __device__ __forceinline__ const RenderArgs &args(uint32_t) const { return a; }
+    __device__ __forceinline__ const FilmPtrs &film(uint32_t) const { return f; }
+    __device__ __forceinline__ unsigned long long total() const { return a.total; }
+    __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
+        local = item;
+        return 0;
+    }
+};
+
+__device__ __forceinline__ v3 ld3_planes(const float *p, uint32_t cap, uint32_t slot) {
+    return mk(ld_s(p + slot), ld_s(p + cap + slot), ld_s(p + 2 * cap + slot));
+}
+__device__ __forceinline__ void st3_planes(float *p, uint32_t cap, uint32_t slot, v3 v) {
+    st_s(p + slot, v.x);
+    st_s(p + cap + slot, v.y);
+    st_s(p + 2 * cap + slot, v.z);
+}
 
 // ------------------------------------------------------------------ kernels
 // Closest hits of n rays (lt_intersect). Persistent: rays are fetched from *fetch.
@@ -813,6 +843,11 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
         p.scene = sid;
         store_path(W.p[0], W.capacity, i, p);
         write_ray(W.ray[0], i, o, tn, d);
+        if constexpr (Src::kDiff) {
+            st3_planes(src.d.C[0], W.capacity, i, mk(0.0f, 0.0f, 0.0f));
+            st3_planes(src.d.Ts[0], W.capacity, i, p.T);
+            st_s(src.d.rec[0] + i, make_uint2(kNoRecord, kNoRecord));
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters->count[0] = (uint32_t)first;
@@ -820,6 +855,7 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
         W.counters->rcount[0] = W.counters->rcount[1] = 0;
         W.counters->ccount[0] = W.counters->ccount[1] = 0;
         W.counters->work_next = first;
+        W.counters->fcount[0] = W.counters->fcount[1] = 0;
         W.counters->trace_fetch = 0;
     }
 }
@@ -1001,33 +1037,57 @@ __global__ void __launch_bounds__(256, Src::kMany ? 3 : 4) k_shade(Src src, Wave
                 else push = true;
             }
         }
-        // Slots of this warp, reserved by one lane: the connection records, the
-        // continuing paths' queue entries and the finished paths' next work items
-        // together, then the camera-ray entries (their number depends on how many
-        // work items were left), so a warp waits for two atomic round trips.
-        const uint32_t lane = threadIdx.x & 31u;
+        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
         const unsigned below = (1u << lane) - 1u;
         const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
         const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
-        uint32_t c_base = 0, q_base = 0, r_base = 0, n_regen = 0;
-        unsigned long long w_base = 0;
+        // The block's slots, reserved by one thread with one atomic per counter:
+        // each warp stages its counts in shared memory, thread 0 reserves the
+        // block's records, queue entries and work items and hands every warp its
+        // share (warps in order, lanes in order within a warp), then the
+        // camera-ray entries, whose number depends on how many work items were left.
+        __shared__ uint32_t s_cnt[3][8];
+        __shared__ uint32_t s_base[4][8];
+        __shared__ unsigned long long s_wbase[8];
         if (lane == 0) {
-            const uint32_t nc = __popc(m_l) + __popc(m_b);
-            if (nc) c_base = atomicAdd(&W.counters->ccount[cur], nc);
-            if (m_p) q_base = atomicAdd(&W.counters->count[nxt], (uint32_t)__popc(m_p));
-            if (m_d) {
-                w_base = atomicAdd(&W.counters->work_next, (unsigned long long)__popc(m_d));
-                const unsigned long long tot = src.total();
-                const unsigned long long left = w_base < tot ? tot - w_base : 0ull;
-                n_regen = left < (unsigned long long)__popc(m_d) ? (uint32_t)left : (uint32_t)__popc(m_d);
-                if (n_regen) r_base = atomicAdd(&W.counters->rcount[nxt], n_regen);
+            s_cnt[0][warp] = __popc(m_l) + __popc(m_b);
+            s_cnt[1][warp] = __popc(m_p);
+            s_cnt[2][warp] = __popc(m_d);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t nw = blockDim.x >> 5;
+            uint32_t tc = 0, tp = 0, td = 0;
+            for (uint32_t w = 0; w < nw; ++w) {
+                tc += s_cnt[0][w];
+                tp += s_cnt[1][w];
+                td += s_cnt[2][w];
+            }
+            const uint32_t c0 = tc ? atomicAdd(&W.counters->ccount[cur], tc) : 0u;
+            const uint32_t q0 = tp ? atomicAdd(&W.counters->count[nxt], tp) : 0u;
+            const unsigned long long w0 = td ? atomicAdd(&W.counters->work_next, (unsigned long long)td) : 0ull;
+            const unsigned long long tot = src.total();
+            const unsigned long long left = w0 < tot ? tot - w0 : 0ull;
+            const uint32_t nreg = left < (unsigned long long)td ? (uint32_t)left : td;
+            const uint32_t r0 = nreg ? atomicAdd(&W.counters->rcount[nxt], nreg) : 0u;
+            uint32_t pc = 0, pp = 0, pd = 0;
+            for (uint32_t w = 0; w < nw; ++w) {
+                s_base[0][w] = c0 + pc;
+                s_base[1][w] = q0 + pp;
+                s_wbase[w] = w0 + pd;
+                const uint32_t before = pd < nreg ? pd : nreg;  // camera rays of the warps before
+                const uint32_t mine = nreg - before < s_cnt[2][w] ? nreg - before : s_cnt[2][w];
+                s_base[2][w] = r0 + before;
+                s_base[3][w] = mine;
+                pc += s_cnt[0][w];
+                pp += s_cnt[1][w];
+                pd += s_cnt[2][w];
             }
         }
-        c_base = __shfl_sync(0xFFFFFFFFu, c_base, 0);
-        q_base = __shfl_sync(0xFFFFFFFFu, q_base, 0);
-        r_base = __shfl_sync(0xFFFFFFFFu, r_base, 0);
-        w_base = __shfl_sync(0xFFFFFFFFu, w_base, 0);
-        n_regen = __shfl_sync(0xFFFFFFFFu, n_regen, 0);
+        __syncthreads();
+        const uint32_t c_base = s_base[0][warp], q_base = s_base[1][warp], r_base = s_base[2][warp];
+        const uint32_t n_regen = s_base[3][warp];
+        const unsigned long long w_base = s_wbase[warp];
         // connection records: the warp's light samples, then its BSDF samples
         {
             conn_light |= p.scene << kConnSceneShift;
@@ -1082,6 +1142,314 @@ __global__ void __launch_bounds__(256, Src::kMany ? 3 : 4) k_shade(Src src, Wave
     }
 }
 
+// One bounce of the differentiable estimator (diff_path below, one bounce of
+// its loop) for every queued path, on the wavefront. It is k_shade with the
+// estimator's arithmetic: per-triangle albedo and emission, the RGB medium form
+// with the detached sigma_s for distances, roulette from the detached
+// throughput Ts, and a path radiance C carried in the path state so that every
+// sample's radiance is summed in the estimator's order. A surface bounce
+// emits the same connection records as k_shade; k_trace writes their
+// contributions into d.res, and the path's next shade adds them to C (light
+// sample, then BSDF sample) before anything of its next bounce. A path that
+// ends with records still to be traced becomes a finishing entry, completed by
+// the next shade. Finished samples write their radiance to d.sample_I; film
+// counts and path lengths are added here, the colour sums later in sample
+// order (k_diff_film).
+__device__ __forceinline__ v3 add_record(const DiffWave &d, uint32_t rec, v3 C) {
+    if (rec == kNoRecord) return C;
+    const float4 v = ld_s(d.res + rec);
+    return v.w != 0.0f ? C + mk(v.x, v.y, v.z) : C;
+}
+
+__device__ __forceinline__ void write_sample(const DiffWave &d, const RenderArgs &A, uint32_t pixel, uint32_t frame,
+                                             v3 C) {
+    const unsigned long long item =
+        (unsigned long long)(frame - A.first_frame) * ((unsigned long long)A.width * A.height) + pixel;
+    st_s(d.sample_I + 3 * item, C.x);
+    st_s(d.sample_I + 3 * item + 1, C.y);
+    st_s(d.sample_I + 3 * item + 2, C.z);
+}
+
+__global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int cur) {
+    const DevScene &S = src.s;
+    const RenderArgs &A = src.a;
+    const DiffParams &P = src.p;
+    const DiffWave &D = src.d;
+    const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
+    const uint32_t n = n_push + n_cam, nf = W.counters->fcount[cur];
+    const uint32_t cap = W.capacity;
+    const int nxt = cur ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
+    uint32_t n_ref_rays = 0, n_ref_rays_b = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n + nf; base += gridDim.x * blockDim.x) {
+        const uint32_t q = base + threadIdx.x;
+        const bool active = q < n;
+        const uint32_t slot = active ? queue_slot(q, n_push, n_cam, cap) : 0u;
+        if (q >= n && q < n + nf) {  // a finishing entry: its last records, then the sample is complete
+            const uint32_t e = q - n;
+            const uint2 id = ld_s(D.fin_id[cur] + e);
+            const float4 c4 = ld_s(D.fin_C[cur] + e);
+            const uint2 rc = ld_s(D.fin_rec[cur] + e);
+            write_sample(D, A, id.x, id.y, add_record(D, rc.y, add_record(D, rc.x, mk(c4.x, c4.y, c4.z))));
+        }
+        Path p;
+        v3 C = mk(0, 0, 0), Ts = mk(0, 0, 0);
+        bool done = false, push = false;
+        v3 norg = mk(0, 0, 0), ndir = mk(0, 0, 0);
+        float ntnear = 0.0f;
+        bool emit_l = false, emit_b = false;
+        v3 l_dir = mk(0, 0, 0), b_dir = mk(0, 0, 0), l_f = mk(0, 0, 0), b_f = mk(0, 0, 0), conn_org = mk(0, 0, 0);
+        float l_pdf = 0.0f, b_pdf = 0.0f, l_tl = 0.0f, b_tl = 0.0f;
+        uint32_t conn_light = 0;
+        v3 conn_T = mk(0, 0, 0);
+        if (active) {
+            load_path(W.p[cur], cap, slot, p);
+            C = ld3_planes(D.C[cur], cap, slot);
+            Ts = ld3_planes(D.Ts[cur], cap, slot);
+            const uint2 rc = ld_s(D.rec[cur] + slot);
+            C = add_record(D, rc.y, add_record(D, rc.x, C));  // the previous bounce's light, then BSDF sample
+            const float4 hv = ld_s(W.hits + slot);
+            const float4 r0 = ld_s(W.ray[cur] + 2 * slot), r1 = ld_s(W.ray[cur] + 2 * slot + 1);
+            const uint32_t prim = __float_as_uint(hv.w);
+            const float t = hv.x;
+            if (prim == kMiss) {
+                C = C + p.T * S.background;
+                done = true;
+            } else {
+                const v3 origin = mk(r0.x, r0.y, r0.z);
+                const v3 direction = normalize(mk(r1.x, r1.y, r1.z));
+                bool hit_surface = true;
+                if (p.medium >= 0) {
+                    const int mi = p.medium;
+                    const MediumInfo M = S.meds[mi];
+                    const v3 sa = ld3(P.sigma_a + 3 * mi), ss = ld3(P.sigma_s + 3 * mi);
+                    const v3 sa_d = ld3(P.sigma_a_s + 3 * mi), ss_d = ld3(P.sigma_s_s + 3 * mi);
+                    float dist;
+                    bool scat = false;
+                    v3 w, ws;
+                    if (M.type == LT_MEDIUM_NON_SCATTERING) {
+                        dist = t;
+                        w = mk(expf(-sa.x * dist), expf(-sa.y * dist), expf(-sa.z * dist));
+                        ws = mk(expf(-sa_d.x * dist), expf(-sa_d.y * dist), expf(-sa_d.z * dist));
+                    } else {
+                        const float sbar = M.type == LT_MEDIUM_ISOTROPIC ? ss_d.x : (ss_d.x + ss_d.y + ss_d.z) / 3.0f;
+                        dist = -logf(p.rng.next_float()) / sbar;
+                        scat = dist < t;
+                        if (!scat) dist = t;
+                        w = mk(expf(-(sa.x + ss.x - sbar) * dist), expf(-(sa.y + ss.y - sbar) * dist),
+                               expf(-(sa.z + ss.z - sbar) * dist));
+                        ws = mk(expf(-(sa_d.x + ss_d.x - sbar) * dist), expf(-(sa_d.y + ss_d.y - sbar) * dist),
+                                expf(-(sa_d.z + ss_d.z - sbar) * dist));
+                        if (scat) {
+                            w = w * (ss / sbar);
+                            ws = ws * (ss_d / sbar);
+                        }
+                    }
+                    p.T = p.T * w;
+                    Ts = Ts * ws;
+                    if (scat) {
+                        hit_surface = false;
+                        norg = origin + direction * dist;
+                        ndir = M.type == LT_MEDIUM_HG ? hg_sample(p.rng, direction, M.g) : uniform_sphere(p.rng);
+                        ntnear = 0.001f;
+                    }
+                }
+                if (hit_surface) {
+                    const GeomInfo G = S.geoms[__ldg(S.tri_geom + prim)];
+                    const MaterialInfo m = S.mats[G.material];
+                    const v3 alb = ld3(P.albedo + 3 * prim), alb_d = ld3(P.albedo_s + 3 * prim);
+                    if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0)
+                        C = C + p.T * ld3(P.emission + 3 * prim);
+                    Inter it;
+                    it.P = origin + direction * t;
+                    it.N = G.has_normals ? normalize(interp_normal(S, prim, hv.y, hv.z)) : normalize(mk(0, 0, 0));
+                    it.wo = -direction;
+                    it.ioro = 0.0f;
+                    it.iori = p.iori;
+                    it.lobe = p.lobe;
+                    it.wi = mk(0, 0, 0);
+                    const uint32_t nl = S.num_lights;
+                    if (!(nl == 0 || (nl == 1 && G.light >= 0))) {
+                        int li;
+                        int guard = 0;
+                        do {
+                            li = (int)p.rng.next_discrete(nl);
+                        } while (li == G.light && ++guard < 1 << 20);
+                        const LightInfo &L = S.lights[li];
+                        Inter c = it;
+                        conn_org = it.P;
+                        conn_light = (uint32_t)li;
+                        conn_T = p.T;
+                        if (m.bsdf == LT_BSDF_LAMBERT) {
+                            float x, y;
+                            sample_disc(p.rng, L.sphere[3], x, y);
+                            const v3 cdir = mk(L.sphere[0], L.sphere[1], L.sphere[2]) - c.P;
+                            const float dl = length(cdir);
+                            const v3 point = rotate_to_world(x, y, dl - L.sphere[3], normalize(cdir));
+                            const v3 ldir = normalize(point);
+                            c.wi = ldir;
+                            const float cosl = dot(ldir, c.N);
+                            if (cosl > 0.0f) {
+                                n_ref_rays++;
+                                const float tl = light_distance(S, L, c.P, ldir, nullptr);
+                                if (tl != 0.0f) {
+                                    emit_l = true;
+                                    l_dir = ldir;
+                                    l_f = (alb * kInvPi) * cosl;
+                                    l_pdf = cosl * kInvPi;
+                                    l_tl = tl;
+                                }
+                            }
+                        }
+                        bsdf_sample(m, c, p.rng);
+                        const float spdf = bsdf_pdf(m, c);
+                        const float cosb = dot(c.wi, c.N);
+                        if (spdf != 0.0f && cosb > 0.0f) {
+                            n_ref_rays_b++;
+                            const float tl = light_distance(S, L, c.P, c.wi, nullptr);
+                            if (tl != 0.0f) {
+                                emit_b = true;
+                                b_dir = c.wi;
+                                b_f = m.bsdf == LT_BSDF_LAMBERT ? (alb * kInvPi) * cosb : alb;
+                                b_pdf = spdf;
+                                b_tl = tl;
+                            }
+                        }
+                    }
+                    bsdf_sample(m, it, p.rng);
+                    const float pdf = bsdf_pdf(m, it);
+                    const v3 f = m.bsdf == LT_BSDF_LAMBERT ? (alb * kInvPi) * dot(it.wi, it.N) : alb;
+                    const v3 fs = m.bsdf == LT_BSDF_LAMBERT ? (alb_d * kInvPi) * dot(it.wi, it.N) : alb_d;
+                    p.T = (p.T * f) / pdf;
+                    Ts = (Ts * fs) / pdf;
+                    if (it.lobe == kLobeSTrans) {
+                        it.iori = it.ioro;
+                        p.medium = m.medium;
+                    }
+                    p.iori = it.iori;
+                    p.lobe = it.lobe;
+                    norg = it.P;
+                    ndir = it.wi;
+                    ntnear = 0.001f;
+                }
+                if (p.bounces > A.rr_depth) {  // roulette from the detached throughput
+                    const float pr = fmaxf(Ts.x, fmaxf(Ts.y, Ts.z));
+                    if (p.rng.next_float() > pr) {
+                        done = true;
+                    } else {
+                        p.T = p.T * (1 / pr);
+                        Ts = Ts * (1 / pr);
+                    }
+                }
+            }
+            if (!done) {
+                p.bounces++;
+                if (p.bounces >= A.max_depth) done = true;
+                else push = true;
+            }
+        }
+        // slots of this warp, reserved by one lane: records, queue entries,
+        // finishing entries, next work items; then the camera-ray entries
+        const uint32_t lane = threadIdx.x & 31u;
+        const unsigned below = (1u << lane) - 1u;
+        const bool fin = done && (emit_l || emit_b);
+        const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
+        const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
+        const unsigned m_f = __ballot_sync(0xFFFFFFFFu, fin);
+        uint32_t c_base = 0, q_base = 0, r_base = 0, f_base = 0, n_regen = 0;
+        unsigned long long w_base = 0;
+        if (lane == 0) {
+            const uint32_t nc = __popc(m_l) + __popc(m_b);
+            if (nc) c_base = atomicAdd(&W.counters->ccount[cur], nc);
+            if (m_p) q_base = atomicAdd(&W.counters->count[nxt], (uint32_t)__popc(m_p));
+            if (m_f) f_base = atomicAdd(&W.counters->fcount[nxt], (uint32_t)__popc(m_f));
+            if (m_d) {
+                w_base = atomicAdd(&W.counters->work_next, (unsigned long long)__popc(m_d));
+                const unsigned long long tot = A.total;
+                const unsigned long long left = w_base < tot ? tot - w_base : 0ull;
+                n_regen = left < (unsigned long long)__popc(m_d) ? (uint32_t)left : (uint32_t)__popc(m_d);
+                if (n_regen) r_base = atomicAdd(&W.counters->rcount[nxt], n_regen);
+            }
+        }
+        c_base = __shfl_sync(0xFFFFFFFFu, c_base, 0);
+        q_base = __shfl_sync(0xFFFFFFFFu, q_base, 0);
+        f_base = __shfl_sync(0xFFFFFFFFu, f_base, 0);
+        r_base = __shfl_sync(0xFFFFFFFFu, r_base, 0);
+        w_base = __shfl_sync(0xFFFFFFFFu, w_base, 0);
+        n_regen = __shfl_sync(0xFFFFFFFFu, n_regen, 0);
+        const uint32_t rec_l = emit_l ? c_base + __popc(m_l & below) : kNoRecord;
+        const uint32_t rec_b = emit_b ? c_base + __popc(m_l) + __popc(m_b & below) : kNoRecord;
+        if (emit_l) {
+            st_s(W.cray + 2 * rec_l, make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light)));
+            st_s(W.cray + 2 * rec_l + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, l_tl));
+            st_s(W.crec + 2 * rec_l, make_float4(l_f.x, l_f.y, l_f.z, l_pdf));
+            st_s(W.crec + 2 * rec_l + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
+        }
+        if (emit_b) {
+            st_s(W.cray + 2 * rec_b,
+                 make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light | kConnectBsdf)));
+            st_s(W.cray + 2 * rec_b + 1, make_float4(b_dir.x, b_dir.y, b_dir.z, b_tl));
+            st_s(W.crec + 2 * rec_b, make_float4(b_f.x, b_f.y, b_f.z, b_pdf));
+            st_s(W.crec + 2 * rec_b + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
+        }
+        bool regen = false;
+        if (done) {
+            atomicAdd(src.f.bounces + p.pixel, p.bounces);
+            atomicAdd(src.f.counts + p.pixel, 1u);
+            if (fin) {
+                const uint32_t e = f_base + __popc(m_f & below);
+                st_s(D.fin_id[nxt] + e, make_uint2(p.pixel, p.frame));
+                st_s(D.fin_C[nxt] + e, make_float4(C.x, C.y, C.z, 0.0f));
+                st_s(D.fin_rec[nxt] + e, make_uint2(rec_l, rec_b));
+            } else {
+                write_sample(D, A, p.pixel, p.frame, C);
+            }
+        }
+        const uint32_t rank_d = __popc(m_d & below);
+        if (done && rank_d < n_regen) {
+            start_path(S, A, w_base + rank_d, p, norg, ndir, ntnear);
+            p.scene = 0;
+            C = mk(0, 0, 0);
+            Ts = p.T;
+            regen = true;
+        }
+        if (push || regen) {
+            const uint32_t qi = push ? q_base + __popc(m_p & below) : cap - 1u - (r_base + rank_d);
+            write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
+            store_path(W.p[nxt], cap, qi, p);
+            st3_planes(D.C[nxt], cap, qi, C);
+            st3_planes(D.Ts[nxt], cap, qi, Ts);
+            st_s(D.rec[nxt] + qi, push ? make_uint2(rec_l, rec_b) : make_uint2(kNoRecord, kNoRecord));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_ref_rays += __shfl_xor_sync(0xFFFFFFFFu, n_ref_rays, o);
+        n_ref_rays_b += __shfl_xor_sync(0xFFFFFFFFu, n_ref_rays_b, o);
+    }
+    if ((threadIdx.x & 31u) == 0 && (n_ref_rays | n_ref_rays_b)) {
+        atomicAdd(&W.counters->light_rays, (unsigned long long)n_ref_rays);
+        atomicAdd(&W.counters->bsdf_rays, (unsigned long long)n_ref_rays_b);
+    }
+}
+
+// Film colour sums of the differentiable forward from its per-sample radiance:
+// per pixel the samples in frame order, then one addition to the film, as the
+// one-thread-per-pixel form (diff_forward_pixel) sums them.
+__global__ void __launch_bounds__(256) k_diff_film(const float *__restrict__ sample_I, RenderArgs A, FilmPtrs F) {
+    const uint32_t npix = A.width * A.height;
+    const uint32_t spp = (uint32_t)(A.total / npix);
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
+        v3 sum = mk(0, 0, 0);
+        for (uint32_t s = 0; s < spp; ++s) {
+            const size_t item = (size_t)s * npix + pixel;
+            sum = sum + mk(ld_s(sample_I + 3 * item), ld_s(sample_I + 3 * item + 1), ld_s(sample_I + 3 * item + 2));
+        }
+        F.rgb[3 * (size_t)pixel] += sum.x;
+        F.rgb[3 * (size_t)pixel + 1] += sum.y;
+        F.rgb[3 * (size_t)pixel + 2] += sum.z;
+    }
+}
+
 // Connection rays and their MIS-weighted contributions (EstimateDirect,
 // integrator.cpp:281-312; SampleLi/PdfLi, area_light.cpp:58-67,100-109).
 //
@@ -1125,6 +1493,51 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     film_contribute(W.counters, F, pixel, T * (c * (float)S.num_lights));
 }
 
+// resolve_connection for the differentiable estimator (diff_path's light and
+// BSDF samples): the emission is the hit light triangle's parameter, and the
+// contribution T * ((f * Le * w) / pdf * numLights) goes to the record's result
+// slot (w = 1) for the path's next shade to add in order; a record that does
+// not contribute gets w = 0.
+template <class State>
+__device__ __forceinline__ void resolve_connection_diff(const DiffOne &src, const Wavefront &W, uint32_t idx,
+                                                        uint32_t kl, const State &r) {
+    const DevScene &S = src.s;
+    const bool is_bsdf = (kl & kConnectBsdf) != 0;
+    const LightInfo &L = S.lights[kl & kConnLightMask];
+    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    Hit h;
+    bool visible;
+    if (r.any) {
+        visible = r.h.prim == kMiss;
+        if (visible) light_distance(S, L, r.O, r.D, &h);  // the same light hit k_dshade found
+    } else {
+        visible = r.h.prim != kMiss && __ldg(S.tri_geom + r.h.prim) == (uint32_t)L.geom;
+        h = r.h;
+    }
+    if (visible) {
+        const v3 org = r.O, dir = r.D;
+        const v3 ip = org + normalize(dir) * h.t;
+        const v3 dd = ip - org;
+        const float d2 = dot(dd, dd);
+        const v3 nrm = normalize(interp_normal(S, h.prim, h.u, h.v));
+        const float cosl = is_bsdf ? dot(nrm, dir) : dot(nrm, -dir);
+        const float lpdf = d2 / (fabsf(cosl) * L.area);
+        const float4 r0 = ld_s(W.crec + 2 * idx), r1 = ld_s(W.crec + 2 * idx + 1);
+        const float spdf = r0.w;
+        if (lpdf != 0.0f && spdf != 0.0f) {
+            const v3 f = mk(r0.x, r0.y, r0.z);
+            const v3 Le = ld3(src.p.emission + 3 * h.prim);
+            const v3 T = mk(r1.x, r1.y, r1.z);
+            const float fn = (float)S.num_lights;
+            v3 c;
+            if (!is_bsdf) c = T * ((((f * Le) * power_heuristic(lpdf, spdf)) / lpdf) * fn);
+            else c = T * ((((f * Le) * power_heuristic(spdf, lpdf)) / spdf) * fn);
+            out = make_float4(c.x, c.y, c.z, 1.0f);
+        }
+    }
+    st_s(src.d.res + idx, out);
+}
+
 // Path rays of iteration `cur` (closest hit into W.hits) and, in the same
 // persistent launch, the connection records that the previous k_shade wrote
 // (parity cur ^ 1; occlusion query or closest hit, then resolve_connection).
@@ -1144,6 +1557,7 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
         W.counters->count[cur ^ 1] = 0;  // filled by the next k_shade
         W.counters->rcount[cur ^ 1] = 0;
         W.counters->ccount[cur] = 0;
+        W.counters->fcount[cur ^ 1] = 0;  // filled by the next differentiable shade
         W.counters->main_rays += n;
     }
     const float4 *rays = W.ray[cur];
@@ -1184,7 +1598,8 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
                      make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
-                resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
+                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r);
+                else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
             }
         }
     }
@@ -1523,17 +1938,34 @@ __device__ __forceinline__ void diff_adjoint_pixel(const DevScene &S, const Diff
     }
 }
 
-__global__ void __launch_bounds__(128) k_diff_forward(DevScene S, DiffParams P, RenderArgs A, FilmPtrs F,
-                                                     float *sample_I) {
-    AlbedoCache ca;
-    EmissionCache ce;
+// Next 32 work items for the calling warp (all lanes call it together).
+__device__ __forceinline__ unsigned long long fetch_chunk(unsigned long long *fetch);
+
+// Gradient terms of samples [s0, s1) of one pixel.
+__device__ __forceinline__ void diff_adjoint_samples(const DevScene &S, const DiffParams &P, const RenderArgs &A,
+                                                     const DiffGrads &G, uint32_t pixel, uint32_t s0, uint32_t s1,
+                                                     float *macc, AlbedoCache &ca, EmissionCache &ce) {
     const uint32_t npix = A.width * A.height;
-    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x)
-        diff_forward_pixel(S, P, A, F, sample_I, pixel, ca, ce);
+    const v3 delta = ld3(G.dI + 3 * (size_t)pixel);
+    if (is_black(delta)) return;
+    for (uint32_t s = s0; s < s1; ++s) {
+        const unsigned long long item = (unsigned long long)s * npix + pixel;
+        uint32_t b = 0;
+        const v3 I = G.sample_I ? ld3(G.sample_I + 3 * item)
+                                : diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
+        diff_path<true>(S, P, G, A, item, I, delta, macc, ca, ce, b);
+    }
 }
 
+// Samples per work item of the adjoint: a pixel's samples are split into
+// chunks of this many, taken from a shared counter 32 at a time per warp, so
+// that no thread is left with a whole pixel's worth of paths at the end; the
+// consecutive samples of a chunk keep hitting the same triangles, which the
+// per-thread gradient caches exploit.
+constexpr uint32_t kAdjointChunk = 8;
+
 __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, RenderArgs A, DiffGrads G,
-                                                     uint32_t num_media) {
+                                                     uint32_t num_media, unsigned long long *fetch) {
     float macc[6 * kMediaAcc];
     for (int k = 0; k < 6 * kMediaAcc; ++k) macc[k] = 0.0f;
     AlbedoCache ca;
@@ -1541,8 +1973,21 @@ __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, 
     ca.init();
     ce.init();
     const uint32_t npix = A.width * A.height;
-    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x)
-        diff_adjoint_pixel(S, P, A, G, pixel, macc, ca, ce);
+    const uint32_t spp = (uint32_t)(A.total / npix);
+    const uint32_t chunks = (spp + kAdjointChunk - 1) / kAdjointChunk;
+    const uint32_t cw = G.x1 - G.x0, ch = G.y1 - G.y0;
+    const unsigned long long items = (unsigned long long)cw * ch * chunks;
+    for (;;) {
+        const unsigned long long base = fetch_chunk(fetch);
+        if (base >= items) break;
+        const unsigned long long it = base + (threadIdx.x & 31u);
+        if (it < items) {
+            const uint32_t k = (uint32_t)(it / chunks), c = (uint32_t)(it - (unsigned long long)k * chunks);
+            const uint32_t pixel = (G.y0 + k / cw) * A.width + G.x0 + k % cw;
+            const uint32_t s0 = c * kAdjointChunk, s1 = s0 + kAdjointChunk < spp ? s0 + kAdjointChunk : spp;
+            diff_adjoint_samples(S, P, A, G, pixel, s0, s1, macc, ca, ce);
+        }
+    }
     ca.flush(G.albedo);
     ce.flush(G.emission);
     // medium gradients: warp sums, one atomic per warp and component
@@ -1678,6 +2123,8 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
                         : w4 ? blocks_for(k_intersect<Bvh4>, 128, sms, trav_smem<Bvh4>(128))
                              : blocks_for(k_intersect<Bvh2>, 128, sms, trav_smem<Bvh2>(128));
     out->diff_blocks = blocks_for(k_diff_adjoint, 128, sms);
+    out->dtrace_blocks = blocks_for(k_trace<DiffOne, Bvh2>, 256, sms, trav_smem<Bvh2>(256));
+    out->dshade_blocks = blocks_for(k_dshade, 256, sms);
     out->diff_fwd_batch_blocks = blocks_for(k_diff_forward_batch, 128, sms);
     out->diff_adj_batch_blocks = blocks_for(k_diff_adjoint_batch, 128, sms);
 }
@@ -1693,17 +2140,36 @@ cudaError_t preload_wave_kernels() {
     return e;
 }
 
-cudaError_t launch_diff_forward(const DevScene &s, const DiffParams &p, const RenderArgs &a, const FilmPtrs &f,
-                                float *sample_I, const LaunchShape &ls, cudaStream_t st) {
-    if (a.total == 0) return cudaSuccess;
-    k_diff_forward<<<ls.diff_blocks, 128, 0, st>>>(s, p, a, f, sample_I);
+cudaError_t launch_dwave_init(const DevScene &s, const DiffParams &p, const DiffWave &d, const Wavefront &w,
+                              const RenderArgs &a, const FilmPtrs &f, const LaunchShape &ls, cudaStream_t st) {
+    k_raygen<DiffOne><<<ls.dshade_blocks, 256, 0, st>>>(DiffOne{s, a, f, p, d}, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dwave_stage(int stage, const DevScene &s, const DiffParams &p, const DiffWave &d,
+                               const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, int cur,
+                               const LaunchShape &ls, cudaStream_t st) {
+    const DiffOne src{s, a, f, p, d};
+    if (stage == kStageTrace) k_trace<DiffOne, Bvh2><<<ls.dtrace_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
+    else k_dshade<<<ls.dshade_blocks, 256, 0, st>>>(src, w, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diff_film(const float *sample_I, const RenderArgs &a, const FilmPtrs &f, cudaStream_t st) {
+    const uint32_t npix = a.width * a.height;
+    if (npix == 0 || a.total == 0) return cudaSuccess;
+    const uint32_t blocks = (npix + 255) / 256 < 65535 ? (npix + 255) / 256 : 65535;
+    k_diff_film<<<blocks, 256, 0, st>>>(sample_I, a, f);
     return cudaGetLastError();
 }
 
 cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const RenderArgs &a, const DiffGrads &g,
-                                uint32_t num_media, const LaunchShape &ls, cudaStream_t st) {
+                                uint32_t num_media, unsigned long long *fetch, const LaunchShape &ls,
+                                cudaStream_t st) {
     if (a.total == 0) return cudaSuccess;
-    k_diff_adjoint<<<ls.diff_blocks, 128, 0, st>>>(s, p, a, g, num_media);
+    cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    k_diff_adjoint<<<ls.diff_blocks, 128, 0, st>>>(s, p, a, g, num_media, fetch);
     return cudaGetLastError();
 }
 

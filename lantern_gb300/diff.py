@@ -225,8 +225,8 @@ def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: 
     deterministic: one thread per pixel, samples summed in frame order).
     Parameters, drawn with `seed`: every sigma_a and sigma_s entry, up to 10
     emission entries whose adjoint gradient is nonzero, then albedo entries with
-    a nonzero gradient up to `count` in all. A parameter is compared when either gradient exceeds 1e-4 of the
-    largest gradient of its array. Returns {"parameters", "checked",
+    in all. A parameter is compared unless both gradients are below 1e-8 of
+    the largest gradient of its array (float noise). Returns {"parameters", "checked",
     "max_rel_err", "failures": [(array, index, adjoint, fd), ...]} with the
     comparisons whose relative difference exceeds rel_tol."""
     base = [t.detach().to(scene.device, torch.float32).contiguous() for t in theta]
@@ -254,16 +254,18 @@ def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: 
     cands = cands[:count]
     gmax = [float(np.abs(g).max()) if g.size else 0.0 for g in grads]
     names = ("albedo", "emission", "sigma_a", "sigma_s")
-    failures, worst, checked = [], 0.0, 0
+    failures, worst, checked, pairs = [], 0.0, 0, []
     for k, i in cands:
         fd = (loss_at(k, i, h) - loss_at(k, i, -h)) / (2 * h)
         ad = float(grads[k][i])
-        if max(abs(fd), abs(ad)) <= 1e-4 * gmax[k]:
+        pairs.append((names[k], i, ad, fd))
+        if max(abs(fd), abs(ad)) <= 1e-8 * gmax[k]:
             continue
         checked += 1
         rel = abs(ad - fd) / max(abs(fd), abs(ad))
         worst = max(worst, rel)
         if rel > rel_tol:
             failures.append((names[k], i, ad, fd))
-    return {"parameters": len(cands), "checked": checked, "max_rel_err": worst, "failures": failures}
+    return {"parameters": len(cands), "checked": checked, "max_rel_err": worst, "failures": failures,
+            "pairs": pairs}
 

@@ -101,7 +101,8 @@ class RenderStats(C.Structure):
     _fields_ = [("main_rays", C.c_uint64), ("light_rays", C.c_uint64), ("bsdf_rays", C.c_uint64),
                 ("samples", C.c_uint64), ("iterations", C.c_uint32), ("kernel_launches", C.c_uint32),
                 ("gpu_ms", C.c_float), ("trace_ms", C.c_float), ("shade_ms", C.c_float),
-                ("light_traversals", C.c_uint64), ("nonfinite_samples", C.c_uint64)]
+                ("light_traversals", C.c_uint64), ("nonfinite_samples", C.c_uint64),
+                ("init_ms", C.c_float), ("idle_ms", C.c_float)]
 
 
 class Tuning(C.Structure):

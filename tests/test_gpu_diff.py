@@ -65,13 +65,13 @@ def _fd_check(path, spp, depth, min_checked):
 
 
 def test_adjoint_matches_finite_differences(scene_dir):
-    _fd_check(_small(scene_dir), spp=8, depth=6, min_checked=32)
+    _fd_check(_small(scene_dir), spp=8, depth=6, min_checked=60)
 
 
 def test_adjoint_matches_finite_differences_on_the_differentiable_workload(scene_dir):
     """The acceptance check at the workload's own size: 512x512, 32 spp, depth 8."""
     path = S.ensure_written(S.differentiable_scene(name="diff_c3"), scene_dir)
-    _fd_check(path, spp=32, depth=8, min_checked=32)
+    _fd_check(path, spp=32, depth=8, min_checked=60)
 
 
 def _crop_check(path, spp, depth, crop):
