@@ -396,16 +396,19 @@ lt_status lt_render_adjoint(lt_ctx *ctx, const lt_render_params *params, const l
 
 /* Batched forms of lt_render_diff and lt_render_adjoint: each job names a
  * scene (a context holding one, on ctx's device), its render params and
- * differentiable parameters; all jobs' pixels run in one persistent launch on
- * ctx's stream (warps take 32 consecutive pixels at a time from a shared
- * counter, so scenes of any size and spp fill the GPU together). Per job the
- * results are those of the single-scene call over the whole film (no crop).
- * - lt_render_diff_batch: film (device, additive) and sample_radiance
- *   (optional, as lt_render_diff's) are outputs;
- * - lt_render_adjoint_batch: d_loss_d_film and sample_radiance (optional) are
- *   inputs, the four gradient arrays outputs (accumulated; sigma arrays may be
- *   NULL for scenes without media). Jobs must not share gradient arrays.
- * n <= LT_MAX_BATCH. The calls return once the work is queued. */
+ * differentiable parameters; all jobs run together on ctx's stream. Per job
+ * the results are those of the single-scene call over the whole film (no crop).
+ * - lt_render_diff_batch: the work items of all jobs share one wavefront owned
+ *   by ctx (as lt_render_batch's); film (device, additive) and sample_radiance
+ *   (optional, as lt_render_diff's) are outputs, the same bits as the
+ *   single-scene call gives. Returns when the batch has finished.
+ * - lt_render_adjoint_batch: one persistent launch over chunks of 8 samples
+ *   of all jobs' pixels (warps take 32 chunks at a time from a shared counter,
+ *   so scenes of any size and spp fill the GPU together); d_loss_d_film and
+ *   sample_radiance (optional) are inputs, the four gradient arrays outputs
+ *   (accumulated; sigma arrays may be NULL for scenes without media). Jobs must
+ *   not share gradient arrays. Returns once the work is queued.
+ * n <= LT_MAX_BATCH. */
 typedef struct lt_diff_job {
     lt_ctx *scene;
     lt_render_params params;

@@ -975,7 +975,7 @@ static size_t carve_dwave(char *base, uint32_t cap, DiffWave *d) {
         d->C[k] = (float *)take(12 * P);
         d->Ts[k] = (float *)take(12 * P);
         d->rec[k] = (uint2 *)take(8 * P);
-        d->fin_id[k] = (uint2 *)take(8 * P);
+        d->fin_id[k] = (uint4 *)take(16 * P);
         d->fin_C[k] = (float4 *)take(16 * P);
         d->fin_rec[k] = (uint2 *)take(8 * P);
     }
@@ -1491,6 +1491,11 @@ extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap,
 } LT_CATCH(c)
 
 // ------------------------------------------------------------------ batched differentiable rendering
+// Batched differentiable forward (adjoint false) or adjoint over one scene
+// table. The forward runs the differentiable wavefront over the work items of
+// all jobs (as lt_render_batch does for plain renders) and returns when it
+// has finished; the adjoint is one persistent launch over sample chunks of all
+// jobs' pixels and returns once queued.
 static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool adjoint) {
     NvtxRange nvtx_("diff_batch");
     if (!c || (n && !jobs)) return fail(c, LT_ERR_INVALID, "NULL argument");
@@ -1499,8 +1504,11 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
     lt_status st = ensure_table(c);
     if (st != LT_OK) return st;
     SceneTable &T = *c->table_host;
-    uint32_t count = 0;
-    unsigned long long pixels = 0, samples = 0;
+    uint32_t count = 0, max_depth = 0, launches = 0;
+    unsigned long long pixels = 0, samples = 0, items = 0, internal = 0;
+    c->stats = lt_render_stats{};
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    std::vector<size_t> internal_at;  // per slot: offset into the internal sample buffer, or SIZE_MAX
     for (uint32_t i = 0; i < n; ++i) {
         const lt_diff_job &j = jobs[i];
         const lt_ctx *s = j.scene;
@@ -1517,12 +1525,22 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         if (adjoint && (!j.d_loss_d_film || !j.grad_albedo || !j.grad_emission ||
                         (media && (!j.grad_sigma_a || !j.grad_sigma_s))))
             return fail(c, LT_ERR_INVALID, "job %u: adjoint inputs or gradient arrays missing", i);
-        if ((unsigned long long)W * H * j.params.spp == 0) continue;
+        const unsigned long long total = (unsigned long long)W * H * j.params.spp;
+        if (total == 0) continue;
+        samples += total;
+        if (j.params.max_depth == 0) {  // no bounce: every sample's radiance is 0, gradients are 0
+            if (!adjoint) {
+                if (j.sample_radiance) CUDA_TRY(c, cudaMemsetAsync(j.sample_radiance, 0, total * 12, c->stream));
+                CUDA_TRY(c, launch_add_counts(FilmPtrs{j.film.rgb, j.film.bounces, j.film.counts}, W * H,
+                                              j.params.spp, c->stream));
+                ++launches;
+            }
+            continue;
+        }
         SceneSlot &sl = T.slots[count];
         DiffSlot &d = T.diff[count];
         sl.s = s->dev;
-        sl.a = RenderArgs{W, H, j.params.first_frame, j.params.max_depth, j.params.rr_depth,
-                          (unsigned long long)W * H * j.params.spp};
+        sl.a = RenderArgs{W, H, j.params.first_frame, j.params.max_depth, j.params.rr_depth, total};
         sl.f = FilmPtrs{j.film.rgb, j.film.bounces, j.film.counts};
         d.p.albedo = j.dp.albedo;
         d.p.emission = j.dp.emission;
@@ -1535,31 +1553,71 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
                         0, 0, W, H, adjoint ? j.sample_radiance : nullptr};
         d.sample_I = adjoint ? nullptr : j.sample_radiance;
         d.num_media = (uint32_t)h.media.size();
+        internal_at.push_back(SIZE_MAX);
+        if (!adjoint && !j.sample_radiance) {  // the forward needs every sample's radiance
+            internal_at.back() = (size_t)internal;
+            internal += (total * 12 + 255) & ~255ull;
+        }
+        T.begin[count] = items;
         T.pbegin[count] = pixels;
+        T.ibegin[count] = items;
         pixels += (unsigned long long)W * H;
-        samples += sl.a.total;
+        // work items: the forward's samples; the adjoint's chunks of kAdjointChunkSamples samples
+        const unsigned long long chunks = (j.params.spp + kAdjointChunkSamples - 1) / kAdjointChunkSamples;
+        items += adjoint ? (unsigned long long)W * H * chunks : total;
+        if (j.params.max_depth > max_depth) max_depth = j.params.max_depth;
         ++count;
     }
-    c->stats = lt_render_stats{};
     c->stats.samples = samples;
-    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
     if (count) {
+        if (internal) {
+            if ((st = ensure_diff_samples(c, (size_t)internal)) != LT_OK) return st;
+            for (uint32_t k = 0; k < count; ++k)
+                if (internal_at[k] != SIZE_MAX) T.diff[k].sample_I = (float *)((char *)c->diff_samples + internal_at[k]);
+        }
         T.count = count;
         T.pad = 0;
-        T.total = 0;
-        T.iteration_limit = 0;
+        T.total = adjoint ? 0 : items;
+        T.total_items = items;
         T.total_pixels = pixels;
         T.fetch = 0;
+        uint32_t cap = 0;
+        Wavefront w;
+        DiffWave dw;
+        if (!adjoint) {
+            if ((st = prepare_wave(c, items, &cap)) != LT_OK) return st;
+            w = wave_view(c, cap);
+            if ((st = ensure_dwave(c, cap, &dw)) != LT_OK) return st;
+        }
+        T.iteration_limit = adjoint ? 0 : drain_limit(items, cap, max_depth);
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev, c->table_host, offsetof(SceneTable, slots),
                                     cudaMemcpyHostToDevice, c->stream));
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->slots, T.slots, count * sizeof(SceneSlot), cudaMemcpyHostToDevice,
                                     c->stream));
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->diff, T.diff, count * sizeof(DiffSlot), cudaMemcpyHostToDevice,
                                     c->stream));
-        CUDA_TRY(c, launch_diff_batch(adjoint, c->table_dev, c->shape, c->stream));
+        if (adjoint) {
+            CUDA_TRY(c, launch_diff_adjoint_batch(c->table_dev, c->shape, c->stream));
+            ++launches;
+        } else {
+            RenderArgs all{};
+            all.max_depth = max_depth;
+            all.total = items;
+            const SceneTable *t = c->table_dev;
+            st = run_loop(
+                c, w, all, false, [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
+                [&](int stage, int cur) {
+                    return launch_dwave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
+                });
+            if (st != LT_OK) return st;
+            launches += c->stats.kernel_launches;
+            CUDA_TRY(c, launch_diff_film_batch(t, pixels, c->shape.sms, c->stream));
+            ++launches;
+        }
         CUDA_TRY(c, (cudaError_t)c->order.table_read_queued(c->rt, c->stream));
-        c->stats.kernel_launches = 1;
     }
+    c->stats.kernel_launches = launches;
+    c->stats.samples = samples;
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     return LT_OK;
 }

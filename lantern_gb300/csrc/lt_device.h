@@ -87,7 +87,7 @@ struct DiffWave {
     float *Ts[2];        // throughput with the detached parameters (roulette), 3 planes
     uint2 *rec[2];       // the path's light and BSDF records of the previous shade, or kNoRecord
     float4 *res;         // per connection record: its contribution (rgb), w = 1 when it contributes
-    uint2 *fin_id[2];    // finishing paths (by parity): (pixel, frame)
+    uint4 *fin_id[2];    // finishing paths (by parity): (pixel, frame, scene slot, 0)
     float4 *fin_C[2];    //   radiance gathered before their last records
     uint2 *fin_rec[2];   //   those records
     float *sample_I;     // 3 floats per sample at ((frame - first_frame) * W * H + pixel)
@@ -117,7 +117,8 @@ struct LaunchShape {
     int trace_blocks = 0, shade_blocks = 0, isect_blocks = 0;
     int diff_blocks = 0;
     int dtrace_blocks = 0, dshade_blocks = 0;  // differentiable forward on the wavefront
-    int diff_fwd_batch_blocks = 0, diff_adj_batch_blocks = 0;
+    int dtrace_batch_blocks = 0, dshade_batch_blocks = 0;
+    int diff_adj_batch_blocks = 0;
 };
 
 // Parameters of the differentiable render (device arrays): per-triangle RGB
@@ -136,6 +137,9 @@ struct DiffGrads {
     uint32_t x0, y0, x1, y1;
     const float *sample_I;  // per-sample radiance from the forward pass, or null (replay twice)
 };
+
+// Samples per work item of the adjoint (a pixel's samples in chunks).
+constexpr uint32_t kAdjointChunkSamples = 8;
 
 // Limits of the bit fields that carry a scene slot, a light and a medium index
 // in the path flags and connection records.
@@ -169,8 +173,10 @@ struct SceneTable {
     unsigned long long iteration_limit;  // a captured loop stops here (counters->error = 2)
     unsigned long long total_pixels;     // pixels of all slots (differentiable kernels)
     unsigned long long fetch;            // pixel counter of the differentiable kernels, 0 on upload
+    unsigned long long total_items;      // batched adjoint: sample chunks of all slots
     unsigned long long begin[kMaxBatchScenes];
     unsigned long long pbegin[kMaxBatchScenes];
+    unsigned long long ibegin[kMaxBatchScenes];  // batched adjoint: first sample chunk of each slot
     SceneSlot slots[kMaxBatchScenes];
     DiffSlot diff[kMaxBatchScenes];
 };
@@ -205,6 +211,13 @@ cudaError_t launch_dwave_stage(int stage, const DevScene &s, const DiffParams &p
                                const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, int cur,
                                const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_diff_film(const float *sample_I, const RenderArgs &a, const FilmPtrs &f, cudaStream_t st);
+// the same for the scenes of a batch's table (lt_render_diff_batch): work items
+// begin[], per-slot sample radiance and films in t->diff / t->slots
+cudaError_t launch_dwave_batch_init(const SceneTable *t, const DiffWave &d, const Wavefront &w, const LaunchShape &ls,
+                                    cudaStream_t st);
+cudaError_t launch_dwave_batch_stage(int stage, const SceneTable *t, const DiffWave &d, const Wavefront &w, int cur,
+                                     const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_diff_film_batch(const SceneTable *t, unsigned long long total_pixels, int sms, cudaStream_t st);
 cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const RenderArgs &a, const DiffGrads &g,
                                 uint32_t num_media, unsigned long long *fetch, const LaunchShape &ls,
                                 cudaStream_t st);
@@ -223,8 +236,8 @@ cudaError_t launch_batch_stage(int stage, const SceneTable *t, const Wavefront &
 // Condition kernel of a captured loop: counters->iterations += iters; the
 // while node `h` continues while path queue `cur` or the connection records
 // of parity cur ^ 1 are not empty and the iteration limit of `t` is not reached.
-// batched differentiable forward (adjoint false) or adjoint over t's slots and diff entries
-cudaError_t launch_diff_batch(bool adjoint, SceneTable *t, const LaunchShape &ls, cudaStream_t st);
+// batched adjoint over the sample chunks of t's slots (ibegin, total_items) and their diff entries
+cudaError_t launch_diff_adjoint_batch(SceneTable *t, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_loop_condition(const Wavefront &w, const SceneTable *t, cudaGraphConditionalHandle h, int cur,
                                   uint32_t iters, cudaStream_t st);
 

@@ -790,10 +790,37 @@ struct DiffOne {
     __device__ __forceinline__ const DevScene &scene(uint32_t) const { return s; }
     __device__ __forceinline__ const RenderArgs &args(uint32_t) const { return a; }
     __device__ __forceinline__ const FilmPtrs &film(uint32_t) const { return f; }
+    __device__ __forceinline__ const DiffParams &params(uint32_t) const { return p; }
+    __device__ __forceinline__ float *samples(uint32_t) const { return d.sample_I; }
     __device__ __forceinline__ unsigned long long total() const { return a.total; }
     __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
         local = item;
         return 0;
+    }
+};
+
+// The batched differentiable forward (lt_render_diff_batch): the scenes of a
+// batch's table, each with its parameters and per-sample radiance
+// (SceneTable::diff), on one wavefront whose path extras are `d`.
+struct DiffMany {
+    static constexpr bool kMany = true, kDiff = true;
+    const SceneTable *t;
+    DiffWave d;
+    __device__ __forceinline__ const DevScene &scene(uint32_t i) const { return t->slots[i].s; }
+    __device__ __forceinline__ const RenderArgs &args(uint32_t i) const { return t->slots[i].a; }
+    __device__ __forceinline__ const FilmPtrs &film(uint32_t i) const { return t->slots[i].f; }
+    __device__ __forceinline__ const DiffParams &params(uint32_t i) const { return t->diff[i].p; }
+    __device__ __forceinline__ float *samples(uint32_t i) const { return t->diff[i].sample_I; }
+    __device__ __forceinline__ unsigned long long total() const { return t->total; }
+    __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
+        uint32_t lo = 0, hi = t->count;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (t->begin[mid] <= item) lo = mid;
+            else hi = mid;
+        }
+        local = item - t->begin[lo];
+        return lo;
     }
 };
 
@@ -1161,19 +1188,17 @@ __device__ __forceinline__ v3 add_record(const DiffWave &d, uint32_t rec, v3 C) 
     return v.w != 0.0f ? C + mk(v.x, v.y, v.z) : C;
 }
 
-__device__ __forceinline__ void write_sample(const DiffWave &d, const RenderArgs &A, uint32_t pixel, uint32_t frame,
+__device__ __forceinline__ void write_sample(float *sample_I, const RenderArgs &A, uint32_t pixel, uint32_t frame,
                                              v3 C) {
     const unsigned long long item =
         (unsigned long long)(frame - A.first_frame) * ((unsigned long long)A.width * A.height) + pixel;
-    st_s(d.sample_I + 3 * item, C.x);
-    st_s(d.sample_I + 3 * item + 1, C.y);
-    st_s(d.sample_I + 3 * item + 2, C.z);
+    st_s(sample_I + 3 * item, C.x);
+    st_s(sample_I + 3 * item + 1, C.y);
+    st_s(sample_I + 3 * item + 2, C.z);
 }
 
-__global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int cur) {
-    const DevScene &S = src.s;
-    const RenderArgs &A = src.a;
-    const DiffParams &P = src.p;
+template <class Src>
+__global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur) {
     const DiffWave &D = src.d;
     const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
     const uint32_t n = n_push + n_cam, nf = W.counters->fcount[cur];
@@ -1187,10 +1212,11 @@ __global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int
         const uint32_t slot = active ? queue_slot(q, n_push, n_cam, cap) : 0u;
         if (q >= n && q < n + nf) {  // a finishing entry: its last records, then the sample is complete
             const uint32_t e = q - n;
-            const uint2 id = ld_s(D.fin_id[cur] + e);
+            const uint4 id = ld_s(D.fin_id[cur] + e);  // pixel, frame, scene slot
             const float4 c4 = ld_s(D.fin_C[cur] + e);
             const uint2 rc = ld_s(D.fin_rec[cur] + e);
-            write_sample(D, A, id.x, id.y, add_record(D, rc.y, add_record(D, rc.x, mk(c4.x, c4.y, c4.z))));
+            write_sample(src.samples(id.z), src.args(id.z), id.x, id.y,
+                         add_record(D, rc.y, add_record(D, rc.x, mk(c4.x, c4.y, c4.z))));
         }
         Path p;
         v3 C = mk(0, 0, 0), Ts = mk(0, 0, 0);
@@ -1204,6 +1230,9 @@ __global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int
         v3 conn_T = mk(0, 0, 0);
         if (active) {
             load_path(W.p[cur], cap, slot, p);
+            const DevScene &S = src.scene(p.scene);
+            const RenderArgs &A = src.args(p.scene);
+            const DiffParams &P = src.params(p.scene);
             C = ld3_planes(D.C[cur], cap, slot);
             Ts = ld3_planes(D.Ts[cur], cap, slot);
             const uint2 rc = ld_s(D.rec[cur] + slot);
@@ -1365,7 +1394,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int
             if (m_f) f_base = atomicAdd(&W.counters->fcount[nxt], (uint32_t)__popc(m_f));
             if (m_d) {
                 w_base = atomicAdd(&W.counters->work_next, (unsigned long long)__popc(m_d));
-                const unsigned long long tot = A.total;
+                const unsigned long long tot = src.total();
                 const unsigned long long left = w_base < tot ? tot - w_base : 0ull;
                 n_regen = left < (unsigned long long)__popc(m_d) ? (uint32_t)left : (uint32_t)__popc(m_d);
                 if (n_regen) r_base = atomicAdd(&W.counters->rcount[nxt], n_regen);
@@ -1379,6 +1408,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int
         n_regen = __shfl_sync(0xFFFFFFFFu, n_regen, 0);
         const uint32_t rec_l = emit_l ? c_base + __popc(m_l & below) : kNoRecord;
         const uint32_t rec_b = emit_b ? c_base + __popc(m_l) + __popc(m_b & below) : kNoRecord;
+        conn_light |= p.scene << kConnSceneShift;
         if (emit_l) {
             st_s(W.cray + 2 * rec_l, make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light)));
             st_s(W.cray + 2 * rec_l + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, l_tl));
@@ -1394,21 +1424,24 @@ __global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int
         }
         bool regen = false;
         if (done) {
-            atomicAdd(src.f.bounces + p.pixel, p.bounces);
-            atomicAdd(src.f.counts + p.pixel, 1u);
+            const FilmPtrs &F = src.film(p.scene);
+            atomicAdd(F.bounces + p.pixel, p.bounces);
+            atomicAdd(F.counts + p.pixel, 1u);
             if (fin) {
                 const uint32_t e = f_base + __popc(m_f & below);
-                st_s(D.fin_id[nxt] + e, make_uint2(p.pixel, p.frame));
+                st_s(D.fin_id[nxt] + e, make_uint4(p.pixel, p.frame, p.scene, 0u));
                 st_s(D.fin_C[nxt] + e, make_float4(C.x, C.y, C.z, 0.0f));
                 st_s(D.fin_rec[nxt] + e, make_uint2(rec_l, rec_b));
             } else {
-                write_sample(D, A, p.pixel, p.frame, C);
+                write_sample(src.samples(p.scene), src.args(p.scene), p.pixel, p.frame, C);
             }
         }
         const uint32_t rank_d = __popc(m_d & below);
         if (done && rank_d < n_regen) {
-            start_path(S, A, w_base + rank_d, p, norg, ndir, ntnear);
-            p.scene = 0;
+            unsigned long long local;
+            const uint32_t sid = src.locate(w_base + rank_d, local);
+            start_path(src.scene(sid), src.args(sid), local, p, norg, ndir, ntnear);
+            p.scene = sid;
             C = mk(0, 0, 0);
             Ts = p.T;
             regen = true;
@@ -1433,12 +1466,37 @@ __global__ void __launch_bounds__(256, 3) k_dshade(DiffOne src, Wavefront W, int
 }
 
 // Film colour sums of the differentiable forward from its per-sample radiance:
-// per pixel the samples in frame order, then one addition to the film, as the
-// one-thread-per-pixel form (diff_forward_pixel) sums them.
+// per pixel the samples in frame order, then one addition to the film, so
+// the film does not depend on the order in which samples finished.
 __global__ void __launch_bounds__(256) k_diff_film(const float *__restrict__ sample_I, RenderArgs A, FilmPtrs F) {
     const uint32_t npix = A.width * A.height;
     const uint32_t spp = (uint32_t)(A.total / npix);
     for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < npix; pixel += gridDim.x * blockDim.x) {
+        v3 sum = mk(0, 0, 0);
+        for (uint32_t s = 0; s < spp; ++s) {
+            const size_t item = (size_t)s * npix + pixel;
+            sum = sum + mk(ld_s(sample_I + 3 * item), ld_s(sample_I + 3 * item + 1), ld_s(sample_I + 3 * item + 2));
+        }
+        F.rgb[3 * (size_t)pixel] += sum.x;
+        F.rgb[3 * (size_t)pixel + 1] += sum.y;
+        F.rgb[3 * (size_t)pixel + 2] += sum.z;
+    }
+}
+
+// k_diff_film over the pixels of all slots of a batch (slot i owns
+// [pbegin[i], pbegin[i] + width * height) of the global pixel sequence).
+__device__ __forceinline__ uint32_t locate_pixel(const SceneTable *t, unsigned long long gp, uint32_t &pixel);
+
+__global__ void __launch_bounds__(256) k_diff_film_batch(const SceneTable *t, unsigned long long total_pixels) {
+    for (unsigned long long gp = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; gp < total_pixels;
+         gp += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t pixel;
+        const uint32_t sid = locate_pixel(t, gp, pixel);
+        const RenderArgs &A = t->slots[sid].a;
+        const FilmPtrs &F = t->slots[sid].f;
+        const float *sample_I = t->diff[sid].sample_I;
+        const uint32_t npix = A.width * A.height;
+        const uint32_t spp = (uint32_t)(A.total / npix);
         v3 sum = mk(0, 0, 0);
         for (uint32_t s = 0; s < spp; ++s) {
             const size_t item = (size_t)s * npix + pixel;
@@ -1498,10 +1556,11 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // contribution T * ((f * Le * w) / pdf * numLights) goes to the record's result
 // slot (w = 1) for the path's next shade to add in order; a record that does
 // not contribute gets w = 0.
-template <class State>
-__device__ __forceinline__ void resolve_connection_diff(const DiffOne &src, const Wavefront &W, uint32_t idx,
+template <class Src, class State>
+__device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wavefront &W, uint32_t idx,
                                                         uint32_t kl, const State &r) {
-    const DevScene &S = src.s;
+    const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
+    const DevScene &S = src.scene(sid);
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
     const LightInfo &L = S.lights[kl & kConnLightMask];
     float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -1526,7 +1585,7 @@ __device__ __forceinline__ void resolve_connection_diff(const DiffOne &src, cons
         const float spdf = r0.w;
         if (lpdf != 0.0f && spdf != 0.0f) {
             const v3 f = mk(r0.x, r0.y, r0.z);
-            const v3 Le = ld3(src.p.emission + 3 * h.prim);
+            const v3 Le = ld3(src.params(sid).emission + 3 * h.prim);
             const v3 T = mk(r1.x, r1.y, r1.z);
             const float fn = (float)S.num_lights;
             v3 c;
@@ -1885,59 +1944,6 @@ __device__ v3 diff_path(const DevScene &S, const DiffParams &P, const DiffGrads 
     return C;
 }
 
-// One thread per pixel, samples in frame order: the film is the same on every
-// run (finite differences of the loss see no summation-order noise).
-// sample_I (optional): each sample's radiance, 3 floats at (frame index * W*H + pixel),
-// so that the adjoint need not replay the path a first time.
-// All spp samples of one pixel: film sums (deterministic, no atomics) and,
-// optionally, every sample's radiance.
-__device__ __forceinline__ void diff_forward_pixel(const DevScene &S, const DiffParams &P, const RenderArgs &A,
-                                                   const FilmPtrs &F, float *sample_I, uint32_t pixel,
-                                                   AlbedoCache &ca, EmissionCache &ce) {
-    const DiffGrads G{};
-    float macc[1];
-    const uint32_t npix = A.width * A.height;
-    const uint32_t spp = (uint32_t)(A.total / npix);
-    v3 sum = mk(0, 0, 0);
-    uint32_t bsum = 0;
-    for (uint32_t s = 0; s < spp; ++s) {
-        uint32_t b = 0;
-        unsigned long long item = (unsigned long long)s * npix + pixel;
-        v3 c = diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
-        if (sample_I) {
-            sample_I[3 * item] = c.x;
-            sample_I[3 * item + 1] = c.y;
-            sample_I[3 * item + 2] = c.z;
-        }
-        sum = sum + c;
-        bsum += b;
-    }
-    F.rgb[3 * (size_t)pixel] += sum.x;
-    F.rgb[3 * (size_t)pixel + 1] += sum.y;
-    F.rgb[3 * (size_t)pixel + 2] += sum.z;
-    F.bounces[pixel] += bsum;
-    F.counts[pixel] += spp;
-}
-
-// Gradient terms of all spp samples of one pixel (inside G's crop).
-__device__ __forceinline__ void diff_adjoint_pixel(const DevScene &S, const DiffParams &P, const RenderArgs &A,
-                                                   const DiffGrads &G, uint32_t pixel, float *macc,
-                                                   AlbedoCache &ca, EmissionCache &ce) {
-    const uint32_t npix = A.width * A.height;
-    const uint32_t spp = (uint32_t)(A.total / npix);
-    uint32_t x = pixel % A.width, y = pixel / A.width;
-    if (x < G.x0 || x >= G.x1 || y < G.y0 || y >= G.y1) return;
-    v3 delta = ld3(G.dI + 3 * (size_t)pixel);
-    if (is_black(delta)) return;
-    for (uint32_t s = 0; s < spp; ++s) {
-        unsigned long long item = (unsigned long long)s * npix + pixel;
-        uint32_t b = 0;
-        v3 I = G.sample_I ? ld3(G.sample_I + 3 * item)
-                          : diff_path<false>(S, P, G, A, item, mk(0, 0, 0), mk(0, 0, 0), macc, ca, ce, b);
-        diff_path<true>(S, P, G, A, item, I, delta, macc, ca, ce, b);
-    }
-}
-
 // Next 32 work items for the calling warp (all lanes call it together).
 __device__ __forceinline__ unsigned long long fetch_chunk(unsigned long long *fetch);
 
@@ -1957,12 +1963,12 @@ __device__ __forceinline__ void diff_adjoint_samples(const DevScene &S, const Di
     }
 }
 
-// Samples per work item of the adjoint: a pixel's samples are split into
-// chunks of this many, taken from a shared counter 32 at a time per warp, so
+// Work items of the adjoint: a pixel's samples in chunks of
+// kAdjointChunkSamples, taken from a shared counter 32 at a time per warp, so
 // that no thread is left with a whole pixel's worth of paths at the end; the
 // consecutive samples of a chunk keep hitting the same triangles, which the
 // per-thread gradient caches exploit.
-constexpr uint32_t kAdjointChunk = 8;
+constexpr uint32_t kAdjointChunk = kAdjointChunkSamples;
 
 __global__ void __launch_bounds__(128) k_diff_adjoint(DevScene S, DiffParams P, RenderArgs A, DiffGrads G,
                                                      uint32_t num_media, unsigned long long *fetch) {
@@ -2026,24 +2032,6 @@ __device__ __forceinline__ unsigned long long fetch_chunk(unsigned long long *fe
     return __shfl_sync(0xFFFFFFFFu, base, 0);
 }
 
-__global__ void __launch_bounds__(128) k_diff_forward_batch(SceneTable *t) {
-    AlbedoCache ca;
-    EmissionCache ce;
-    const unsigned long long total = t->total_pixels;
-    for (;;) {
-        const unsigned long long base = fetch_chunk(&t->fetch);
-        if (base >= total) break;
-        const unsigned long long gp = base + (threadIdx.x & 31u);
-        if (gp < total) {
-            uint32_t pixel;
-            const uint32_t sid = locate_pixel(t, gp, pixel);
-            const SceneSlot &sl = t->slots[sid];
-            const DiffSlot &d = t->diff[sid];
-            diff_forward_pixel(sl.s, d.p, sl.a, sl.f, d.sample_I, pixel, ca, ce);
-        }
-    }
-}
-
 // Adds a thread's cached gradient terms to slot d's arrays and clears them.
 __device__ __forceinline__ void flush_diff_slot(const DiffSlot &d, float *macc, AlbedoCache &ca, EmissionCache &ce) {
     ca.flush(d.g.albedo);
@@ -2066,21 +2054,33 @@ __global__ void __launch_bounds__(128) k_diff_adjoint_batch(SceneTable *t) {
     ca.init();
     ce.init();
     uint32_t held = 0xFFFFFFFFu;  // slot whose gradients the caches hold
-    const unsigned long long total = t->total_pixels;
+    const unsigned long long total = t->total_items;
     for (;;) {
         const unsigned long long base = fetch_chunk(&t->fetch);
         if (base >= total) break;
-        const unsigned long long gp = base + (threadIdx.x & 31u);
-        if (gp < total) {
-            uint32_t pixel;
-            const uint32_t sid = locate_pixel(t, gp, pixel);
+        const unsigned long long gi = base + (threadIdx.x & 31u);
+        if (gi < total) {
+            // the slot of sample chunk gi: the last i with ibegin[i] <= gi
+            uint32_t lo = 0, hi = t->count;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (t->ibegin[mid] <= gi) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t sid = lo;
             if (sid != held) {
                 if (held != 0xFFFFFFFFu) flush_diff_slot(t->diff[held], macc, ca, ce);
                 held = sid;
             }
             const SceneSlot &sl = t->slots[sid];
             const DiffSlot &d = t->diff[sid];
-            diff_adjoint_pixel(sl.s, d.p, sl.a, d.g, pixel, macc, ca, ce);
+            const uint32_t npix = sl.a.width * sl.a.height;
+            const uint32_t spp = (uint32_t)(sl.a.total / npix);
+            const uint32_t chunks = (spp + kAdjointChunk - 1) / kAdjointChunk;
+            const unsigned long long local = gi - t->ibegin[sid];
+            const uint32_t pixel = (uint32_t)(local / chunks), c = (uint32_t)(local - (unsigned long long)pixel * chunks);
+            const uint32_t s0 = c * kAdjointChunk, s1 = s0 + kAdjointChunk < spp ? s0 + kAdjointChunk : spp;
+            diff_adjoint_samples(sl.s, d.p, sl.a, d.g, pixel, s0, s1, macc, ca, ce);
         }
     }
     if (held != 0xFFFFFFFFu) flush_diff_slot(t->diff[held], macc, ca, ce);
@@ -2124,8 +2124,9 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
                              : blocks_for(k_intersect<Bvh2>, 128, sms, trav_smem<Bvh2>(128));
     out->diff_blocks = blocks_for(k_diff_adjoint, 128, sms);
     out->dtrace_blocks = blocks_for(k_trace<DiffOne, Bvh2>, 256, sms, trav_smem<Bvh2>(256));
-    out->dshade_blocks = blocks_for(k_dshade, 256, sms);
-    out->diff_fwd_batch_blocks = blocks_for(k_diff_forward_batch, 128, sms);
+    out->dshade_blocks = blocks_for(k_dshade<DiffOne>, 256, sms);
+    out->dtrace_batch_blocks = blocks_for(k_trace<DiffMany, Bvh2>, 256, sms, trav_smem<Bvh2>(256));
+    out->dshade_batch_blocks = blocks_for(k_dshade<DiffMany>, 256, sms);
     out->diff_adj_batch_blocks = blocks_for(k_diff_adjoint_batch, 128, sms);
 }
 
@@ -2151,7 +2152,28 @@ cudaError_t launch_dwave_stage(int stage, const DevScene &s, const DiffParams &p
                                const LaunchShape &ls, cudaStream_t st) {
     const DiffOne src{s, a, f, p, d};
     if (stage == kStageTrace) k_trace<DiffOne, Bvh2><<<ls.dtrace_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
-    else k_dshade<<<ls.dshade_blocks, 256, 0, st>>>(src, w, cur);
+    else k_dshade<DiffOne><<<ls.dshade_blocks, 256, 0, st>>>(src, w, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dwave_batch_init(const SceneTable *t, const DiffWave &d, const Wavefront &w, const LaunchShape &ls,
+                                    cudaStream_t st) {
+    k_raygen<DiffMany><<<ls.dshade_batch_blocks, 256, 0, st>>>(DiffMany{t, d}, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dwave_batch_stage(int stage, const SceneTable *t, const DiffWave &d, const Wavefront &w, int cur,
+                                     const LaunchShape &ls, cudaStream_t st) {
+    const DiffMany src{t, d};
+    if (stage == kStageTrace)
+        k_trace<DiffMany, Bvh2><<<ls.dtrace_batch_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
+    else k_dshade<DiffMany><<<ls.dshade_batch_blocks, 256, 0, st>>>(src, w, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diff_film_batch(const SceneTable *t, unsigned long long total_pixels, int sms, cudaStream_t st) {
+    if (total_pixels == 0) return cudaSuccess;
+    k_diff_film_batch<<<sms * 8, 256, 0, st>>>(t, total_pixels);
     return cudaGetLastError();
 }
 
@@ -2173,9 +2195,8 @@ cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const Re
     return cudaGetLastError();
 }
 
-cudaError_t launch_diff_batch(bool adjoint, SceneTable *t, const LaunchShape &ls, cudaStream_t st) {
-    if (adjoint) k_diff_adjoint_batch<<<ls.diff_adj_batch_blocks, 128, 0, st>>>(t);
-    else k_diff_forward_batch<<<ls.diff_fwd_batch_blocks, 128, 0, st>>>(t);
+cudaError_t launch_diff_adjoint_batch(SceneTable *t, const LaunchShape &ls, cudaStream_t st) {
+    k_diff_adjoint_batch<<<ls.diff_adj_batch_blocks, 128, 0, st>>>(t);
     return cudaGetLastError();
 }
 
