@@ -1003,6 +1003,25 @@ static lt_status ensure_dwave(lt_ctx *c, uint32_t cap, DiffWave *d) {
     return LT_OK;
 }
 
+// The wavefront of a differentiable forward for `total` samples: the plain
+// arena (prepare_wave) and the path extras for as many paths. When the extras
+// do not fit, the number of paths in flight is halved (down to
+// kMinDefaultPaths) rather than failing: the plain arena then serves a
+// smaller view. Returns the capacity in *cap.
+static lt_status prepare_dwave(lt_ctx *c, unsigned long long total, uint32_t *cap, Wavefront *w, DiffWave *d) {
+    lt_status st = prepare_wave(c, total, cap);
+    if (st != LT_OK) return st;
+    for (;;) {
+        st = ensure_dwave(c, *cap, d);
+        if (st == LT_OK) break;
+        if (st != LT_ERR_OOM || *cap / 2 < kMinDefaultPaths) return st;
+        cudaGetLastError();
+        *cap /= 2;
+    }
+    *w = wave_view(c, *cap);
+    return LT_OK;
+}
+
 static lt_status ensure_diff_samples(lt_ctx *c, size_t bytes) {
     if (c->diff_samples_bytes >= bytes && c->diff_samples) return LT_OK;
     if (c->diff_samples) {
@@ -1037,10 +1056,9 @@ lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_par
         c->stats.kernel_launches = 1;
     } else if (a.total > 0) {
         uint32_t cap = 0;
-        if ((st = prepare_wave(c, a.total, &cap)) != LT_OK) return st;
-        const Wavefront w = wave_view(c, cap);
+        Wavefront w;
         DiffWave d;
-        if ((st = ensure_dwave(c, cap, &d)) != LT_OK) return st;
+        if ((st = prepare_dwave(c, a.total, &cap, &w, &d)) != LT_OK) return st;
         if (sample_radiance) {
             d.sample_I = sample_radiance;
         } else {
@@ -1584,11 +1602,7 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         uint32_t cap = 0;
         Wavefront w;
         DiffWave dw;
-        if (!adjoint) {
-            if ((st = prepare_wave(c, items, &cap)) != LT_OK) return st;
-            w = wave_view(c, cap);
-            if ((st = ensure_dwave(c, cap, &dw)) != LT_OK) return st;
-        }
+        if (!adjoint && (st = prepare_dwave(c, items, &cap, &w, &dw)) != LT_OK) return st;
         T.iteration_limit = adjoint ? 0 : drain_limit(items, cap, max_depth);
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev, c->table_host, offsetof(SceneTable, slots),
                                     cudaMemcpyHostToDevice, c->stream));

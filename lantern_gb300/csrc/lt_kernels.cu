@@ -887,6 +887,77 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
     }
 }
 
+// Queue slots of one warp of a shade kernel: first connection record, first
+// continuing-path entry, first finishing entry, first camera-ray entry and how
+// many of the warp's finished paths start a camera ray, first work item.
+struct Slots {
+    uint32_t c, q, f, r, n_regen;
+    unsigned long long w;
+};
+
+// The block's slots, reserved by one thread with one atomic per counter: each
+// warp's lane 0 stages the warp's counts (connection records, continuing
+// paths, finishing entries, finished paths) in shared memory, thread 0
+// reserves the block's records, queue entries, finishing entries and work
+// items and hands every warp its share (warps in order), then the camera-ray
+// entries, whose number depends on how many work items were left. Every
+// thread of the block calls it (block-uniform loops), at most 256 threads.
+__device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32_t nc, uint32_t np, uint32_t nf,
+                                               uint32_t nd, unsigned long long total) {
+    const int nxt = cur ^ 1;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __shared__ uint32_t s_cnt[4][8];
+    __shared__ uint32_t s_base[5][8];
+    __shared__ unsigned long long s_wbase[8];
+    if (lane == 0) {
+        s_cnt[0][warp] = nc;
+        s_cnt[1][warp] = np;
+        s_cnt[2][warp] = nf;
+        s_cnt[3][warp] = nd;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t nw = blockDim.x >> 5;
+        uint32_t tc = 0, tp = 0, tf = 0, td = 0;
+        for (uint32_t w = 0; w < nw; ++w) {
+            tc += s_cnt[0][w];
+            tp += s_cnt[1][w];
+            tf += s_cnt[2][w];
+            td += s_cnt[3][w];
+        }
+        const uint32_t c0 = tc ? atomicAdd(&wc->ccount[cur], tc) : 0u;
+        const uint32_t q0 = tp ? atomicAdd(&wc->count[nxt], tp) : 0u;
+        const uint32_t f0 = tf ? atomicAdd(&wc->fcount[nxt], tf) : 0u;
+        const unsigned long long w0 = td ? atomicAdd(&wc->work_next, (unsigned long long)td) : 0ull;
+        const unsigned long long left = w0 < total ? total - w0 : 0ull;
+        const uint32_t nreg = left < (unsigned long long)td ? (uint32_t)left : td;
+        const uint32_t r0 = nreg ? atomicAdd(&wc->rcount[nxt], nreg) : 0u;
+        uint32_t pc = 0, pp = 0, pf = 0, pd = 0;
+        for (uint32_t w = 0; w < nw; ++w) {
+            s_base[0][w] = c0 + pc;
+            s_base[1][w] = q0 + pp;
+            s_base[2][w] = f0 + pf;
+            s_wbase[w] = w0 + pd;
+            const uint32_t before = pd < nreg ? pd : nreg;  // camera rays of the warps before
+            s_base[3][w] = r0 + before;
+            s_base[4][w] = nreg - before < s_cnt[3][w] ? nreg - before : s_cnt[3][w];
+            pc += s_cnt[0][w];
+            pp += s_cnt[1][w];
+            pf += s_cnt[2][w];
+            pd += s_cnt[3][w];
+        }
+    }
+    __syncthreads();
+    Slots r;
+    r.c = s_base[0][warp];
+    r.q = s_base[1][warp];
+    r.f = s_base[2][warp];
+    r.r = s_base[3][warp];
+    r.n_regen = s_base[4][warp];
+    r.w = s_wbase[warp];
+    return r;
+}
+
 // One iteration of the bounce loop of Integrator::RenderPixel (integrator.cpp:115-243).
 // Register budget: 1024 threads per SM (64 registers, a few spilled) for the
 // single-scene instantiation, measured 1.1% faster than 768 threads (76
@@ -1064,57 +1135,14 @@ __global__ void __launch_bounds__(256, Src::kMany ? 3 : 4) k_shade(Src src, Wave
                 else push = true;
             }
         }
-        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+        const uint32_t lane = threadIdx.x & 31u;
         const unsigned below = (1u << lane) - 1u;
         const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
         const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
-        // The block's slots, reserved by one thread with one atomic per counter:
-        // each warp stages its counts in shared memory, thread 0 reserves the
-        // block's records, queue entries and work items and hands every warp its
-        // share (warps in order, lanes in order within a warp), then the
-        // camera-ray entries, whose number depends on how many work items were left.
-        __shared__ uint32_t s_cnt[3][8];
-        __shared__ uint32_t s_base[4][8];
-        __shared__ unsigned long long s_wbase[8];
-        if (lane == 0) {
-            s_cnt[0][warp] = __popc(m_l) + __popc(m_b);
-            s_cnt[1][warp] = __popc(m_p);
-            s_cnt[2][warp] = __popc(m_d);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const uint32_t nw = blockDim.x >> 5;
-            uint32_t tc = 0, tp = 0, td = 0;
-            for (uint32_t w = 0; w < nw; ++w) {
-                tc += s_cnt[0][w];
-                tp += s_cnt[1][w];
-                td += s_cnt[2][w];
-            }
-            const uint32_t c0 = tc ? atomicAdd(&W.counters->ccount[cur], tc) : 0u;
-            const uint32_t q0 = tp ? atomicAdd(&W.counters->count[nxt], tp) : 0u;
-            const unsigned long long w0 = td ? atomicAdd(&W.counters->work_next, (unsigned long long)td) : 0ull;
-            const unsigned long long tot = src.total();
-            const unsigned long long left = w0 < tot ? tot - w0 : 0ull;
-            const uint32_t nreg = left < (unsigned long long)td ? (uint32_t)left : td;
-            const uint32_t r0 = nreg ? atomicAdd(&W.counters->rcount[nxt], nreg) : 0u;
-            uint32_t pc = 0, pp = 0, pd = 0;
-            for (uint32_t w = 0; w < nw; ++w) {
-                s_base[0][w] = c0 + pc;
-                s_base[1][w] = q0 + pp;
-                s_wbase[w] = w0 + pd;
-                const uint32_t before = pd < nreg ? pd : nreg;  // camera rays of the warps before
-                const uint32_t mine = nreg - before < s_cnt[2][w] ? nreg - before : s_cnt[2][w];
-                s_base[2][w] = r0 + before;
-                s_base[3][w] = mine;
-                pc += s_cnt[0][w];
-                pp += s_cnt[1][w];
-                pd += s_cnt[2][w];
-            }
-        }
-        __syncthreads();
-        const uint32_t c_base = s_base[0][warp], q_base = s_base[1][warp], r_base = s_base[2][warp];
-        const uint32_t n_regen = s_base[3][warp];
-        const unsigned long long w_base = s_wbase[warp];
+        const Slots sl = reserve_block(W.counters, cur, __popc(m_l) + __popc(m_b), __popc(m_p), 0u, __popc(m_d),
+                                       src.total());
+        const uint32_t c_base = sl.c, q_base = sl.q, r_base = sl.r, n_regen = sl.n_regen;
+        const unsigned long long w_base = sl.w;
         // connection records: the warp's light samples, then its BSDF samples
         {
             conn_light |= p.scene << kConnSceneShift;
@@ -1377,35 +1405,18 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                 else push = true;
             }
         }
-        // slots of this warp, reserved by one lane: records, queue entries,
-        // finishing entries, next work items; then the camera-ray entries
+        // slots of this warp: records, queue entries, finishing entries, next
+        // work items, then camera-ray entries (reserve_block)
         const uint32_t lane = threadIdx.x & 31u;
         const unsigned below = (1u << lane) - 1u;
         const bool fin = done && (emit_l || emit_b);
         const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
         const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
         const unsigned m_f = __ballot_sync(0xFFFFFFFFu, fin);
-        uint32_t c_base = 0, q_base = 0, r_base = 0, f_base = 0, n_regen = 0;
-        unsigned long long w_base = 0;
-        if (lane == 0) {
-            const uint32_t nc = __popc(m_l) + __popc(m_b);
-            if (nc) c_base = atomicAdd(&W.counters->ccount[cur], nc);
-            if (m_p) q_base = atomicAdd(&W.counters->count[nxt], (uint32_t)__popc(m_p));
-            if (m_f) f_base = atomicAdd(&W.counters->fcount[nxt], (uint32_t)__popc(m_f));
-            if (m_d) {
-                w_base = atomicAdd(&W.counters->work_next, (unsigned long long)__popc(m_d));
-                const unsigned long long tot = src.total();
-                const unsigned long long left = w_base < tot ? tot - w_base : 0ull;
-                n_regen = left < (unsigned long long)__popc(m_d) ? (uint32_t)left : (uint32_t)__popc(m_d);
-                if (n_regen) r_base = atomicAdd(&W.counters->rcount[nxt], n_regen);
-            }
-        }
-        c_base = __shfl_sync(0xFFFFFFFFu, c_base, 0);
-        q_base = __shfl_sync(0xFFFFFFFFu, q_base, 0);
-        f_base = __shfl_sync(0xFFFFFFFFu, f_base, 0);
-        r_base = __shfl_sync(0xFFFFFFFFu, r_base, 0);
-        w_base = __shfl_sync(0xFFFFFFFFu, w_base, 0);
-        n_regen = __shfl_sync(0xFFFFFFFFu, n_regen, 0);
+        const Slots sl = reserve_block(W.counters, cur, __popc(m_l) + __popc(m_b), __popc(m_p), __popc(m_f),
+                                       __popc(m_d), src.total());
+        const uint32_t c_base = sl.c, q_base = sl.q, f_base = sl.f, r_base = sl.r, n_regen = sl.n_regen;
+        const unsigned long long w_base = sl.w;
         const uint32_t rec_l = emit_l ? c_base + __popc(m_l & below) : kNoRecord;
         const uint32_t rec_b = emit_b ? c_base + __popc(m_l) + __popc(m_b & below) : kNoRecord;
         conn_light |= p.scene << kConnSceneShift;
