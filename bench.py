@@ -585,6 +585,16 @@ def batch_bench(local, count=64, reps=3):
     adj_samples = sum(ds.width * ds.height * n for ds, n in zip(dss, asp))
     adj_seq = timed(adj_sequential)
     adj_bat = timed(adj_batched)
+    # the two passes apart: differentiable forwards, then adjoints from their samples
+    fw = {}
+    fwd_seq = timed(lambda: fw.update(seq=[ds.render(*p, n, 0, d, 3, keep_samples=True)
+                                           for ds, p, n, d in zip(dss, prm, asp, adep)]))
+    fwd_bat = timed(lambda: fw.update(bat=render_batch(dss, prm, asp, 0, adep, 3, keep_samples=True)))
+    dIs = [(2.0 * o[0] / n) / n for o, n in zip(fw["seq"], asp)]
+    bwd_seq = timed(lambda: [ds.adjoint(*p, dI, n, 0, d, 3, samples=o[3])
+                             for ds, p, dI, n, d, o in zip(dss, prm, dIs, asp, adep, fw["seq"])])
+    bwd_bat = timed(lambda: adjoint_batch(dss, prm, dIs, asp, 0, adep, 3, samples=[o[3] for o in fw["seq"]]))
+    del fw
     return {"workload": f"{count} scenes (seed 5): 128^2-1024^2, 1k-500k triangles, 4/16/64 spp, 30% medium; "
                         f"{len(marked)} also run the adjoint",
             "samples": samples, "triangles": sum(s.info().num_triangles for s in scenes),
@@ -601,6 +611,8 @@ def batch_bench(local, count=64, reps=3):
             "adjoint_scenes": len(marked), "adjoint_samples": adj_samples,
             "adjoint_sequential_ms": round(adj_seq, 2), "adjoint_batched_ms": round(adj_bat, 2),
             "adjoint_speedup": round(adj_seq / adj_bat, 3),
+            "adjoint_passes_ms": {"forward_sequential": round(fwd_seq, 2), "forward_batched": round(fwd_bat, 2),
+                                  "adjoint_sequential": round(bwd_seq, 2), "adjoint_batched": round(bwd_bat, 2)},
             "total_sequential_ms": round(seq + adj_seq, 2), "total_batched_ms": round(bat + adj_bat, 2),
             "total_speedup": round((seq + adj_seq) / (bat + adj_bat), 3)}
 
