@@ -372,6 +372,7 @@ def main():
     micro = None
     if args.microbench and args.workload == "icosphere-1.3M":
         micro = microbench(scene, path, local)
+    scene.ctx.trim()  # the headline render's buffers (the whole render in flight) go back
     adjoint = adjoint_bench(local) if args.adjoint else None
     batch = batch_bench(local) if args.batch else None
 
@@ -561,6 +562,10 @@ def batch_bench(local, count=64, reps=3):
         s.ctx.set_tuning(**{k: v for k, v in tuned.items() if k != "ms"})
     seq_tuned = timed(sequential)
     seq = min(seq_default, seq_tuned)
+    # every context keeps its wavefront until trimmed: give the plain renders'
+    # buffers back before the differentiable part allocates its own
+    for s in scenes:
+        s.ctx.trim()
 
     # the scenes marked for the adjoint: differentiable forward (keeping every
     # sample's radiance) and the adjoint of loss = sum(image^2), per scene vs batched
@@ -585,16 +590,44 @@ def batch_bench(local, count=64, reps=3):
     adj_samples = sum(ds.width * ds.height * n for ds, n in zip(dss, asp))
     adj_seq = timed(adj_sequential)
     adj_bat = timed(adj_batched)
-    # the two passes apart: differentiable forwards, then adjoints from their samples
-    fw = {}
-    fwd_seq = timed(lambda: fw.update(seq=[ds.render(*p, n, 0, d, 3, keep_samples=True)
-                                           for ds, p, n, d in zip(dss, prm, asp, adep)]))
-    fwd_bat = timed(lambda: fw.update(bat=render_batch(dss, prm, asp, 0, adep, 3, keep_samples=True)))
-    dIs = [(2.0 * o[0] / n) / n for o, n in zip(fw["seq"], asp)]
-    bwd_seq = timed(lambda: [ds.adjoint(*p, dI, n, 0, d, 3, samples=o[3])
-                             for ds, p, dI, n, d, o in zip(dss, prm, dIs, asp, adep, fw["seq"])])
-    bwd_bat = timed(lambda: adjoint_batch(dss, prm, dIs, asp, 0, adep, 3, samples=[o[3] for o in fw["seq"]]))
-    del fw
+
+    # the two passes apart (one more run of each, events between the passes):
+    # differentiable forwards, then adjoints from their samples
+    def split(run):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        run(evs)
+        evs[2].synchronize()
+        return evs[0].elapsed_time(evs[1]), evs[1].elapsed_time(evs[2])
+
+    def seq_split(evs):
+        evs[0].record(stream)
+        fw, bw = 0.0, 0.0
+        for ds, p, n, d in zip(dss, prm, asp, adep):
+            a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            a.record(stream)
+            rgb, _, _, smp = ds.render(*p, n, 0, d, 3, keep_samples=True)
+            b.record(stream)
+            ds.adjoint(*p, (2.0 * rgb / n) / n, n, 0, d, 3, samples=smp)
+            c.record(stream)
+            c.synchronize()
+            fw += a.elapsed_time(b)
+            bw += b.elapsed_time(c)
+            del smp
+        evs[1].record(stream)
+        evs[2].record(stream)
+        seq_split.ms = (fw, bw)
+
+    def bat_split(evs):
+        evs[0].record(stream)
+        outs = render_batch(dss, prm, asp, 0, adep, 3, keep_samples=True)
+        evs[1].record(stream)
+        adjoint_batch(dss, prm, [(2.0 * o[0] / n) / n for o, n in zip(outs, asp)], asp, 0, adep, 3,
+                      samples=[o[3] for o in outs])
+        evs[2].record(stream)
+
+    split(seq_split)
+    fwd_seq, bwd_seq = seq_split.ms
+    fwd_bat, bwd_bat = split(bat_split)
     return {"workload": f"{count} scenes (seed 5): 128^2-1024^2, 1k-500k triangles, 4/16/64 spp, 30% medium; "
                         f"{len(marked)} also run the adjoint",
             "samples": samples, "triangles": sum(s.info().num_triangles for s in scenes),

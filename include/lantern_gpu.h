@@ -60,6 +60,15 @@ lt_status lt_set_stream(lt_ctx *ctx, void *stream);
 void *lt_get_stream(const lt_ctx *ctx);
 /* Waits for all work queued on the context's stream. */
 lt_status lt_sync(lt_ctx *ctx);
+/* Frees the context's work buffers -- the wavefront arenas (up to
+ * paths_in_flight x 464 bytes), the per-sample radiance buffer of the
+ * differentiable forward and the staging buffer of host-memory calls -- and
+ * keeps its scene; the next call that needs them allocates them again. For
+ * applications that keep many contexts alive (one per scene): an idle context
+ * otherwise holds its buffers until it is destroyed. Waits for the context's
+ * work first. No counterpart in the reference, whose integrator allocates
+ * nothing per render. */
+lt_status lt_trim(lt_ctx *ctx);
 int lt_abi_version(void);
 
 /* ---------------------------------------------------------------- scene */

@@ -335,6 +335,25 @@ lt_status lt_sync(lt_ctx *c) try {
     return LT_OK;
 } LT_CATCH(c)
 
+lt_status lt_trim(lt_ctx *c) try {
+    if (!c) return LT_ERR_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (c->own_stream != c->stream) CUDA_TRY(c, cudaStreamSynchronize(c->own_stream));
+    free_wave(c);  // with the captured batch loop, which points into it
+    if (c->diff_arena) cudaFree(c->diff_arena);
+    c->diff_arena = nullptr;
+    c->diff_arena_bytes = 0;
+    c->diff_capacity = 0;
+    if (c->diff_samples) cudaFree(c->diff_samples);
+    c->diff_samples = nullptr;
+    c->diff_samples_bytes = 0;
+    if (c->scratch) cudaFree(c->scratch);
+    c->scratch = nullptr;
+    c->scratch_bytes = 0;
+    return LT_OK;
+} LT_CATCH(c)
+
 }  // extern "C"
 
 // Temporary device buffers of one call, freed when it returns (after the

@@ -21,7 +21,7 @@ MISS = 0xFFFFFFFF
 
 # exported symbols (include/lantern_gpu.h)
 SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error", "lt_set_stream", "lt_get_stream",
-           "lt_sync",
+           "lt_sync", "lt_trim",
            "lt_scene_create", "lt_scene_destroy", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_scene_lights_get", "lt_render",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
@@ -144,6 +144,7 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_get_stream.argtypes = [p]
         L.lt_get_stream.restype = p
         L.lt_sync.argtypes = [p]
+        L.lt_trim.argtypes = [p]
         L.lt_scene_create.argtypes = [p, C.POINTER(SceneDesc)]
         L.lt_scene_load_json.argtypes = [p, C.c_char_p]
         L.lt_scene_destroy.argtypes = [p]
@@ -228,6 +229,11 @@ class Context:
 
     def sync(self):
         self._check(self.L.lt_sync(self.h))
+
+    def trim(self):
+        """lt_trim: free the work buffers (wavefronts, sample buffer, staging);
+        the scene stays."""
+        self._check(self.L.lt_trim(self.h))
 
     def set_bvh_builder(self, builder: int):
         """BVH_GPU (default) or BVH_HOST for the next scene load."""
