@@ -2057,7 +2057,10 @@ __device__ __forceinline__ void flush_diff_slot(const DiffSlot &d, float *macc, 
     }
 }
 
-__global__ void __launch_bounds__(128) k_diff_adjoint_batch(SceneTable *t) {
+// Register budget: six 128-thread blocks per SM (80 registers, some spilled),
+// as the single-scene adjoint runs: measured 5% faster than the compiler's
+// 96 registers (five blocks) on the batched adjoints of the 64-scene workload.
+__global__ void __launch_bounds__(128, 6) k_diff_adjoint_batch(SceneTable *t) {
     float macc[6 * kMediaAcc];
     for (int k = 0; k < 6 * kMediaAcc; ++k) macc[k] = 0.0f;
     AlbedoCache ca;
