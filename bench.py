@@ -41,9 +41,13 @@ sys.path.insert(0, ROOT)
 METRIC = "Msamples/s & Mrays/s on 1 GB300 vs host CPU at matched RMSE; adjoint grads/s"
 SCENES = os.path.join(ROOT, "_scenes")
 # DRAM bytes (read + write) per ray traced by k_trace on the icosphere workload, measured
-# with ncu dram__bytes_{read,write}.sum over every k_trace launch of a 4-spp render
-# (profiles/k_trace_k_shade_icosphere-1.3M.md)
-TRACE_DRAM_BYTES_PER_RAY = 97.1
+# with ncu dram__bytes_{read,write}.sum over the 11 k_trace launches of one render of this
+# workload (13.14 GB for 171,793,933 traced rays; profiles/k_trace_k_shade_icosphere-1.3M.md)
+TRACE_DRAM_BYTES_PER_RAY = 76.5
+# L2 throughput of k_trace as a fraction of the L2's peak (ncu
+# lts__throughput.avg.pct_of_peak_sustained_elapsed of iterations 0 and 1 of a
+# 4-spp render of the same scene; profiles/k_trace_k_shade_icosphere-1.3M.md)
+TRACE_L2_FRAC = 0.132
 
 
 def max_over_ranks(value: float, dist=None, device="cpu") -> float:
@@ -392,6 +396,7 @@ def main():
                     "traffic": (round(TRACE_DRAM_BYTES_PER_RAY * traced_per_launch)
                                 if args.workload == "icosphere-1.3M" else None),
                     "algorithmic_bytes_per_launch": round(bpr * traced_per_launch),
+                    "l2_frac": TRACE_L2_FRAC if args.workload == "icosphere-1.3M" else None,
                     "bytes_per_ray": round(bpr, 1), "node_tests_per_ray": round(n_node, 2),
                     "tri_tests_per_ray": round(n_tri, 2), "peak_kind": peak_kind,
                     "rays_traced_per_step": (main_rays + conn_traced) // args.steps,
