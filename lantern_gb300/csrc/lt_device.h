@@ -203,8 +203,8 @@ cudaError_t launch_intersect(const DevScene &s, const float4 *rays, float4 *hits
 cudaError_t launch_add_counts(const FilmPtrs &f, uint32_t npix, uint32_t spp, cudaStream_t st);
 // differentiable forward on the wavefront: camera rays (with the path extras
 // of d), then per iteration k_trace (connection records resolved into d.res)
-// and k_dshade; last, the film from the per-sample radiance (sample order, as
-// the one-thread-per-pixel form sums it)
+// and k_dshade; last, the film from the per-sample radiance, per pixel in
+// sample order (the film does not depend on the order in which samples finished)
 cudaError_t launch_dwave_init(const DevScene &s, const DiffParams &p, const DiffWave &d, const Wavefront &w,
                               const RenderArgs &a, const FilmPtrs &f, const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_dwave_stage(int stage, const DevScene &s, const DiffParams &p, const DiffWave &d,

@@ -222,7 +222,8 @@ def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: 
     each difference renders twice with one parameter moved by +-h and the
     sampling copies (detached albedo, sigma_a, sigma_s) held at theta, so both
     sides differentiate the same function of the parameters (the forward is
-    deterministic: one thread per pixel, samples summed in frame order).
+    deterministic: every sample's radiance is gathered in the estimator's order
+    and the film sums the samples per pixel in frame order).
     Parameters, drawn with `seed`: every sigma_a and sigma_s entry, up to 10
     emission entries whose adjoint gradient is nonzero, then albedo entries with
     in all. A parameter is compared unless both gradients are below 1e-8 of

@@ -138,7 +138,7 @@ def test_diff_batch_equals_individual(scene_dir):
     for k, sc in enumerate(scenes):
         ref = sc.render(*params[k], spp[k], ff[k], 8, 3, keep_samples=True)
         for x, y in zip(outs[k], ref):
-            assert torch.equal(x, y)  # one thread per pixel: identical arithmetic, no atomics
+            assert torch.equal(x, y)  # same per-sample arithmetic, films summed in sample order
         dI.append(torch.rand((sc.height, sc.width, 3), generator=g, device="cuda:0") - 0.5)
     for samples in ([o[3] for o in outs], None):
         gb = adjoint_batch(scenes, params, dI, spp, ff, 8, 3, samples=samples)
