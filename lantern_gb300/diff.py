@@ -226,7 +226,8 @@ def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: 
     and the film sums the samples per pixel in frame order).
     Parameters, drawn with `seed`: every sigma_a and sigma_s entry, up to 10
     emission entries whose adjoint gradient is nonzero, then albedo entries with
-    in all. A parameter is compared unless both gradients are below 1e-8 of
+    a nonzero gradient up to `count` in all. A parameter is compared unless
+    both gradients are below 1e-8 of
     the largest gradient of its array (float noise). Returns {"parameters", "checked",
     "max_rel_err", "failures": [(array, index, adjoint, fd), ...]} with the
     comparisons whose relative difference exceeds rel_tol."""
