@@ -229,8 +229,9 @@ def finite_difference_check(scene: DiffScene, theta, target: torch.Tensor, spp: 
     a nonzero gradient up to `count` in all. A parameter is compared unless
     both gradients are below 1e-8 of
     the largest gradient of its array (float noise). Returns {"parameters", "checked",
-    "max_rel_err", "failures": [(array, index, adjoint, fd), ...]} with the
-    comparisons whose relative difference exceeds rel_tol."""
+    "max_rel_err", "failures": [(array, index, adjoint, fd), ...], "pairs"}:
+    failures are the comparisons whose relative difference exceeds rel_tol,
+    pairs every (array, index, adjoint, fd) drawn."""
     base = [t.detach().to(scene.device, torch.float32).contiguous() for t in theta]
     tgt = target.detach().to(scene.device).double()
     th = [t.clone().requires_grad_() for t in base]

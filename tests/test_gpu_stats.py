@@ -1,0 +1,32 @@
+"""lt_render_stats: the kernel times of the stages (events around every
+launch), the device time of the whole render and the time between its
+kernels are consistent, and the ray counts add up to what was traced."""
+import pytest
+import torch
+
+import lantern_gb300.scenes as S
+from lantern_gb300.integrator import FrameBuffer, Integrator, Scene
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("paths", [0, 4096])  # the whole render in flight, and refills from work items
+def test_stage_times_and_counts(scene_dir, paths):
+    s = Scene(0)
+    s.LoadSceneFromJSON(S.nine_spheres(width=64, height=48, slices=16, stacks=8, name="stats_nine").write(scene_dir))
+    if paths:
+        s.ctx.set_tuning(paths_in_flight=paths)
+    fb = FrameBuffer(s.width, s.height, "cuda:0")
+    it = Integrator(s, fb, max_depth=8, rr_depth=3)
+    it.RenderFrame(8)
+    torch.cuda.synchronize()
+    st = it.stats()
+    assert st.samples == 64 * 48 * 8
+    assert st.init_ms > 0 and st.trace_ms > 0 and st.shade_ms > 0
+    busy = st.init_ms + st.trace_ms + st.shade_ms
+    assert busy <= st.gpu_ms * 1.001 + 1e-3
+    assert st.idle_ms >= 0 and abs(busy + st.idle_ms - st.gpu_ms) <= 1e-3 * st.gpu_ms + 1e-3
+    assert st.kernel_launches == 1 + 2 * st.iterations
+    assert st.main_rays >= st.samples  # every sample traces its camera ray
+    assert st.light_traversals <= st.light_rays + st.bsdf_rays
+    assert int(fb.ColorSampleCount.min()) == 8
