@@ -276,6 +276,10 @@ def main():
                          "up to 67,108,864")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 4, 8],
                     help="BVH width of the traversal (lt_tuning.bvh_width)")
+    ap.add_argument("--trace-threads", type=int, default=0, choices=[0, 64, 128, 256],
+                    help="threads per block of the trace kernel (lt_tuning.trace_threads; 0 = the library's)")
+    ap.add_argument("--shade-threads", type=int, default=0, choices=[0, 64, 128, 256],
+                    help="threads per block of the shade kernel (lt_tuning.shade_threads; 0 = the library's)")
     ap.add_argument("--batch", action=argparse.BooleanOptionalAction, default=True,
                     help="also time the 64-scene batch: one lt_render_batch vs one lt_render per scene")
     args = ap.parse_args()
@@ -311,7 +315,9 @@ def main():
     scene = Scene(local)
     scene.LoadSceneFromJSON(path)
     paths_in_flight = args.paths_in_flight or min(scene.width * scene.height * rp["spp"], 1 << 26)
-    scene.ctx.set_tuning(bvh_width=args.bvh_width, paths_in_flight=paths_in_flight)
+    scene.ctx.set_tuning(bvh_width=args.bvh_width, paths_in_flight=paths_in_flight,
+                         **({"trace_threads": args.trace_threads} if args.trace_threads else {}),
+                         **({"shade_threads": args.shade_threads} if args.shade_threads else {}))
     info = scene.info()
     fb = FrameBuffer(scene.width, scene.height, f"cuda:{local}")
     integ = Integrator(scene, fb, max_depth=rp["max_depth"], rr_depth=rp["rr_depth"])
@@ -419,6 +425,8 @@ def main():
                            "max_depth": rp["max_depth"], "rr_depth": rp["rr_depth"],
                            "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
                            "bvh_width": args.bvh_width, "paths_in_flight": paths_in_flight,
+                           "trace_threads": scene.ctx.tuning().trace_threads,
+                           "shade_threads": scene.ctx.tuning().shade_threads,
                            "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1
                            else "single GPU"},
                 "mrays": round(mrays, 2), "gpu_launches": launches,
