@@ -28,7 +28,9 @@
 extern "C" {
 #endif
 
-#define LT_ABI_VERSION 1
+/* 2: lt_render_stats gained init_ms and idle_ms; lt_light_info, lt_scene_lights_get,
+ * lt_trim and lt_debug_set_iteration_limit were added. */
+#define LT_ABI_VERSION 2
 
 typedef enum lt_status {
     LT_OK = 0,

@@ -30,6 +30,7 @@ SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error",
 BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 MAX_BATCH = 2048  # LT_MAX_BATCH
+ABI_VERSION = 2  # LT_ABI_VERSION
 TONEMAP_CLAMP, TONEMAP_FILMIC = 0, 1
 
 
@@ -135,6 +136,8 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L = C.CDLL(path)
         p = C.c_void_p
         L.lt_abi_version.restype = C.c_int
+        if L.lt_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"liblantern_gpu.so has ABI {L.lt_abi_version()}, this binding expects {ABI_VERSION}")
         L.lt_ctx_create.argtypes = [C.c_int, C.POINTER(p)]
         L.lt_ctx_destroy.argtypes = [p]
         L.lt_ctx_destroy.restype = None

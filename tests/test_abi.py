@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_no_device_error():
     lib = native.load()
-    assert lib.lt_abi_version() == 1
+    assert lib.lt_abi_version() == 2
     import torch
     if not torch.cuda.is_available():
         h = ctypes.c_void_p()
