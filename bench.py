@@ -278,7 +278,7 @@ def main():
                     help="BVH width of the traversal (lt_tuning.bvh_width)")
     ap.add_argument("--trace-threads", type=int, default=0, choices=[0, 64, 128, 256],
                     help="threads per block of the trace kernel (lt_tuning.trace_threads; 0 = the library's)")
-    ap.add_argument("--shade-threads", type=int, default=0, choices=[0, 64, 128, 256],
+    ap.add_argument("--shade-threads", type=int, default=0, choices=[0, 64, 128, 256, 512],
                     help="threads per block of the shade kernel (lt_tuning.shade_threads; 0 = the library's)")
     ap.add_argument("--batch", action=argparse.BooleanOptionalAction, default=True,
                     help="also time the 64-scene batch: one lt_render_batch vs one lt_render per scene")

@@ -314,7 +314,8 @@ typedef struct lt_tuning {
                                   each); 0 = min(samples, 16,777,216), halved while the
                                   allocation fails (down to 1,048,576) */
     uint32_t trace_threads;    /* threads per block of the trace kernel: 64, 128 or 256 */
-    uint32_t shade_threads;    /* ... of the shade kernel (and camera-ray generation) */
+    uint32_t shade_threads;    /* ... of the shade kernel: 64, 128, 256 or 512 (lt_render_batch's
+                                  shade kernel uses at most 256) */
     uint32_t loop_iterations;  /* wavefront iterations per body of lt_render_batch's loop: 2, 4 or 8 */
     uint32_t bvh_width;        /* children per BVH node: 2 (BVH2), 4 (4-wide) or 8 (compressed 8-wide);
                                   the wide trees are built from the BVH2 on first use */
@@ -322,7 +323,8 @@ typedef struct lt_tuning {
 } lt_tuning;
 /* The context's tuning; it applies to lt_render, lt_render_batch and the
  * tuner's starting point. Zero fields of lt_set_tuning keep their defaults
- * (0 paths = automatic, 128 threads, 2 iterations, width 2). Width 8 builds
+ * (0 paths = automatic, 128 trace threads, 256 shade threads, 2 iterations,
+ * width 2). Width 8 builds
  * the scene's compressed 8-wide BVH from its BVH2 (Ylitie, Karras, Laine, HPG
  * 2017 node layout), width 4 an uncompressed 4-wide one sharing the BVH2's
  * triangles; lt_scene_create then builds it for every new scene. */

@@ -230,7 +230,8 @@ static uint32_t first_batch(unsigned long long total, uint32_t cap, uint32_t max
 
 static void default_tuning(lt_tuning *t) {
     *t = lt_tuning{};
-    t->trace_threads = t->shade_threads = 128;
+    t->trace_threads = 128;
+    t->shade_threads = 256;
     t->loop_iterations = 2;
     t->bvh_width = 2;
 }
@@ -242,6 +243,8 @@ static void apply_tuning(lt_ctx *c) {
         ls->trace_threads = (int)c->tuning.trace_threads;
         ls->shade_threads = (int)c->tuning.shade_threads;
     }
+    // the batched shade kernel holds 256 threads per block at most
+    if (c->batch_shape.shade_threads > 256) c->batch_shape.shade_threads = 256;
     query_launch_shape(c->device, false, &c->shape);
     query_launch_shape(c->device, true, &c->batch_shape);
 }
@@ -1208,6 +1211,7 @@ extern "C" lt_status lt_get_tuning(const lt_ctx *c, lt_tuning *out) {
 }
 
 static bool valid_threads(uint32_t t) { return t == 64 || t == 128 || t == 256; }
+static bool valid_shade_threads(uint32_t t) { return valid_threads(t) || t == 512; }
 
 extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) try {
     if (!c || !t) return fail(c, LT_ERR_INVALID, "NULL argument");
@@ -1219,8 +1223,8 @@ extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) try {
     if (t->loop_iterations) n.loop_iterations = t->loop_iterations;
     if (t->bvh_width) n.bvh_width = t->bvh_width;
     n.ms = t->ms;
-    if (!valid_threads(n.trace_threads) || !valid_threads(n.shade_threads))
-        return fail(c, LT_ERR_INVALID, "threads per block must be 64, 128 or 256");
+    if (!valid_threads(n.trace_threads) || !valid_shade_threads(n.shade_threads))
+        return fail(c, LT_ERR_INVALID, "threads per block must be 64, 128 or 256 (512 also for the shade kernel)");
     if (n.loop_iterations != 2 && n.loop_iterations != 4 && n.loop_iterations != 8)
         return fail(c, LT_ERR_INVALID, "loop_iterations must be 2, 4 or 8");
     if (n.bvh_width != 2 && n.bvh_width != 4 && n.bvh_width != 8)

@@ -901,14 +901,14 @@ struct Slots {
 // reserves the block's records, queue entries, finishing entries and work
 // items and hands every warp its share (warps in order), then the camera-ray
 // entries, whose number depends on how many work items were left. Every
-// thread of the block calls it (block-uniform loops), at most 256 threads.
+// thread of the block calls it (block-uniform loops), at most 512 threads.
 __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32_t nc, uint32_t np, uint32_t nf,
                                                uint32_t nd, unsigned long long total) {
     const int nxt = cur ^ 1;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    __shared__ uint32_t s_cnt[4][8];
-    __shared__ uint32_t s_base[5][8];
-    __shared__ unsigned long long s_wbase[8];
+    __shared__ uint32_t s_cnt[4][16];
+    __shared__ uint32_t s_base[5][16];
+    __shared__ unsigned long long s_wbase[16];
     if (lane == 0) {
         s_cnt[0][warp] = nc;
         s_cnt[1][warp] = np;
@@ -963,7 +963,7 @@ __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32
 // single-scene instantiation, measured 1.1% faster than 768 threads (76
 // registers) with the whole render in flight; the batched one keeps 768.
 template <class Src>
-__global__ void __launch_bounds__(256, Src::kMany ? 3 : 4) k_shade(Src src, Wavefront W, int cur) {
+__global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_shade(Src src, Wavefront W, int cur) {
     const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
     const uint32_t n = n_push + n_cam;
     const uint32_t cap = W.capacity;
@@ -2257,7 +2257,7 @@ static cudaError_t stage(int stage, const Src &src, const Wavefront &w, int cur,
 
 cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
                              const LaunchShape &ls, cudaStream_t st) {
-    k_raygen<OneScene><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(OneScene{s, a, f}, w);
+    k_raygen<OneScene><<<ls.sms * 8, 256, 0, st>>>(OneScene{s, a, f}, w);
     return cudaGetLastError();
 }
 
@@ -2267,7 +2267,7 @@ cudaError_t launch_wave_stage(int st_, const DevScene &s, const Wavefront &w, co
 }
 
 cudaError_t launch_batch_init(const SceneTable *t, const Wavefront &w, const LaunchShape &ls, cudaStream_t st) {
-    k_raygen<ManyScenes><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(ManyScenes{t}, w);
+    k_raygen<ManyScenes><<<ls.sms * 8, 256, 0, st>>>(ManyScenes{t}, w);
     return cudaGetLastError();
 }
 
