@@ -30,3 +30,23 @@ def test_stage_times_and_counts(scene_dir, paths):
     assert st.main_rays >= st.samples  # every sample traces its camera ray
     assert st.light_traversals <= st.light_rays + st.bsdf_rays
     assert int(fb.ColorSampleCount.min()) == 8
+
+
+def test_launch_shapes_render_the_same_samples(scene_dir):
+    """Threads per block of both stage kernels (64 to 256, 512 for the shade
+    kernel) change the order of the queues and of the film additions, not the
+    samples: counts and path lengths are equal, colours equal up to the order
+    of float additions."""
+    s = Scene(0)
+    s.LoadSceneFromJSON(S.medium_sphere_scene(width=48, height=40, name="stats_shapes").write(scene_dir))
+    films = []
+    for tt, st in ((128, 256), (64, 512), (256, 64), (128, 128)):
+        s.ctx.set_tuning(trace_threads=tt, shade_threads=st, paths_in_flight=2048)
+        fb = FrameBuffer(s.width, s.height, "cuda:0")
+        Integrator(s, fb, max_depth=16, rr_depth=3).RenderFrame(6)
+        films.append(fb)
+    torch.cuda.synchronize()
+    a = films[0]
+    for b in films[1:]:
+        assert torch.equal(a.ColorSampleCount, b.ColorSampleCount) and torch.equal(a.Bounces, b.Bounces)
+        assert torch.allclose(a.ColorData, b.ColorData, rtol=1e-5, atol=1e-6)
