@@ -1000,8 +1000,10 @@ static size_t carve_dwave(char *base, uint32_t cap, DiffWave *d) {
         d->fin_id[k] = (uint4 *)take(16 * P);
         d->fin_C[k] = (float4 *)take(16 * P);
         d->fin_rec[k] = (uint2 *)take(8 * P);
+        d->pend[k] = (uint32_t *)take(4 * P);
     }
     d->res = (float4 *)take(32 * P);  // two connection records per path
+    d->aux = (float2 *)take(16 * P);
     d->sample_I = nullptr;
     d->bytes = off;
     return off;
@@ -1122,12 +1124,31 @@ lt_status lt_render_adjoint(lt_ctx *c, const lt_render_params *p, const lt_diff_
     }
     c->stats = lt_render_stats{};
     CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-    // the adjoint's work counter: 8 bytes of the context's counter block, after lt_intersect's
-    CUDA_TRY(c, launch_diff_adjoint(c->dev, P, a, G, (uint32_t)c->host.media.size(),
-                                    (unsigned long long *)(c->isect_fetch + 16), c->shape, c->stream));
+    const unsigned long long crop_samples =
+        (unsigned long long)(G.x1 - G.x0) * (G.y1 - G.y0) * (a.total / ((unsigned long long)a.width * a.height));
+    if (sample_radiance && crop_samples > 0 && p->max_depth > 0) {
+        // on the wavefront: the forward's paths replayed over the crop's samples
+        RenderArgs aa = a;
+        aa.total = crop_samples;
+        uint32_t cap = 0;
+        Wavefront w;
+        DiffWave d;
+        if ((st = prepare_dwave(c, aa.total, &cap, &w, &d)) != LT_OK) return st;
+        st = run_loop(
+            c, w, aa, true, [&]() { return launch_awave_init(c->dev, P, d, G, w, aa, c->shape, c->stream); },
+            [&](int stage, int cur) {
+                return launch_awave_stage(stage, c->dev, P, d, G, w, aa, cur, c->shape, c->stream);
+            });
+        if (st != LT_OK) return st;
+    } else if (!sample_radiance) {
+        // without the forward's radiance: one thread replays each sample twice
+        // (the adjoint's work counter: 8 bytes of the context's counter block, after lt_intersect's)
+        CUDA_TRY(c, launch_diff_adjoint(c->dev, P, a, G, (uint32_t)c->host.media.size(),
+                                        (unsigned long long *)(c->isect_fetch + 16), c->shape, c->stream));
+        c->stats.kernel_launches = 1;
+    }
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
-    c->stats.samples = a.total;
-    c->stats.kernel_launches = 1;
+    c->stats.samples = crop_samples;
     return LT_OK;
 } LT_CATCH(c)
 
@@ -1535,13 +1556,26 @@ extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap,
 // Batched differentiable forward (adjoint false) or adjoint over one scene
 // table. The forward runs the differentiable wavefront over the work items of
 // all jobs (as lt_render_batch does for plain renders) and returns when it
-// has finished; the adjoint is one persistent launch over sample chunks of all
-// jobs' pixels and returns once queued.
+// has finished. The adjoint runs on the same wavefront when every job that
+// has samples to replay brings the forward's per-sample radiance (and then
+// also returns when finished); otherwise it is one persistent launch over
+// sample chunks of all jobs' pixels and returns once queued.
 static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool adjoint) {
     NvtxRange nvtx_("diff_batch");
     if (!c || (n && !jobs)) return fail(c, LT_ERR_INVALID, "NULL argument");
     if (n > LT_MAX_BATCH) return fail(c, LT_ERR_INVALID, "%u jobs; a batch holds at most %u", n, LT_MAX_BATCH);
     CUDA_TRY(c, cudaSetDevice(c->device));
+    bool wave = !adjoint;  // the wavefront (forward, or adjoint replaying the forward's samples)
+    if (adjoint) {
+        wave = true;
+        for (uint32_t i = 0; i < n; ++i) {
+            const lt_ctx *s = jobs[i].scene;
+            if (!s || !s->has_scene) continue;  // rejected below
+            const unsigned long long total =
+                (unsigned long long)s->host.camera.width * s->host.camera.height * jobs[i].params.spp;
+            if (total && jobs[i].params.max_depth && !jobs[i].sample_radiance) wave = false;
+        }
+    }
     lt_status st = ensure_table(c);
     if (st != LT_OK) return st;
     SceneTable &T = *c->table_host;
@@ -1603,9 +1637,9 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         T.pbegin[count] = pixels;
         T.ibegin[count] = items;
         pixels += (unsigned long long)W * H;
-        // work items: the forward's samples; the adjoint's chunks of kAdjointChunkSamples samples
+        // work items: the samples on the wavefront; else chunks of kAdjointChunkSamples samples
         const unsigned long long chunks = (j.params.spp + kAdjointChunkSamples - 1) / kAdjointChunkSamples;
-        items += adjoint ? (unsigned long long)W * H * chunks : total;
+        items += wave ? total : (unsigned long long)W * H * chunks;
         if (j.params.max_depth > max_depth) max_depth = j.params.max_depth;
         ++count;
     }
@@ -1618,22 +1652,22 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         }
         T.count = count;
         T.pad = 0;
-        T.total = adjoint ? 0 : items;
+        T.total = wave ? items : 0;
         T.total_items = items;
         T.total_pixels = pixels;
         T.fetch = 0;
         uint32_t cap = 0;
         Wavefront w;
         DiffWave dw;
-        if (!adjoint && (st = prepare_dwave(c, items, &cap, &w, &dw)) != LT_OK) return st;
-        T.iteration_limit = adjoint ? 0 : drain_limit(items, cap, max_depth);
+        if (wave && (st = prepare_dwave(c, items, &cap, &w, &dw)) != LT_OK) return st;
+        T.iteration_limit = wave ? drain_limit(items, cap, max_depth) : 0;
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev, c->table_host, offsetof(SceneTable, slots),
                                     cudaMemcpyHostToDevice, c->stream));
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->slots, T.slots, count * sizeof(SceneSlot), cudaMemcpyHostToDevice,
                                     c->stream));
         CUDA_TRY(c, cudaMemcpyAsync(c->table_dev->diff, T.diff, count * sizeof(DiffSlot), cudaMemcpyHostToDevice,
                                     c->stream));
-        if (adjoint) {
+        if (!wave) {
             CUDA_TRY(c, launch_diff_adjoint_batch(c->table_dev, c->shape, c->stream));
             ++launches;
         } else {
@@ -1641,15 +1675,24 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
             all.max_depth = max_depth;
             all.total = items;
             const SceneTable *t = c->table_dev;
-            st = run_loop(
-                c, w, all, false, [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
-                [&](int stage, int cur) {
-                    return launch_dwave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
-                });
+            if (adjoint)
+                st = run_loop(
+                    c, w, all, false, [&]() { return launch_awave_batch_init(t, dw, w, c->batch_shape, c->stream); },
+                    [&](int stage, int cur) {
+                        return launch_awave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
+                    });
+            else
+                st = run_loop(
+                    c, w, all, false, [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
+                    [&](int stage, int cur) {
+                        return launch_dwave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
+                    });
             if (st != LT_OK) return st;
             launches += c->stats.kernel_launches;
-            CUDA_TRY(c, launch_diff_film_batch(t, pixels, c->shape.sms, c->stream));
-            ++launches;
+            if (!adjoint) {
+                CUDA_TRY(c, launch_diff_film_batch(t, pixels, c->shape.sms, c->stream));
+                ++launches;
+            }
         }
         CUDA_TRY(c, (cudaError_t)c->order.table_read_queued(c->rt, c->stream));
     }

@@ -77,19 +77,24 @@ struct Wavefront {
     size_t arena_bytes = 0;
 };
 
-// The differentiable forward on the wavefront (lt_render_diff): what a path
-// carries beyond PathState (ping-pong in queue order like it), the result of
-// every connection record, the paths that finished while their last records
-// were still to be traced, and the per-sample radiance.
+// The differentiable estimator on the wavefront (lt_render_diff, and the
+// adjoint of lt_render_adjoint): what a path carries beyond PathState
+// (ping-pong in queue order like it), the result of every connection record,
+// the paths that finished while their last records were still to be traced,
+// and the per-sample radiance. The adjoint also keeps, per path, the triangle
+// whose albedo term waits for the records of its bounce (pend), and per
+// record the shading triangle and the factor f / albedo of the sample (aux).
 constexpr uint32_t kNoRecord = 0xFFFFFFFFu;
 struct DiffWave {
     float *C[2];         // radiance gathered so far, 3 planes of capacity
     float *Ts[2];        // throughput with the detached parameters (roulette), 3 planes
     uint2 *rec[2];       // the path's light and BSDF records of the previous shade, or kNoRecord
     float4 *res;         // per connection record: its contribution (rgb), w = 1 when it contributes
-    uint4 *fin_id[2];    // finishing paths (by parity): (pixel, frame, scene slot, 0)
+    uint4 *fin_id[2];    // finishing paths (by parity): (pixel, frame, scene slot, pending triangle)
     float4 *fin_C[2];    //   radiance gathered before their last records
     uint2 *fin_rec[2];   //   those records
+    uint32_t *pend[2];   // adjoint: triangle of the previous bounce's deferred albedo term, or kMiss
+    float2 *aux;         // adjoint, per connection record: (shading triangle, f / albedo)
     float *sample_I;     // 3 floats per sample at ((frame - first_frame) * W * H + pixel)
     size_t bytes = 0;
 };
@@ -119,6 +124,8 @@ struct LaunchShape {
     int dtrace_blocks = 0, dshade_blocks = 0;  // differentiable forward on the wavefront
     int dtrace_batch_blocks = 0, dshade_batch_blocks = 0;
     int diff_adj_batch_blocks = 0;
+    int atrace_blocks = 0, ashade_blocks = 0;  // adjoint on the wavefront
+    int atrace_batch_blocks = 0, ashade_batch_blocks = 0;
 };
 
 // Parameters of the differentiable render (device arrays): per-triangle RGB
@@ -221,6 +228,21 @@ cudaError_t launch_diff_film_batch(const SceneTable *t, unsigned long long total
 cudaError_t launch_diff_adjoint(const DevScene &s, const DiffParams &p, const RenderArgs &a, const DiffGrads &g,
                                 uint32_t num_media, unsigned long long *fetch, const LaunchShape &ls,
                                 cudaStream_t st);
+// adjoint on the wavefront (lt_render_adjoint with the forward's per-sample
+// radiance g.sample_I): the differentiable forward's paths replayed over the
+// crop's samples (a.total = spp * crop pixels), gradient terms added per block
+// in shared memory; leaves the film alone
+cudaError_t launch_awave_init(const DevScene &s, const DiffParams &p, const DiffWave &d, const DiffGrads &g,
+                              const Wavefront &w, const RenderArgs &a, const LaunchShape &ls, cudaStream_t st);
+cudaError_t launch_awave_stage(int stage, const DevScene &s, const DiffParams &p, const DiffWave &d,
+                               const DiffGrads &g, const Wavefront &w, const RenderArgs &a, int cur,
+                               const LaunchShape &ls, cudaStream_t st);
+// the same over the jobs of a batch's table (lt_render_adjoint_batch, every
+// job with its per-sample radiance): work items begin[] as the forward's
+cudaError_t launch_awave_batch_init(const SceneTable *t, const DiffWave &d, const Wavefront &w, const LaunchShape &ls,
+                                    cudaStream_t st);
+cudaError_t launch_awave_batch_stage(int stage, const SceneTable *t, const DiffWave &d, const Wavefront &w, int cur,
+                                     const LaunchShape &ls, cudaStream_t st);
 cudaError_t launch_wave_init(const DevScene &s, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f,
                              const LaunchShape &ls, cudaStream_t st);
 // Per wavefront iteration: k_trace (path rays of this iteration + connection

@@ -742,7 +742,7 @@ __device__ __forceinline__ void film_contribute(WaveCounters *counters, const Fi
 // one sequence, slot i owning [begin[i], begin[i] + slots[i].a.total), and every
 // path carries its slot in its flags and connection records.
 struct OneScene {
-    static constexpr bool kMany = false, kDiff = false;
+    static constexpr bool kMany = false, kDiff = false, kAdj = false;
     DevScene s;
     RenderArgs a;
     FilmPtrs f;
@@ -757,7 +757,7 @@ struct OneScene {
 };
 
 struct ManyScenes {
-    static constexpr bool kMany = true, kDiff = false;
+    static constexpr bool kMany = true, kDiff = false, kAdj = false;
     const SceneTable *t;
     __device__ __forceinline__ const DevScene &scene(uint32_t i) const { return t->slots[i].s; }
     __device__ __forceinline__ const RenderArgs &args(uint32_t i) const { return t->slots[i].a; }
@@ -781,7 +781,7 @@ struct ManyScenes {
 // stage writes each connection record's contribution into d.res instead of
 // the film.
 struct DiffOne {
-    static constexpr bool kMany = false, kDiff = true;
+    static constexpr bool kMany = false, kDiff = true, kAdj = false;
     DevScene s;
     RenderArgs a;
     FilmPtrs f;
@@ -803,7 +803,7 @@ struct DiffOne {
 // batch's table, each with its parameters and per-sample radiance
 // (SceneTable::diff), on one wavefront whose path extras are `d`.
 struct DiffMany {
-    static constexpr bool kMany = true, kDiff = true;
+    static constexpr bool kMany = true, kDiff = true, kAdj = false;
     const SceneTable *t;
     DiffWave d;
     __device__ __forceinline__ const DevScene &scene(uint32_t i) const { return t->slots[i].s; }
@@ -811,6 +811,62 @@ struct DiffMany {
     __device__ __forceinline__ const FilmPtrs &film(uint32_t i) const { return t->slots[i].f; }
     __device__ __forceinline__ const DiffParams &params(uint32_t i) const { return t->diff[i].p; }
     __device__ __forceinline__ float *samples(uint32_t i) const { return t->diff[i].sample_I; }
+    __device__ __forceinline__ unsigned long long total() const { return t->total; }
+    __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
+        uint32_t lo = 0, hi = t->count;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (t->begin[mid] <= item) lo = mid;
+            else hi = mid;
+        }
+        local = item - t->begin[lo];
+        return lo;
+    }
+};
+
+// The adjoint (lt_render_adjoint with the forward's per-sample radiance) as a
+// fourth source: DiffOne's paths replayed from their seeds over the samples of
+// a crop, with the loss gradient and the gradient arrays of g. Work item i is
+// sample i / (crop pixels) of crop pixel i % (crop pixels); a.total counts
+// them. The adjoint leaves the film alone.
+struct AdjOne {
+    static constexpr bool kMany = false, kDiff = true, kAdj = true;
+    DevScene s;
+    RenderArgs a;
+    DiffParams p;
+    DiffWave d;
+    DiffGrads g;
+    __device__ __forceinline__ const DevScene &scene(uint32_t) const { return s; }
+    __device__ __forceinline__ const RenderArgs &args(uint32_t) const { return a; }
+    __device__ __forceinline__ const DiffParams &params(uint32_t) const { return p; }
+    __device__ __forceinline__ const DiffGrads &grads(uint32_t) const { return g; }
+    __device__ __forceinline__ unsigned long long total() const { return a.total; }
+    __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
+        const uint32_t cw = g.x1 - g.x0, ch = g.y1 - g.y0;
+        if (cw == a.width && ch == a.height) {
+            local = item;
+            return 0;
+        }
+        const uint32_t ncrop = cw * ch;
+        const unsigned long long smp = item / ncrop;
+        const uint32_t k = (uint32_t)(item - smp * ncrop), y = k / cw;
+        local = smp * ((unsigned long long)a.width * a.height) + (unsigned long long)(g.y0 + y) * a.width + g.x0 +
+                (k - y * cw);
+        return 0;
+    }
+};
+
+// The batched adjoint (lt_render_adjoint_batch, every job with its per-sample
+// radiance): the whole films of a batch's table on one wavefront, work items
+// as DiffMany's.
+struct AdjMany {
+    static constexpr bool kMany = true, kDiff = true, kAdj = true;
+    const SceneTable *t;
+    DiffWave d;
+    __device__ __forceinline__ const DevScene &scene(uint32_t i) const { return t->slots[i].s; }
+    __device__ __forceinline__ const RenderArgs &args(uint32_t i) const { return t->slots[i].a; }
+    __device__ __forceinline__ const DiffParams &params(uint32_t i) const { return t->diff[i].p; }
+    __device__ __forceinline__ const DiffGrads &grads(uint32_t i) const { return t->diff[i].g; }
     __device__ __forceinline__ unsigned long long total() const { return t->total; }
     __device__ __forceinline__ uint32_t locate(unsigned long long item, unsigned long long &local) const {
         uint32_t lo = 0, hi = t->count;
@@ -875,6 +931,7 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
             st3_planes(src.d.Ts[0], W.capacity, i, p.T);
             st_s(src.d.rec[0] + i, make_uint2(kNoRecord, kNoRecord));
         }
+        if constexpr (Src::kAdj) st_s(src.d.pend[0] + i, kMiss);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters->count[0] = (uint32_t)first;
@@ -1197,6 +1254,93 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
     }
 }
 
+__device__ __forceinline__ void add3(float *g, v3 v) {
+    if (v.x != 0.0f) atomicAdd(g, v.x);
+    if (v.y != 0.0f) atomicAdd(g + 1, v.y);
+    if (v.z != 0.0f) atomicAdd(g + 2, v.z);
+}
+
+// Per-block sums of the adjoint's gradient terms in shared memory, keyed by
+// the address of the gradient triple they add to: direct mapped by a
+// multiplicative hash of the address, a slot is claimed by the first key that
+// lands on it and kept until the kernel ends. Most terms fall on a few
+// triangles (a ground quad, a light's triangles) and on the media, whose sums
+// then stay in shared memory instead of queueing at one L2 address; a term
+// whose slot holds another key goes straight to the gradient array. Every
+// block adds its sums to the gradient arrays once, at its end.
+constexpr int kGradSlotBits = 9, kGradSlots = 1 << kGradSlotBits;
+struct GradTable {
+    unsigned long long key[kGradSlots];
+    float val[3 * kGradSlots];
+};
+
+// The table of the calling kernel (one per adjoint kernel instantiation).
+template <class Src>
+__device__ __forceinline__ GradTable *grad_table() {
+    __shared__ GradTable t;
+    return &t;
+}
+
+// Every thread of the block calls it; a barrier follows before the first add.
+__device__ __forceinline__ void gt_init(GradTable *t) {
+    for (int i = threadIdx.x; i < kGradSlots; i += blockDim.x) {
+        t->key[i] = 0ull;
+        t->val[3 * i] = t->val[3 * i + 1] = t->val[3 * i + 2] = 0.0f;
+    }
+}
+
+__device__ __forceinline__ void gt_add(GradTable *t, float *g, v3 v) {
+    if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f) return;
+    const unsigned long long k = (unsigned long long)g;
+    const uint32_t s = (uint32_t)(((k >> 2) * 0x9E3779B97F4A7C15ull) >> (64 - kGradSlotBits));
+    unsigned long long held = *(volatile unsigned long long *)&t->key[s];
+    if (held == 0ull) {
+        held = atomicCAS(&t->key[s], 0ull, k);
+        if (held == 0ull) held = k;
+    }
+    if (held == k) {
+        float *val = t->val + 3 * s;
+        if (v.x != 0.0f) atomicAdd(val, v.x);
+        if (v.y != 0.0f) atomicAdd(val + 1, v.y);
+        if (v.z != 0.0f) atomicAdd(val + 2, v.z);
+    } else {
+        add3(g, v);
+    }
+}
+
+// Every thread of the block calls it, after a barrier that follows the last add.
+__device__ __forceinline__ void gt_flush(GradTable *t) {
+    for (int i = threadIdx.x; i < kGradSlots; i += blockDim.x) {
+        const unsigned long long k = t->key[i];
+        if (k) add3((float *)k, mk(t->val[3 * i], t->val[3 * i + 1], t->val[3 * i + 2]));
+    }
+}
+
+// The adjoint's inputs for sample (pixel, frame) of slot sid: the sample's
+// radiance I from the forward and delta = d loss / d film colour sum.
+template <class Src>
+__device__ __forceinline__ void adj_inputs(const Src &src, uint32_t sid, uint32_t pixel, uint32_t frame, v3 &I,
+                                           v3 &delta) {
+    const RenderArgs &A = src.args(sid);
+    const DiffGrads &G = src.grads(sid);
+    const unsigned long long item =
+        (unsigned long long)(frame - A.first_frame) * ((unsigned long long)A.width * A.height) + pixel;
+    I = mk(ld_s(G.sample_I + 3 * item), ld_s(G.sample_I + 3 * item + 1), ld_s(G.sample_I + 3 * item + 2));
+    delta = ld3(G.dI + 3 * (size_t)pixel);
+}
+
+// The albedo term of a surface bounce on triangle prim, delta * (I - C) *
+// dlog(f)/d albedo (f is linear in the albedo), once C holds the bounce's
+// connection contributions.
+template <class Src>
+__device__ __forceinline__ void albedo_term(GradTable *t, const Src &src, uint32_t sid, uint32_t prim, v3 I, v3 delta,
+                                            v3 C) {
+    const v3 R = (I - C) * delta;
+    const v3 alb = ld3(src.params(sid).albedo + 3 * prim);
+    gt_add(t, src.grads(sid).albedo + 3 * prim,
+           mk(alb.x > 0.0f ? R.x / alb.x : 0.0f, alb.y > 0.0f ? R.y / alb.y : 0.0f, alb.z > 0.0f ? R.z / alb.z : 0.0f));
+}
+
 // One bounce of the differentiable estimator (diff_path below, one bounce of
 // its loop) for every queued path, on the wavefront. It is k_shade with the
 // estimator's arithmetic: per-triangle albedo and emission, the RGB medium form
@@ -1234,6 +1378,12 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
     uint32_t n_ref_rays = 0, n_ref_rays_b = 0;
+    GradTable *gt = nullptr;
+    if constexpr (Src::kAdj) {
+        gt = grad_table<Src>();
+        gt_init(gt);
+        __syncthreads();
+    }
     for (uint32_t base = blockIdx.x * blockDim.x; base < n + nf; base += gridDim.x * blockDim.x) {
         const uint32_t q = base + threadIdx.x;
         const bool active = q < n;
@@ -1243,8 +1393,16 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             const uint4 id = ld_s(D.fin_id[cur] + e);  // pixel, frame, scene slot
             const float4 c4 = ld_s(D.fin_C[cur] + e);
             const uint2 rc = ld_s(D.fin_rec[cur] + e);
-            write_sample(src.samples(id.z), src.args(id.z), id.x, id.y,
-                         add_record(D, rc.y, add_record(D, rc.x, mk(c4.x, c4.y, c4.z))));
+            const v3 Cf = add_record(D, rc.y, add_record(D, rc.x, mk(c4.x, c4.y, c4.z)));
+            if constexpr (Src::kAdj) {  // the deferred albedo term of its last bounce
+                if (id.w != kMiss) {
+                    v3 I, delta;
+                    adj_inputs(src, id.z, id.x, id.y, I, delta);
+                    albedo_term(gt, src, id.z, id.w, I, delta, Cf);
+                }
+            } else {
+                write_sample(src.samples(id.z), src.args(id.z), id.x, id.y, Cf);
+            }
         }
         Path p;
         v3 C = mk(0, 0, 0), Ts = mk(0, 0, 0);
@@ -1256,6 +1414,11 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
         float l_pdf = 0.0f, b_pdf = 0.0f, l_tl = 0.0f, b_tl = 0.0f;
         uint32_t conn_light = 0;
         v3 conn_T = mk(0, 0, 0);
+        // adjoint: the sample's radiance and loss gradient, the triangle whose
+        // albedo term waits for this bounce's records, the BSDF sample's f / albedo
+        v3 I = mk(0, 0, 0), delta = mk(0, 0, 0);
+        uint32_t pend = kMiss, shade_prim = kMiss;
+        float b_dfa = 0.0f;
         if (active) {
             load_path(W.p[cur], cap, slot, p);
             const DevScene &S = src.scene(p.scene);
@@ -1265,11 +1428,20 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             Ts = ld3_planes(D.Ts[cur], cap, slot);
             const uint2 rc = ld_s(D.rec[cur] + slot);
             C = add_record(D, rc.y, add_record(D, rc.x, C));  // the previous bounce's light, then BSDF sample
+            bool skip = false;
+            if constexpr (Src::kAdj) {
+                adj_inputs(src, p.scene, p.pixel, p.frame, I, delta);
+                const uint32_t pp = ld_s(D.pend[cur] + slot);
+                if (pp != kMiss) albedo_term(gt, src, p.scene, pp, I, delta, C);
+                skip = is_black(delta);  // every term of the sample is 0
+            }
             const float4 hv = ld_s(W.hits + slot);
             const float4 r0 = ld_s(W.ray[cur] + 2 * slot), r1 = ld_s(W.ray[cur] + 2 * slot + 1);
             const uint32_t prim = __float_as_uint(hv.w);
             const float t = hv.x;
-            if (prim == kMiss) {
+            if (skip) {
+                done = true;
+            } else if (prim == kMiss) {
                 C = C + p.T * S.background;
                 done = true;
             } else {
@@ -1302,6 +1474,17 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                             ws = ws * (ss_d / sbar);
                         }
                     }
+                    if constexpr (Src::kAdj) {  // d log(w) / d sigma, with C before this segment's end
+                        const v3 R = (I - C) * delta;
+                        const v3 ga = R * (-dist);
+                        v3 gs = mk(0, 0, 0);
+                        if (M.type != LT_MEDIUM_NON_SCATTERING)
+                            gs = mk(R.x * (-dist + (scat ? 1.0f / ss.x : 0.0f)),
+                                    R.y * (-dist + (scat ? 1.0f / ss.y : 0.0f)),
+                                    R.z * (-dist + (scat ? 1.0f / ss.z : 0.0f)));
+                        gt_add(gt, src.grads(p.scene).sigma_a + 3 * mi, ga);
+                        gt_add(gt, src.grads(p.scene).sigma_s + 3 * mi, gs);
+                    }
                     p.T = p.T * w;
                     Ts = Ts * ws;
                     if (scat) {
@@ -1315,8 +1498,11 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                     const GeomInfo G = S.geoms[__ldg(S.tri_geom + prim)];
                     const MaterialInfo m = S.mats[G.material];
                     const v3 alb = ld3(P.albedo + 3 * prim), alb_d = ld3(P.albedo_s + 3 * prim);
-                    if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0)
+                    if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0) {
                         C = C + p.T * ld3(P.emission + 3 * prim);
+                        if constexpr (Src::kAdj) gt_add(gt, src.grads(p.scene).emission + 3 * prim, p.T * delta);
+                    }
+                    shade_prim = prim;
                     Inter it;
                     it.P = origin + direction * t;
                     it.N = G.has_normals ? normalize(interp_normal(S, prim, hv.y, hv.z)) : normalize(mk(0, 0, 0));
@@ -1368,6 +1554,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                                 emit_b = true;
                                 b_dir = c.wi;
                                 b_f = m.bsdf == LT_BSDF_LAMBERT ? (alb * kInvPi) * cosb : alb;
+                                b_dfa = m.bsdf == LT_BSDF_LAMBERT ? kInvPi * cosb : 1.0f;
                                 b_pdf = spdf;
                                 b_tl = tl;
                             }
@@ -1377,6 +1564,10 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                     const float pdf = bsdf_pdf(m, it);
                     const v3 f = m.bsdf == LT_BSDF_LAMBERT ? (alb * kInvPi) * dot(it.wi, it.N) : alb;
                     const v3 fs = m.bsdf == LT_BSDF_LAMBERT ? (alb_d * kInvPi) * dot(it.wi, it.N) : alb_d;
+                    if constexpr (Src::kAdj) {
+                        if (emit_l || emit_b) pend = prim;  // once this bounce's records are traced
+                        else albedo_term(gt, src, p.scene, prim, I, delta, C);
+                    }
                     p.T = (p.T * f) / pdf;
                     Ts = (Ts * fs) / pdf;
                     if (it.lobe == kLobeSTrans) {
@@ -1433,18 +1624,24 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             st_s(W.crec + 2 * rec_b, make_float4(b_f.x, b_f.y, b_f.z, b_pdf));
             st_s(W.crec + 2 * rec_b + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
         }
+        if constexpr (Src::kAdj) {  // what the trace stage needs for the records' gradient terms
+            if (emit_l) st_s(D.aux + rec_l, make_float2(__uint_as_float(shade_prim), l_pdf));  // f / albedo = cos / pi
+            if (emit_b) st_s(D.aux + rec_b, make_float2(__uint_as_float(shade_prim), b_dfa));
+        }
         bool regen = false;
         if (done) {
-            const FilmPtrs &F = src.film(p.scene);
-            atomicAdd(F.bounces + p.pixel, p.bounces);
-            atomicAdd(F.counts + p.pixel, 1u);
+            if constexpr (!Src::kAdj) {
+                const FilmPtrs &F = src.film(p.scene);
+                atomicAdd(F.bounces + p.pixel, p.bounces);
+                atomicAdd(F.counts + p.pixel, 1u);
+            }
             if (fin) {
                 const uint32_t e = f_base + __popc(m_f & below);
-                st_s(D.fin_id[nxt] + e, make_uint4(p.pixel, p.frame, p.scene, 0u));
+                st_s(D.fin_id[nxt] + e, make_uint4(p.pixel, p.frame, p.scene, Src::kAdj ? pend : 0u));
                 st_s(D.fin_C[nxt] + e, make_float4(C.x, C.y, C.z, 0.0f));
                 st_s(D.fin_rec[nxt] + e, make_uint2(rec_l, rec_b));
             } else {
-                write_sample(src.samples(p.scene), src.args(p.scene), p.pixel, p.frame, C);
+                if constexpr (!Src::kAdj) write_sample(src.samples(p.scene), src.args(p.scene), p.pixel, p.frame, C);
             }
         }
         const uint32_t rank_d = __popc(m_d & below);
@@ -1464,6 +1661,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             st3_planes(D.C[nxt], cap, qi, C);
             st3_planes(D.Ts[nxt], cap, qi, Ts);
             st_s(D.rec[nxt] + qi, push ? make_uint2(rec_l, rec_b) : make_uint2(kNoRecord, kNoRecord));
+            if constexpr (Src::kAdj) st_s(D.pend[nxt] + qi, push ? pend : kMiss);
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1473,6 +1671,10 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
     if ((threadIdx.x & 31u) == 0 && (n_ref_rays | n_ref_rays_b)) {
         atomicAdd(&W.counters->light_rays, (unsigned long long)n_ref_rays);
         atomicAdd(&W.counters->bsdf_rays, (unsigned long long)n_ref_rays_b);
+    }
+    if constexpr (Src::kAdj) {
+        __syncthreads();
+        gt_flush(gt);
     }
 }
 
@@ -1566,10 +1768,13 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // BSDF samples): the emission is the hit light triangle's parameter, and the
 // contribution T * ((f * Le * w) / pdf * numLights) goes to the record's result
 // slot (w = 1) for the path's next shade to add in order; a record that does
-// not contribute gets w = 0.
+// not contribute gets w = 0. The adjoint also adds the contribution's
+// derivatives: delta * T * Le * (numLights * (f / albedo) * w / pdf) to the
+// shading triangle's albedo and delta * T * f * (numLights * w / pdf) to the
+// hit light triangle's emission (gt: the block's gradient table).
 template <class Src, class State>
 __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wavefront &W, uint32_t idx,
-                                                        uint32_t kl, const State &r) {
+                                                        uint32_t kl, const State &r, GradTable *gt) {
     const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
     const DevScene &S = src.scene(sid);
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
@@ -1603,6 +1808,16 @@ __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wa
             if (!is_bsdf) c = T * ((((f * Le) * power_heuristic(lpdf, spdf)) / lpdf) * fn);
             else c = T * ((((f * Le) * power_heuristic(spdf, lpdf)) / spdf) * fn);
             out = make_float4(c.x, c.y, c.z, 1.0f);
+            if constexpr (Src::kAdj) {
+                const float2 aux = ld_s(src.d.aux + idx);  // shading triangle, f / albedo
+                const uint32_t pixel = __float_as_uint(r1.w);
+                const DiffGrads &G = src.grads(sid);
+                const v3 Td = T * ld3(G.dI + 3 * (size_t)pixel);
+                const float wgt = is_bsdf ? power_heuristic(spdf, lpdf) : power_heuristic(lpdf, spdf);
+                const float pdf = is_bsdf ? spdf : lpdf;
+                gt_add(gt, G.albedo + 3 * (size_t)__float_as_uint(aux.x), Td * (Le * (fn * aux.y * wgt / pdf)));
+                gt_add(gt, G.emission + 3 * (size_t)h.prim, Td * (f * (fn * wgt / pdf)));
+            }
         }
     }
     st_s(src.d.res + idx, out);
@@ -1629,6 +1844,12 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
         W.counters->ccount[cur] = 0;
         W.counters->fcount[cur ^ 1] = 0;  // filled by the next differentiable shade
         W.counters->main_rays += n;
+    }
+    GradTable *gt = nullptr;
+    if constexpr (Src::kAdj) {
+        gt = grad_table<Src>();
+        gt_init(gt);
+        __syncthreads();
     }
     const float4 *rays = W.ray[cur];
     Geo g = B::geo(src.scene(0));
@@ -1668,12 +1889,16 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
                      make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
-                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r);
+                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, gt);
                 else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
             }
         }
     }
     if (n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
+    if constexpr (Src::kAdj) {
+        __syncthreads();
+        gt_flush(gt);
+    }
 }
 
 // While-node condition of a captured wavefront loop (one thread): continue
@@ -1735,12 +1960,6 @@ __device__ __forceinline__ bool diff_light_visible(const DevScene &S, const Ligh
     if (tl > 0.0f) return trace_all(S, P, dir, 0.001f, tl, true, (uint32_t)L.geom).prim == kMiss;
     h = trace_all(S, P, dir, 0.001f, __int_as_float(0x7f800000), false, 0);
     return h.prim != kMiss && __ldg(S.tri_geom + h.prim) == (uint32_t)L.geom;
-}
-
-__device__ __forceinline__ void add3(float *g, v3 v) {
-    if (v.x != 0.0f) atomicAdd(g, v.x);
-    if (v.y != 0.0f) atomicAdd(g + 1, v.y);
-    if (v.z != 0.0f) atomicAdd(g + 2, v.z);
 }
 
 // Per-thread sums of gradient terms keyed by triangle (direct mapped). A
@@ -2142,6 +2361,10 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
     out->dtrace_batch_blocks = blocks_for(k_trace<DiffMany, Bvh2>, 256, sms, trav_smem<Bvh2>(256));
     out->dshade_batch_blocks = blocks_for(k_dshade<DiffMany>, 256, sms);
     out->diff_adj_batch_blocks = blocks_for(k_diff_adjoint_batch, 128, sms);
+    out->atrace_blocks = blocks_for(k_trace<AdjOne, Bvh2>, 256, sms, trav_smem<Bvh2>(256));
+    out->ashade_blocks = blocks_for(k_dshade<AdjOne>, 256, sms);
+    out->atrace_batch_blocks = blocks_for(k_trace<AdjMany, Bvh2>, 256, sms, trav_smem<Bvh2>(256));
+    out->ashade_batch_blocks = blocks_for(k_dshade<AdjMany>, 256, sms);
 }
 
 cudaError_t preload_wave_kernels() {
@@ -2182,6 +2405,36 @@ cudaError_t launch_dwave_batch_stage(int stage, const SceneTable *t, const DiffW
     if (stage == kStageTrace)
         k_trace<DiffMany, Bvh2><<<ls.dtrace_batch_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
     else k_dshade<DiffMany><<<ls.dshade_batch_blocks, 256, 0, st>>>(src, w, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_awave_init(const DevScene &s, const DiffParams &p, const DiffWave &d, const DiffGrads &g,
+                              const Wavefront &w, const RenderArgs &a, const LaunchShape &ls, cudaStream_t st) {
+    k_raygen<AdjOne><<<ls.ashade_blocks, 256, 0, st>>>(AdjOne{s, a, p, d, g}, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_awave_stage(int stage, const DevScene &s, const DiffParams &p, const DiffWave &d,
+                               const DiffGrads &g, const Wavefront &w, const RenderArgs &a, int cur,
+                               const LaunchShape &ls, cudaStream_t st) {
+    const AdjOne src{s, a, p, d, g};
+    if (stage == kStageTrace) k_trace<AdjOne, Bvh2><<<ls.atrace_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
+    else k_dshade<AdjOne><<<ls.ashade_blocks, 256, 0, st>>>(src, w, cur);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_awave_batch_init(const SceneTable *t, const DiffWave &d, const Wavefront &w, const LaunchShape &ls,
+                                    cudaStream_t st) {
+    k_raygen<AdjMany><<<ls.ashade_batch_blocks, 256, 0, st>>>(AdjMany{t, d}, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_awave_batch_stage(int stage, const SceneTable *t, const DiffWave &d, const Wavefront &w, int cur,
+                                     const LaunchShape &ls, cudaStream_t st) {
+    const AdjMany src{t, d};
+    if (stage == kStageTrace)
+        k_trace<AdjMany, Bvh2><<<ls.atrace_batch_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
+    else k_dshade<AdjMany><<<ls.ashade_batch_blocks, 256, 0, st>>>(src, w, cur);
     return cudaGetLastError();
 }
 
