@@ -401,7 +401,10 @@ lt_status lt_render_diff(lt_ctx *ctx, const lt_render_params *params, const lt_d
  * (same shapes as the parameters; not cleared). crop = {x0, y0, x1, y1} limits
  * the pixels whose samples are replayed, or NULL for the whole film.
  * sample_radiance: from lt_render_diff with the same parameters and render
- * params, or NULL (each path is then replayed twice). */
+ * params; with it the paths are replayed on the forward's wavefront (gradient
+ * terms summed per block in shared memory; returns when finished), without it
+ * (NULL) one thread replays each sample twice (returns once queued). Both
+ * forms add the same terms; only the order of the float sums differs. */
 lt_status lt_render_adjoint(lt_ctx *ctx, const lt_render_params *params, const lt_diff_params *dp,
                             const float *d_loss_d_film, float *grad_albedo, float *grad_emission,
                             float *grad_sigma_a, float *grad_sigma_s, const uint32_t *crop,
@@ -415,12 +418,15 @@ lt_status lt_render_adjoint(lt_ctx *ctx, const lt_render_params *params, const l
  *   by ctx (as lt_render_batch's); film (device, additive) and sample_radiance
  *   (optional, as lt_render_diff's) are outputs, the same bits as the
  *   single-scene call gives. Returns when the batch has finished.
- * - lt_render_adjoint_batch: one persistent launch over chunks of 8 samples
- *   of all jobs' pixels (warps take 32 chunks at a time from a shared counter,
- *   so scenes of any size and spp fill the GPU together); d_loss_d_film and
- *   sample_radiance (optional) are inputs, the four gradient arrays outputs
- *   (accumulated; sigma arrays may be NULL for scenes without media). Jobs must
- *   not share gradient arrays. Returns once the work is queued.
+ * - lt_render_adjoint_batch: d_loss_d_film and sample_radiance are inputs,
+ *   the four gradient arrays outputs (accumulated; sigma arrays may be NULL for
+ *   scenes without media). When every job brings its sample_radiance, the
+ *   samples of all jobs are replayed on one wavefront owned by ctx (as the
+ *   forward's) and the call returns when finished; otherwise it is one
+ *   persistent launch over chunks of 8 samples of all jobs' pixels (warps take
+ *   32 chunks at a time from a shared counter) that replays each sample twice,
+ *   and the call returns once the work is queued. Jobs must not share gradient
+ *   arrays.
  * n <= LT_MAX_BATCH. */
 typedef struct lt_diff_job {
     lt_ctx *scene;

@@ -1003,7 +1003,8 @@ static size_t carve_dwave(char *base, uint32_t cap, DiffWave *d) {
         d->pend[k] = (uint32_t *)take(4 * P);
     }
     d->res = (float4 *)take(32 * P);  // two connection records per path
-    d->aux = (float2 *)take(16 * P);
+    d->fa = (float *)take(8 * P);
+    d->gres = (float4 *)take(64 * P);
     d->sample_I = nullptr;
     d->bytes = off;
     return off;
@@ -1677,13 +1678,13 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
             const SceneTable *t = c->table_dev;
             if (adjoint)
                 st = run_loop(
-                    c, w, all, false, [&]() { return launch_awave_batch_init(t, dw, w, c->batch_shape, c->stream); },
+                    c, w, all, true, [&]() { return launch_awave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_awave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
                     });
             else
                 st = run_loop(
-                    c, w, all, false, [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
+                    c, w, all, true, [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_dwave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
                     });

@@ -83,7 +83,8 @@ struct Wavefront {
 // the paths that finished while their last records were still to be traced,
 // and the per-sample radiance. The adjoint also keeps, per path, the triangle
 // whose albedo term waits for the records of its bounce (pend), and per
-// record the shading triangle and the factor f / albedo of the sample (aux).
+// record the factor f / albedo of the sample (fa) and the two gradient terms
+// that the trace stage computes for the next shade to add (gres).
 constexpr uint32_t kNoRecord = 0xFFFFFFFFu;
 struct DiffWave {
     float *C[2];         // radiance gathered so far, 3 planes of capacity
@@ -94,7 +95,8 @@ struct DiffWave {
     float4 *fin_C[2];    //   radiance gathered before their last records
     uint2 *fin_rec[2];   //   those records
     uint32_t *pend[2];   // adjoint: triangle of the previous bounce's deferred albedo term, or kMiss
-    float2 *aux;         // adjoint, per connection record: (shading triangle, f / albedo)
+    float *fa;           // adjoint, per connection record: f / albedo of its sample
+    float4 *gres;        // adjoint, 2 per record: (albedo term, hit light triangle), (emission term, 0)
     float *sample_I;     // 3 floats per sample at ((frame - first_frame) * W * H + pixel)
     size_t bytes = 0;
 };

@@ -950,6 +950,7 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
 struct Slots {
     uint32_t c, q, f, r, n_regen;
     unsigned long long w;
+    uint32_t flag;  // the block's flag word as it stood once every warp had staged its counts
 };
 
 // The block's slots, reserved by one thread with one atomic per counter: each
@@ -959,13 +960,17 @@ struct Slots {
 // items and hands every warp its share (warps in order), then the camera-ray
 // entries, whose number depends on how many work items were left. Every
 // thread of the block calls it (block-uniform loops), at most 512 threads.
+// `flag` (shared, optional): a word that the block's threads set before the
+// call; every thread gets its value in Slots::flag (the same for all) and the
+// word is cleared for the next round.
 __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32_t nc, uint32_t np, uint32_t nf,
-                                               uint32_t nd, unsigned long long total) {
+                                               uint32_t nd, unsigned long long total, uint32_t *flag = nullptr) {
     const int nxt = cur ^ 1;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ uint32_t s_cnt[4][16];
     __shared__ uint32_t s_base[5][16];
     __shared__ unsigned long long s_wbase[16];
+    __shared__ uint32_t s_flag;
     if (lane == 0) {
         s_cnt[0][warp] = nc;
         s_cnt[1][warp] = np;
@@ -974,6 +979,10 @@ __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+        if (flag) {
+            s_flag = *flag;
+            *flag = 0u;
+        }
         const uint32_t nw = blockDim.x >> 5;
         uint32_t tc = 0, tp = 0, tf = 0, td = 0;
         for (uint32_t w = 0; w < nw; ++w) {
@@ -1012,6 +1021,7 @@ __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32
     r.r = s_base[3][warp];
     r.n_regen = s_base[4][warp];
     r.w = s_wbase[warp];
+    r.flag = flag ? s_flag : 0u;
     return r;
 }
 
@@ -1272,6 +1282,8 @@ constexpr int kGradSlotBits = 9, kGradSlots = 1 << kGradSlotBits;
 struct GradTable {
     unsigned long long key[kGradSlots];
     float val[3 * kGradSlots];
+    uint32_t scene;  // batched adjoint: the scene slot the table was last given to
+    uint32_t other;  // 1 + a scene slot seen since the last round, or 0
 };
 
 // The table of the calling kernel (one per adjoint kernel instantiation).
@@ -1286,6 +1298,10 @@ __device__ __forceinline__ void gt_init(GradTable *t) {
     for (int i = threadIdx.x; i < kGradSlots; i += blockDim.x) {
         t->key[i] = 0ull;
         t->val[3 * i] = t->val[3 * i + 1] = t->val[3 * i + 2] = 0.0f;
+    }
+    if (threadIdx.x == 0) {
+        t->scene = kMiss;
+        t->other = 0u;
     }
 }
 
@@ -1360,6 +1376,20 @@ __device__ __forceinline__ v3 add_record(const DiffWave &d, uint32_t rec, v3 C) 
     return v.w != 0.0f ? C + mk(v.x, v.y, v.z) : C;
 }
 
+// add_record for the adjoint: a contributing record also adds its gradient
+// terms (d.gres, from the trace stage) to the albedo of the triangle it was
+// sampled on (prim) and to the emission of the light triangle it reached.
+__device__ __forceinline__ v3 add_record_adj(const DiffWave &d, uint32_t rec, v3 C, GradTable *gt,
+                                             const DiffGrads &G, uint32_t prim) {
+    if (rec == kNoRecord) return C;
+    const float4 v = ld_s(d.res + rec);
+    if (v.w == 0.0f) return C;
+    const float4 a = ld_s(d.gres + 2 * rec), e = ld_s(d.gres + 2 * rec + 1);
+    gt_add(gt, G.albedo + 3 * (size_t)prim, mk(a.x, a.y, a.z));
+    gt_add(gt, G.emission + 3 * (size_t)__float_as_uint(a.w), mk(e.x, e.y, e.z));
+    return C + mk(v.x, v.y, v.z);
+}
+
 __device__ __forceinline__ void write_sample(float *sample_I, const RenderArgs &A, uint32_t pixel, uint32_t frame,
                                              v3 C) {
     const unsigned long long item =
@@ -1393,15 +1423,19 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             const uint4 id = ld_s(D.fin_id[cur] + e);  // pixel, frame, scene slot
             const float4 c4 = ld_s(D.fin_C[cur] + e);
             const uint2 rc = ld_s(D.fin_rec[cur] + e);
-            const v3 Cf = add_record(D, rc.y, add_record(D, rc.x, mk(c4.x, c4.y, c4.z)));
-            if constexpr (Src::kAdj) {  // the deferred albedo term of its last bounce
+            if constexpr (Src::kAdj) {  // its records' terms, then the deferred albedo term of its last bounce
+                const DiffGrads &Gr = src.grads(id.z);
+                const v3 Cf = add_record_adj(D, rc.y, add_record_adj(D, rc.x, mk(c4.x, c4.y, c4.z), gt, Gr, id.w), gt,
+                                             Gr, id.w);
+                if (Src::kMany && id.z != gt->scene) gt->other = id.z + 1u;
                 if (id.w != kMiss) {
                     v3 I, delta;
                     adj_inputs(src, id.z, id.x, id.y, I, delta);
                     albedo_term(gt, src, id.z, id.w, I, delta, Cf);
                 }
             } else {
-                write_sample(src.samples(id.z), src.args(id.z), id.x, id.y, Cf);
+                write_sample(src.samples(id.z), src.args(id.z), id.x, id.y,
+                             add_record(D, rc.y, add_record(D, rc.x, mk(c4.x, c4.y, c4.z))));
             }
         }
         Path p;
@@ -1417,7 +1451,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
         // adjoint: the sample's radiance and loss gradient, the triangle whose
         // albedo term waits for this bounce's records, the BSDF sample's f / albedo
         v3 I = mk(0, 0, 0), delta = mk(0, 0, 0);
-        uint32_t pend = kMiss, shade_prim = kMiss;
+        uint32_t pend = kMiss;
         float b_dfa = 0.0f;
         if (active) {
             load_path(W.p[cur], cap, slot, p);
@@ -1427,13 +1461,17 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             C = ld3_planes(D.C[cur], cap, slot);
             Ts = ld3_planes(D.Ts[cur], cap, slot);
             const uint2 rc = ld_s(D.rec[cur] + slot);
-            C = add_record(D, rc.y, add_record(D, rc.x, C));  // the previous bounce's light, then BSDF sample
             bool skip = false;
             if constexpr (Src::kAdj) {
                 adj_inputs(src, p.scene, p.pixel, p.frame, I, delta);
-                const uint32_t pp = ld_s(D.pend[cur] + slot);
+                const uint32_t pp = ld_s(D.pend[cur] + slot);  // the previous bounce's triangle
+                const DiffGrads &Gr = src.grads(p.scene);
+                C = add_record_adj(D, rc.y, add_record_adj(D, rc.x, C, gt, Gr, pp), gt, Gr, pp);
                 if (pp != kMiss) albedo_term(gt, src, p.scene, pp, I, delta, C);
+                if (Src::kMany && p.scene != gt->scene) gt->other = p.scene + 1u;
                 skip = is_black(delta);  // every term of the sample is 0
+            } else {
+                C = add_record(D, rc.y, add_record(D, rc.x, C));  // the previous bounce's light, then BSDF sample
             }
             const float4 hv = ld_s(W.hits + slot);
             const float4 r0 = ld_s(W.ray[cur] + 2 * slot), r1 = ld_s(W.ray[cur] + 2 * slot + 1);
@@ -1502,7 +1540,6 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                         C = C + p.T * ld3(P.emission + 3 * prim);
                         if constexpr (Src::kAdj) gt_add(gt, src.grads(p.scene).emission + 3 * prim, p.T * delta);
                     }
-                    shade_prim = prim;
                     Inter it;
                     it.P = origin + direction * t;
                     it.N = G.has_normals ? normalize(interp_normal(S, prim, hv.y, hv.z)) : normalize(mk(0, 0, 0));
@@ -1605,7 +1642,19 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
         const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
         const unsigned m_f = __ballot_sync(0xFFFFFFFFu, fin);
         const Slots sl = reserve_block(W.counters, cur, __popc(m_l) + __popc(m_b), __popc(m_p), __popc(m_f),
-                                       __popc(m_d), src.total());
+                                       __popc(m_d), src.total(), Src::kAdj && Src::kMany ? &gt->other : nullptr);
+        if constexpr (Src::kAdj && Src::kMany) {
+            // paths of another scene came: the table's sums go to the gradient
+            // arrays and its slots to the new scene's triangles (a block-uniform
+            // decision; every add of this round is done)
+            if (sl.flag != 0u) {
+                gt_flush(gt);
+                __syncthreads();
+                gt_init(gt);
+                if (threadIdx.x == 0) gt->scene = sl.flag - 1u;
+                __syncthreads();
+            }
+        }
         const uint32_t c_base = sl.c, q_base = sl.q, f_base = sl.f, r_base = sl.r, n_regen = sl.n_regen;
         const unsigned long long w_base = sl.w;
         const uint32_t rec_l = emit_l ? c_base + __popc(m_l & below) : kNoRecord;
@@ -1624,9 +1673,9 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             st_s(W.crec + 2 * rec_b, make_float4(b_f.x, b_f.y, b_f.z, b_pdf));
             st_s(W.crec + 2 * rec_b + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
         }
-        if constexpr (Src::kAdj) {  // what the trace stage needs for the records' gradient terms
-            if (emit_l) st_s(D.aux + rec_l, make_float2(__uint_as_float(shade_prim), l_pdf));  // f / albedo = cos / pi
-            if (emit_b) st_s(D.aux + rec_b, make_float2(__uint_as_float(shade_prim), b_dfa));
+        if constexpr (Src::kAdj) {  // f / albedo of each record's sample, for its gradient terms
+            if (emit_l) st_s(D.fa + rec_l, l_pdf);  // cos / pi
+            if (emit_b) st_s(D.fa + rec_b, b_dfa);
         }
         bool regen = false;
         if (done) {
@@ -1768,13 +1817,14 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // BSDF samples): the emission is the hit light triangle's parameter, and the
 // contribution T * ((f * Le * w) / pdf * numLights) goes to the record's result
 // slot (w = 1) for the path's next shade to add in order; a record that does
-// not contribute gets w = 0. The adjoint also adds the contribution's
-// derivatives: delta * T * Le * (numLights * (f / albedo) * w / pdf) to the
-// shading triangle's albedo and delta * T * f * (numLights * w / pdf) to the
-// hit light triangle's emission (gt: the block's gradient table).
+// not contribute gets w = 0. For the adjoint, a contributing record also gets
+// the contribution's derivatives in d.gres, which the path's next shade adds:
+// delta * T * Le * (numLights * (f / albedo) * w / pdf) for the shading
+// triangle's albedo and delta * T * f * (numLights * w / pdf) for the emission
+// of the light triangle hit.
 template <class Src, class State>
 __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wavefront &W, uint32_t idx,
-                                                        uint32_t kl, const State &r, GradTable *gt) {
+                                                        uint32_t kl, const State &r) {
     const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
     const DevScene &S = src.scene(sid);
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
@@ -1809,14 +1859,14 @@ __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wa
             else c = T * ((((f * Le) * power_heuristic(spdf, lpdf)) / spdf) * fn);
             out = make_float4(c.x, c.y, c.z, 1.0f);
             if constexpr (Src::kAdj) {
-                const float2 aux = ld_s(src.d.aux + idx);  // shading triangle, f / albedo
+                const float fa = ld_s(src.d.fa + idx);  // f / albedo
                 const uint32_t pixel = __float_as_uint(r1.w);
-                const DiffGrads &G = src.grads(sid);
-                const v3 Td = T * ld3(G.dI + 3 * (size_t)pixel);
+                const v3 Td = T * ld3(src.grads(sid).dI + 3 * (size_t)pixel);
                 const float wgt = is_bsdf ? power_heuristic(spdf, lpdf) : power_heuristic(lpdf, spdf);
                 const float pdf = is_bsdf ? spdf : lpdf;
-                gt_add(gt, G.albedo + 3 * (size_t)__float_as_uint(aux.x), Td * (Le * (fn * aux.y * wgt / pdf)));
-                gt_add(gt, G.emission + 3 * (size_t)h.prim, Td * (f * (fn * wgt / pdf)));
+                const v3 ga = Td * (Le * (fn * fa * wgt / pdf)), ge = Td * (f * (fn * wgt / pdf));
+                st_s(src.d.gres + 2 * idx, make_float4(ga.x, ga.y, ga.z, __uint_as_float(h.prim)));
+                st_s(src.d.gres + 2 * idx + 1, make_float4(ge.x, ge.y, ge.z, 0.0f));
             }
         }
     }
@@ -1844,12 +1894,6 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
         W.counters->ccount[cur] = 0;
         W.counters->fcount[cur ^ 1] = 0;  // filled by the next differentiable shade
         W.counters->main_rays += n;
-    }
-    GradTable *gt = nullptr;
-    if constexpr (Src::kAdj) {
-        gt = grad_table<Src>();
-        gt_init(gt);
-        __syncthreads();
     }
     const float4 *rays = W.ray[cur];
     Geo g = B::geo(src.scene(0));
@@ -1889,16 +1933,12 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
                      make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
-                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, gt);
+                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r);
                 else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
             }
         }
     }
     if (n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
-    if constexpr (Src::kAdj) {
-        __syncthreads();
-        gt_flush(gt);
-    }
 }
 
 // While-node condition of a captured wavefront loop (one thread): continue
