@@ -1003,7 +1003,7 @@ static size_t carve_dwave(char *base, uint32_t cap, DiffWave *d) {
         d->pend[k] = (uint32_t *)take(4 * P);
     }
     d->res = (float4 *)take(32 * P);  // two connection records per path
-    d->fa = (float *)take(8 * P);
+    d->aux = (float2 *)take(16 * P);
     d->gres = (float4 *)take(64 * P);
     d->sample_I = nullptr;
     d->bytes = off;

@@ -82,9 +82,10 @@ struct Wavefront {
 // (ping-pong in queue order like it), the result of every connection record,
 // the paths that finished while their last records were still to be traced,
 // and the per-sample radiance. The adjoint also keeps, per path, the triangle
-// whose albedo term waits for the records of its bounce (pend), and per
-// record the factor f / albedo of the sample (fa) and the two gradient terms
-// that the trace stage computes for the next shade to add (gres).
+// whose albedo term waits for the records of its bounce (pend), per record the
+// triangle it was sampled on and the factor f / albedo of the sample (aux),
+// and, in its batched form, the two gradient terms that the trace stage
+// computes for the next shade to add (gres).
 constexpr uint32_t kNoRecord = 0xFFFFFFFFu;
 struct DiffWave {
     float *C[2];         // radiance gathered so far, 3 planes of capacity
@@ -95,8 +96,8 @@ struct DiffWave {
     float4 *fin_C[2];    //   radiance gathered before their last records
     uint2 *fin_rec[2];   //   those records
     uint32_t *pend[2];   // adjoint: triangle of the previous bounce's deferred albedo term, or kMiss
-    float *fa;           // adjoint, per connection record: f / albedo of its sample
-    float4 *gres;        // adjoint, 2 per record: (albedo term, hit light triangle), (emission term, 0)
+    float2 *aux;         // adjoint, per connection record: (shading triangle, f / albedo of its sample)
+    float4 *gres;        // batched adjoint, 2 per record: (albedo term, light triangle hit), (emission term, 0)
     float *sample_I;     // 3 floats per sample at ((frame - first_frame) * W * H + pixel)
     size_t bytes = 0;
 };

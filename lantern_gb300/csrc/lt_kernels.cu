@@ -1376,9 +1376,9 @@ __device__ __forceinline__ v3 add_record(const DiffWave &d, uint32_t rec, v3 C) 
     return v.w != 0.0f ? C + mk(v.x, v.y, v.z) : C;
 }
 
-// add_record for the adjoint: a contributing record also adds its gradient
-// terms (d.gres, from the trace stage) to the albedo of the triangle it was
-// sampled on (prim) and to the emission of the light triangle it reached.
+// add_record for the batched adjoint: a contributing record also adds its
+// gradient terms (d.gres, from the trace stage) to the albedo of the triangle
+// it was sampled on (prim) and to the emission of the light triangle it reached.
 __device__ __forceinline__ v3 add_record_adj(const DiffWave &d, uint32_t rec, v3 C, GradTable *gt,
                                              const DiffGrads &G, uint32_t prim) {
     if (rec == kNoRecord) return C;
@@ -1423,10 +1423,11 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             const uint4 id = ld_s(D.fin_id[cur] + e);  // pixel, frame, scene slot
             const float4 c4 = ld_s(D.fin_C[cur] + e);
             const uint2 rc = ld_s(D.fin_rec[cur] + e);
-            if constexpr (Src::kAdj) {  // its records' terms, then the deferred albedo term of its last bounce
+            if constexpr (Src::kAdj) {  // its records (and their terms), then its last bounce's albedo term
                 const DiffGrads &Gr = src.grads(id.z);
-                const v3 Cf = add_record_adj(D, rc.y, add_record_adj(D, rc.x, mk(c4.x, c4.y, c4.z), gt, Gr, id.w), gt,
-                                             Gr, id.w);
+                const v3 C4 = mk(c4.x, c4.y, c4.z);
+                const v3 Cf = Src::kMany ? add_record_adj(D, rc.y, add_record_adj(D, rc.x, C4, gt, Gr, id.w), gt, Gr, id.w)
+                                         : add_record(D, rc.y, add_record(D, rc.x, C4));
                 if (Src::kMany && id.z != gt->scene) gt->other = id.z + 1u;
                 if (id.w != kMiss) {
                     v3 I, delta;
@@ -1451,7 +1452,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
         // adjoint: the sample's radiance and loss gradient, the triangle whose
         // albedo term waits for this bounce's records, the BSDF sample's f / albedo
         v3 I = mk(0, 0, 0), delta = mk(0, 0, 0);
-        uint32_t pend = kMiss;
+        uint32_t pend = kMiss, shade_prim = kMiss;
         float b_dfa = 0.0f;
         if (active) {
             load_path(W.p[cur], cap, slot, p);
@@ -1466,7 +1467,8 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                 adj_inputs(src, p.scene, p.pixel, p.frame, I, delta);
                 const uint32_t pp = ld_s(D.pend[cur] + slot);  // the previous bounce's triangle
                 const DiffGrads &Gr = src.grads(p.scene);
-                C = add_record_adj(D, rc.y, add_record_adj(D, rc.x, C, gt, Gr, pp), gt, Gr, pp);
+                C = Src::kMany ? add_record_adj(D, rc.y, add_record_adj(D, rc.x, C, gt, Gr, pp), gt, Gr, pp)
+                               : add_record(D, rc.y, add_record(D, rc.x, C));
                 if (pp != kMiss) albedo_term(gt, src, p.scene, pp, I, delta, C);
                 if (Src::kMany && p.scene != gt->scene) gt->other = p.scene + 1u;
                 skip = is_black(delta);  // every term of the sample is 0
@@ -1540,6 +1542,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                         C = C + p.T * ld3(P.emission + 3 * prim);
                         if constexpr (Src::kAdj) gt_add(gt, src.grads(p.scene).emission + 3 * prim, p.T * delta);
                     }
+                    shade_prim = prim;
                     Inter it;
                     it.P = origin + direction * t;
                     it.N = G.has_normals ? normalize(interp_normal(S, prim, hv.y, hv.z)) : normalize(mk(0, 0, 0));
@@ -1673,9 +1676,9 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             st_s(W.crec + 2 * rec_b, make_float4(b_f.x, b_f.y, b_f.z, b_pdf));
             st_s(W.crec + 2 * rec_b + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
         }
-        if constexpr (Src::kAdj) {  // f / albedo of each record's sample, for its gradient terms
-            if (emit_l) st_s(D.fa + rec_l, l_pdf);  // cos / pi
-            if (emit_b) st_s(D.fa + rec_b, b_dfa);
+        if constexpr (Src::kAdj) {  // what the trace stage needs for the records' gradient terms
+            if (emit_l) st_s(D.aux + rec_l, make_float2(__uint_as_float(shade_prim), l_pdf));  // f / albedo = cos / pi
+            if (emit_b) st_s(D.aux + rec_b, make_float2(__uint_as_float(shade_prim), b_dfa));
         }
         bool regen = false;
         if (done) {
@@ -1817,14 +1820,16 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // BSDF samples): the emission is the hit light triangle's parameter, and the
 // contribution T * ((f * Le * w) / pdf * numLights) goes to the record's result
 // slot (w = 1) for the path's next shade to add in order; a record that does
-// not contribute gets w = 0. For the adjoint, a contributing record also gets
-// the contribution's derivatives in d.gres, which the path's next shade adds:
-// delta * T * Le * (numLights * (f / albedo) * w / pdf) for the shading
-// triangle's albedo and delta * T * f * (numLights * w / pdf) for the emission
-// of the light triangle hit.
+// not contribute gets w = 0. For the adjoint, a contributing record also
+// yields the contribution's derivatives: delta * T * Le * (numLights * (f /
+// albedo) * w / pdf) for the shading triangle's albedo and delta * T * f *
+// (numLights * w / pdf) for the emission of the light triangle hit. The
+// single-scene adjoint adds them to its block's gradient table gt here; the
+// batched one writes them to d.gres for the path's next shade to add (its
+// table follows the scenes, which only the shade's block-uniform rounds allow).
 template <class Src, class State>
 __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wavefront &W, uint32_t idx,
-                                                        uint32_t kl, const State &r) {
+                                                        uint32_t kl, const State &r, GradTable *gt) {
     const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
     const DevScene &S = src.scene(sid);
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
@@ -1859,14 +1864,20 @@ __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wa
             else c = T * ((((f * Le) * power_heuristic(spdf, lpdf)) / spdf) * fn);
             out = make_float4(c.x, c.y, c.z, 1.0f);
             if constexpr (Src::kAdj) {
-                const float fa = ld_s(src.d.fa + idx);  // f / albedo
+                const float2 aux = ld_s(src.d.aux + idx);  // shading triangle, f / albedo
                 const uint32_t pixel = __float_as_uint(r1.w);
-                const v3 Td = T * ld3(src.grads(sid).dI + 3 * (size_t)pixel);
+                const DiffGrads &G = src.grads(sid);
+                const v3 Td = T * ld3(G.dI + 3 * (size_t)pixel);
                 const float wgt = is_bsdf ? power_heuristic(spdf, lpdf) : power_heuristic(lpdf, spdf);
                 const float pdf = is_bsdf ? spdf : lpdf;
-                const v3 ga = Td * (Le * (fn * fa * wgt / pdf)), ge = Td * (f * (fn * wgt / pdf));
-                st_s(src.d.gres + 2 * idx, make_float4(ga.x, ga.y, ga.z, __uint_as_float(h.prim)));
-                st_s(src.d.gres + 2 * idx + 1, make_float4(ge.x, ge.y, ge.z, 0.0f));
+                const v3 ga = Td * (Le * (fn * aux.y * wgt / pdf)), ge = Td * (f * (fn * wgt / pdf));
+                if constexpr (Src::kMany) {
+                    st_s(src.d.gres + 2 * idx, make_float4(ga.x, ga.y, ga.z, __uint_as_float(h.prim)));
+                    st_s(src.d.gres + 2 * idx + 1, make_float4(ge.x, ge.y, ge.z, 0.0f));
+                } else {
+                    gt_add(gt, G.albedo + 3 * (size_t)__float_as_uint(aux.x), ga);
+                    gt_add(gt, G.emission + 3 * (size_t)h.prim, ge);
+                }
             }
         }
     }
@@ -1894,6 +1905,12 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
         W.counters->ccount[cur] = 0;
         W.counters->fcount[cur ^ 1] = 0;  // filled by the next differentiable shade
         W.counters->main_rays += n;
+    }
+    GradTable *gt = nullptr;  // the single-scene adjoint's connection terms
+    if constexpr (Src::kAdj && !Src::kMany) {
+        gt = grad_table<Src>();
+        gt_init(gt);
+        __syncthreads();
     }
     const float4 *rays = W.ray[cur];
     Geo g = B::geo(src.scene(0));
@@ -1933,12 +1950,16 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
                      make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
-                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r);
+                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, gt);
                 else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
             }
         }
     }
     if (n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
+    if constexpr (Src::kAdj && !Src::kMany) {
+        __syncthreads();
+        gt_flush(gt);
+    }
 }
 
 // While-node condition of a captured wavefront loop (one thread): continue
