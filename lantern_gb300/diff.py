@@ -189,8 +189,9 @@ def adjoint_batch(scenes, params, d_loss_d_sum, spp, first_frame=0, max_depth: i
                   samples=None):
     """lt_render_adjoint_batch: per scene the gradients (albedo, emission,
     sigma_a, sigma_s) of the loss whose derivative with respect to the film
-    colour sums is d_loss_d_sum[k], in one launch. samples: per-scene
-    per-sample radiance from render_batch(keep_samples=True), or None."""
+    colour sums is d_loss_d_sum[k], in one call. samples: per-scene
+    per-sample radiance from render_batch(keep_samples=True) (the paths are
+    then replayed on the wavefront), or None."""
     n = len(scenes)
     per = lambda v: list(v) if isinstance(v, (list, tuple)) else [v] * n
     spp, first_frame, max_depth, rr_depth = per(spp), per(first_frame), per(max_depth), per(rr_depth)

@@ -157,3 +157,27 @@ def test_batch_with_textures_and_procedural_primitives(scene_dir):
               _load(scene_dir, S.procedural_scene(width=32, height=24, name="bt_proc")),
               _load(scene_dir, S.tiny_scene(width=24, height=20, name="bt_tiny2"))]
     _check_batch(scenes, [3, 4, 2], [8, 8, 6], [2, 9, 0])
+
+
+def test_adjoint_batch_with_a_job_that_runs_alone(scene_dir):
+    """lt_render_adjoint_batch replays a job of 2^24 samples or more (here
+    512x512 at 64 spp) on its own wavefront and the other jobs together on
+    one: every job's gradients equal its single-scene adjoint's (up to the
+    order of the float sums)."""
+    from lantern_gb300.diff import DiffScene, adjoint_batch, render_batch
+    big = DiffScene(S.differentiable_scene(width=512, height=512, slices=16, stacks=8, name="ba_big").write(scene_dir))
+    s1 = DiffScene(S.tiny_scene(width=40, height=32, name="ba_tiny").write(scene_dir))
+    s2 = DiffScene(S.medium_sphere_scene(width=32, height=24, name="ba_med").write(scene_dir))
+    scenes, spp = [s1, big, s2], [3, 64, 2]
+    assert big.width * big.height * spp[1] >= 1 << 24
+    params = [sc.defaults() for sc in scenes]
+    outs = render_batch(scenes, params, spp, 0, max_depth=6, rr_depth=3, keep_samples=True)
+    g = torch.Generator(device="cuda:0").manual_seed(5)
+    dI = [torch.rand((sc.height, sc.width, 3), generator=g, device="cuda:0") - 0.5 for sc in scenes]
+    gb = adjoint_batch(scenes, params, dI, spp, 0, 6, 3, samples=[o[3] for o in outs])
+    for k, sc in enumerate(scenes):
+        gs = sc.adjoint(*params[k], dI[k], spp[k], 0, 6, 3, samples=outs[k][3])
+        for x, y in zip(gb[k], gs):
+            scale = float(y.abs().max()) + 1e-30
+            assert float((x - y).abs().max()) <= 1e-4 * scale, (k, float((x - y).abs().max()) / scale)
+        assert float(gb[k][0].abs().max()) > 0
