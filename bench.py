@@ -269,6 +269,10 @@ def main():
                     help="also time lt_intersect on 16,777,216 random rays of the same mesh")
     ap.add_argument("--adjoint", action=argparse.BooleanOptionalAction, default=True,
                     help="also time the path-replay adjoint on the differentiable workload")
+    ap.add_argument("--adjoint-spp", type=int, default=32,
+                    help="samples per pixel of the differentiable workload (small cases for profiling)")
+    ap.add_argument("--fd-check", action=argparse.BooleanOptionalAction, default=True,
+                    help="with --adjoint: check 64 gradients against central differences (after the timings)")
     ap.add_argument("--spp", type=int, default=None,
                     help="override the workload's samples per pixel (small cases for profiling)")
     ap.add_argument("--paths-in-flight", type=int, default=None,
@@ -383,7 +387,7 @@ def main():
     if args.microbench and args.workload == "icosphere-1.3M":
         micro = microbench(scene, path, local)
     scene.ctx.trim()  # the headline render's buffers (the whole render in flight) go back
-    adjoint = adjoint_bench(local) if args.adjoint else None
+    adjoint = adjoint_bench(local, args.fd_check, args.adjoint_spp) if args.adjoint else None
     batch = batch_bench(local) if args.batch else None
 
     line = None
@@ -438,8 +442,8 @@ def main():
         dist.destroy_process_group()
 
 
-def adjoint_bench(local):
-    """Differentiable workload: nine spheres + HG medium sphere, 512x512, 32 spp,
+def adjoint_bench(local, fd_check=True, spp=32):
+    """Differentiable workload: nine spheres + HG medium sphere, 512x512, `spp` (32),
     depth 8. Times the plain forward render (wavefront), the differentiable
     forward that keeps per-sample radiance, and the path-replay adjoint of the
     L2 loss to the true-parameter image; grads/s = full gradients per second."""
@@ -461,7 +465,7 @@ def adjoint_bench(local):
     with torch.no_grad():
         target = render_image(ds, torch.from_numpy(true["albedo"]).to(dev), e0,
                               torch.from_numpy(true["sigma_a"]).to(dev), torch.from_numpy(true["sigma_s"]).to(dev),
-                              32, 0, 8, 3)
+                              spp, 0, 8, 3)
 
     def timed(f, n=3):
         f()
@@ -475,28 +479,31 @@ def adjoint_bench(local):
         e1_.synchronize()
         return e0_.elapsed_time(e1_) / n
 
-    fwd = timed(lambda: it.RenderFrame(32))
+    fwd = timed(lambda: it.RenderFrame(spp))
     out = {}
-    dfw = timed(lambda: out.update(r=ds.render(*th, 32, 0, 8, 3, keep_samples=True)))
+    dfw = timed(lambda: out.update(r=ds.render(*th, spp, 0, 8, 3, keep_samples=True)))
     rgb, _, _, samples = out["r"]
-    dI = (2.0 * (rgb / 32 - target) / 32).contiguous()
-    adj = timed(lambda: ds.adjoint(*th, dI, 32, 0, 8, 3, samples=samples))
+    dI = (2.0 * (rgb / spp - target) / spp).contiguous()
+    adj = timed(lambda: ds.adjoint(*th, dI, spp, 0, 8, 3, samples=samples))
     nparams = 6 * ds.num_triangles + 6 * ds.num_media
     # acceptance check of the gradients (outside the timings): 64 parameters
     # (seed 4) against central differences, h = 1e-3
-    from lantern_gb300.diff import finite_difference_check
-    fdc = finite_difference_check(ds, th, target, 32, max_depth=8, count=64, seed=4, h=1e-3)
+    fdc = None
+    if fd_check:
+        from lantern_gb300.diff import finite_difference_check
+        fdc = finite_difference_check(ds, th, target, spp, max_depth=8, count=64, seed=4, h=1e-3)
     step = dfw + adj
-    return {"config": "differentiable scene 512x512, 32 spp, depth 8", "parameters": nparams,
+    return {"config": f"differentiable scene 512x512, {spp} spp, depth 8", "parameters": nparams,
             "forward_ms": round(fwd, 3), "diff_forward_ms": round(dfw, 3), "adjoint_ms": round(adj, 3),
             "adjoint_over_forward": round(adj / fwd, 3), "grads_per_s": round(1e3 / adj, 2),
             "step_ms": round(step, 3), "step_over_forward": round(step / fwd, 3),
             "grads_per_s_step": round(1e3 / step, 2),
             "ratios": "adjoint_over_forward: adjoint pass / plain forward render; step_over_forward: "
                       "(differentiable forward + adjoint) / plain forward render",
-            "fd_check": {"parameters": fdc["parameters"], "checked": fdc["checked"],
-                         "max_rel_err": round(fdc["max_rel_err"], 5), "h": 1e-3, "seed": 4,
-                         "within_2pct": not fdc["failures"]}}
+            "fd_check": None if fdc is None else {
+                "parameters": fdc["parameters"], "checked": fdc["checked"],
+                "max_rel_err": round(fdc["max_rel_err"], 5), "h": 1e-3, "seed": 4,
+                "within_2pct": not fdc["failures"]}}
 
 
 def batch_bench(local, count=64, reps=3):
