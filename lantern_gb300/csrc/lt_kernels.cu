@@ -1273,63 +1273,70 @@ __device__ __forceinline__ void add3(float *g, v3 v) {
 // Per-block sums of the adjoint's gradient terms in shared memory, keyed by
 // the address of the gradient triple they add to: direct mapped by a
 // multiplicative hash of the address, a slot is claimed by the first key that
-// lands on it and kept until the kernel ends. Most terms fall on a few
-// triangles (a ground quad, a light's triangles) and on the media, whose sums
-// then stay in shared memory instead of queueing at one L2 address; a term
-// whose slot holds another key goes straight to the gradient array. Every
-// block adds its sums to the gradient arrays once, at its end.
-constexpr int kGradSlotBits = 9, kGradSlots = 1 << kGradSlotBits;
+// lands on it and kept until the kernel ends (or, in the batched shade, until
+// the table moves to a new scene). Most terms fall on a few triangles (a
+// ground quad, a light's triangles) and on the media, whose sums then stay in
+// shared memory instead of queueing at one L2 address; a term whose slot holds
+// another key goes straight to the gradient array. Every block adds its sums
+// to the gradient arrays once, at its end. 2^kBits slots: the fewer, the more
+// L1 the kernel keeps (measured: 256 slots 2% faster than 512 on the whole
+// adjoint, 1024 slower still).
+template <int kBits>
 struct GradTable {
-    unsigned long long key[kGradSlots];
-    float val[3 * kGradSlots];
+    static constexpr int kSlots = 1 << kBits;
+    unsigned long long key[kSlots];
+    float val[3 * kSlots];
     uint32_t scene;  // batched adjoint: the scene slot the table was last given to
     uint32_t other;  // 1 + a scene slot seen since the last round, or 0
+
+    // Every thread of the block calls it; a barrier follows before the first add.
+    __device__ __forceinline__ void init() {
+        for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
+            key[i] = 0ull;
+            val[3 * i] = val[3 * i + 1] = val[3 * i + 2] = 0.0f;
+        }
+        if (threadIdx.x == 0) {
+            scene = kMiss;
+            other = 0u;
+        }
+    }
+
+    __device__ __forceinline__ void add(float *g, v3 v) {
+        if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f) return;
+        const unsigned long long k = (unsigned long long)g;
+        const uint32_t s = (uint32_t)(((k >> 2) * 0x9E3779B97F4A7C15ull) >> (64 - kBits));
+        unsigned long long held = *(volatile unsigned long long *)&key[s];
+        if (held == 0ull) {
+            held = atomicCAS(&key[s], 0ull, k);
+            if (held == 0ull) held = k;
+        }
+        if (held == k) {
+            float *vs = val + 3 * s;
+            if (v.x != 0.0f) atomicAdd(vs, v.x);
+            if (v.y != 0.0f) atomicAdd(vs + 1, v.y);
+            if (v.z != 0.0f) atomicAdd(vs + 2, v.z);
+        } else {
+            add3(g, v);
+        }
+    }
+
+    // Every thread of the block calls it, after a barrier that follows the last add.
+    __device__ __forceinline__ void flush() {
+        for (int i = threadIdx.x; i < kSlots; i += blockDim.x) {
+            const unsigned long long k = key[i];
+            if (k) add3((float *)k, mk(val[3 * i], val[3 * i + 1], val[3 * i + 2]));
+        }
+    }
 };
+constexpr int kTraceGradBits = 8, kShadeGradBits = 8;
+using TraceGrads = GradTable<kTraceGradBits>;
+using ShadeGrads = GradTable<kShadeGradBits>;
 
 // The table of the calling kernel (one per adjoint kernel instantiation).
-template <class Src>
-__device__ __forceinline__ GradTable *grad_table() {
-    __shared__ GradTable t;
+template <class Src, class T>
+__device__ __forceinline__ T *grad_table() {
+    __shared__ T t;
     return &t;
-}
-
-// Every thread of the block calls it; a barrier follows before the first add.
-__device__ __forceinline__ void gt_init(GradTable *t) {
-    for (int i = threadIdx.x; i < kGradSlots; i += blockDim.x) {
-        t->key[i] = 0ull;
-        t->val[3 * i] = t->val[3 * i + 1] = t->val[3 * i + 2] = 0.0f;
-    }
-    if (threadIdx.x == 0) {
-        t->scene = kMiss;
-        t->other = 0u;
-    }
-}
-
-__device__ __forceinline__ void gt_add(GradTable *t, float *g, v3 v) {
-    if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f) return;
-    const unsigned long long k = (unsigned long long)g;
-    const uint32_t s = (uint32_t)(((k >> 2) * 0x9E3779B97F4A7C15ull) >> (64 - kGradSlotBits));
-    unsigned long long held = *(volatile unsigned long long *)&t->key[s];
-    if (held == 0ull) {
-        held = atomicCAS(&t->key[s], 0ull, k);
-        if (held == 0ull) held = k;
-    }
-    if (held == k) {
-        float *val = t->val + 3 * s;
-        if (v.x != 0.0f) atomicAdd(val, v.x);
-        if (v.y != 0.0f) atomicAdd(val + 1, v.y);
-        if (v.z != 0.0f) atomicAdd(val + 2, v.z);
-    } else {
-        add3(g, v);
-    }
-}
-
-// Every thread of the block calls it, after a barrier that follows the last add.
-__device__ __forceinline__ void gt_flush(GradTable *t) {
-    for (int i = threadIdx.x; i < kGradSlots; i += blockDim.x) {
-        const unsigned long long k = t->key[i];
-        if (k) add3((float *)k, mk(t->val[3 * i], t->val[3 * i + 1], t->val[3 * i + 2]));
-    }
 }
 
 // The adjoint's inputs for sample (pixel, frame) of slot sid: the sample's
@@ -1349,11 +1356,11 @@ __device__ __forceinline__ void adj_inputs(const Src &src, uint32_t sid, uint32_
 // dlog(f)/d albedo (f is linear in the albedo), once C holds the bounce's
 // connection contributions.
 template <class Src>
-__device__ __forceinline__ void albedo_term(GradTable *t, const Src &src, uint32_t sid, uint32_t prim, v3 I, v3 delta,
+__device__ __forceinline__ void albedo_term(ShadeGrads *t, const Src &src, uint32_t sid, uint32_t prim, v3 I, v3 delta,
                                             v3 C) {
     const v3 R = (I - C) * delta;
     const v3 alb = ld3(src.params(sid).albedo + 3 * prim);
-    gt_add(t, src.grads(sid).albedo + 3 * prim,
+    t->add(src.grads(sid).albedo + 3 * prim,
            mk(alb.x > 0.0f ? R.x / alb.x : 0.0f, alb.y > 0.0f ? R.y / alb.y : 0.0f, alb.z > 0.0f ? R.z / alb.z : 0.0f));
 }
 
@@ -1379,14 +1386,14 @@ __device__ __forceinline__ v3 add_record(const DiffWave &d, uint32_t rec, v3 C) 
 // add_record for the batched adjoint: a contributing record also adds its
 // gradient terms (d.gres, from the trace stage) to the albedo of the triangle
 // it was sampled on (prim) and to the emission of the light triangle it reached.
-__device__ __forceinline__ v3 add_record_adj(const DiffWave &d, uint32_t rec, v3 C, GradTable *gt,
+__device__ __forceinline__ v3 add_record_adj(const DiffWave &d, uint32_t rec, v3 C, ShadeGrads *gt,
                                              const DiffGrads &G, uint32_t prim) {
     if (rec == kNoRecord) return C;
     const float4 v = ld_s(d.res + rec);
     if (v.w == 0.0f) return C;
     const float4 a = ld_s(d.gres + 2 * rec), e = ld_s(d.gres + 2 * rec + 1);
-    gt_add(gt, G.albedo + 3 * (size_t)prim, mk(a.x, a.y, a.z));
-    gt_add(gt, G.emission + 3 * (size_t)__float_as_uint(a.w), mk(e.x, e.y, e.z));
+    gt->add(G.albedo + 3 * (size_t)prim, mk(a.x, a.y, a.z));
+    gt->add(G.emission + 3 * (size_t)__float_as_uint(a.w), mk(e.x, e.y, e.z));
     return C + mk(v.x, v.y, v.z);
 }
 
@@ -1408,10 +1415,10 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
     uint32_t n_ref_rays = 0, n_ref_rays_b = 0;
-    GradTable *gt = nullptr;
+    ShadeGrads *gt = nullptr;
     if constexpr (Src::kAdj) {
-        gt = grad_table<Src>();
-        gt_init(gt);
+        gt = grad_table<Src, ShadeGrads>();
+        gt->init();
         __syncthreads();
     }
     for (uint32_t base = blockIdx.x * blockDim.x; base < n + nf; base += gridDim.x * blockDim.x) {
@@ -1522,8 +1529,8 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                             gs = mk(R.x * (-dist + (scat ? 1.0f / ss.x : 0.0f)),
                                     R.y * (-dist + (scat ? 1.0f / ss.y : 0.0f)),
                                     R.z * (-dist + (scat ? 1.0f / ss.z : 0.0f)));
-                        gt_add(gt, src.grads(p.scene).sigma_a + 3 * mi, ga);
-                        gt_add(gt, src.grads(p.scene).sigma_s + 3 * mi, gs);
+                        gt->add(src.grads(p.scene).sigma_a + 3 * mi, ga);
+                        gt->add(src.grads(p.scene).sigma_s + 3 * mi, gs);
                     }
                     p.T = p.T * w;
                     Ts = Ts * ws;
@@ -1540,7 +1547,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
                     const v3 alb = ld3(P.albedo + 3 * prim), alb_d = ld3(P.albedo_s + 3 * prim);
                     if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0) {
                         C = C + p.T * ld3(P.emission + 3 * prim);
-                        if constexpr (Src::kAdj) gt_add(gt, src.grads(p.scene).emission + 3 * prim, p.T * delta);
+                        if constexpr (Src::kAdj) gt->add(src.grads(p.scene).emission + 3 * prim, p.T * delta);
                     }
                     shade_prim = prim;
                     Inter it;
@@ -1651,9 +1658,9 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
             // arrays and its slots to the new scene's triangles (a block-uniform
             // decision; every add of this round is done)
             if (sl.flag != 0u) {
-                gt_flush(gt);
+                gt->flush();
                 __syncthreads();
-                gt_init(gt);
+                gt->init();
                 if (threadIdx.x == 0) gt->scene = sl.flag - 1u;
                 __syncthreads();
             }
@@ -1726,7 +1733,7 @@ __global__ void __launch_bounds__(256, 3) k_dshade(Src src, Wavefront W, int cur
     }
     if constexpr (Src::kAdj) {
         __syncthreads();
-        gt_flush(gt);
+        gt->flush();
     }
 }
 
@@ -1829,7 +1836,7 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
 // table follows the scenes, which only the shade's block-uniform rounds allow).
 template <class Src, class State>
 __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wavefront &W, uint32_t idx,
-                                                        uint32_t kl, const State &r, GradTable *gt) {
+                                                        uint32_t kl, const State &r, TraceGrads *gt) {
     const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
     const DevScene &S = src.scene(sid);
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
@@ -1875,8 +1882,8 @@ __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wa
                     st_s(src.d.gres + 2 * idx, make_float4(ga.x, ga.y, ga.z, __uint_as_float(h.prim)));
                     st_s(src.d.gres + 2 * idx + 1, make_float4(ge.x, ge.y, ge.z, 0.0f));
                 } else {
-                    gt_add(gt, G.albedo + 3 * (size_t)__float_as_uint(aux.x), ga);
-                    gt_add(gt, G.emission + 3 * (size_t)h.prim, ge);
+                    gt->add(G.albedo + 3 * (size_t)__float_as_uint(aux.x), ga);
+                    gt->add(G.emission + 3 * (size_t)h.prim, ge);
                 }
             }
         }
@@ -1906,10 +1913,10 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
         W.counters->fcount[cur ^ 1] = 0;  // filled by the next differentiable shade
         W.counters->main_rays += n;
     }
-    GradTable *gt = nullptr;  // the single-scene adjoint's connection terms
+    TraceGrads *gt = nullptr;  // the single-scene adjoint's connection terms
     if constexpr (Src::kAdj && !Src::kMany) {
-        gt = grad_table<Src>();
-        gt_init(gt);
+        gt = grad_table<Src, TraceGrads>();
+        gt->init();
         __syncthreads();
     }
     const float4 *rays = W.ray[cur];
@@ -1958,7 +1965,7 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
     if (n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
     if constexpr (Src::kAdj && !Src::kMany) {
         __syncthreads();
-        gt_flush(gt);
+        gt->flush();
     }
 }
 
