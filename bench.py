@@ -512,7 +512,8 @@ def batch_bench(local, count=64, reps=3):
     scene rendered by its own Integrator.RenderFrame (lt_render, one after the
     other: the sequential baseline, with the default and with the tuned launch
     configuration) against one RenderBatch (lt_render_batch: one captured
-    graph launch) after lt_autotune_batch. Device time on the stream, best of
+    graph launch for the scenes below the wavefront size, the ones that fill
+    it alone after it) after lt_autotune_batch. Device time on the stream, best of
     `reps`; films accumulate across repetitions (additive, like RenderFrame)."""
     import torch
     import lantern_gb300.scenes as S

@@ -338,7 +338,10 @@ lt_status lt_set_tuning(lt_ctx *ctx, const lt_tuning *t);
  * iteration loop is captured once into a CUDA graph (a while node whose
  * condition kernel stops when no path is left) and the whole batch runs as one
  * graph launch on ctx's stream; the graph is kept and reused while the
- * wavefront and tuning stay the same.
+ * wavefront and tuning stay the same. A scene whose samples fill the wavefront
+ * by themselves (at least paths_in_flight of ctx's tuning, 16M by default)
+ * gains nothing from the others' company: it is rendered after the loop with
+ * the single-scene kernels on the same wavefront.
  * - films must be on the device (on_device = 1), of each camera's size, and
  *   must not overlap;
  * - n <= LT_MAX_BATCH; each scene may have at most 1,048,576 lights and 8,190 media;

@@ -150,8 +150,9 @@ def intersect(ctx: Context, rays, on_device: Optional[bool] = None):
 
 def RenderBatch(integrators, frames=1, owner: Optional[Context] = None):
     """RenderFrame(frames[i]) of every integrator, done together by
-    lt_render_batch: all scenes' samples share one wavefront and one captured
-    loop. `owner` holds that wavefront (default: the first integrator's scene
+    lt_render_batch: the scenes' samples share one wavefront and one captured
+    loop (a scene that fills the wavefront by itself is rendered alone after
+    it). `owner` holds that wavefront (default: the first integrator's scene
     context). Each integrator's frame number advances as RenderFrame's would."""
     if isinstance(frames, int):
         frames = [frames] * len(integrators)

@@ -64,6 +64,23 @@ def test_batch_equals_individual_renders(scene_dir):
     _check_batch([scenes[i] for i in order], [4, 3, 16, 5, 2], [8, 10, 32, 6, 8], [0, 7, 1, 100, 4])
 
 
+def test_batch_renders_wavefront_filling_scenes_alone(scene_dir):
+    """A scene whose samples fill the owner's wavefront (here paths_in_flight
+    8192: three of the five renders) is rendered with the single-scene kernels
+    after the captured loop of the others; every film is still the
+    single-scene render's, and the statistics count every sample."""
+    scenes = [_load(scene_dir, S.tiny_scene(width=48, height=40, name="bt_tiny")),
+              _load(scene_dir, S.nine_spheres(width=64, height=64, name="bt_c0", slices=16, stacks=8)),
+              _load(scene_dir, S.medium_sphere_scene(width=40, height=56, name="bt_med")),
+              _load(scene_dir, S.displaced_icosphere_scene(width=64, height=48, levels=4, name="bt_ico"))]
+    scenes[0].ctx.set_tuning(paths_in_flight=8192)
+    order, spps = [0, 1, 2, 3, 0], [4, 3, 16, 5, 2]
+    _check_batch([scenes[i] for i in order], spps, [8, 10, 32, 6, 8], [0, 7, 1, 100, 4])
+    st = scenes[0].ctx.stats()
+    assert st.samples == sum(scenes[i].width * scenes[i].height * n for i, n in zip(order, spps))
+    assert st.main_rays > 0 and st.kernel_launches > 0
+
+
 def test_batch_edge_cases(scene_dir):
     s = _load(scene_dir, S.tiny_scene(width=24, height=24, name="bt_edge"))
     # spp 0 (no work) and max_depth 0 (counts only) next to a normal scene
