@@ -1060,6 +1060,31 @@ static lt_status ensure_diff_samples(lt_ctx *c, size_t bytes) {
     return LT_OK;
 }
 
+}  // extern "C"
+
+// The differentiable forward on the wavefront over a.total samples of scene
+// `dev` into film f, every sample's radiance into sample_I, on c's arena and
+// stream; then the film's colour sums in sample order. Fills c->stats as
+// run_loop does.
+static lt_status diff_wave(lt_ctx *c, const DevScene &dev, const DiffParams &P, const RenderArgs &a,
+                           const FilmPtrs &f, float *sample_I) {
+    uint32_t cap = 0;
+    Wavefront w;
+    DiffWave d;
+    lt_status st = prepare_dwave(c, a.total, &cap, &w, &d);
+    if (st != LT_OK) return st;
+    d.sample_I = sample_I;
+    st = run_loop(
+        c, w, a, true, [&]() { return launch_dwave_init(dev, P, d, w, a, f, c->shape, c->stream); },
+        [&](int stage, int cur) { return launch_dwave_stage(stage, dev, P, d, w, a, f, cur, c->shape, c->stream); });
+    if (st != LT_OK) return st;
+    CUDA_TRY(c, launch_diff_film(d.sample_I, a, f, c->stream));
+    c->stats.kernel_launches += 1;
+    return LT_OK;
+}
+
+extern "C" {
+
 lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_params *dp, lt_film *film,
                          float *sample_radiance) try {
     NvtxRange nvtx_("lt_render_diff");
@@ -1080,24 +1105,11 @@ lt_status lt_render_diff(lt_ctx *c, const lt_render_params *p, const lt_diff_par
         CUDA_TRY(c, launch_add_counts(f, npix, p->spp, c->stream));
         c->stats.kernel_launches = 1;
     } else if (a.total > 0) {
-        uint32_t cap = 0;
-        Wavefront w;
-        DiffWave d;
-        if ((st = prepare_dwave(c, a.total, &cap, &w, &d)) != LT_OK) return st;
-        if (sample_radiance) {
-            d.sample_I = sample_radiance;
-        } else {
+        if (!sample_radiance) {
             if ((st = ensure_diff_samples(c, a.total * 12)) != LT_OK) return st;
-            d.sample_I = c->diff_samples;
+            sample_radiance = c->diff_samples;
         }
-        st = run_loop(
-            c, w, a, true, [&]() { return launch_dwave_init(c->dev, P, d, w, a, f, c->shape, c->stream); },
-            [&](int stage, int cur) {
-                return launch_dwave_stage(stage, c->dev, P, d, w, a, f, cur, c->shape, c->stream);
-            });
-        if (st != LT_OK) return st;
-        CUDA_TRY(c, launch_diff_film(d.sample_I, a, f, c->stream));
-        c->stats.kernel_launches += 1;
+        if ((st = diff_wave(c, c->dev, P, a, f, sample_radiance)) != LT_OK) return st;
     }
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     c->stats.samples = a.total;
@@ -1603,7 +1615,11 @@ extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap,
 // themselves: they run one after the other on the single-scene wavefront
 // (whose trace stage sums the connection terms in shared memory), the others
 // together on one wavefront. On the 32 adjoints of the 64-scene workload:
-// everything on one wavefront 219 ms, one by one 204 ms, this split 186 ms.
+// everything on one wavefront 219 ms, one by one 204 ms, this split 186 ms
+// (2^26: 192 ms). The batched differentiable forward sends the jobs that fill
+// the wavefront by themselves (the tuning's paths in flight) to the
+// single-scene wavefront the same way (its 32 forwards: 166.6 ms all together,
+// 158.6 ms with the two of 2^26 samples alone).
 constexpr unsigned long long kAdjointAloneSamples = 1ull << 24;
 
 // Batched differentiable forward (adjoint false) or adjoint over one scene
@@ -1638,7 +1654,13 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
     c->stats = lt_render_stats{};
     CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
     std::vector<size_t> internal_at;  // per slot: offset into the internal sample buffer, or SIZE_MAX
-    std::vector<uint32_t> alone;       // adjoint jobs replayed one by one
+    struct Alone {
+        uint32_t job;
+        size_t internal;  // forward without sample_radiance: offset into the internal sample buffer
+    };
+    std::vector<Alone> alone;  // jobs run one by one on the single-scene wavefront
+    const unsigned long long alone_from =
+        adjoint ? kAdjointAloneSamples : (c->tuning.paths_in_flight ? c->tuning.paths_in_flight : kDefaultPaths);
     for (uint32_t i = 0; i < n; ++i) {
         const lt_diff_job &j = jobs[i];
         const lt_ctx *s = j.scene;
@@ -1667,8 +1689,12 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
             }
             continue;
         }
-        if (adjoint && wave && total >= kAdjointAloneSamples) {
-            alone.push_back(i);
+        if (wave && total >= alone_from) {
+            alone.push_back(Alone{i, SIZE_MAX});
+            if (!adjoint && !j.sample_radiance) {
+                alone.back().internal = (size_t)internal;
+                internal += (total * 12 + 255) & ~255ull;
+            }
             continue;
         }
         SceneSlot &sl = T.slots[count];
@@ -1703,12 +1729,12 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         ++count;
     }
     c->stats.samples = samples;
+    if (internal) {
+        if ((st = ensure_diff_samples(c, (size_t)internal)) != LT_OK) return st;
+        for (uint32_t k = 0; k < count; ++k)
+            if (internal_at[k] != SIZE_MAX) T.diff[k].sample_I = (float *)((char *)c->diff_samples + internal_at[k]);
+    }
     if (count) {
-        if (internal) {
-            if ((st = ensure_diff_samples(c, (size_t)internal)) != LT_OK) return st;
-            for (uint32_t k = 0; k < count; ++k)
-                if (internal_at[k] != SIZE_MAX) T.diff[k].sample_I = (float *)((char *)c->diff_samples + internal_at[k]);
-        }
         T.count = count;
         T.pad = 0;
         T.total = wave ? items : 0;
@@ -1756,8 +1782,8 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         CUDA_TRY(c, (cudaError_t)c->order.table_read_queued(c->rt, c->stream));
     }
     lt_render_stats acc = c->stats;
-    for (uint32_t i : alone) {
-        const lt_diff_job &j = jobs[i];
+    for (const Alone &al : alone) {
+        const lt_diff_job &j = jobs[al.job];
         const HostScene &h = j.scene->host;
         const uint32_t W = h.camera.width, H = h.camera.height;
         const RenderArgs a{W, H, j.params.first_frame, j.params.max_depth, j.params.rr_depth,
@@ -1770,9 +1796,15 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         P.albedo_s = j.dp.albedo_detached ? j.dp.albedo_detached : j.dp.albedo;
         P.sigma_a_s = j.dp.sigma_a_detached ? j.dp.sigma_a_detached : j.dp.sigma_a;
         P.sigma_s_s = j.dp.sigma_s_detached ? j.dp.sigma_s_detached : j.dp.sigma_s;
-        const DiffGrads G{j.d_loss_d_film, j.grad_albedo, j.grad_emission, j.grad_sigma_a, j.grad_sigma_s,
-                          0, 0, W, H, j.sample_radiance};
-        if ((st = adjoint_wave(c, j.scene->dev, P, a, G)) != LT_OK) return st;
+        if (adjoint) {
+            const DiffGrads G{j.d_loss_d_film, j.grad_albedo, j.grad_emission, j.grad_sigma_a, j.grad_sigma_s,
+                              0, 0, W, H, j.sample_radiance};
+            if ((st = adjoint_wave(c, j.scene->dev, P, a, G)) != LT_OK) return st;
+        } else {
+            float *smp = al.internal == SIZE_MAX ? j.sample_radiance : (float *)((char *)c->diff_samples + al.internal);
+            const FilmPtrs f{j.film.rgb, j.film.bounces, j.film.counts};
+            if ((st = diff_wave(c, j.scene->dev, P, a, f, smp)) != LT_OK) return st;
+        }
         launches += c->stats.kernel_launches;
         acc.iterations += c->stats.iterations;
         acc.main_rays += c->stats.main_rays;

@@ -176,11 +176,13 @@ def test_batch_with_textures_and_procedural_primitives(scene_dir):
     _check_batch(scenes, [3, 4, 2], [8, 8, 6], [2, 9, 0])
 
 
-def test_adjoint_batch_with_a_job_that_runs_alone(scene_dir):
-    """lt_render_adjoint_batch replays a job of 2^24 samples or more (here
-    512x512 at 64 spp) on its own wavefront and the other jobs together on
-    one: every job's gradients equal its single-scene adjoint's (up to the
-    order of the float sums)."""
+def test_diff_batch_with_a_job_that_runs_alone(scene_dir):
+    """A job of 2^24 samples or more (here 512x512 at 64 spp) fills the
+    default wavefront by itself: lt_render_diff_batch renders it on the
+    single-scene wavefront and lt_render_adjoint_batch replays it there, the
+    other jobs together on one wavefront. Films and per-sample radiance equal
+    the single-scene calls' bit for bit; every job's gradients equal its
+    single-scene adjoint's (up to the order of the float sums)."""
     from lantern_gb300.diff import DiffScene, adjoint_batch, render_batch
     big = DiffScene(S.differentiable_scene(width=512, height=512, slices=16, stacks=8, name="ba_big").write(scene_dir))
     s1 = DiffScene(S.tiny_scene(width=40, height=32, name="ba_tiny").write(scene_dir))
@@ -189,6 +191,10 @@ def test_adjoint_batch_with_a_job_that_runs_alone(scene_dir):
     assert big.width * big.height * spp[1] >= 1 << 24
     params = [sc.defaults() for sc in scenes]
     outs = render_batch(scenes, params, spp, 0, max_depth=6, rr_depth=3, keep_samples=True)
+    for k, sc in enumerate(scenes):
+        ref = sc.render(*params[k], spp[k], 0, 6, 3, keep_samples=True)
+        for x, y in zip(outs[k], ref):
+            assert torch.equal(x, y), k
     g = torch.Generator(device="cuda:0").manual_seed(5)
     dI = [torch.rand((sc.height, sc.width, 3), generator=g, device="cuda:0") - 0.5 for sc in scenes]
     gb = adjoint_batch(scenes, params, dI, spp, 0, 6, 3, samples=[o[3] for o in outs])
