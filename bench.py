@@ -583,6 +583,22 @@ def batch_bench(local, count=64, reps=3):
         s.ctx.set_tuning(**{k: v for k, v in tuned.items() if k != "ms"})
     seq_tuned = timed(sequential)
     seq = min(seq_default, seq_tuned)
+    # where batching pays: the scenes that do not fill the wavefront by
+    # themselves (lt_render_batch renders the others alone), batched vs one by one
+    limit = tuned["paths_in_flight"] or (1 << 24)
+    small = [k for k in range(len(scenes)) if scenes[k].width * scenes[k].height * spps[k] < limit]
+
+    def small_sequential():
+        its = integrators()
+        for k in small:
+            its[k].RenderFrame(spps[k])
+
+    def small_batched():
+        its = integrators()
+        RenderBatch([its[k] for k in small], [spps[k] for k in small])
+
+    small_seq = timed(small_sequential) if small else 0.0
+    small_bat = timed(small_batched) if small else 0.0
     # every context keeps its wavefront until trimmed: give the plain renders'
     # buffers back before the differentiable part allocates its own
     for s in scenes:
@@ -662,6 +678,12 @@ def batch_bench(local, count=64, reps=3):
                                    "note": "max_speedup = wall / kernel time: what batching reaches if it "
                                            "removes every gap and runs the same kernels as fast"},
             "batched_iterations": st.iterations, "batched_kernel_launches": st.kernel_launches,
+            "scenes_below_wavefront": {"count": len(small),
+                                       "samples": sum(scenes[k].width * scenes[k].height * spps[k] for k in small),
+                                       "sequential_ms": round(small_seq, 2), "batched_ms": round(small_bat, 2),
+                                       "speedup": round(small_seq / small_bat, 3) if small else None,
+                                       "note": "the scenes with fewer samples than the wavefront holds, rendered "
+                                               "one by one vs in one lt_render_batch"},
             "adjoint_scenes": len(marked), "adjoint_samples": adj_samples,
             "adjoint_sequential_ms": round(adj_seq, 2), "adjoint_batched_ms": round(adj_bat, 2),
             "adjoint_speedup": round(adj_seq / adj_bat, 3),
