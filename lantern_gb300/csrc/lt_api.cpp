@@ -1622,6 +1622,19 @@ extern "C" lt_status lt_resolve(lt_ctx *c, const lt_film *film, int32_t tonemap,
 // 158.6 ms with the two of 2^26 samples alone).
 constexpr unsigned long long kAdjointAloneSamples = 1ull << 24;
 
+// A job's parameters with the detached copies defaulted to the parameters.
+static DiffParams job_params(const lt_diff_job &j) {
+    DiffParams P;
+    P.albedo = j.dp.albedo;
+    P.emission = j.dp.emission;
+    P.sigma_a = j.dp.sigma_a;
+    P.sigma_s = j.dp.sigma_s;
+    P.albedo_s = j.dp.albedo_detached ? j.dp.albedo_detached : j.dp.albedo;
+    P.sigma_a_s = j.dp.sigma_a_detached ? j.dp.sigma_a_detached : j.dp.sigma_a;
+    P.sigma_s_s = j.dp.sigma_s_detached ? j.dp.sigma_s_detached : j.dp.sigma_s;
+    return P;
+}
+
 // Batched differentiable forward (adjoint false) or adjoint over one scene
 // table. The forward runs the differentiable wavefront over the work items of
 // all jobs (as lt_render_batch does for plain renders) and returns when it
@@ -1702,13 +1715,7 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         sl.s = s->dev;
         sl.a = RenderArgs{W, H, j.params.first_frame, j.params.max_depth, j.params.rr_depth, total};
         sl.f = FilmPtrs{j.film.rgb, j.film.bounces, j.film.counts};
-        d.p.albedo = j.dp.albedo;
-        d.p.emission = j.dp.emission;
-        d.p.sigma_a = j.dp.sigma_a;
-        d.p.sigma_s = j.dp.sigma_s;
-        d.p.albedo_s = j.dp.albedo_detached ? j.dp.albedo_detached : j.dp.albedo;
-        d.p.sigma_a_s = j.dp.sigma_a_detached ? j.dp.sigma_a_detached : j.dp.sigma_a;
-        d.p.sigma_s_s = j.dp.sigma_s_detached ? j.dp.sigma_s_detached : j.dp.sigma_s;
+        d.p = job_params(j);
         d.g = DiffGrads{j.d_loss_d_film, j.grad_albedo, j.grad_emission, j.grad_sigma_a, j.grad_sigma_s,
                         0, 0, W, H, adjoint ? j.sample_radiance : nullptr};
         d.sample_I = adjoint ? nullptr : j.sample_radiance;
@@ -1788,14 +1795,7 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
         const uint32_t W = h.camera.width, H = h.camera.height;
         const RenderArgs a{W, H, j.params.first_frame, j.params.max_depth, j.params.rr_depth,
                            (unsigned long long)W * H * j.params.spp};
-        DiffParams P;
-        P.albedo = j.dp.albedo;
-        P.emission = j.dp.emission;
-        P.sigma_a = j.dp.sigma_a;
-        P.sigma_s = j.dp.sigma_s;
-        P.albedo_s = j.dp.albedo_detached ? j.dp.albedo_detached : j.dp.albedo;
-        P.sigma_a_s = j.dp.sigma_a_detached ? j.dp.sigma_a_detached : j.dp.sigma_a;
-        P.sigma_s_s = j.dp.sigma_s_detached ? j.dp.sigma_s_detached : j.dp.sigma_s;
+        const DiffParams P = job_params(j);
         if (adjoint) {
             const DiffGrads G{j.d_loss_d_film, j.grad_albedo, j.grad_emission, j.grad_sigma_a, j.grad_sigma_s,
                               0, 0, W, H, j.sample_radiance};
