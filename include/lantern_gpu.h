@@ -418,18 +418,20 @@ lt_status lt_render_adjoint(lt_ctx *ctx, const lt_render_params *params, const l
  * differentiable parameters; all jobs run together on ctx's stream. Per job
  * the results are those of the single-scene call over the whole film (no crop).
  * - lt_render_diff_batch: the work items of all jobs share one wavefront owned
- *   by ctx (as lt_render_batch's); film (device, additive) and sample_radiance
- *   (optional, as lt_render_diff's) are outputs, the same bits as the
- *   single-scene call gives. Returns when the batch has finished.
+ *   by ctx (as lt_render_batch's; a job that fills the wavefront by itself, at
+ *   least the tuning's paths in flight, runs alone on it after the others);
+ *   film (device, additive) and sample_radiance (optional, as lt_render_diff's)
+ *   are outputs, the same bits as the single-scene call gives. Returns when the
+ *   batch has finished.
  * - lt_render_adjoint_batch: d_loss_d_film and sample_radiance are inputs,
  *   the four gradient arrays outputs (accumulated; sigma arrays may be NULL for
  *   scenes without media). When every job brings its sample_radiance, the
- *   samples of all jobs are replayed on one wavefront owned by ctx (as the
- *   forward's) and the call returns when finished; otherwise it is one
- *   persistent launch over chunks of 8 samples of all jobs' pixels (warps take
- *   32 chunks at a time from a shared counter) that replays each sample twice,
- *   and the call returns once the work is queued. Jobs must not share gradient
- *   arrays.
+ *   samples of the jobs below 2^24 samples are replayed together on one
+ *   wavefront owned by ctx, the larger jobs one by one on it, and the call
+ *   returns when finished; otherwise it is one persistent launch over chunks of
+ *   8 samples of all jobs' pixels (warps take 32 chunks at a time from a shared
+ *   counter) that replays each sample twice, and the call returns once the work
+ *   is queued. Jobs must not share gradient arrays.
  * n <= LT_MAX_BATCH. */
 typedef struct lt_diff_job {
     lt_ctx *scene;
