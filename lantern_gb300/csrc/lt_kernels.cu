@@ -598,6 +598,9 @@ struct Path {
 
 // Path flags: bits 0-7 sampled lobe, 8-20 medium index + 1, 21-31 scene slot.
 constexpr uint32_t kFlagMediumShift = 8, kFlagMediumMask = 0x1FFFu, kFlagSceneShift = 21;
+// A path that starts with its camera ray: throughput 1, no bounce, IOR 1, no
+// lobe, no medium; only its sampler, pixel, frame and flags are stored.
+constexpr uint32_t kFlagFresh = 0x80u;
 // Connection record word: bits 0-19 light index, 20-30 scene slot, bit 31 BSDF sample.
 constexpr uint32_t kConnLightMask = 0xFFFFFu, kConnSceneShift = 20, kConnSceneMask = 0x7FFu;
 static_assert(kMaxBatchScenes <= kConnSceneMask + 1 && kMaxBatchScenes <= (1u << (32 - kFlagSceneShift)),
@@ -645,18 +648,35 @@ __device__ __forceinline__ void store_path(const PathState &ps, uint32_t cap, ui
     st_s(ps.iori + slot, p.iori);
 }
 
+// A fresh path (a camera ray's): the state start_path gives, with only the
+// sampler, pixel, frame and flags stored.
+__device__ __forceinline__ void store_fresh_path(const PathState &ps, uint32_t slot, const Path &p) {
+    st_s(ps.rng + slot, (uint64_t)p.rng.state);
+    st_s(ps.pixel + slot, p.pixel);
+    st_s(ps.frame + slot, p.frame);
+    st_s(ps.flags + slot, kLobeNull | kFlagFresh | (p.scene << kFlagSceneShift));
+}
+
 __device__ __forceinline__ void load_path(const PathState &ps, uint32_t cap, uint32_t slot, Path &p) {
     p.rng.state = ld_s(ps.rng + slot);
     p.pixel = ld_s(ps.pixel + slot);
     p.frame = ld_s(ps.frame + slot);
     p.rng.inc = (uint64_t)p.frame | 1u;
-    p.T = mk(ld_s(ps.T + slot), ld_s(ps.T + cap + slot), ld_s(ps.T + 2 * cap + slot));
-    p.bounces = ld_s(ps.bounces + slot);
-    uint32_t fl = ld_s(ps.flags + slot);
-    p.lobe = fl & 0xFFu;
-    p.medium = (int)((fl >> kFlagMediumShift) & kFlagMediumMask) - 1;
+    const uint32_t fl = ld_s(ps.flags + slot);
     p.scene = fl >> kFlagSceneShift;
-    p.iori = ld_s(ps.iori + slot);
+    if (fl & kFlagFresh) {
+        p.T = mk(1.0f, 1.0f, 1.0f);
+        p.bounces = 0;
+        p.lobe = kLobeNull;
+        p.medium = -1;
+        p.iori = 1.0f;
+    } else {
+        p.T = mk(ld_s(ps.T + slot), ld_s(ps.T + cap + slot), ld_s(ps.T + 2 * cap + slot));
+        p.bounces = ld_s(ps.bounces + slot);
+        p.lobe = fl & 0xFFu;
+        p.medium = (int)((fl >> kFlagMediumShift) & kFlagMediumMask) - 1;
+        p.iori = ld_s(ps.iori + slot);
+    }
 }
 
 __device__ __forceinline__ void write_ray(float4 *rays, uint32_t i, v3 o, float tnear, v3 d) {
@@ -924,7 +944,7 @@ __global__ void __launch_bounds__(256) k_raygen(Src src, Wavefront W) {
         const uint32_t sid = src.locate(i, local);
         start_path(src.scene(sid), src.args(sid), local, p, o, d, tn);
         p.scene = sid;
-        store_path(W.p[0], W.capacity, i, p);
+        store_fresh_path(W.p[0], i, p);
         write_ray(W.ray[0], i, o, tn, d);
         if constexpr (Src::kDiff) {
             st3_planes(src.d.C[0], W.capacity, i, mk(0.0f, 0.0f, 0.0f));
@@ -1250,7 +1270,8 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
         if (push || regen) {
             const uint32_t qi = push ? q_base + __popc(m_p & below) : cap - 1u - (r_base + rank_d);
             write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
-            store_path(W.p[nxt], cap, qi, p);
+            if (push) store_path(W.p[nxt], cap, qi, p);
+            else store_fresh_path(W.p[nxt], qi, p);
         }
     }
     // ray tallies in the reference's terms (every SampleLi / PdfLi trace), one atomic per warp
