@@ -95,7 +95,9 @@ struct lt_ctx {
 
     lt_render_stats stats{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // stage timing: one event before each stage launch and one after the last
+    // stage timing (lt_set_stage_timing, off by default): an event before and
+    // after every stage launch of the wavefront renders
+    bool stage_timing = false;
     std::vector<cudaEvent_t> stage_events;
     std::vector<int> stage_of_event;
 };
@@ -894,7 +896,7 @@ lt_status lt_render(lt_ctx *c, const lt_render_params *p, lt_film *film) try {
         lt_status st = prepare_wave(c, a.total, &cap);
         if (st != LT_OK) return st;
         const Wavefront w = wave_view(c, cap);
-        if ((st = run_wave(c, w, a, f, true)) != LT_OK) return st;
+        if ((st = run_wave(c, w, a, f, c->stage_timing)) != LT_OK) return st;
     }
     c->stats.samples = a.total;
     CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -1075,7 +1077,7 @@ static lt_status diff_wave(lt_ctx *c, const DevScene &dev, const DiffParams &P, 
     if (st != LT_OK) return st;
     d.sample_I = sample_I;
     st = run_loop(
-        c, w, a, true, [&]() { return launch_dwave_init(dev, P, d, w, a, f, c->shape, c->stream); },
+        c, w, a, c->stage_timing, [&]() { return launch_dwave_init(dev, P, d, w, a, f, c->shape, c->stream); },
         [&](int stage, int cur) { return launch_dwave_stage(stage, dev, P, d, w, a, f, cur, c->shape, c->stream); });
     if (st != LT_OK) return st;
     CUDA_TRY(c, launch_diff_film(d.sample_I, a, f, c->stream));
@@ -1129,7 +1131,7 @@ static lt_status adjoint_wave(lt_ctx *c, const DevScene &dev, const DiffParams &
     lt_status st = prepare_dwave(c, a.total, &cap, &w, &d);
     if (st != LT_OK) return st;
     return run_loop(
-        c, w, a, true, [&]() { return launch_awave_init(dev, P, d, G, w, a, c->shape, c->stream); },
+        c, w, a, c->stage_timing, [&]() { return launch_awave_init(dev, P, d, G, w, a, c->shape, c->stream); },
         [&](int stage, int cur) { return launch_awave_stage(stage, dev, P, d, G, w, a, cur, c->shape, c->stream); });
 }
 
@@ -1255,6 +1257,12 @@ extern "C" lt_status lt_get_tuning(const lt_ctx *c, lt_tuning *out) {
 
 static bool valid_threads(uint32_t t) { return t == 64 || t == 128 || t == 256; }
 static bool valid_shade_threads(uint32_t t) { return valid_threads(t) || t == 512; }
+
+extern "C" lt_status lt_set_stage_timing(lt_ctx *c, int32_t on) try {
+    if (!c) return LT_ERR_INVALID;
+    c->stage_timing = on != 0;
+    return LT_OK;
+} LT_CATCH(c)
 
 extern "C" lt_status lt_set_tuning(lt_ctx *c, const lt_tuning *t) try {
     if (!c || !t) return fail(c, LT_ERR_INVALID, "NULL argument");
@@ -1769,13 +1777,15 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
             const SceneTable *t = c->table_dev;
             if (adjoint)
                 st = run_loop(
-                    c, w, all, true, [&]() { return launch_awave_batch_init(t, dw, w, c->batch_shape, c->stream); },
+                    c, w, all, c->stage_timing,
+                    [&]() { return launch_awave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_awave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
                     });
             else
                 st = run_loop(
-                    c, w, all, true, [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
+                    c, w, all, c->stage_timing,
+                    [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_dwave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
                     });

@@ -24,7 +24,7 @@ SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error",
            "lt_sync", "lt_trim",
            "lt_scene_create", "lt_scene_destroy", "lt_scene_load_json", "lt_scene_info_get", "lt_scene_mesh_offsets", "lt_scene_lights_get", "lt_render",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
-           "lt_set_tuning", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
+           "lt_set_tuning", "lt_set_stage_timing", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
            "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load",
            "lt_debug_fail_allocations", "lt_debug_set_iteration_limit"]
 BVH_GPU, BVH_HOST = 0, 1
@@ -161,6 +161,7 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_set_bvh_builder.argtypes = [p, C.c_int32]
         L.lt_get_tuning.argtypes = [p, C.POINTER(Tuning)]
         L.lt_set_tuning.argtypes = [p, C.POINTER(Tuning)]
+        L.lt_set_stage_timing.argtypes = [p, C.c_int32]
         L.lt_render_batch.argtypes = [p, C.POINTER(p), C.POINTER(RenderParams), C.POINTER(Film), C.c_uint32]
         L.lt_autotune_batch.argtypes = [p, C.POINTER(p), C.POINTER(RenderParams), C.c_uint32, C.c_uint32,
                                         C.POINTER(Tuning)]
@@ -294,6 +295,10 @@ class Context:
         t = Tuning()
         self._check(self.L.lt_get_tuning(self.h, C.byref(t)))
         return t
+
+    def set_stage_timing(self, on: bool):
+        """lt_set_stage_timing: per-stage kernel times in stats() (events around every launch)."""
+        self._check(self.L.lt_set_stage_timing(self.h, 1 if on else 0))
 
     def set_tuning(self, **fields):
         """lt_set_tuning with the given fields changed from the current tuning."""

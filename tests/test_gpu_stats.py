@@ -1,6 +1,8 @@
-"""lt_render_stats: the kernel times of the stages (events around every
-launch), the device time of the whole render and the time between its
-kernels are consistent, and the ray counts add up to what was traced."""
+"""lt_render_stats: with stage timing on, the kernel times of the stages
+(events around every launch), the device time of the whole render and the
+time between its kernels are consistent; with it off (the default) the stage
+times stay 0 and the render is the same; the ray counts add up to what was
+traced."""
 import pytest
 import torch
 
@@ -16,6 +18,7 @@ def test_stage_times_and_counts(scene_dir, paths):
     s.LoadSceneFromJSON(S.nine_spheres(width=64, height=48, slices=16, stacks=8, name="stats_nine").write(scene_dir))
     if paths:
         s.ctx.set_tuning(paths_in_flight=paths)
+    s.ctx.set_stage_timing(True)
     fb = FrameBuffer(s.width, s.height, "cuda:0")
     it = Integrator(s, fb, max_depth=8, rr_depth=3)
     it.RenderFrame(8)
@@ -30,6 +33,15 @@ def test_stage_times_and_counts(scene_dir, paths):
     assert st.main_rays >= st.samples  # every sample traces its camera ray
     assert st.light_traversals <= st.light_rays + st.bsdf_rays
     assert int(fb.ColorSampleCount.min()) == 8
+    # stage timing off: no stage times, the same samples
+    s.ctx.set_stage_timing(False)
+    fb2 = FrameBuffer(s.width, s.height, "cuda:0")
+    Integrator(s, fb2, max_depth=8, rr_depth=3).RenderFrame(8)
+    torch.cuda.synchronize()
+    st2 = s.ctx.stats()
+    assert st2.trace_ms == 0 and st2.shade_ms == 0 and st2.init_ms == 0 and st2.gpu_ms > 0
+    assert st2.kernel_launches == st.kernel_launches and st2.main_rays == st.main_rays
+    assert torch.equal(fb.ColorSampleCount, fb2.ColorSampleCount) and torch.equal(fb.Bounces, fb2.Bounces)
 
 
 def test_launch_shapes_render_the_same_samples(scene_dir):
