@@ -284,6 +284,9 @@ def main():
                     help="threads per block of the trace kernel (lt_tuning.trace_threads; 0 = the library's)")
     ap.add_argument("--shade-threads", type=int, default=0, choices=[0, 64, 128, 256, 512],
                     help="threads per block of the shade kernel (lt_tuning.shade_threads; 0 = the library's)")
+    ap.add_argument("--stage-timing", action=argparse.BooleanOptionalAction, default=True,
+                    help="events around every launch in the timed region (the roofline's kernel time); "
+                         "without them lt_render runs as the library does by default")
     ap.add_argument("--batch", action=argparse.BooleanOptionalAction, default=True,
                     help="also time the 64-scene batch: one lt_render_batch vs one lt_render per scene")
     args = ap.parse_args()
@@ -330,7 +333,7 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     # events around every launch in the timed region: the roofline's kernel
     # time (lt_render is a little faster without them, the library default)
-    scene.ctx.set_stage_timing(True)
+    scene.ctx.set_stage_timing(args.stage_timing)
 
     for _ in range(args.warmup):
         integ.RenderFrame(spp)
@@ -402,6 +405,8 @@ def main():
             bpr, n_node, n_tri = bytes_per_ray(path, scene.width, scene.height, rp["max_depth"], rp["rr_depth"])
             # k_trace traces the path rays and the connection rays that needed a
             # query; both are charged the closest-hit bytes of one ray
+            if trace_ms <= 0.0:
+                raise ValueError("no stage times (--no-stage-timing): no kernel time for the roofline")
             achieved = (main_rays + conn_traced) * bpr / (trace_ms / 1e3) / 1e9
             traced_per_launch = (main_rays + conn_traced) / max(trace_launches, 1)
             roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
