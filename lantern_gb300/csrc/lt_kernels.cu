@@ -10,9 +10,11 @@
 //            emits up to two connection rays; finished paths are added to the
 //            film and their slot starts the next (pixel, frame) sample
 //
-// Queues are compacted with warp ballots (one atomic per warp). Every random
-// number is drawn in shade, in the reference's order, so that a path's
-// decisions do not depend on when its connection rays are traced.
+// Queues are compacted with warp ballots and reserved once per block (one
+// atomic per counter per block). Every random number is drawn in shade, in the
+// reference's order, so that a path's decisions do not depend on when its
+// connection rays are traced. The differentiable estimator and its adjoint run
+// on the same two stages (k_trace and k_dshade instantiated for their sources).
 #include <cuda_runtime.h>
 
 #include "lt_device.h"
