@@ -1310,7 +1310,8 @@ struct GradTable {
     unsigned long long key[kSlots];
     float val[3 * kSlots];
     uint32_t scene;  // batched adjoint: the scene slot the table was last given to
-    uint32_t other;  // 1 + a scene slot seen since the last round, or 0
+    uint32_t other;  // 1 + a scene slot seen since the last round, or 0 (plain stores by
+                     // any thread: which of the values written wins does not matter)
 
     // Every thread of the block calls it; a barrier follows before the first add.
     __device__ __forceinline__ void init() {
