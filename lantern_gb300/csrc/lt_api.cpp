@@ -767,10 +767,11 @@ static lt_status ensure_width(lt_ctx *c, uint32_t width) {
 // lt_render_stats gets each stage's kernel time (init_ms, trace_ms, shade_ms)
 // apart from the time the stream waits for the host between batches; without
 // it nothing is created or allocated. Fills c->stats (except samples and gpu_ms).
-// `init` and `stage(stage, cur)` launch the kernels (plain or differentiable).
+// `init` and `stage(stage, cur)` launch the kernels (plain or differentiable);
+// an iteration is `per_iteration` launches.
 template <class Init, class Stage>
-static lt_status run_loop(lt_ctx *c, const Wavefront &w, const RenderArgs &a, bool stage_timing, Init init,
-                          Stage launch_stage) {
+static lt_status run_loop(lt_ctx *c, const Wavefront &w, const RenderArgs &a, bool stage_timing,
+                          uint32_t per_iteration, Init init, Stage launch_stage) {
     const uint32_t cap = w.capacity;
     size_t nev = 0;
     if (stage_timing) c->stage_of_event.clear();
@@ -807,7 +808,7 @@ static lt_status run_loop(lt_ctx *c, const Wavefront &w, const RenderArgs &a, bo
                 CUDA_TRY(c, launch_stage(stage, cur));
                 CUDA_TRY(c, mark(stage, true));
             }
-            launches += kStages;
+            launches += per_iteration;
             cur ^= 1;
             ++iters;
         }
@@ -847,7 +848,8 @@ static lt_status run_loop(lt_ctx *c, const Wavefront &w, const RenderArgs &a, bo
 
 static lt_status run_wave(lt_ctx *c, const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, bool stage_timing) {
     return run_loop(
-        c, w, a, stage_timing, [&]() { return launch_wave_init(c->dev, w, a, f, c->shape, c->stream); },
+        c, w, a, stage_timing, launches_per_iteration(c->shape),
+        [&]() { return launch_wave_init(c->dev, w, a, f, c->shape, c->stream); },
         [&](int stage, int cur) { return launch_wave_stage(stage, c->dev, w, a, f, cur, c->shape, c->stream); });
 }
 
@@ -1077,7 +1079,7 @@ static lt_status diff_wave(lt_ctx *c, const DevScene &dev, const DiffParams &P, 
     if (st != LT_OK) return st;
     d.sample_I = sample_I;
     st = run_loop(
-        c, w, a, c->stage_timing, [&]() { return launch_dwave_init(dev, P, d, w, a, f, c->shape, c->stream); },
+        c, w, a, c->stage_timing, kStages, [&]() { return launch_dwave_init(dev, P, d, w, a, f, c->shape, c->stream); },
         [&](int stage, int cur) { return launch_dwave_stage(stage, dev, P, d, w, a, f, cur, c->shape, c->stream); });
     if (st != LT_OK) return st;
     CUDA_TRY(c, launch_diff_film(d.sample_I, a, f, c->stream));
@@ -1131,7 +1133,7 @@ static lt_status adjoint_wave(lt_ctx *c, const DevScene &dev, const DiffParams &
     lt_status st = prepare_dwave(c, a.total, &cap, &w, &d);
     if (st != LT_OK) return st;
     return run_loop(
-        c, w, a, c->stage_timing, [&]() { return launch_awave_init(dev, P, d, G, w, a, c->shape, c->stream); },
+        c, w, a, c->stage_timing, kStages, [&]() { return launch_awave_init(dev, P, d, G, w, a, c->shape, c->stream); },
         [&](int stage, int cur) { return launch_awave_stage(stage, dev, P, d, G, w, a, cur, c->shape, c->stream); });
 }
 
@@ -1301,7 +1303,8 @@ static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
     std::vector<uintptr_t> key = {(uintptr_t)c->wave.arena, w.capacity, (uintptr_t)c->table_dev,
                                   (uintptr_t)c->batch_shape.trace_threads, (uintptr_t)c->batch_shape.trace_blocks,
                                   (uintptr_t)c->batch_shape.shade_threads, (uintptr_t)c->batch_shape.shade_blocks,
-                                  (uintptr_t)c->batch_shape.bvh_width, c->tuning.loop_iterations};
+                                  (uintptr_t)c->batch_shape.bvh_width, c->tuning.loop_iterations,
+                                  (uintptr_t)c->batch_shape.tail_blocks, (uintptr_t)c->batch_shape.coop_limit};
     if (c->graph_exec && key == c->graph_key) return LT_OK;
     free_graph(c);
     cudaStream_t cs = c->own_stream;
@@ -1448,7 +1451,8 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
         c->stats.light_rays = k.light_rays;
         c->stats.bsdf_rays = k.bsdf_rays;
         c->stats.iterations = (uint32_t)k.iterations;
-        launches += 1 + kStages * (uint32_t)k.iterations + (uint32_t)(k.iterations / c->tuning.loop_iterations);
+        launches += 1 + launches_per_iteration(c->batch_shape) * (uint32_t)k.iterations +
+                    (uint32_t)(k.iterations / c->tuning.loop_iterations);
         c->stats.light_traversals = k.light_traversals;
         c->stats.nonfinite_samples = k.nonfinite;
     }
@@ -1461,7 +1465,8 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
         const FilmPtrs fp{films[i].rgb, films[i].bounces, films[i].counts};
         const Wavefront w = wave_view(c, (uint32_t)(a.total < cap_max ? a.total : cap_max));
         const lt_status st = run_loop(
-            c, w, a, false, [&]() { return launch_wave_init(s->dev, w, a, fp, c->shape, c->stream); },
+            c, w, a, false, launches_per_iteration(c->shape),
+            [&]() { return launch_wave_init(s->dev, w, a, fp, c->shape, c->stream); },
             [&](int stage, int cur) { return launch_wave_stage(stage, s->dev, w, a, fp, cur, c->shape, c->stream); });
         if (st != LT_OK) return st;
         launches += c->stats.kernel_launches;
@@ -1777,14 +1782,14 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
             const SceneTable *t = c->table_dev;
             if (adjoint)
                 st = run_loop(
-                    c, w, all, c->stage_timing,
+                    c, w, all, c->stage_timing, kStages,
                     [&]() { return launch_awave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_awave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
                     });
             else
                 st = run_loop(
-                    c, w, all, c->stage_timing,
+                    c, w, all, c->stage_timing, kStages,
                     [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_dwave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);

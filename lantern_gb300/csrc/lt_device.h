@@ -129,7 +129,13 @@ struct LaunchShape {
     int diff_adj_batch_blocks = 0;
     int atrace_blocks = 0, ashade_blocks = 0;  // adjoint on the wavefront
     int atrace_batch_blocks = 0, ashade_batch_blocks = 0;
+    // plain renders with the BVH2: iterations of at most coop_limit rays are
+    // traced by k_trace_tail (one warp per ray) on tail_blocks blocks
+    int tail_blocks = 0;
+    uint32_t coop_limit = 0;
 };
+// Kernel launches per wavefront iteration of a plain render with this shape.
+inline uint32_t launches_per_iteration(const LaunchShape &ls) { return ls.coop_limit ? 3u : 2u; }
 
 // Parameters of the differentiable render (device arrays): per-triangle RGB
 // albedo and emission, per-medium RGB sigma_a / sigma_s, and the detached

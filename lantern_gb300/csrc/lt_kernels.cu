@@ -1927,7 +1927,8 @@ __device__ __forceinline__ void resolve_connection_diff(const Src &src, const Wa
 // counters->trace_fetch (zeroed by the launch before). Path rays come first so
 // that the short connection queries fill the tail.
 template <class Src, class B>
-__global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trace(Src src, Wavefront W, int cur) {
+__global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256)
+    k_trace(Src src, Wavefront W, int cur, uint32_t coop_limit = 0) {
     const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
     const uint32_t n = n_push + n_cam;
     const uint32_t nc = W.counters->ccount[cur ^ 1];
@@ -1940,6 +1941,7 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
         W.counters->fcount[cur ^ 1] = 0;  // filled by the next differentiable shade
         W.counters->main_rays += n;
     }
+    if (total <= coop_limit) return;  // k_trace_tail traces this iteration
     TraceGrads *gt = nullptr;  // the single-scene adjoint's connection terms
     if constexpr (Src::kAdj && !Src::kMany) {
         gt = grad_table<Src, TraceGrads>();
@@ -1994,6 +1996,178 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256) k_trac
         __syncthreads();
         gt->flush();
     }
+}
+
+// ------------------------------------------------------------------ small iterations
+// The last iterations of a render trace few rays (a 1-spp 1024x1024 frame:
+// 50-7,000 paths from its sixth bounce on), and a launch then lasts as long as
+// its slowest ray, one dependent node fetch after the other (about 180 us for
+// a ray inside the 1.3M-triangle glass mesh). When an iteration has at most
+// `coop_limit` rays, k_trace returns at once and k_trace_tail gives every ray
+// a warp: each step the warp takes up to 32 entries off the ray's stack in
+// shared memory, tests their child boxes (inner nodes) or triangles (leaves)
+// in parallel with the closest distance found so far, and pushes the children
+// hit; the warp's closest hit (or any occluder) is the ray's. The same
+// triangles are tested with the same arithmetic, so the hit is the sequential
+// traversal's up to the choice between hits at exactly the same distance.
+constexpr int kCoopStack = 1024;     // stack entries per warp
+constexpr int kCoopWarps = 8;        // warps per block (256 threads)
+constexpr uint32_t kCoopRaysPerWarp = 2;
+
+__device__ __forceinline__ Hit coop_traverse(const Geo &g, v3 O, v3 D, float tnear, float tfar, bool any,
+                                             uint32_t skip_geom, int *st) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned full = 0xFFFFFFFFu;
+    const v3 inv = mk(safe_inv(D.x), safe_inv(D.y), safe_inv(D.z));
+    Hit best;
+    best.t = tfar;
+    best.u = best.v = 0.0f;
+    best.prim = kMiss;
+    if (lane == 0) st[0] = 0;  // the root (an inner node)
+    int sp = 1;                // warp-uniform
+    __syncwarp();
+    while (sp > 0) {
+        // at most 32 entries: each taken entry pushes at most two, so a step
+        // grows the stack by at most 32 (to kCoopStack - 96 from at most
+        // kCoopStack - 128); above that, one entry per step, depth first, which
+        // adds at most the tree's depth (< 64, as the sequential stack holds)
+        int m = sp < 32 ? sp : 32;
+        if (sp > kCoopStack - 128) m = 1;
+        const bool have = (int)lane < m;
+        const int node = have ? st[sp - 1 - (int)lane] : 0;
+        __syncwarp();
+        sp -= m;
+        const float tmax = best.t;
+        int push0 = 0, push1 = 0, npush = 0;  // children to push, far one first
+        Hit mine = best;
+        bool occluded = false;
+        if (have && node >= 0) {
+            const float4 *nd = g.nodes + 4 * node;
+            const float4 n0 = ldg4(nd), n1 = ldg4(nd + 1), n2 = ldg4(nd + 2), n3 = ldg4(nd + 3);
+            float t0, t1;
+            const bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, O, inv, tnear, tmax, t0);
+            const bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, O, inv, tnear, tmax, t1);
+            const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+            if (h0 && h1) {
+                npush = 2;
+                if (t1 < t0) {
+                    push0 = c0;
+                    push1 = c1;
+                } else {
+                    push0 = c1;
+                    push1 = c0;
+                }
+            } else if (h0 || h1) {
+                npush = 1;
+                push0 = h0 ? c0 : c1;
+            }
+        } else if (have) {
+            const uint32_t code = ~(uint32_t)node;
+            const uint32_t first = code >> kLeafBits, count = code & ((1u << kLeafBits) - 1u);
+            for (uint32_t k = 0; k < count; ++k) {
+                const float4 *tri = g.tris + 3 * (first + k);
+                if (!any) {
+                    tri_test(tri, O, D, tnear, mine);
+                } else if (!occluded) {
+                    Hit c = best;
+                    tri_test(tri, O, D, tnear, c);
+                    if (c.prim != kMiss && __ldg(g.tri_geom + c.prim) != skip_geom) {
+                        occluded = true;
+                        mine.prim = c.prim;
+                    }
+                }
+            }
+        }
+        if (any) {
+            const unsigned occ = __ballot_sync(full, occluded);
+            if (occ) {
+                best.prim = __shfl_sync(full, mine.prim, __ffs(occ) - 1);
+                return best;
+            }
+        } else {
+            float tmin = mine.t;
+            for (int o = 16; o > 0; o >>= 1) tmin = fminf(tmin, __shfl_xor_sync(full, tmin, o));
+            if (tmin < best.t) {  // the lowest lane holding the closest new hit
+                const int src = __ffs(__ballot_sync(full, mine.prim != kMiss && mine.t == tmin)) - 1;
+                best.t = tmin;
+                best.u = __shfl_sync(full, mine.u, src);
+                best.v = __shfl_sync(full, mine.v, src);
+                best.prim = __shfl_sync(full, mine.prim, src);
+            }
+        }
+        // push: the entries of higher lanes first, so that lane 0's (the top
+        // entry's children) end on top
+        const unsigned b1 = __ballot_sync(full, npush >= 1), b2 = __ballot_sync(full, npush == 2);
+        const unsigned above = lane == 31u ? 0u : full << (lane + 1u);
+        const int off = sp + __popc(b1 & above) + __popc(b2 & above);
+        if (npush == 2) {
+            st[off] = push0;
+            st[off + 1] = push1;
+        } else if (npush == 1) {
+            st[off] = push0;
+        }
+        sp += __popc(b1) + __popc(b2);
+        __syncwarp();
+    }
+    return best;
+}
+
+// The rays of an iteration with at most coop_limit of them (k_trace returned):
+// one warp per path ray or connection record, fetched from trace_fetch.
+template <class Src>
+__global__ void __launch_bounds__(kCoopWarps * 32) k_trace_tail(Src src, Wavefront W, int cur, uint32_t coop_limit) {
+    const uint32_t n_push = W.counters->count[cur], n_cam = W.counters->rcount[cur];
+    const uint32_t n = n_push + n_cam;
+    const uint32_t nc = W.counters->ccount[cur ^ 1];
+    const uint32_t total = n + nc;
+    if (total > coop_limit) return;  // k_trace traced them
+    __shared__ int stacks[kCoopWarps][kCoopStack];
+    const uint32_t lane = threadIdx.x & 31u;
+    int *st = stacks[threadIdx.x >> 5];
+    const uint32_t cap = W.capacity;
+    uint32_t n_trav = 0;
+    for (;;) {
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(&W.counters->trace_fetch, 1u);
+        idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
+        if (idx >= total) break;
+        Trav r;  // the ray and its result, in the form the resolve functions read
+        uint32_t kl = 0, s = 0;
+        Geo g;
+        if (idx < n) {
+            s = queue_slot(idx, n_push, n_cam, cap);
+            g = geo_of(src.scene(Src::kMany ? ld_s(W.p[cur].flags + s) >> kFlagSceneShift : 0u));
+            const float4 a = ld_s(W.ray[cur] + 2 * s), b = ld_s(W.ray[cur] + 2 * s + 1);
+            r.O = mk(a.x, a.y, a.z);
+            r.D = mk(b.x, b.y, b.z);
+            r.any = false;
+            r.h = coop_traverse(g, r.O, r.D, a.w, b.w, false, 0, st);
+        } else {
+            const uint32_t c = idx - n;
+            const float4 a = ld_s(W.cray + 2 * c), b = ld_s(W.cray + 2 * c + 1);
+            kl = __float_as_uint(a.w);
+            const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
+            g = geo_of(S);
+            const LightInfo &L = S.lights[kl & kConnLightMask];
+            r.O = mk(a.x, a.y, a.z);
+            r.D = mk(b.x, b.y, b.z);
+            r.any = b.w > 0.0f;
+            r.h = coop_traverse(g, r.O, r.D, 0.001f, r.any ? b.w : __int_as_float(0x7f800000), r.any,
+                                (uint32_t)L.geom, st);
+            n_trav++;
+        }
+        if (lane == 0) {
+            if (idx < n) {
+                st_s(W.hits + s, make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
+            } else {
+                const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
+                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, nullptr);
+                else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
 }
 
 // While-node condition of a captured wavefront loop (one thread): continue
@@ -2447,6 +2621,9 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
                                  : blocks_for(k_trace<OneScene, Bvh2>, tt, sms, trav_smem<Bvh2>(tt));
         out->shade_blocks = blocks_for(k_shade<OneScene>, out->shade_threads, sms);
     }
+    out->tail_blocks = batch ? blocks_for(k_trace_tail<ManyScenes>, kCoopWarps * 32, sms)
+                             : blocks_for(k_trace_tail<OneScene>, kCoopWarps * 32, sms);
+    out->coop_limit = out->bvh_width == 2 ? (uint32_t)out->tail_blocks * kCoopWarps * kCoopRaysPerWarp : 0u;
     out->isect_blocks = w8   ? blocks_for(k_intersect<Bvh8>, 128, sms, trav_smem<Bvh8>(128))
                         : w4 ? blocks_for(k_intersect<Bvh4>, 128, sms, trav_smem<Bvh4>(128))
                              : blocks_for(k_intersect<Bvh2>, 128, sms, trav_smem<Bvh2>(128));
@@ -2469,6 +2646,7 @@ cudaError_t preload_wave_kernels() {
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_trace<OneScene, Bvh4>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_trace<OneScene, Bvh8>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<OneScene>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_trace_tail<OneScene>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_add_counts);
     return e;
 }
@@ -2596,7 +2774,10 @@ static cudaError_t stage(int stage, const Src &src, const Wavefront &w, int cur,
         const int tt = ls.trace_threads;
         if (w8) k_trace<Src, Bvh8><<<ls.trace_blocks, tt, trav_smem<Bvh8>(tt), st>>>(src, w, cur);
         else if (ls.bvh_width == 4) k_trace<Src, Bvh4><<<ls.trace_blocks, tt, trav_smem<Bvh4>(tt), st>>>(src, w, cur);
-        else k_trace<Src, Bvh2><<<ls.trace_blocks, tt, trav_smem<Bvh2>(tt), st>>>(src, w, cur);
+        else {  // BVH2: the iterations of at most coop_limit rays go to k_trace_tail
+            k_trace<Src, Bvh2><<<ls.trace_blocks, tt, trav_smem<Bvh2>(tt), st>>>(src, w, cur, ls.coop_limit);
+            if (ls.coop_limit) k_trace_tail<Src><<<ls.tail_blocks, kCoopWarps * 32, 0, st>>>(src, w, cur, ls.coop_limit);
+        }
     } else {
         k_shade<Src><<<ls.shade_blocks, ls.shade_threads, 0, st>>>(src, w, cur);
     }

@@ -29,7 +29,7 @@ def test_stage_times_and_counts(scene_dir, paths):
     busy = st.init_ms + st.trace_ms + st.shade_ms
     assert busy <= st.gpu_ms * 1.001 + 1e-3
     assert st.idle_ms >= 0 and abs(busy + st.idle_ms - st.gpu_ms) <= 1e-3 * st.gpu_ms + 1e-3
-    assert st.kernel_launches == 1 + 2 * st.iterations
+    assert st.kernel_launches == 1 + 3 * st.iterations  # camera rays; trace, small-iteration trace, shade
     assert st.main_rays >= st.samples  # every sample traces its camera ray
     assert st.light_traversals <= st.light_rays + st.bsdf_rays
     assert int(fb.ColorSampleCount.min()) == 8
