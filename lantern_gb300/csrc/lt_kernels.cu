@@ -2012,7 +2012,7 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256)
 // traversal's up to the choice between hits at exactly the same distance.
 constexpr int kCoopStack = 1024;     // stack entries per warp
 constexpr int kCoopWarps = 8;        // warps per block (256 threads)
-constexpr uint32_t kCoopRaysPerWarp = 2;
+constexpr uint32_t kCoopRaysPerWarp = 8;
 
 __device__ __forceinline__ Hit coop_traverse(const Geo &g, v3 O, v3 D, float tnear, float tfar, bool any,
                                              uint32_t skip_geom, int *st) {
