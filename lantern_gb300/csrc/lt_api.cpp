@@ -1079,7 +1079,7 @@ static lt_status diff_wave(lt_ctx *c, const DevScene &dev, const DiffParams &P, 
     if (st != LT_OK) return st;
     d.sample_I = sample_I;
     st = run_loop(
-        c, w, a, c->stage_timing, kStages, [&]() { return launch_dwave_init(dev, P, d, w, a, f, c->shape, c->stream); },
+        c, w, a, c->stage_timing, kStages + 1u, [&]() { return launch_dwave_init(dev, P, d, w, a, f, c->shape, c->stream); },
         [&](int stage, int cur) { return launch_dwave_stage(stage, dev, P, d, w, a, f, cur, c->shape, c->stream); });
     if (st != LT_OK) return st;
     CUDA_TRY(c, launch_diff_film(d.sample_I, a, f, c->stream));
@@ -1133,7 +1133,7 @@ static lt_status adjoint_wave(lt_ctx *c, const DevScene &dev, const DiffParams &
     lt_status st = prepare_dwave(c, a.total, &cap, &w, &d);
     if (st != LT_OK) return st;
     return run_loop(
-        c, w, a, c->stage_timing, kStages, [&]() { return launch_awave_init(dev, P, d, G, w, a, c->shape, c->stream); },
+        c, w, a, c->stage_timing, kStages + 1u, [&]() { return launch_awave_init(dev, P, d, G, w, a, c->shape, c->stream); },
         [&](int stage, int cur) { return launch_awave_stage(stage, dev, P, d, G, w, a, cur, c->shape, c->stream); });
 }
 
@@ -1782,14 +1782,14 @@ static lt_status diff_batch(lt_ctx *c, const lt_diff_job *jobs, uint32_t n, bool
             const SceneTable *t = c->table_dev;
             if (adjoint)
                 st = run_loop(
-                    c, w, all, c->stage_timing, kStages,
+                    c, w, all, c->stage_timing, kStages + 1u,
                     [&]() { return launch_awave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_awave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);
                     });
             else
                 st = run_loop(
-                    c, w, all, c->stage_timing, kStages,
+                    c, w, all, c->stage_timing, kStages + 1u,
                     [&]() { return launch_dwave_batch_init(t, dw, w, c->batch_shape, c->stream); },
                     [&](int stage, int cur) {
                         return launch_dwave_batch_stage(stage, t, dw, w, cur, c->batch_shape, c->stream);

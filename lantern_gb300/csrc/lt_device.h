@@ -133,8 +133,11 @@ struct LaunchShape {
     // traced by k_trace_tail (one warp per ray) on tail_blocks blocks
     int tail_blocks = 0;
     uint32_t coop_limit = 0;
+    // the same kernel for the differentiable forward and the adjoint (always BVH2)
+    int dtail_blocks = 0, dtail_batch_blocks = 0, atail_blocks = 0, atail_batch_blocks = 0;
 };
-// Kernel launches per wavefront iteration of a plain render with this shape.
+// Kernel launches per wavefront iteration of a plain render with this shape
+// (the differentiable ones always launch three: trace, small-iteration trace, shade).
 inline uint32_t launches_per_iteration(const LaunchShape &ls) { return ls.coop_limit ? 3u : 2u; }
 
 // Parameters of the differentiable render (device arrays): per-triangle RGB

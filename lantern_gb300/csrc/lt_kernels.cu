@@ -2121,6 +2121,12 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_trace_tail(Src src, Wavefro
     const uint32_t nc = W.counters->ccount[cur ^ 1];
     const uint32_t total = n + nc;
     if (total > coop_limit) return;  // k_trace traced them
+    TraceGrads *gt = nullptr;  // the single-scene adjoint's connection terms
+    if constexpr (Src::kAdj && !Src::kMany) {
+        gt = grad_table<Src, TraceGrads>();
+        gt->init();
+        __syncthreads();
+    }
     __shared__ int stacks[kCoopWarps][kCoopStack];
     const uint32_t lane = threadIdx.x & 31u;
     int *st = stacks[threadIdx.x >> 5];
@@ -2161,13 +2167,17 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_trace_tail(Src src, Wavefro
                 st_s(W.hits + s, make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
-                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, nullptr);
+                if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, gt);
                 else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
             }
         }
         __syncwarp();
     }
     if (lane == 0 && n_trav) atomicAdd(&W.counters->light_traversals, (unsigned long long)n_trav);
+    if constexpr (Src::kAdj && !Src::kMany) {
+        __syncthreads();
+        gt->flush();
+    }
 }
 
 // While-node condition of a captured wavefront loop (one thread): continue
@@ -2590,6 +2600,9 @@ __global__ void __launch_bounds__(128, 6) k_diff_adjoint_batch(SceneTable *t) {
 
 }  // namespace
 
+// Rays of an iteration up to which k_trace_tail traces it on `blocks` blocks.
+static uint32_t coop_limit(int blocks) { return (uint32_t)blocks * kCoopWarps * kCoopRaysPerWarp; }
+
 template <class F>
 static int blocks_for(F kernel, int threads, int sms, size_t smem = 0) {
     int b = 0;
@@ -2623,7 +2636,11 @@ void query_launch_shape(int device, bool batch, LaunchShape *out) {
     }
     out->tail_blocks = batch ? blocks_for(k_trace_tail<ManyScenes>, kCoopWarps * 32, sms)
                              : blocks_for(k_trace_tail<OneScene>, kCoopWarps * 32, sms);
-    out->coop_limit = out->bvh_width == 2 ? (uint32_t)out->tail_blocks * kCoopWarps * kCoopRaysPerWarp : 0u;
+    out->coop_limit = out->bvh_width == 2 ? coop_limit(out->tail_blocks) : 0u;
+    out->dtail_blocks = blocks_for(k_trace_tail<DiffOne>, kCoopWarps * 32, sms);
+    out->dtail_batch_blocks = blocks_for(k_trace_tail<DiffMany>, kCoopWarps * 32, sms);
+    out->atail_blocks = blocks_for(k_trace_tail<AdjOne>, kCoopWarps * 32, sms);
+    out->atail_batch_blocks = blocks_for(k_trace_tail<AdjMany>, kCoopWarps * 32, sms);
     out->isect_blocks = w8   ? blocks_for(k_intersect<Bvh8>, 128, sms, trav_smem<Bvh8>(128))
                         : w4 ? blocks_for(k_intersect<Bvh4>, 128, sms, trav_smem<Bvh4>(128))
                              : blocks_for(k_intersect<Bvh2>, 128, sms, trav_smem<Bvh2>(128));
@@ -2661,8 +2678,13 @@ cudaError_t launch_dwave_stage(int stage, const DevScene &s, const DiffParams &p
                                const Wavefront &w, const RenderArgs &a, const FilmPtrs &f, int cur,
                                const LaunchShape &ls, cudaStream_t st) {
     const DiffOne src{s, a, f, p, d};
-    if (stage == kStageTrace) k_trace<DiffOne, Bvh2><<<ls.dtrace_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
-    else k_dshade<DiffOne><<<ls.dshade_blocks, 256, 0, st>>>(src, w, cur);
+    if (stage == kStageTrace) {
+        const uint32_t coop = coop_limit(ls.dtail_blocks);
+        k_trace<DiffOne, Bvh2><<<ls.dtrace_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur, coop);
+        k_trace_tail<DiffOne><<<ls.dtail_blocks, kCoopWarps * 32, 0, st>>>(src, w, cur, coop);
+    } else {
+        k_dshade<DiffOne><<<ls.dshade_blocks, 256, 0, st>>>(src, w, cur);
+    }
     return cudaGetLastError();
 }
 
@@ -2675,9 +2697,13 @@ cudaError_t launch_dwave_batch_init(const SceneTable *t, const DiffWave &d, cons
 cudaError_t launch_dwave_batch_stage(int stage, const SceneTable *t, const DiffWave &d, const Wavefront &w, int cur,
                                      const LaunchShape &ls, cudaStream_t st) {
     const DiffMany src{t, d};
-    if (stage == kStageTrace)
-        k_trace<DiffMany, Bvh2><<<ls.dtrace_batch_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
-    else k_dshade<DiffMany><<<ls.dshade_batch_blocks, 256, 0, st>>>(src, w, cur);
+    if (stage == kStageTrace) {
+        const uint32_t coop = coop_limit(ls.dtail_batch_blocks);
+        k_trace<DiffMany, Bvh2><<<ls.dtrace_batch_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur, coop);
+        k_trace_tail<DiffMany><<<ls.dtail_batch_blocks, kCoopWarps * 32, 0, st>>>(src, w, cur, coop);
+    } else {
+        k_dshade<DiffMany><<<ls.dshade_batch_blocks, 256, 0, st>>>(src, w, cur);
+    }
     return cudaGetLastError();
 }
 
@@ -2691,8 +2717,13 @@ cudaError_t launch_awave_stage(int stage, const DevScene &s, const DiffParams &p
                                const DiffGrads &g, const Wavefront &w, const RenderArgs &a, int cur,
                                const LaunchShape &ls, cudaStream_t st) {
     const AdjOne src{s, a, p, d, g};
-    if (stage == kStageTrace) k_trace<AdjOne, Bvh2><<<ls.atrace_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
-    else k_dshade<AdjOne><<<ls.ashade_blocks, 256, 0, st>>>(src, w, cur);
+    if (stage == kStageTrace) {
+        const uint32_t coop = coop_limit(ls.atail_blocks);
+        k_trace<AdjOne, Bvh2><<<ls.atrace_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur, coop);
+        k_trace_tail<AdjOne><<<ls.atail_blocks, kCoopWarps * 32, 0, st>>>(src, w, cur, coop);
+    } else {
+        k_dshade<AdjOne><<<ls.ashade_blocks, 256, 0, st>>>(src, w, cur);
+    }
     return cudaGetLastError();
 }
 
@@ -2705,9 +2736,13 @@ cudaError_t launch_awave_batch_init(const SceneTable *t, const DiffWave &d, cons
 cudaError_t launch_awave_batch_stage(int stage, const SceneTable *t, const DiffWave &d, const Wavefront &w, int cur,
                                      const LaunchShape &ls, cudaStream_t st) {
     const AdjMany src{t, d};
-    if (stage == kStageTrace)
-        k_trace<AdjMany, Bvh2><<<ls.atrace_batch_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur);
-    else k_dshade<AdjMany><<<ls.ashade_batch_blocks, 256, 0, st>>>(src, w, cur);
+    if (stage == kStageTrace) {
+        const uint32_t coop = coop_limit(ls.atail_batch_blocks);
+        k_trace<AdjMany, Bvh2><<<ls.atrace_batch_blocks, 256, trav_smem<Bvh2>(256), st>>>(src, w, cur, coop);
+        k_trace_tail<AdjMany><<<ls.atail_batch_blocks, kCoopWarps * 32, 0, st>>>(src, w, cur, coop);
+    } else {
+        k_dshade<AdjMany><<<ls.ashade_batch_blocks, 256, 0, st>>>(src, w, cur);
+    }
     return cudaGetLastError();
 }
 
