@@ -29,8 +29,9 @@ extern "C" {
 #endif
 
 /* 2: lt_render_stats gained init_ms and idle_ms; lt_light_info, lt_scene_lights_get,
- * lt_trim and lt_debug_set_iteration_limit were added. */
-#define LT_ABI_VERSION 2
+ * lt_trim and lt_debug_set_iteration_limit were added.
+ * 3: LT_ERR_CHECK and lt_debug_set_check_pixel_limit were added. */
+#define LT_ABI_VERSION 3
 
 typedef enum lt_status {
     LT_OK = 0,
@@ -41,7 +42,8 @@ typedef enum lt_status {
     LT_ERR_IO = 5,          /* file missing or unreadable */
     LT_ERR_PARSE = 6,       /* malformed scene JSON or LMF */
     LT_ERR_UNSUPPORTED = 7, /* feature outside this build */
-    LT_ERR_STATE = 8        /* call out of order (e.g. render without a scene) */
+    LT_ERR_STATE = 8,       /* call out of order (e.g. render without a scene) */
+    LT_ERR_CHECK = 9        /* a device-side bound check failed (liblantern_gpu_checked.so only) */
 } lt_status;
 
 typedef struct lt_ctx lt_ctx;
@@ -480,6 +482,27 @@ void lt_debug_fail_allocations(uint32_t after);
  * such bound (its loop constant is 1500 bounces, integrator.cpp:114) and
  * reports failures as bool + printf (scene.cpp:200-213). */
 void lt_debug_set_iteration_limit(uint64_t limit);
+
+/* Bound-checked build. liblantern_gpu_checked.so is this library with its
+ * kernels compiled with -DLT_CHECKS=1: the wavefront's trace, small-iteration
+ * trace and shade kernels (plain, batched and differentiable) and the BVH2 and
+ * 4-wide traversals check every queue slot, connection record, BVH node, leaf
+ * range, traversal stack entry, hit primitive, scene slot, light, medium, mesh,
+ * material and film pixel index they form against its array before the access
+ * (the 8-wide traversal bounds its indices in both builds). A failed check
+ * records its kind and the index (the first failure of a render wins), skips
+ * the access, and the render's later kernels return at once; the render call
+ * then returns LT_ERR_CHECK, its message naming the check and the index. The
+ * stand-in for compute-sanitizer, which this library's test machines cannot
+ * run. In the plain library the checks compile to nothing (the same registers
+ * and spills per kernel) and this status never occurs.
+ *
+ * For the checked build's own tests: film pixel checks accept only pixels
+ * below `pixels` (0, the initial state: the film's own size), so that a normal
+ * render fails a check whose access would have been in bounds. Applies to
+ * wavefronts laid out after the call; process-wide; ignored by the plain
+ * library. No counterpart in the reference. */
+void lt_debug_set_check_pixel_limit(uint32_t pixels);
 
 #ifdef __cplusplus
 }

@@ -1,5 +1,9 @@
 """Build liblantern_gpu.so in-tree (lantern_gb300/_build) for sm_103a.
 
+Beside it, liblantern_gpu_checked.so: the same objects with the kernels
+compiled with -DLT_CHECKS=1 (device-side bound checks, LT_ERR_CHECK), for test
+runs (lantern_gb300.native loads it when LANTERN_GPU_CHECKED=1).
+
 nvcc compiles the kernels with -gencode arch=compute_103a,code=sm_103a and
 -fmad=false (the integrator's arithmetic is spelled out operation by
 operation; the traversal writes its fused multiply-adds explicitly); g++
@@ -19,6 +23,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liblantern_gpu.so")
+CHECKED_LIB = os.path.join(BUILD, "liblantern_gpu_checked.so")
+CHECKED_SOURCE = "lt_kernels.cu"  # the translation unit that holds the checks
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -42,9 +48,9 @@ def _headers():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CHECKED_LIB):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CHECKED_LIB))
     return all(os.path.getmtime(f) <= t for f in _sources() + _headers() + [__file__])
 
 
@@ -59,6 +65,9 @@ def build(force: bool = False, verbose: bool = False, extra_nvcc=()) -> str:
         o = os.path.join(BUILD, f + ".o")
         objs.append(o)
         jobs.append([NVCC] + NVCC_FLAGS + list(extra_nvcc) + ["-c", os.path.join(CSRC, f), "-o", o])
+    checked_obj = os.path.join(BUILD, CHECKED_SOURCE + ".checked.o")
+    jobs.append([NVCC] + NVCC_FLAGS + list(extra_nvcc) + ["-DLT_CHECKS=1", "-c", os.path.join(CSRC, CHECKED_SOURCE),
+                                                          "-o", checked_obj])
     for f in CPP_SOURCES:
         o = os.path.join(BUILD, f + ".o")
         objs.append(o)
@@ -74,12 +83,14 @@ def build(force: bool = False, verbose: bool = False, extra_nvcc=()) -> str:
     if failed:
         msg = "\n".join(" ".join(j) + "\n" + out for j, out in failed)
         raise RuntimeError("liblantern_gpu build failed:\n" + msg)
-    tmp = LIB + f".{os.getpid()}.tmp"
-    link = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"]
-    r = subprocess.run(link, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-    os.replace(tmp, LIB)
+    plain_obj = os.path.join(BUILD, CHECKED_SOURCE + ".o")
+    for lib, lib_objs in ((CHECKED_LIB, [checked_obj if o == plain_obj else o for o in objs]), (LIB, objs)):
+        tmp = lib + f".{os.getpid()}.tmp"
+        link = [NVCC] + ARCH + ["-shared", "-o", tmp] + lib_objs + ["-lpthread", "-ldl"]
+        r = subprocess.run(link, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+        os.replace(tmp, lib)
     return LIB
 
 

@@ -128,6 +128,8 @@ static bool injected_alloc_failure() {
 // Wavefront iteration cap for failure-handling tests
 // (lt_debug_set_iteration_limit); 0 = the library's own bound.
 static std::atomic<unsigned long long> g_iteration_limit{0};
+// Film pixels that the bound checks of an LT_CHECKS build accept (0: the film's own size).
+static std::atomic<uint32_t> g_check_pixels{0};
 
 // Iterations a render may take before it reports LT_ERR_TIMEOUT: every path
 // ends within max_depth iterations of its start and at most `cap` work items
@@ -162,6 +164,19 @@ static lt_status fail(lt_ctx *c, lt_status st, const char *fmt, ...) {
     } catch (...) {  // no memory for the message: the status still goes back
     }
     return st;
+}
+
+// Names of the device-side bound checks (LT_CHECKS builds), by code.
+static const char *check_name(uint32_t code) {
+    static const char *names[] = {"none", "path queue slot", "connection record", "output queue slot",
+                                  "BVH node", "leaf triangles", "traversal stack", "hit primitive",
+                                  "scene slot", "light", "medium", "film pixel", "mesh", "material"};
+    return code < sizeof(names) / sizeof(names[0]) ? names[code] : "unknown";
+}
+
+// A failed device-side bound check recorded in the counters (LT_CHECKS builds).
+static lt_status check_failed(lt_ctx *c, const WaveCounters &k) {
+    return fail(c, LT_ERR_CHECK, "device bound check failed: %s (index %u)", check_name(k.check), k.check_value);
 }
 
 // No C++ exception crosses the C ABI: every entry point's body is a function
@@ -581,6 +596,10 @@ lt_status lt_scene_create(lt_ctx *c, const lt_scene_desc *desc) try {
     }
     d.num_lights = (uint32_t)h.lights.size();
     d.num_tris = (uint32_t)h.tri_geom.size();
+    d.num_nodes = c->num_nodes;
+    d.num_geoms = (uint32_t)h.geoms.size();
+    d.num_mats = (uint32_t)h.materials.size();
+    d.num_media = (uint32_t)h.media.size();
     d.background = h.background;
     d.cam = h.camera;
     d.filter = h.filter;
@@ -672,6 +691,7 @@ static size_t carve_wave(char *base, uint32_t cap, Wavefront *w) {
     w->cray = (float4 *)take(64 * P);
     w->crec = (float4 *)take(64 * P);
     w->counters = (WaveCounters *)take(sizeof(WaveCounters));
+    w->check_pixels = g_check_pixels.load();
     return off;
 }
 
@@ -815,6 +835,7 @@ static lt_status run_loop(lt_ctx *c, const Wavefront &w, const RenderArgs &a, bo
         CUDA_TRY(c, cudaMemcpyAsync(c->counters_host, w.counters, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
                                     c->stream));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if (c->counters_host->check) return check_failed(c, *c->counters_host);
         // done when no path ray is queued and the last shade emitted no connection
         if (c->counters_host->count[cur] == 0 && c->counters_host->rcount[cur] == 0 &&
             c->counters_host->ccount[cur ^ 1] == 0)
@@ -1304,7 +1325,8 @@ static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
                                   (uintptr_t)c->batch_shape.trace_threads, (uintptr_t)c->batch_shape.trace_blocks,
                                   (uintptr_t)c->batch_shape.shade_threads, (uintptr_t)c->batch_shape.shade_blocks,
                                   (uintptr_t)c->batch_shape.bvh_width, c->tuning.loop_iterations,
-                                  (uintptr_t)c->batch_shape.tail_blocks, (uintptr_t)c->batch_shape.coop_limit};
+                                  (uintptr_t)c->batch_shape.tail_blocks, (uintptr_t)c->batch_shape.coop_limit,
+                                  (uintptr_t)w.check_pixels};
     if (c->graph_exec && key == c->graph_key) return LT_OK;
     free_graph(c);
     cudaStream_t cs = c->own_stream;
@@ -1446,6 +1468,7 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
                                     c->stream));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
         const WaveCounters &k = *c->counters_host;
+        if (k.check) return check_failed(c, k);
         if (k.error == 2) return fail(c, LT_ERR_TIMEOUT, "batched wavefront did not drain in %llu iterations", k.iterations);
         c->stats.main_rays = k.main_rays;
         c->stats.light_rays = k.light_rays;
@@ -1865,3 +1888,5 @@ extern "C" lt_status lt_image_load(const char *path, uint8_t *texels, size_t cap
 extern "C" void lt_debug_fail_allocations(uint32_t after) { g_alloc_left.store(after); }
 
 extern "C" void lt_debug_set_iteration_limit(uint64_t limit) { g_iteration_limit.store(limit); }
+
+extern "C" void lt_debug_set_check_pixel_limit(uint32_t pixels) { g_check_pixels.store(pixels); }

@@ -32,6 +32,8 @@ struct DevScene {
     uint32_t num_lights;
     uint32_t num_tris;
     uint32_t num_nodes8;
+    uint32_t num_nodes;         // BVH2 nodes
+    uint32_t num_geoms, num_mats, num_media;
     v3 background;
     Camera cam;
     TentFilter filter;
@@ -63,6 +65,8 @@ struct WaveCounters {
     unsigned long long iterations;        // wavefront iterations of a captured loop
     unsigned long long nonfinite;         // film contributions with a NaN or infinite channel
     uint32_t fcount[2];                   // differentiable forward: finishing entries by parity
+    uint32_t check;                       // builds with LT_CHECKS: code of the first failed bound check
+    uint32_t check_value;                 // and the index it rejected
 };
 
 struct Wavefront {
@@ -73,6 +77,7 @@ struct Wavefront {
     float4 *cray = nullptr;                 // 2 float4 per record: (org, kind|light) (dir, light distance)
     float4 *crec = nullptr;                 // 2 float4 per record: (f, bsdf pdf) (throughput, pixel)
     WaveCounters *counters = nullptr;
+    uint32_t check_pixels = 0;              // builds with LT_CHECKS: film pixels the checks accept (0: all)
     void *arena = nullptr;
     size_t arena_bytes = 0;
 };

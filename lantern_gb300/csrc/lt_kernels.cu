@@ -42,6 +42,59 @@ __device__ __forceinline__ T ld_s(const T *p) { return __ldcs(p); }
 template <class T>
 __device__ __forceinline__ void st_s(T *p, T v) { __stcs(p, v); }
 
+// ------------------------------------------------------------------ bound checks
+// Compiled with -DLT_CHECKS=1 (liblantern_gpu_checked.so), the wavefront
+// kernels check the indices they form against their arrays before each access:
+// a failed check records its kind and the index in the wave counters (the
+// first failure of a render wins), the access is skipped, and the render's
+// later kernels return at once; the host reports LT_ERR_CHECK. Without
+// LT_CHECKS, LT_CHECK is `true` and its condition is not compiled, so the plain
+// kernels are unchanged. The kinds, in the host's order of check names:
+#ifndef LT_CHECKS
+#define LT_CHECKS 0
+#endif
+enum CheckKind : uint32_t {
+    kChkSlot = 1,  // path queue slot
+    kChkRecord,    // connection record
+    kChkOutSlot,   // output queue slot
+    kChkNode,      // BVH node
+    kChkLeaf,      // leaf triangle range
+    kChkStack,     // traversal stack
+    kChkPrim,      // hit primitive
+    kChkScene,     // scene slot of a batch
+    kChkLight,
+    kChkMedium,
+    kChkPixel,     // film pixel
+    kChkGeom,      // mesh of a triangle
+    kChkMaterial
+};
+#if LT_CHECKS
+__device__ __noinline__ void check_failed(WaveCounters *wc, uint32_t kind, uint32_t value) {
+    if (wc && atomicCAS(&wc->check, 0u, kind) == 0u) wc->check_value = value;
+}
+#define LT_CHECK(wc, cond, kind, value) ((cond) ? true : (check_failed((wc), (kind), (uint32_t)(value)), false))
+// A whole block leaves a kernel of a render whose check failed (thread 0 reads
+// the flag for the block, so that every thread takes the same branch).
+#define LT_STOP_IF_FAILED(wc)                                                  \
+    do {                                                                        \
+        __shared__ uint32_t lt_stop_;                                           \
+        if (threadIdx.x == 0) lt_stop_ = *(volatile uint32_t *)&(wc)->check;    \
+        __syncthreads();                                                        \
+        if (lt_stop_) return;                                                   \
+    } while (0)
+// a film pixel index: below the film's size, or below the test limit
+// Wavefront::check_pixels when that is set and lower
+#define LT_PIXEL_OK(W, pixel, npix)                                                                            \
+    LT_CHECK((W).counters, (pixel) < ((W).check_pixels && (W).check_pixels < (npix) ? (W).check_pixels : (npix)), \
+             kChkPixel, (pixel))
+#else
+#define LT_CHECK(wc, cond, kind, value) (sizeof(cond) > 0)  // not evaluated
+#define LT_PIXEL_OK(W, pixel, npix) true
+#define LT_STOP_IF_FAILED(wc) \
+    do {                      \
+    } while (0)
+#endif
+
 __device__ __forceinline__ float safe_inv(float d) {
     return 1.0f / (fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
 }
@@ -163,10 +216,34 @@ __device__ __forceinline__ void trav_start(Trav &r, St stack, v3 O, v3 D, float 
 struct Geo {
     const float4 *nodes, *tris;
     const uint32_t *tri_geom;
-    uint32_t num_nodes, num_tris;  // bounds of the 8-wide traversal's indices
+    uint32_t num_nodes, num_tris;  // bounds of the node and triangle indices
+#if LT_CHECKS
+    WaveCounters *chk = nullptr;  // where a failed bound check is recorded
+#endif
 };
 
-__device__ __forceinline__ Geo geo_of(const DevScene &S) { return Geo{S.nodes, S.tris, S.tri_geom, 0u, 0u}; }
+__device__ __forceinline__ Geo geo_of(const DevScene &S) {
+    return Geo{S.nodes, S.tris, S.tri_geom, S.num_nodes, S.num_tris};
+}
+
+#if LT_CHECKS
+#define LT_GEO_CHK(g) ((g).chk)
+#define LT_SET_GEO_CHK(g, wc) ((g).chk = (wc))
+#else
+#define LT_GEO_CHK(g) nullptr
+#define LT_SET_GEO_CHK(g, wc) ((void)0)
+#endif
+
+// Checked stack pop of the BVH2 / 4-wide traversals: a failed check ends the ray.
+#define LT_TRAV_POP(S, r, stack)                                               \
+    do {                                                                        \
+        if (LT_CHECK(LT_GEO_CHK(S), (r).sp >= 0, kChkStack, (r).sp)) {          \
+            (r).node = (stack).get((r).sp--);                                   \
+        } else {                                                                \
+            (r).node = kSentinel;                                               \
+            (r).leaf = 0;                                                       \
+        }                                                                       \
+    } while (0)
 
 // Advances the ray until it is finished (r.node == kSentinel) or the warp
 // should refill idle lanes.
@@ -174,6 +251,11 @@ template <class St>
 __device__ __forceinline__ void traverse(const Geo &S, Trav &r, St stack) {
     while (r.node != kSentinel) {
         while ((unsigned)r.node < (unsigned)kSentinel) {
+            if (!LT_CHECK(LT_GEO_CHK(S), (uint32_t)r.node < S.num_nodes, kChkNode, r.node)) {
+                r.node = kSentinel;
+                r.leaf = 0;
+                return;
+            }
             const float4 *n = S.nodes + 4 * r.node;
             float4 n0 = ldg4(n), n1 = ldg4(n + 1), n2 = ldg4(n + 2), n3 = ldg4(n + 3);
             float t0, t1;
@@ -181,24 +263,35 @@ __device__ __forceinline__ void traverse(const Geo &S, Trav &r, St stack) {
             bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r.O, r.inv, r.tnear, r.h.t, t1);
             int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
             if (!h0 && !h1) {
-                r.node = stack.get(r.sp--);
+                LT_TRAV_POP(S, r, stack);
             } else {
                 r.node = h0 ? c0 : c1;
                 if (h0 && h1) {
                     int far = c1;
                     if (t1 < t0) { far = c0; r.node = c1; }
-                    stack.set(++r.sp, far);
+                    if (LT_CHECK(LT_GEO_CHK(S), r.sp + 1 < kStack, kChkStack, r.sp + 1)) {
+                        stack.set(++r.sp, far);
+                    } else {
+                        r.node = kSentinel;
+                        r.leaf = 0;
+                        return;
+                    }
                 }
             }
             if (r.node < 0 && r.leaf >= 0) {  // postpone the first leaf, keep descending
                 r.leaf = r.node;
-                r.node = stack.get(r.sp--);
+                LT_TRAV_POP(S, r, stack);
             }
             if (!__any_sync(__activemask(), r.leaf >= 0)) break;
         }
         while (r.leaf < 0) {
             uint32_t code = ~(uint32_t)r.leaf;
             uint32_t first = code >> kLeafBits, count = code & ((1u << kLeafBits) - 1u);
+            if (!LT_CHECK(LT_GEO_CHK(S), first + count <= S.num_tris, kChkLeaf, first)) {
+                r.node = kSentinel;
+                r.leaf = 0;
+                return;
+            }
             for (uint32_t k = 0; k < count; ++k) {
                 const float4 *tri = S.tris + 3 * (first + k);
                 if (!r.any) {
@@ -206,6 +299,11 @@ __device__ __forceinline__ void traverse(const Geo &S, Trav &r, St stack) {
                 } else {
                     Hit c = r.h;
                     tri_test(tri, r.O, r.D, r.tnear, c);
+                    if (c.prim != kMiss && !LT_CHECK(LT_GEO_CHK(S), c.prim < S.num_tris, kChkPrim, c.prim)) {
+                        r.node = kSentinel;
+                        r.leaf = 0;
+                        return;
+                    }
                     if (c.prim != kMiss && __ldg(S.tri_geom + c.prim) != r.skip_geom) {
                         r.h.prim = c.prim;  // occluded
                         r.node = kSentinel;
@@ -215,7 +313,7 @@ __device__ __forceinline__ void traverse(const Geo &S, Trav &r, St stack) {
                 }
             }
             r.leaf = r.node;
-            if (r.node < 0) r.node = stack.get(r.sp--);
+            if (r.node < 0) LT_TRAV_POP(S, r, stack);
         }
         if (__popc(__activemask()) < kFetchThreshold) return;
     }
@@ -242,6 +340,11 @@ __device__ __forceinline__ void traverse4(const Geo &S, Trav &r, St stack) {
     const float kInf = __int_as_float(0x7f800000);
     while (r.node != kSentinel) {
         while ((unsigned)r.node < (unsigned)kSentinel) {
+            if (!LT_CHECK(LT_GEO_CHK(S), (uint32_t)r.node < S.num_nodes, kChkNode, r.node)) {
+                r.node = kSentinel;
+                r.leaf = 0;
+                return;
+            }
             const float4 *n = S.nodes + 8 * (size_t)r.node;
             const float4 lx = ldg4(n), hx = ldg4(n + 1), ly = ldg4(n + 2), hy = ldg4(n + 3), lz = ldg4(n + 4),
                          hz = ldg4(n + 5), rf = ldg4(n + 6);
@@ -254,7 +357,7 @@ __device__ __forceinline__ void traverse4(const Geo &S, Trav &r, St stack) {
             const bool b3 = slab(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, r.O, r.inv, r.tnear, r.h.t, t3) && c3 != kEmptyRef4;
             const int nh = (int)b0 + (int)b1 + (int)b2 + (int)b3;
             if (nh == 0) {
-                r.node = stack.get(r.sp--);
+                LT_TRAV_POP(S, r, stack);
             } else {
                 if (!b0) t0 = kInf;
                 if (!b1) t1 = kInf;
@@ -265,6 +368,11 @@ __device__ __forceinline__ void traverse4(const Geo &S, Trav &r, St stack) {
                 cswap(t0, c0, t2, c2);
                 cswap(t1, c1, t3, c3);
                 cswap(t1, c1, t2, c2);
+                if (!LT_CHECK(LT_GEO_CHK(S), r.sp + nh - 1 < kStack, kChkStack, r.sp + nh - 1)) {
+                    r.node = kSentinel;
+                    r.leaf = 0;
+                    return;
+                }
                 if (nh > 3) stack.set(++r.sp, c3);
                 if (nh > 2) stack.set(++r.sp, c2);
                 if (nh > 1) stack.set(++r.sp, c1);
@@ -272,13 +380,18 @@ __device__ __forceinline__ void traverse4(const Geo &S, Trav &r, St stack) {
             }
             if (r.node < 0 && r.leaf >= 0) {  // postpone the first leaf, keep descending
                 r.leaf = r.node;
-                r.node = stack.get(r.sp--);
+                LT_TRAV_POP(S, r, stack);
             }
             if (!__any_sync(__activemask(), r.leaf >= 0)) break;
         }
         while (r.leaf < 0) {
             const uint32_t code = ~(uint32_t)r.leaf;
             const uint32_t first = code >> kLeafBits, count = code & ((1u << kLeafBits) - 1u);
+            if (!LT_CHECK(LT_GEO_CHK(S), first + count <= S.num_tris, kChkLeaf, first)) {
+                r.node = kSentinel;
+                r.leaf = 0;
+                return;
+            }
             for (uint32_t k = 0; k < count; ++k) {
                 const float4 *tri = S.tris + 3 * (first + k);
                 if (!r.any) {
@@ -286,6 +399,11 @@ __device__ __forceinline__ void traverse4(const Geo &S, Trav &r, St stack) {
                 } else {
                     Hit c = r.h;
                     tri_test(tri, r.O, r.D, r.tnear, c);
+                    if (c.prim != kMiss && !LT_CHECK(LT_GEO_CHK(S), c.prim < S.num_tris, kChkPrim, c.prim)) {
+                        r.node = kSentinel;
+                        r.leaf = 0;
+                        return;
+                    }
                     if (c.prim != kMiss && __ldg(S.tri_geom + c.prim) != r.skip_geom) {
                         r.h.prim = c.prim;  // occluded
                         r.node = kSentinel;
@@ -295,7 +413,7 @@ __device__ __forceinline__ void traverse4(const Geo &S, Trav &r, St stack) {
                 }
             }
             r.leaf = r.node;
-            if (r.node < 0) r.node = stack.get(r.sp--);
+            if (r.node < 0) LT_TRAV_POP(S, r, stack);
         }
         if (__popc(__activemask()) < kFetchThreshold) return;
     }
@@ -776,6 +894,7 @@ struct OneScene {
         local = item;
         return 0;
     }
+    __device__ __forceinline__ bool valid(uint32_t sid) const { return sid == 0; }
 };
 
 struct ManyScenes {
@@ -796,6 +915,7 @@ struct ManyScenes {
         local = item - t->begin[lo];
         return lo;
     }
+    __device__ __forceinline__ bool valid(uint32_t sid) const { return sid < t->count; }
 };
 
 // The differentiable forward (lt_render_diff) as a third source: one scene,
@@ -819,6 +939,7 @@ struct DiffOne {
         local = item;
         return 0;
     }
+    __device__ __forceinline__ bool valid(uint32_t sid) const { return sid == 0; }
 };
 
 // The batched differentiable forward (lt_render_diff_batch): the scenes of a
@@ -844,6 +965,7 @@ struct DiffMany {
         local = item - t->begin[lo];
         return lo;
     }
+    __device__ __forceinline__ bool valid(uint32_t sid) const { return sid < t->count; }
 };
 
 // The adjoint (lt_render_adjoint with the forward's per-sample radiance) as a
@@ -876,6 +998,7 @@ struct AdjOne {
                 (k - y * cw);
         return 0;
     }
+    __device__ __forceinline__ bool valid(uint32_t sid) const { return sid == 0; }
 };
 
 // The batched adjoint (lt_render_adjoint_batch, every job with its per-sample
@@ -900,6 +1023,7 @@ struct AdjMany {
         local = item - t->begin[lo];
         return lo;
     }
+    __device__ __forceinline__ bool valid(uint32_t sid) const { return sid < t->count; }
 };
 
 __device__ __forceinline__ v3 ld3_planes(const float *p, uint32_t cap, uint32_t slot) {
@@ -1047,6 +1171,19 @@ __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32
     return r;
 }
 
+// k_shade's checks of a surface hit (LT_CHECKS builds): the triangle's mesh,
+// the mesh's material and its light.
+__device__ __forceinline__ bool surface_ok(const DevScene &S, WaveCounters *wc, uint32_t prim) {
+#if LT_CHECKS
+    const uint32_t gid = __ldg(S.tri_geom + prim);
+    if (!LT_CHECK(wc, gid < S.num_geoms, kChkGeom, gid)) return false;
+    const GeomInfo &G = S.geoms[gid];
+    if (!LT_CHECK(wc, (uint32_t)G.material < S.num_mats, kChkMaterial, G.material)) return false;
+    if (!LT_CHECK(wc, G.light < 0 || (uint32_t)G.light < S.num_lights, kChkLight, G.light)) return false;
+#endif
+    return true;
+}
+
 // One iteration of the bounce loop of Integrator::RenderPixel (integrator.cpp:115-243).
 // Register budget: 1024 threads per SM (64 registers, a few spilled) for the
 // single-scene instantiation, measured 1.1% faster than 768 threads (76
@@ -1058,11 +1195,12 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
+    LT_STOP_IF_FAILED(W.counters);
     uint32_t n_ref_rays = 0, n_ref_rays_b = 0;  // connection rays the reference would trace
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t q = base + threadIdx.x;
-        const bool active = q < n;
-        const uint32_t slot = active ? queue_slot(q, n_push, n_cam, cap) : 0u;
+        const uint32_t slot = q < n ? queue_slot(q, n_push, n_cam, cap) : 0u;
+        const bool active = q < n && LT_CHECK(W.counters, slot < cap, kChkSlot, slot);
         Path p;
         bool done = false, push = false;
         v3 norg = mk(0, 0, 0), ndir = mk(0, 0, 0);
@@ -1073,8 +1211,8 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
         float l_pdf = 0.0f, b_pdf = 0.0f, l_tl = 0.0f, b_tl = 0.0f;
         uint32_t conn_light = 0;
         v3 conn_T = mk(0, 0, 0);
-        if (active) {
-            load_path(W.p[cur], cap, slot, p);
+        if (active) load_path(W.p[cur], cap, slot, p);
+        if (active && LT_CHECK(W.counters, src.valid(p.scene), kChkScene, p.scene)) {
             const DevScene &S = src.scene(p.scene);
             const RenderArgs &A = src.args(p.scene);
             float4 hv = ld_s(W.hits + slot);
@@ -1082,12 +1220,24 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
             uint32_t prim = __float_as_uint(hv.w);
             float t = hv.x;
             if (prim == kMiss) {
-                film_contribute(W.counters, src.film(p.scene), p.pixel, p.T * S.background);
+                if (LT_PIXEL_OK(W, p.pixel, A.width * A.height))
+                    film_contribute(W.counters, src.film(p.scene), p.pixel, p.T * S.background);
+                done = true;
+            } else if (!LT_CHECK(W.counters, prim < S.num_tris, kChkPrim, prim)) {
                 done = true;
             } else {
                 v3 origin = mk(r0.x, r0.y, r0.z);
                 v3 direction = normalize(mk(r1.x, r1.y, r1.z));
                 bool hit_surface = true;
+                if (p.medium >= 0 && !LT_CHECK(W.counters, (uint32_t)p.medium < S.num_media, kChkMedium, p.medium)) {
+                    done = true;
+                    hit_surface = false;
+                    p.medium = -1;
+                }
+                if (hit_surface && !surface_ok(S, W.counters, prim)) {
+                    done = true;
+                    hit_surface = false;
+                }
                 if (p.medium >= 0) {
                     const MediumInfo M = S.meds[p.medium];
                     float dist;
@@ -1125,7 +1275,8 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
                 if (hit_surface) {
                     const GeomInfo G = S.geoms[__ldg(S.tri_geom + prim)];
                     const MaterialInfo m = S.mats[G.material];
-                    if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0) {
+                    if ((p.bounces == 0 || (p.lobe & kLobeSpecular) != 0) && G.light >= 0 &&
+                        LT_PIXEL_OK(W, p.pixel, A.width * A.height)) {
                         const LightInfo &L = S.lights[G.light];
                         film_contribute(W.counters, src.film(p.scene), p.pixel,
                                         p.T * mk(L.radiance[0], L.radiance[1], L.radiance[2]));
@@ -1236,14 +1387,14 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
         {
             conn_light |= p.scene << kConnSceneShift;
             uint32_t idx = c_base + __popc(m_l & below);
-            if (emit_l) {
+            if (emit_l && LT_CHECK(W.counters, idx < 2u * cap, kChkRecord, idx)) {
                 st_s(W.cray + 2 * idx, make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light)));
                 st_s(W.cray + 2 * idx + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, l_tl));
                 st_s(W.crec + 2 * idx, make_float4(l_f.x, l_f.y, l_f.z, l_pdf));
                 st_s(W.crec + 2 * idx + 1, make_float4(conn_T.x, conn_T.y, conn_T.z, __uint_as_float(p.pixel)));
             }
             idx = c_base + __popc(m_l) + __popc(m_b & below);
-            if (emit_b) {
+            if (emit_b && LT_CHECK(W.counters, idx < 2u * cap, kChkRecord, idx)) {
                 st_s(W.cray + 2 * idx,
                      make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light | kConnectBsdf)));
                 st_s(W.cray + 2 * idx + 1, make_float4(b_dir.x, b_dir.y, b_dir.z, b_tl));
@@ -1255,7 +1406,7 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
         // the film as it was found); the thread then starts the next work item
         // in their place
         bool regen = false;
-        if (done) {
+        if (done && LT_PIXEL_OK(W, p.pixel, src.args(p.scene).width * src.args(p.scene).height)) {
             const FilmPtrs &F = src.film(p.scene);
             atomicAdd(F.bounces + p.pixel, p.bounces);
             atomicAdd(F.counts + p.pixel, 1u);
@@ -1271,9 +1422,11 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
         }
         if (push || regen) {
             const uint32_t qi = push ? q_base + __popc(m_p & below) : cap - 1u - (r_base + rank_d);
-            write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
-            if (push) store_path(W.p[nxt], cap, qi, p);
-            else store_fresh_path(W.p[nxt], qi, p);
+            if (LT_CHECK(W.counters, qi < cap, kChkOutSlot, qi)) {
+                write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
+                if (push) store_path(W.p[nxt], cap, qi, p);
+                else store_fresh_path(W.p[nxt], qi, p);
+            }
         }
     }
     // ray tallies in the reference's terms (every SampleLi / PdfLi trace), one atomic per warp
@@ -1441,6 +1594,7 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
     const uint32_t cap = W.capacity;
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
+    LT_STOP_IF_FAILED(W.counters);
     uint32_t n_ref_rays = 0, n_ref_rays_b = 0;
     ShadeGrads *gt = nullptr;
     if constexpr (Src::kAdj) {
@@ -1450,8 +1604,8 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
     }
     for (uint32_t base = blockIdx.x * blockDim.x; base < n + nf; base += gridDim.x * blockDim.x) {
         const uint32_t q = base + threadIdx.x;
-        const bool active = q < n;
-        const uint32_t slot = active ? queue_slot(q, n_push, n_cam, cap) : 0u;
+        const uint32_t slot = q < n ? queue_slot(q, n_push, n_cam, cap) : 0u;
+        const bool active = q < n && LT_CHECK(W.counters, slot < cap, kChkSlot, slot);
         if (q >= n && q < n + nf) {  // a finishing entry: its last records, then the sample is complete
             const uint32_t e = q - n;
             const uint4 id = ld_s(D.fin_id[cur] + e);  // pixel, frame, scene slot
@@ -1697,6 +1851,8 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
         const uint32_t rec_l = emit_l ? c_base + __popc(m_l & below) : kNoRecord;
         const uint32_t rec_b = emit_b ? c_base + __popc(m_l) + __popc(m_b & below) : kNoRecord;
         conn_light |= p.scene << kConnSceneShift;
+        if (emit_l && !LT_CHECK(W.counters, rec_l < 2u * cap, kChkRecord, rec_l)) emit_l = false;
+        if (emit_b && !LT_CHECK(W.counters, rec_b < 2u * cap, kChkRecord, rec_b)) emit_b = false;
         if (emit_l) {
             st_s(W.cray + 2 * rec_l, make_float4(conn_org.x, conn_org.y, conn_org.z, __uint_as_float(conn_light)));
             st_s(W.cray + 2 * rec_l + 1, make_float4(l_dir.x, l_dir.y, l_dir.z, l_tl));
@@ -1723,6 +1879,7 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
             }
             if (fin) {
                 const uint32_t e = f_base + __popc(m_f & below);
+                if (!LT_CHECK(W.counters, e < cap, kChkOutSlot, e)) continue;
                 st_s(D.fin_id[nxt] + e, make_uint4(p.pixel, p.frame, p.scene, Src::kAdj ? pend : 0u));
                 st_s(D.fin_C[nxt] + e, make_float4(C.x, C.y, C.z, 0.0f));
                 st_s(D.fin_rec[nxt] + e, make_uint2(rec_l, rec_b));
@@ -1742,6 +1899,7 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
         }
         if (push || regen) {
             const uint32_t qi = push ? q_base + __popc(m_p & below) : cap - 1u - (r_base + rank_d);
+            if (!LT_CHECK(W.counters, qi < cap, kChkOutSlot, qi)) continue;
             write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
             store_path(W.p[nxt], cap, qi, p);
             st3_planes(D.C[nxt], cap, qi, C);
@@ -1819,7 +1977,7 @@ __global__ void __launch_bounds__(256) k_diff_film_batch(const SceneTable *t, un
 // kLightBrute triangles (distance -1 in the record) use a full closest-hit query.
 template <class State>
 __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wavefront &W, const FilmPtrs &F,
-                                                   uint32_t idx, uint32_t kl, const State &r) {
+                                                   uint32_t idx, uint32_t kl, const State &r, uint32_t npix) {
     const bool is_bsdf = (kl & kConnectBsdf) != 0;
     const LightInfo &L = S.lights[kl & kConnLightMask];
     Hit h;
@@ -1827,7 +1985,9 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
         if (r.h.prim != kMiss) return;  // occluded
         light_distance(S, L, r.O, r.D, &h);  // the same light hit k_shade found
     } else {
-        if (r.h.prim == kMiss || __ldg(S.tri_geom + r.h.prim) != (uint32_t)L.geom) return;
+        if (r.h.prim == kMiss) return;
+        if (!LT_CHECK(W.counters, r.h.prim < S.num_tris, kChkPrim, r.h.prim)) return;
+        if (__ldg(S.tri_geom + r.h.prim) != (uint32_t)L.geom) return;
         h = r.h;
     }
     v3 org = r.O, dir = r.D;
@@ -1847,6 +2007,7 @@ __device__ __forceinline__ void resolve_connection(const DevScene &S, const Wave
     if (!is_bsdf) c = ((f * Le) * power_heuristic(lpdf, spdf)) / lpdf;
     else c = ((f * Le) * power_heuristic(spdf, lpdf)) / spdf;
     v3 T = mk(r1.x, r1.y, r1.z);
+    if (!LT_PIXEL_OK(W, pixel, npix)) return;
     film_contribute(W.counters, F, pixel, T * (c * (float)S.num_lights));
 }
 
@@ -1942,6 +2103,7 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256)
         W.counters->main_rays += n;
     }
     if (total <= coop_limit) return;  // k_trace_tail traces this iteration
+    LT_STOP_IF_FAILED(W.counters);
     TraceGrads *gt = nullptr;  // the single-scene adjoint's connection terms
     if constexpr (Src::kAdj && !Src::kMany) {
         gt = grad_table<Src, TraceGrads>();
@@ -1950,26 +2112,57 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256)
     }
     const float4 *rays = W.ray[cur];
     Geo g = B::geo(src.scene(0));
+    LT_SET_GEO_CHK(g, W.counters);
     typename B::State r;
     typename B::Entry stack[B::kDepth];
     B::idle(r);
     uint32_t idx = 0, kl = 0, n_trav = 0;
+    bool bad = false;  // a bound check rejected the current item: nothing is written for it
     for (;;) {
         if (B::done(r)) {
             idx = fetch_next(&W.counters->trace_fetch);
             if (idx >= total) break;
+            bad = false;
             if (idx < n) {
                 const uint32_t s = queue_slot(idx, n_push, n_cam, cap);
-                if (Src::kMany) g = B::geo(src.scene(ld_s(W.p[cur].flags + s) >> kFlagSceneShift));
+                if (!LT_CHECK(W.counters, s < cap, kChkSlot, s)) {
+                    bad = true;
+                    continue;
+                }
+                if (Src::kMany) {
+                    const uint32_t sid = ld_s(W.p[cur].flags + s) >> kFlagSceneShift;
+                    if (!LT_CHECK(W.counters, src.valid(sid), kChkScene, sid)) {
+                        bad = true;
+                        continue;
+                    }
+                    g = B::geo(src.scene(sid));
+                    LT_SET_GEO_CHK(g, W.counters);
+                }
                 float4 a = ld_s(rays + 2 * s), b = ld_s(rays + 2 * s + 1);
                 B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, false, 0);
             } else {
                 const uint32_t c = idx - n;
+                if (!LT_CHECK(W.counters, c < 2u * cap, kChkRecord, c)) {
+                    bad = true;
+                    continue;
+                }
                 float4 a = ld_s(W.cray + 2 * c), b = ld_s(W.cray + 2 * c + 1);
                 const float tl = b.w;
                 kl = __float_as_uint(a.w);
-                const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
-                if (Src::kMany) g = B::geo(S);
+                const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
+                if (!LT_CHECK(W.counters, src.valid(sid), kChkScene, sid)) {
+                    bad = true;
+                    continue;
+                }
+                const DevScene &S = src.scene(sid);
+                if (!LT_CHECK(W.counters, (kl & kConnLightMask) < S.num_lights, kChkLight, kl & kConnLightMask)) {
+                    bad = true;
+                    continue;
+                }
+                if (Src::kMany) {
+                    g = B::geo(S);
+                    LT_SET_GEO_CHK(g, W.counters);
+                }
                 const LightInfo &L = S.lights[kl & kConnLightMask];
                 if (tl > 0.0f)
                     B::start(r, stack, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.001f, tl, true, (uint32_t)L.geom);
@@ -1980,14 +2173,15 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256)
             }
         }
         B::run(g, r, stack);
-        if (B::done(r)) {
+        if (B::done(r) && !bad) {
             if (idx < n) {
                 st_s(W.hits + queue_slot(idx, n_push, n_cam, cap),
                      make_float4(r.h.t, r.h.u, r.h.v, __uint_as_float(r.h.prim)));
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
                 if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, gt);
-                else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
+                else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r,
+                                        src.args(sid).width * src.args(sid).height);
             }
         }
     }
@@ -2041,7 +2235,13 @@ __device__ __forceinline__ Hit coop_traverse(const Geo &g, v3 O, v3 D, float tne
         int push0 = 0, push1 = 0, npush = 0;  // children to push, far one first
         Hit mine = best;
         bool occluded = false;
-        if (have && node >= 0) {
+        const bool entry_ok =
+            !have || (node >= 0 ? LT_CHECK(LT_GEO_CHK(g), (uint32_t)node < g.num_nodes, kChkNode, node)
+                                : LT_CHECK(LT_GEO_CHK(g),
+                                           (~(uint32_t)node >> kLeafBits) + (~(uint32_t)node & ((1u << kLeafBits) - 1u)) <=
+                                               g.num_tris,
+                                           kChkLeaf, ~(uint32_t)node >> kLeafBits));
+        if (have && entry_ok && node >= 0) {
             const float4 *nd = g.nodes + 4 * node;
             const float4 n0 = ldg4(nd), n1 = ldg4(nd + 1), n2 = ldg4(nd + 2), n3 = ldg4(nd + 3);
             float t0, t1;
@@ -2061,7 +2261,7 @@ __device__ __forceinline__ Hit coop_traverse(const Geo &g, v3 O, v3 D, float tne
                 npush = 1;
                 push0 = h0 ? c0 : c1;
             }
-        } else if (have) {
+        } else if (have && entry_ok) {
             const uint32_t code = ~(uint32_t)node;
             const uint32_t first = code >> kLeafBits, count = code & ((1u << kLeafBits) - 1u);
             for (uint32_t k = 0; k < count; ++k) {
@@ -2071,6 +2271,7 @@ __device__ __forceinline__ Hit coop_traverse(const Geo &g, v3 O, v3 D, float tne
                 } else if (!occluded) {
                     Hit c = best;
                     tri_test(tri, O, D, tnear, c);
+                    if (c.prim != kMiss && !LT_CHECK(LT_GEO_CHK(g), c.prim < g.num_tris, kChkPrim, c.prim)) break;
                     if (c.prim != kMiss && __ldg(g.tri_geom + c.prim) != skip_geom) {
                         occluded = true;
                         mine.prim = c.prim;
@@ -2098,6 +2299,9 @@ __device__ __forceinline__ Hit coop_traverse(const Geo &g, v3 O, v3 D, float tne
         // push: the entries of higher lanes first, so that lane 0's (the top
         // entry's children) end on top
         const unsigned b1 = __ballot_sync(full, npush >= 1), b2 = __ballot_sync(full, npush == 2);
+        if (!LT_CHECK(LT_GEO_CHK(g), sp + __popc(b1) + __popc(b2) <= kCoopStack, kChkStack,
+                      sp + __popc(b1) + __popc(b2)))
+            return best;  // warp-uniform: the ballots are the warp's
         const unsigned above = lane == 31u ? 0u : full << (lane + 1u);
         const int off = sp + __popc(b1 & above) + __popc(b2 & above);
         if (npush == 2) {
@@ -2121,6 +2325,7 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_trace_tail(Src src, Wavefro
     const uint32_t nc = W.counters->ccount[cur ^ 1];
     const uint32_t total = n + nc;
     if (total > coop_limit) return;  // k_trace traced them
+    LT_STOP_IF_FAILED(W.counters);
     TraceGrads *gt = nullptr;  // the single-scene adjoint's connection terms
     if constexpr (Src::kAdj && !Src::kMany) {
         gt = grad_table<Src, TraceGrads>();
@@ -2142,7 +2347,11 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_trace_tail(Src src, Wavefro
         Geo g;
         if (idx < n) {
             s = queue_slot(idx, n_push, n_cam, cap);
-            g = geo_of(src.scene(Src::kMany ? ld_s(W.p[cur].flags + s) >> kFlagSceneShift : 0u));
+            if (!LT_CHECK(W.counters, s < cap, kChkSlot, s)) continue;  // warp-uniform: one item per warp
+            const uint32_t sid = Src::kMany ? ld_s(W.p[cur].flags + s) >> kFlagSceneShift : 0u;
+            if (!LT_CHECK(W.counters, src.valid(sid), kChkScene, sid)) continue;
+            g = geo_of(src.scene(sid));
+            LT_SET_GEO_CHK(g, W.counters);
             const float4 a = ld_s(W.ray[cur] + 2 * s), b = ld_s(W.ray[cur] + 2 * s + 1);
             r.O = mk(a.x, a.y, a.z);
             r.D = mk(b.x, b.y, b.z);
@@ -2150,10 +2359,15 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_trace_tail(Src src, Wavefro
             r.h = coop_traverse(g, r.O, r.D, a.w, b.w, false, 0, st);
         } else {
             const uint32_t c = idx - n;
+            if (!LT_CHECK(W.counters, c < 2u * cap, kChkRecord, c)) continue;
             const float4 a = ld_s(W.cray + 2 * c), b = ld_s(W.cray + 2 * c + 1);
             kl = __float_as_uint(a.w);
-            const DevScene &S = src.scene((kl >> kConnSceneShift) & kConnSceneMask);
+            const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
+            if (!LT_CHECK(W.counters, src.valid(sid), kChkScene, sid)) continue;
+            const DevScene &S = src.scene(sid);
+            if (!LT_CHECK(W.counters, (kl & kConnLightMask) < S.num_lights, kChkLight, kl & kConnLightMask)) continue;
             g = geo_of(S);
+            LT_SET_GEO_CHK(g, W.counters);
             const LightInfo &L = S.lights[kl & kConnLightMask];
             r.O = mk(a.x, a.y, a.z);
             r.D = mk(b.x, b.y, b.z);
@@ -2168,7 +2382,8 @@ __global__ void __launch_bounds__(kCoopWarps * 32) k_trace_tail(Src src, Wavefro
             } else {
                 const uint32_t sid = (kl >> kConnSceneShift) & kConnSceneMask;
                 if constexpr (Src::kDiff) resolve_connection_diff(src, W, idx - n, kl, r, gt);
-                else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r);
+                else resolve_connection(src.scene(sid), W, src.film(sid), idx - n, kl, r,
+                                        src.args(sid).width * src.args(sid).height);
             }
         }
         __syncwarp();
@@ -2186,6 +2401,7 @@ __global__ void k_loop_condition(WaveCounters *c, const SceneTable *t, cudaGraph
                                  uint32_t iters) {
     c->iterations += iters;
     unsigned int more = c->count[cur] != 0u || c->rcount[cur] != 0u || c->ccount[cur ^ 1] != 0u;
+    if (LT_CHECKS && c->check != 0u) more = 0;  // a bound check failed: the host reports it
     if (more && c->iterations >= t->iteration_limit) {
         c->error = 2;
         more = 0;

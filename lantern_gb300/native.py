@@ -14,7 +14,8 @@ from . import build as _build
 
 LT_OK = 0
 STATUS = {0: "LT_OK", 1: "LT_ERR_INVALID", 2: "LT_ERR_CUDA", 3: "LT_ERR_OOM", 4: "LT_ERR_TIMEOUT",
-          5: "LT_ERR_IO", 6: "LT_ERR_PARSE", 7: "LT_ERR_UNSUPPORTED", 8: "LT_ERR_STATE"}
+          5: "LT_ERR_IO", 6: "LT_ERR_PARSE", 7: "LT_ERR_UNSUPPORTED", 8: "LT_ERR_STATE",
+          9: "LT_ERR_CHECK"}
 BSDF_LAMBERT, BSDF_MIRROR, BSDF_DIELECTRIC = 0, 1, 2
 MEDIUM_NON_SCATTERING, MEDIUM_ISOTROPIC, MEDIUM_HG = 1, 2, 3
 MISS = 0xFFFFFFFF
@@ -26,11 +27,11 @@ SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_set_stage_timing", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
            "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load",
-           "lt_debug_fail_allocations", "lt_debug_set_iteration_limit"]
+           "lt_debug_fail_allocations", "lt_debug_set_iteration_limit", "lt_debug_set_check_pixel_limit"]
 BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 MAX_BATCH = 2048  # LT_MAX_BATCH
-ABI_VERSION = 2  # LT_ABI_VERSION
+ABI_VERSION = 3  # LT_ABI_VERSION
 TONEMAP_CLAMP, TONEMAP_FILMIC = 0, 1
 
 
@@ -123,12 +124,17 @@ _lib = None
 
 
 def load(build_if_needed: bool = True) -> C.CDLL:
-    """Load liblantern_gpu.so, building it first if it is missing or stale."""
+    """Load liblantern_gpu.so, building it first if it is missing or stale.
+
+    With LANTERN_GPU_CHECKED=1 in the environment the process loads
+    liblantern_gpu_checked.so instead: the same library with its kernels'
+    bound checks compiled in (renders fail with LT_ERR_CHECK where an index
+    would leave its array), for test runs."""
     global _lib
     with _lock:
         if _lib is not None:
             return _lib
-        path = _build.LIB
+        path = _build.CHECKED_LIB if os.environ.get("LANTERN_GPU_CHECKED") == "1" else _build.LIB
         if build_if_needed and not _build.up_to_date():
             _build.build()
         if not os.path.exists(path):
@@ -172,6 +178,8 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_debug_fail_allocations.restype = None
         L.lt_debug_set_iteration_limit.argtypes = [C.c_uint64]
         L.lt_debug_set_iteration_limit.restype = None
+        L.lt_debug_set_check_pixel_limit.argtypes = [C.c_uint32]
+        L.lt_debug_set_check_pixel_limit.restype = None
         _lib = L
         return L
 

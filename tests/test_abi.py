@@ -19,17 +19,20 @@ def _declared():
 
 
 def test_library_exports_every_declared_symbol():
-    lib = ctypes.CDLL(build.build())
+    """Both builds: the library and its bound-checked twin."""
+    build.build()
     declared = _declared()
     assert declared, "no declarations found"
-    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
-    assert not missing, missing
+    for path in (build.LIB, build.CHECKED_LIB):
+        lib = ctypes.CDLL(path)
+        missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+        assert not missing, (path, missing)
     assert set(native.SYMBOLS) <= declared
 
 
 def test_abi_version_and_no_device_error():
     lib = native.load()
-    assert lib.lt_abi_version() == 2
+    assert lib.lt_abi_version() == native.ABI_VERSION
     import torch
     if not torch.cuda.is_available():
         h = ctypes.c_void_p()
