@@ -390,6 +390,14 @@ def main():
         e2e = {"value": round(whole_job_rate(samples, world, e2e_s), 3), "unit": "Msamples/s",
                "h2d_bytes_per_step": npix * 20, "d2h_bytes_per_step": npix * 20}
 
+    # the wavefront's queue lengths per iteration, from one more render after the
+    # timed ones (lt_set_queue_trace): (path rays, camera rays, connection records)
+    scene.ctx.set_queue_trace(1024)
+    integ.RenderFrame(spp)
+    torch.cuda.synchronize()
+    queue_lengths = scene.ctx.queue_trace().tolist()
+    scene.ctx.set_queue_trace(0)
+
     micro = None
     if args.microbench and args.workload == "icosphere-1.3M":
         micro = microbench(scene, path, local)
@@ -444,6 +452,8 @@ def main():
                            else "single GPU"},
                 "mrays": round(mrays, 2), "gpu_launches": launches,
                 "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "queue_lengths": {"columns": ["path_rays", "camera_rays", "connection_records"],
+                                  "per_iteration": queue_lengths},
                 "intersect_microbench": micro, "adjoint": adjoint, "batch": batch}
         print(json.dumps(line))
     if dist:

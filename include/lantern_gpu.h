@@ -30,7 +30,8 @@ extern "C" {
 
 /* 2: lt_render_stats gained init_ms and idle_ms; lt_light_info, lt_scene_lights_get,
  * lt_trim and lt_debug_set_iteration_limit were added.
- * 3: LT_ERR_CHECK and lt_debug_set_check_pixel_limit were added. */
+ * 3: LT_ERR_CHECK, lt_debug_set_check_pixel_limit and the queue trace
+ * (lt_set_queue_trace, lt_queue_trace_get) were added. */
 #define LT_ABI_VERSION 3
 
 typedef enum lt_status {
@@ -298,6 +299,28 @@ lt_status lt_render_stats_get(lt_ctx *ctx, lt_render_stats *out);
  * 16 spp 1.164 ms with them, 1.081 ms without; 1 spp 0.616 vs 0.533 ms). No
  * counterpart in the reference. */
 lt_status lt_set_stage_timing(lt_ctx *ctx, int32_t on);
+
+/* Queue trace: the wavefront's queue lengths at the start of every iteration,
+ * as the trace kernel reads them (path rays that continue, paths that start
+ * with a camera ray, connection records of the previous shade), recorded on
+ * the device by that kernel. lt_set_queue_trace(ctx, rows) allocates room for
+ * `rows` iterations (at most LT_QUEUE_TRACE_MAX_ROWS; 0, the initial state,
+ * frees it and records nothing); call it outside a render, since it allocates.
+ * lt_queue_trace_get copies up to `capacity` rows of the context's last
+ * wavefront loop (an lt_render, one scene of a batch that renders alone, or a
+ * batch's captured loop; lt_render_noalloc records none) into `out` (host
+ * memory) and sets *rows to the number recorded. Summed over the rows,
+ * path_rays + camera_rays is lt_render_stats.main_rays and
+ * connection_records is light_traversals. No counterpart in the reference,
+ * which has no queues; its per-pixel bounce counts are the film's Bounces. */
+#define LT_QUEUE_TRACE_MAX_ROWS 65536u
+typedef struct lt_queue_lengths {
+    uint32_t path_rays;           /* continuing paths' rays (queue bottom) */
+    uint32_t camera_rays;         /* paths started this iteration from a work item (queue top) */
+    uint32_t connection_records;  /* light-sample and BSDF-MIS records of the previous shade */
+} lt_queue_lengths;
+lt_status lt_set_queue_trace(lt_ctx *ctx, uint32_t rows);
+lt_status lt_queue_trace_get(lt_ctx *ctx, lt_queue_lengths *out, uint32_t capacity, uint32_t *rows);
 
 /* ---------------------------------------------------------------- resolve */
 /* The visualizer's final pass into a headless buffer (the window, swapchain and

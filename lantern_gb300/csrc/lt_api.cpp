@@ -100,6 +100,11 @@ struct lt_ctx {
     bool stage_timing = false;
     std::vector<cudaEvent_t> stage_events;
     std::vector<int> stage_of_event;
+
+    // queue trace (lt_set_queue_trace, off by default): k_trace writes each
+    // iteration's queue lengths into qtrace_dev; qtrace_rows of the last loop
+    uint3 *qtrace_dev = nullptr;
+    uint32_t qtrace_cap = 0, qtrace_rows = 0;
 };
 
 static thread_local std::string g_create_error;
@@ -320,6 +325,7 @@ void lt_ctx_destroy(lt_ctx *c) {
     if (c->diff_samples) cudaFree(c->diff_samples);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->isect_fetch) cudaFree(c->isect_fetch);
+    if (c->qtrace_dev) cudaFree(c->qtrace_dev);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->order.switch_ev) cudaEventDestroy(c->order.switch_ev);
@@ -742,6 +748,8 @@ static Wavefront wave_view(const lt_ctx *c, uint32_t cap) {
     Wavefront w;
     w.arena_bytes = carve_wave((char *)c->wave.arena, cap, &w);
     w.arena = c->wave.arena;
+    w.qtrace = c->qtrace_dev;
+    w.qtrace_cap = c->qtrace_cap;
     return w;
 }
 
@@ -852,6 +860,7 @@ static lt_status run_loop(lt_ctx *c, const Wavefront &w, const RenderArgs &a, bo
     c->stats.nonfinite_samples = k.nonfinite;
     c->stats.light_traversals = k.light_traversals;
     c->stats.iterations = (uint32_t)iters;
+    c->qtrace_rows = w.qtrace ? (k.trace_launches < w.qtrace_cap ? k.trace_launches : w.qtrace_cap) : 0u;
     c->stats.kernel_launches = launches;
     if (stage_timing) {  // the stream has been synchronised: every event has completed
         float acc[kStages + 1] = {0, 0, 0};
@@ -1281,6 +1290,35 @@ extern "C" lt_status lt_get_tuning(const lt_ctx *c, lt_tuning *out) {
 static bool valid_threads(uint32_t t) { return t == 64 || t == 128 || t == 256; }
 static bool valid_shade_threads(uint32_t t) { return valid_threads(t) || t == 512; }
 
+extern "C" lt_status lt_set_queue_trace(lt_ctx *c, uint32_t rows) try {
+    if (!c) return LT_ERR_INVALID;
+    if (rows > LT_QUEUE_TRACE_MAX_ROWS)
+        return fail(c, LT_ERR_INVALID, "%u rows; the queue trace holds at most %u", rows, LT_QUEUE_TRACE_MAX_ROWS);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // no queued kernel still writes the old rows
+    if (c->qtrace_dev) cudaFree(c->qtrace_dev);
+    c->qtrace_dev = nullptr;
+    c->qtrace_cap = c->qtrace_rows = 0;
+    if (rows) {
+        CUDA_TRY(c, dev_malloc((void **)&c->qtrace_dev, (size_t)rows * sizeof(uint3)));
+        c->qtrace_cap = rows;
+    }
+    return LT_OK;
+} LT_CATCH(c)
+
+extern "C" lt_status lt_queue_trace_get(lt_ctx *c, lt_queue_lengths *out, uint32_t capacity, uint32_t *rows) try {
+    if (!c || !rows || (capacity && !out)) return fail(c, LT_ERR_INVALID, "NULL argument");
+    *rows = c->qtrace_rows;
+    const uint32_t n = c->qtrace_rows < capacity ? c->qtrace_rows : capacity;
+    if (n) {
+        static_assert(sizeof(lt_queue_lengths) == sizeof(uint3), "queue trace row layout");
+        CUDA_TRY(c, cudaSetDevice(c->device));
+        CUDA_TRY(c, cudaMemcpyAsync(out, c->qtrace_dev, (size_t)n * sizeof(uint3), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    return LT_OK;
+} LT_CATCH(c)
+
 extern "C" lt_status lt_set_stage_timing(lt_ctx *c, int32_t on) try {
     if (!c) return LT_ERR_INVALID;
     c->stage_timing = on != 0;
@@ -1326,7 +1364,7 @@ static lt_status build_batch_graph(lt_ctx *c, const Wavefront &w) {
                                   (uintptr_t)c->batch_shape.shade_threads, (uintptr_t)c->batch_shape.shade_blocks,
                                   (uintptr_t)c->batch_shape.bvh_width, c->tuning.loop_iterations,
                                   (uintptr_t)c->batch_shape.tail_blocks, (uintptr_t)c->batch_shape.coop_limit,
-                                  (uintptr_t)w.check_pixels};
+                                  (uintptr_t)w.check_pixels, (uintptr_t)w.qtrace, (uintptr_t)w.qtrace_cap};
     if (c->graph_exec && key == c->graph_key) return LT_OK;
     free_graph(c);
     cudaStream_t cs = c->own_stream;
@@ -1478,6 +1516,7 @@ extern "C" lt_status lt_render_batch(lt_ctx *c, lt_ctx *const *scenes, const lt_
                     (uint32_t)(k.iterations / c->tuning.loop_iterations);
         c->stats.light_traversals = k.light_traversals;
         c->stats.nonfinite_samples = k.nonfinite;
+        c->qtrace_rows = w.qtrace ? (k.trace_launches < w.qtrace_cap ? k.trace_launches : w.qtrace_cap) : 0u;
     }
     lt_render_stats acc = c->stats;
     for (uint32_t i : alone) {

@@ -67,6 +67,7 @@ struct WaveCounters {
     uint32_t fcount[2];                   // differentiable forward: finishing entries by parity
     uint32_t check;                       // builds with LT_CHECKS: code of the first failed bound check
     uint32_t check_value;                 // and the index it rejected
+    uint32_t trace_launches;              // k_trace launches of this loop (the queue trace's next row)
 };
 
 struct Wavefront {
@@ -78,6 +79,8 @@ struct Wavefront {
     float4 *crec = nullptr;                 // 2 float4 per record: (f, bsdf pdf) (throughput, pixel)
     WaveCounters *counters = nullptr;
     uint32_t check_pixels = 0;              // builds with LT_CHECKS: film pixels the checks accept (0: all)
+    uint3 *qtrace = nullptr;                // queue lengths per iteration (lt_set_queue_trace), or null
+    uint32_t qtrace_cap = 0;                // rows of qtrace
     void *arena = nullptr;
     size_t arena_bytes = 0;
 };

@@ -2101,6 +2101,8 @@ __global__ void __launch_bounds__(256, Src::kMany ? 0 : B::kMinBlocks256)
         W.counters->ccount[cur] = 0;
         W.counters->fcount[cur ^ 1] = 0;  // filled by the next differentiable shade
         W.counters->main_rays += n;
+        const uint32_t it = W.counters->trace_launches++;  // one launch per iteration, stream-ordered
+        if (it < W.qtrace_cap) W.qtrace[it] = make_uint3(n_push, n_cam, nc);
     }
     if (total <= coop_limit) return;  // k_trace_tail traces this iteration
     LT_STOP_IF_FAILED(W.counters);

@@ -27,7 +27,7 @@ SYMBOLS = ["lt_abi_version", "lt_ctx_create", "lt_ctx_destroy", "lt_last_error",
            "lt_render_stats_get", "lt_intersect", "lt_render_noalloc", "lt_set_bvh_builder", "lt_get_tuning",
            "lt_set_tuning", "lt_set_stage_timing", "lt_render_batch", "lt_autotune_batch", "lt_resolve",
            "lt_render_diff_batch", "lt_render_adjoint_batch", "lt_image_load",
-           "lt_debug_fail_allocations", "lt_debug_set_iteration_limit", "lt_debug_set_check_pixel_limit"]
+           "lt_debug_fail_allocations", "lt_debug_set_iteration_limit", "lt_debug_set_check_pixel_limit", "lt_set_queue_trace", "lt_queue_trace_get"]
 BVH_GPU, BVH_HOST = 0, 1
 NOALLOC_MAX_PATHS = 65536  # LT_NOALLOC_MAX_PATHS
 MAX_BATCH = 2048  # LT_MAX_BATCH
@@ -115,6 +115,10 @@ class Tuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class QueueLengths(C.Structure):
+    _fields_ = [("path_rays", C.c_uint32), ("camera_rays", C.c_uint32), ("connection_records", C.c_uint32)]
+
+
 class SppRange(C.Structure):
     _fields_ = [("min_spp", C.c_uint32), ("max_spp", C.c_uint32), ("sum_spp", C.c_uint64)]
 
@@ -178,6 +182,8 @@ def load(build_if_needed: bool = True) -> C.CDLL:
         L.lt_debug_fail_allocations.restype = None
         L.lt_debug_set_iteration_limit.argtypes = [C.c_uint64]
         L.lt_debug_set_iteration_limit.restype = None
+        L.lt_set_queue_trace.argtypes = [p, C.c_uint32]
+        L.lt_queue_trace_get.argtypes = [p, C.POINTER(QueueLengths), C.c_uint32, C.POINTER(C.c_uint32)]
         L.lt_debug_set_check_pixel_limit.argtypes = [C.c_uint32]
         L.lt_debug_set_check_pixel_limit.restype = None
         _lib = L
@@ -307,6 +313,22 @@ class Context:
     def set_stage_timing(self, on: bool):
         """lt_set_stage_timing: per-stage kernel times in stats() (events around every launch)."""
         self._check(self.L.lt_set_stage_timing(self.h, 1 if on else 0))
+
+    def set_queue_trace(self, rows: int):
+        """lt_set_queue_trace: record the queue lengths of up to `rows`
+        iterations of every later wavefront loop (0: off)."""
+        self._check(self.L.lt_set_queue_trace(self.h, rows))
+
+    def queue_trace(self):
+        """lt_queue_trace_get: the last loop's rows as a (rows, 3) uint32 array
+        of (path rays, camera rays, connection records)."""
+        import numpy as np
+        n = C.c_uint32()
+        self._check(self.L.lt_queue_trace_get(self.h, None, 0, C.byref(n)))
+        arr = (QueueLengths * max(n.value, 1))()
+        self._check(self.L.lt_queue_trace_get(self.h, arr, n.value, C.byref(n)))
+        return np.array([(r.path_rays, r.camera_rays, r.connection_records) for r in arr[:n.value]],
+                        dtype=np.uint32).reshape(-1, 3)
 
     def set_tuning(self, **fields):
         """lt_set_tuning with the given fields changed from the current tuning."""

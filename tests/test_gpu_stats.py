@@ -62,3 +62,37 @@ def test_launch_shapes_render_the_same_samples(scene_dir):
     for b in films[1:]:
         assert torch.equal(a.ColorSampleCount, b.ColorSampleCount) and torch.equal(a.Bounces, b.Bounces)
         assert torch.allclose(a.ColorData, b.ColorData, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("paths", [0, 4096])
+def test_queue_trace_adds_up_to_the_ray_counts(scene_dir, paths):
+    """lt_set_queue_trace / lt_queue_trace_get: one row per iteration; the path
+    and camera rays sum to main_rays and the connection records to
+    light_traversals. With every sample in flight the first row holds all
+    camera rays as path rays and the paths only end; with a 4,096-path
+    wavefront the later rows start paths from work items (camera rays)."""
+    from lantern_gb300.native import LanternError
+    s = Scene(0)
+    s.LoadSceneFromJSON(S.nine_spheres(width=64, height=48, slices=16, stacks=8, name="qtrace_nine").write(scene_dir))
+    if paths:
+        s.ctx.set_tuning(paths_in_flight=paths)
+    s.ctx.set_queue_trace(4096)
+    fb = FrameBuffer(s.width, s.height, "cuda:0")
+    it = Integrator(s, fb, max_depth=8, rr_depth=3)
+    it.RenderFrame(8)
+    torch.cuda.synchronize()
+    st = it.stats()
+    q = s.ctx.queue_trace().astype("int64")
+    assert q.shape == (st.iterations, 3)
+    assert int(q[:, 0].sum() + q[:, 1].sum()) == st.main_rays
+    assert int(q[:, 2].sum()) == st.light_traversals
+    assert q[0, 2] == 0  # no connection record before the first shade
+    if paths == 0:
+        assert q[0, 0] == 64 * 48 * 8 and q[:, 1].sum() == 0 and (q[1:, 0] <= q[:-1, 0]).all()
+    else:
+        assert q[0, 0] == paths and q[:, 1].sum() == 64 * 48 * 8 - paths
+    with pytest.raises(LanternError, match="LT_ERR_INVALID"):
+        s.ctx.set_queue_trace(1 << 20)
+    s.ctx.set_queue_trace(0)  # off: the next render records nothing
+    Integrator(s, FrameBuffer(s.width, s.height, "cuda:0"), max_depth=8, rr_depth=3).RenderFrame(1)
+    assert s.ctx.queue_trace().shape == (0, 3)
