@@ -42,12 +42,12 @@ METRIC = "Msamples/s & Mrays/s on 1 GB300 vs host CPU at matched RMSE; adjoint g
 SCENES = os.path.join(ROOT, "_scenes")
 # DRAM bytes (read + write) per ray traced by k_trace on the icosphere workload, measured
 # with ncu dram__bytes_{read,write}.sum over the 11 k_trace launches of one render of this
-# workload (13.14 GB for 171,793,933 traced rays; profiles/k_trace_k_shade_icosphere-1.3M.md)
-TRACE_DRAM_BYTES_PER_RAY = 76.6
+# workload (11.34 GB for 171,793,118 traced rays; profiles/k_trace_k_shade_icosphere-1.3M.md)
+TRACE_DRAM_BYTES_PER_RAY = 66.0
 # L2 throughput of k_trace as a fraction of the L2's peak (ncu
 # lts__throughput.avg.pct_of_peak_sustained_elapsed of iterations 0 and 1 of a
 # 4-spp render of the same scene; profiles/k_trace_k_shade_icosphere-1.3M.md)
-TRACE_L2_FRAC = 0.132
+TRACE_L2_FRAC = 0.095
 
 
 def max_over_ranks(value: float, dist=None, device="cpu") -> float:
