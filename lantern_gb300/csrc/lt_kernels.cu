@@ -1134,6 +1134,7 @@ struct Slots {
     uint32_t c, q, f, r, n_regen;
     unsigned long long w;
     uint32_t flag;  // the block's flag word as it stood once every warp had staged its counts
+    uint32_t qpos;  // with octant keys: the lane's continuing-path entry
 };
 
 // The block's slots, reserved by one thread with one atomic per counter: each
@@ -1146,14 +1147,38 @@ struct Slots {
 // `flag` (shared, optional): a word that the block's threads set before the
 // call; every thread gets its value in Slots::flag (the same for all) and the
 // word is cleared for the next round.
+// kOct: the continuing paths take the block's entries grouped by `okey`, the
+// octant of their next direction (0-7; 8 for a lane that does not continue),
+// octants in order. A warp of the next trace then holds rays of a few
+// neighbouring pixels that leave in the same octant. Each warp counts its
+// octants into one of two per-block buffers of 8 counters (a shared atomic per
+// octant present, `it` = the caller's iteration, whose parity picks the
+// buffer; the first call zeroes both), thread 0 turns the counts into offsets
+// and zeroes the other buffer, so no barrier is added after the first call.
+template <bool kOct = false>
 __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32_t nc, uint32_t np, uint32_t nf,
-                                               uint32_t nd, unsigned long long total, uint32_t *flag = nullptr) {
+                                               uint32_t nd, unsigned long long total, uint32_t *flag = nullptr,
+                                               uint32_t okey = 8u, uint32_t it = 0u) {
     const int nxt = cur ^ 1;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ uint32_t s_cnt[4][16];
     __shared__ uint32_t s_base[5][16];
     __shared__ unsigned long long s_wbase[16];
     __shared__ uint32_t s_flag;
+    __shared__ uint32_t s_oct[2][8];  // kOct: continuing paths per octant, then their offsets (by parity)
+    uint32_t orank = 0;               // kOct: the lane's place within its octant's entries
+    const uint32_t ob = it & 1u;
+    if constexpr (kOct) {
+        if (it == 0u) {  // block-uniform
+            if (threadIdx.x < 16u) s_oct[threadIdx.x >> 3][threadIdx.x & 7u] = 0u;
+            __syncthreads();
+        }
+        const unsigned same = __match_any_sync(0xFFFFFFFFu, okey);
+        const int leader = __ffs(same) - 1;
+        uint32_t b = 0;
+        if (okey < 8u && (int)lane == leader) b = atomicAdd(&s_oct[ob][okey], (uint32_t)__popc(same));
+        orank = __shfl_sync(0xFFFFFFFFu, b, leader) + __popc(same & ((1u << lane) - 1u));
+    }
     if (lane == 0) {
         s_cnt[0][warp] = nc;
         s_cnt[1][warp] = np;
@@ -1181,6 +1206,16 @@ __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32
         const unsigned long long left = w0 < total ? total - w0 : 0ull;
         const uint32_t nreg = left < (unsigned long long)td ? (uint32_t)left : td;
         const uint32_t r0 = nreg ? atomicAdd(&wc->rcount[nxt], nreg) : 0u;
+        if constexpr (kOct) {  // octant offsets; the other buffer is zeroed for the next call
+            uint32_t a = 0;
+#pragma unroll
+            for (uint32_t k = 0; k < 8u; ++k) {
+                const uint32_t v = s_oct[ob][k];
+                s_oct[ob][k] = a;
+                a += v;
+                s_oct[ob ^ 1u][k] = 0u;
+            }
+        }
         uint32_t pc = 0, pp = 0, pf = 0, pd = 0;
         for (uint32_t w = 0; w < nw; ++w) {
             s_base[0][w] = c0 + pc;
@@ -1205,6 +1240,10 @@ __device__ __forceinline__ Slots reserve_block(WaveCounters *wc, int cur, uint32
     r.n_regen = s_base[4][warp];
     r.w = s_wbase[warp];
     r.flag = flag ? s_flag : 0u;
+    r.qpos = 0u;
+    if constexpr (kOct) {
+        if (okey < 8u) r.qpos = s_base[1][0] + s_oct[ob][okey] + orank;
+    }
     return r;
 }
 
@@ -1234,6 +1273,7 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counters->trace_fetch = 0;  // for the next k_trace
     LT_STOP_IF_FAILED(W.counters);
     uint32_t n_ref_rays = 0, n_ref_rays_b = 0;  // connection rays the reference would trace
+    uint32_t it = 0;                            // this block's iteration of the loop below
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t q = base + threadIdx.x;
         const uint32_t slot = q < n ? queue_slot(q, n_push, n_cam, cap) : 0u;
@@ -1416,9 +1456,11 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
         const unsigned below = (1u << lane) - 1u;
         const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
         const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
-        const Slots sl = reserve_block(W.counters, cur, __popc(m_l) + __popc(m_b), __popc(m_p), 0u, __popc(m_d),
-                                       src.total());
-        const uint32_t c_base = sl.c, q_base = sl.q, r_base = sl.r, n_regen = sl.n_regen;
+        const uint32_t okey =
+            push ? (ndir.x < 0.0f ? 1u : 0u) | (ndir.y < 0.0f ? 2u : 0u) | (ndir.z < 0.0f ? 4u : 0u) : 8u;
+        const Slots sl = reserve_block<true>(W.counters, cur, __popc(m_l) + __popc(m_b), __popc(m_p), 0u, __popc(m_d),
+                                             src.total(), nullptr, okey, it++);
+        const uint32_t c_base = sl.c, r_base = sl.r, n_regen = sl.n_regen;
         const unsigned long long w_base = sl.w;
         // connection records: the warp's light samples, then its BSDF samples
         {
@@ -1458,7 +1500,7 @@ __global__ void __launch_bounds__(Src::kMany ? 256 : 512, Src::kMany ? 3 : 2) k_
             regen = true;
         }
         if (push || regen) {
-            const uint32_t qi = push ? q_base + __popc(m_p & below) : cap - 1u - (r_base + rank_d);
+            const uint32_t qi = push ? sl.qpos : cap - 1u - (r_base + rank_d);
             if (LT_CHECK(W.counters, qi < cap, kChkOutSlot, qi)) {
                 write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
                 if (push) store_path(W.p[nxt], cap, qi, p);
