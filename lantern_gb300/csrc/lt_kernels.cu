@@ -1681,6 +1681,7 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
         gt->init();
         __syncthreads();
     }
+    uint32_t it = 0;  // this block's iteration of the loop below
     for (uint32_t base = blockIdx.x * blockDim.x; base < n + nf; base += gridDim.x * blockDim.x) {
         const uint32_t q = base + threadIdx.x;
         const uint32_t slot = q < n ? queue_slot(q, n_push, n_cam, cap) : 0u;
@@ -1911,8 +1912,11 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
         const unsigned m_l = __ballot_sync(0xFFFFFFFFu, emit_l), m_b = __ballot_sync(0xFFFFFFFFu, emit_b);
         const unsigned m_d = __ballot_sync(0xFFFFFFFFu, done), m_p = __ballot_sync(0xFFFFFFFFu, push);
         const unsigned m_f = __ballot_sync(0xFFFFFFFFu, fin);
-        const Slots sl = reserve_block(W.counters, cur, __popc(m_l) + __popc(m_b), __popc(m_p), __popc(m_f),
-                                       __popc(m_d), src.total(), Src::kAdj && Src::kMany ? &gt->other : nullptr);
+        const uint32_t okey =
+            push ? (ndir.x < 0.0f ? 1u : 0u) | (ndir.y < 0.0f ? 2u : 0u) | (ndir.z < 0.0f ? 4u : 0u) : 8u;
+        const Slots sl = reserve_block<true>(W.counters, cur, __popc(m_l) + __popc(m_b), __popc(m_p), __popc(m_f),
+                                             __popc(m_d), src.total(), Src::kAdj && Src::kMany ? &gt->other : nullptr,
+                                             okey, it++);
         if constexpr (Src::kAdj && Src::kMany) {
             // paths of another scene came: the table's sums go to the gradient
             // arrays and its slots to the new scene's triangles (a block-uniform
@@ -1925,7 +1929,7 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
                 __syncthreads();
             }
         }
-        const uint32_t c_base = sl.c, q_base = sl.q, f_base = sl.f, r_base = sl.r, n_regen = sl.n_regen;
+        const uint32_t c_base = sl.c, f_base = sl.f, r_base = sl.r, n_regen = sl.n_regen;
         const unsigned long long w_base = sl.w;
         const uint32_t rec_l = emit_l ? c_base + __popc(m_l & below) : kNoRecord;
         const uint32_t rec_b = emit_b ? c_base + __popc(m_l) + __popc(m_b & below) : kNoRecord;
@@ -1977,7 +1981,7 @@ __global__ void __launch_bounds__(256, Src::kAdj ? 4 : 3) k_dshade(Src src, Wave
             regen = true;
         }
         if (push || regen) {
-            const uint32_t qi = push ? q_base + __popc(m_p & below) : cap - 1u - (r_base + rank_d);
+            const uint32_t qi = push ? sl.qpos : cap - 1u - (r_base + rank_d);
             if (!LT_CHECK(W.counters, qi < cap, kChkOutSlot, qi)) continue;
             write_ray(W.ray[nxt], qi, norg, ntnear, ndir);
             store_path(W.p[nxt], cap, qi, p);
