@@ -47,7 +47,7 @@ TRACE_DRAM_BYTES_PER_RAY = 66.0
 # L2 throughput of k_trace as a fraction of the L2's peak (ncu
 # lts__throughput.avg.pct_of_peak_sustained_elapsed of iterations 0 and 1 of a
 # 4-spp render of the same scene; profiles/k_trace_k_shade_icosphere-1.3M.md)
-TRACE_L2_FRAC = 0.095
+TRACE_L2_FRAC = 0.105
 
 
 def max_over_ranks(value: float, dist=None, device="cpu") -> float:
