@@ -877,13 +877,15 @@ __device__ __forceinline__ void film_contribute(WaveCounters *counters, const Fi
 // Work item -> sample index (frame offset * pixels + pixel, as start_path reads
 // it) of a render of npix pixels x spp samples. Work items run in groups of G
 // consecutive samples of one pixel, G the largest power of two up to
-// min(spp, 32): a warp's camera rays then start in the same pixel and walk the
-// same BVH nodes (icosphere render 1,641 -> 1,801 Msamples/s with G = 32). The
-// spp % G samples left of every pixel follow as groups of spp % G. A bijection
-// on [0, npix * spp): the same samples in another order.
+// min(spp, 64): a warp's camera rays then start in the same pixel and walk the
+// same BVH nodes (icosphere render 1,641 -> 1,801 Msamples/s with G = 32, and
+// 1,856 -> 1,871 with G = 64 once the shade groups continuing paths by
+// octant: a block's paths come from fewer pixels). The spp % G samples left of
+// every pixel follow as groups of spp % G. A bijection on [0, npix * spp): the
+// same samples in another order.
 __device__ __forceinline__ unsigned long long sample_of_item(unsigned long long item, unsigned long long npix,
                                                              uint32_t spp) {
-    const uint32_t g = spp >= 32u ? 32u : 1u << (31 - __clz(spp | 1u));
+    const uint32_t g = spp >= 64u ? 64u : 1u << (31 - __clz(spp | 1u));
     const uint32_t sh = __ffs(g) - 1, rem = spp & (g - 1u);
     const unsigned long long full = npix * (spp - rem);
     unsigned long long fo, pixel;
