@@ -171,14 +171,6 @@ static lt_status fail(lt_ctx *c, lt_status st, const char *fmt, ...) {
     return st;
 }
 
-// Names of the device-side bound checks (LT_CHECKS builds), by code.
-static const char *check_name(uint32_t code) {
-    static const char *names[] = {"none", "path queue slot", "connection record", "output queue slot",
-                                  "BVH node", "leaf triangles", "traversal stack", "hit primitive",
-                                  "scene slot", "light", "medium", "film pixel", "mesh", "material"};
-    return code < sizeof(names) / sizeof(names[0]) ? names[code] : "unknown";
-}
-
 // A failed device-side bound check recorded in the counters (LT_CHECKS builds).
 static lt_status check_failed(lt_ctx *c, const WaveCounters &k) {
     return fail(c, LT_ERR_CHECK, "device bound check failed: %s (index %u)", check_name(k.check), k.check_value);

@@ -53,6 +53,31 @@ struct PathState {
     float *iori;
 };
 
+// Kinds of the device-side bound checks of an LT_CHECKS build (recorded in
+// WaveCounters::check) and the names the host reports them by.
+enum CheckKind : uint32_t {
+    kChkSlot = 1,  // path queue slot
+    kChkRecord,    // connection record
+    kChkOutSlot,   // output queue slot
+    kChkNode,      // BVH node
+    kChkLeaf,      // leaf triangle range
+    kChkStack,     // traversal stack
+    kChkPrim,      // hit primitive
+    kChkScene,     // scene slot of a batch
+    kChkLight,
+    kChkMedium,
+    kChkPixel,     // film pixel
+    kChkGeom,      // mesh of a triangle
+    kChkMaterial,
+    kChkKinds
+};
+inline const char *check_name(uint32_t kind) {
+    static const char *const names[kChkKinds] = {"none", "path queue slot", "connection record", "output queue slot",
+                                                 "BVH node", "leaf triangles", "traversal stack", "hit primitive",
+                                                 "scene slot", "light", "medium", "film pixel", "mesh", "material"};
+    return kind < kChkKinds ? names[kind] : "unknown";
+}
+
 struct WaveCounters {
     uint32_t count[2];           // path-ray queue lengths (ping-pong by iteration parity): continuing paths
     uint32_t rcount[2];          // and regenerated paths (camera rays), kept apart at the top of the queue

@@ -49,25 +49,10 @@ __device__ __forceinline__ void st_s(T *p, T v) { __stcs(p, v); }
 // first failure of a render wins), the access is skipped, and the render's
 // later kernels return at once; the host reports LT_ERR_CHECK. Without
 // LT_CHECKS, LT_CHECK is `true` and its condition is not compiled, so the plain
-// kernels are unchanged. The kinds, in the host's order of check names:
+// kernels are unchanged. The kinds (CheckKind) and their names are in lt_device.h.
 #ifndef LT_CHECKS
 #define LT_CHECKS 0
 #endif
-enum CheckKind : uint32_t {
-    kChkSlot = 1,  // path queue slot
-    kChkRecord,    // connection record
-    kChkOutSlot,   // output queue slot
-    kChkNode,      // BVH node
-    kChkLeaf,      // leaf triangle range
-    kChkStack,     // traversal stack
-    kChkPrim,      // hit primitive
-    kChkScene,     // scene slot of a batch
-    kChkLight,
-    kChkMedium,
-    kChkPixel,     // film pixel
-    kChkGeom,      // mesh of a triangle
-    kChkMaterial
-};
 #if LT_CHECKS
 __device__ __noinline__ void check_failed(WaveCounters *wc, uint32_t kind, uint32_t value) {
     if (wc && atomicCAS(&wc->check, 0u, kind) == 0u) wc->check_value = value;
