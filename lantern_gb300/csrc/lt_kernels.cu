@@ -11,7 +11,10 @@
 //            film and their slot starts the next (pixel, frame) sample
 //
 // Queues are compacted with warp ballots and reserved once per block (one
-// atomic per counter per block). Every random number is drawn in shade, in the
+// atomic per counter per block). Work items start in groups of one pixel's
+// samples (sample_of_item), and each shade block writes its continuing paths
+// grouped by the octant of their next direction, so that a trace warp holds
+// rays that walk the same nodes. Every random number is drawn in shade, in the
 // reference's order, so that a path's decisions do not depend on when its
 // connection rays are traced. The differentiable estimator and its adjoint run
 // on the same two stages (k_trace and k_dshade instantiated for their sources).
