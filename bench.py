@@ -433,6 +433,14 @@ def main():
                     "shade_share": round(shade_ms / max(total_ms, 1e-9), 3),
                     "init_share": round(init_ms / max(total_ms, 1e-9), 3),
                     "idle_share": round(idle_ms / max(total_ms, 1e-9), 3)}
+            # the whole render against the same bandwidth: bytes per sample = rays
+            # per sample (path, light-sample and BSDF-sample rays, the reference's
+            # count) x bytes per ray + 20 B of film update; above 1 where the
+            # caches serve what the model charges to HBM
+            b_sample = rays / samples * bpr + 20.0
+            roof["bytes_per_sample"] = round(b_sample, 1)
+            roof["sample_roofline"] = round(peak * 1e3 / b_sample, 1)  # Msamples/s
+            roof["sample_frac"] = round(value / world / (peak * 1e3 / b_sample), 4)
         except Exception as e:  # the oracle is a checker; report its absence
             roof = {"error": str(e)[:200]}
         cpu = None
