@@ -38,3 +38,17 @@ def test_abi_version_and_no_device_error():
         h = ctypes.c_void_p()
         st = lib.lt_ctx_create(0, ctypes.byref(h))
         assert st != 0 and lib.lt_last_error(None)
+
+
+def test_status_names_and_constants_match_the_header():
+    """The binding's status names and constants are the header's."""
+    text = open(os.path.join(ROOT, "include", "lantern_gpu.h")).read()
+    enum = re.search(r"typedef enum lt_status \{(.*?)\} lt_status;", text, re.S).group(1)
+    values = {int(v): n for n, v in re.findall(r"\b(LT_\w+)\s*=\s*(\d+)", enum)}
+    assert values == native.STATUS
+    consts = dict(re.findall(r"#define (LT_\w+) (\d+)u?\b", text))
+    assert int(consts["LT_ABI_VERSION"]) == native.ABI_VERSION
+    assert int(consts["LT_MAX_BATCH"]) == native.MAX_BATCH
+    assert int(consts["LT_NOALLOC_MAX_PATHS"]) == native.NOALLOC_MAX_PATHS
+    fields = re.search(r"typedef struct lt_queue_lengths \{(.*?)\} lt_queue_lengths;", text, re.S).group(1)
+    assert re.findall(r"uint32_t (\w+);", fields) == [f for f, _ in native.QueueLengths._fields_]
